@@ -1,0 +1,160 @@
+// sm_icp.h - arithmetic of one symmetric point-to-plane ICP step and of rigid-pose
+// handling, shared by the CUDA kernels and the CPU oracle.
+//
+// Follows icp.cpp:39-121 (symmetric_rigid_matching / minimizePointToPlaneMetric) and
+// util.cpp:209-232 (transformPointCloud). Precision design: the 21 + 6 entries of the
+// normal equations and the centroid sums are accumulated in FP32 with Kahan compensation;
+// only the 6x6 solve and the pose composition run in FP64. Both sides use the same
+// summation layout (kIcpThreads strided partial sums merged by a fixed binary tree), so
+// the GPU and the oracle produce bit-identical poses.
+#pragma once
+
+#include "sm_linalg.h"
+#include "sm_math.h"
+
+namespace smi {
+
+constexpr int kIcpThreads = 256; // ICP CTA size; also the oracle's emulated partial count
+
+// Kahan-compensated FP32 accumulator; value() = s - c.
+struct KahanF {
+    float s, c;
+    SM_HD void init() {
+        s = 0.0f;
+        c = 0.0f;
+    }
+    SM_HD void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c             = (t - s) - y;
+        s             = t;
+    }
+    // merge another partial: its sum, then its negated compensation, as two more terms
+    SM_HD void merge(const KahanF &o) {
+        add(o.s);
+        add(-o.c);
+    }
+    SM_HD float value() const { return s - c; }
+};
+
+// A rigid pose as a row-major 3x4 [R | t] in float.
+struct Pose34 {
+    float m[12];
+};
+
+SM_HD void pose_identity(Pose34 &p) {
+    for (int i = 0; i < 12; i++)
+        p.m[i] = (i % 5 == 0) ? 1.0f : 0.0f;
+}
+
+// x' = R x + t with Eigen's 3-term order r0*x + (r1*y + r2*z), then + t.
+SM_HD void pose_apply(const Pose34 &T, float x, float y, float z, float &ox, float &oy,
+                      float &oz) {
+    ox = (T.m[0] * x + (T.m[1] * y + T.m[2] * z)) + T.m[3];
+    oy = (T.m[4] * x + (T.m[5] * y + T.m[6] * z)) + T.m[7];
+    oz = (T.m[8] * x + (T.m[9] * y + T.m[10] * z)) + T.m[11];
+}
+SM_HD void pose_rotate(const Pose34 &T, float x, float y, float z, float &ox, float &oy,
+                       float &oz) {
+    ox = T.m[0] * x + (T.m[1] * y + T.m[2] * z);
+    oy = T.m[4] * x + (T.m[5] * y + T.m[6] * z);
+    oz = T.m[8] * x + (T.m[9] * y + T.m[10] * z);
+}
+
+// out = a * b, evaluated in FP64 and rounded to float.
+SM_HD Pose34 pose_mul(const Pose34 &a, const Pose34 &b) {
+    Pose34 o;
+    for (int i = 0; i < 3; i++) {
+        for (int j = 0; j < 4; j++) {
+            double s = (j == 3) ? (double)a.m[i * 4 + 3] : 0.0;
+            for (int k = 0; k < 3; k++)
+                s += (double)a.m[i * 4 + k] * (double)b.m[k * 4 + j];
+            o.m[i * 4 + j] = (float)s;
+        }
+    }
+    return o;
+}
+
+// Number of accumulated quantities of one ICP step.
+constexpr int kNumMoments = 6;  // sum of source and target points (centroids)
+constexpr int kNumSystem  = 27; // 21 upper-triangular A entries + 6 entries of b
+
+// Terms of one correspondence (icp.cpp:56-65): with p, q centred source / target points
+// and n = n_p + n_q, x = [(p+q) x n ; n], b_i = (p-q).n; contributes x x^T to A and b_i x
+// to b. All in float, as the reference computes them.
+SM_HD void system_terms(float px, float py, float pz, float qx, float qy, float qz, float nx,
+                        float ny, float nz, float out[kNumSystem]) {
+    const float sx = px + qx, sy = py + qy, sz = pz + qz;
+    float       x[6];
+    x[0]           = sy * nz - sz * ny;
+    x[1]           = sz * nx - sx * nz;
+    x[2]           = sx * ny - sy * nx;
+    x[3]           = nx;
+    x[4]           = ny;
+    x[5]           = nz;
+    const float bi = (px - qx) * nx + ((py - qy) * ny + (pz - qz) * nz);
+    int         k  = 0;
+    for (int i = 0; i < 6; i++)
+        for (int j = i; j < 6; j++)
+            out[k++] = x[i] * x[j];
+    for (int i = 0; i < 6; i++)
+        out[21 + i] = bi * x[i];
+}
+
+// Solve A u = -b (FP64 Cholesky, pseudo-inverse fallback) and compose the pose
+// (icp.cpp:68-86): theta = atan(|a~|) with sin/cos taken exactly as |a~|/sqrt(1+|a~|^2) and
+// 1/sqrt(1+|a~|^2), R_i = I + sin W + (1-cos) W^2, R = R_i^2,
+// t = R_i^2 (-Pmean) + R_i (cos * t~) + Qmean.
+SM_HD Pose34 solve_step(const float sys[kNumSystem], const float Pm[3], const float Qm[3]) {
+    double A[6][6], r[6], u[6];
+    int    k = 0;
+    for (int i = 0; i < 6; i++)
+        for (int j = i; j < 6; j++) {
+            A[i][j] = (double)sys[k];
+            A[j][i] = A[i][j];
+            k++;
+        }
+    for (int i = 0; i < 6; i++)
+        r[i] = -(double)sys[21 + i];
+    if (!sml::cholesky6(A, r, u))
+        sml::pinv6(A, r, u);
+    const double an = sml::dsqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+    const double h  = sml::dsqrt(1.0 + an * an);
+    const double sn = an / h, cs = 1.0 / h;
+    double       a[3] = {0.0, 0.0, 0.0};
+    if (an > 0.0) {
+        a[0] = u[0] / an;
+        a[1] = u[1] / an;
+        a[2] = u[2] / an;
+    }
+    const double W[3][3] = {{0.0, -a[2], a[1]}, {a[2], 0.0, -a[0]}, {-a[1], a[0], 0.0}};
+    double       Ri[3][3], R[3][3];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            double w2 = 0.0;
+            for (int m = 0; m < 3; m++)
+                w2 += W[i][m] * W[m][j];
+            Ri[i][j] = (i == j ? 1.0 : 0.0) + sn * W[i][j] + (1.0 - cs) * w2;
+        }
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            double s = 0.0;
+            for (int m = 0; m < 3; m++)
+                s += Ri[i][m] * Ri[m][j];
+            R[i][j] = s;
+        }
+    const double tt[3] = {cs * u[3], cs * u[4], cs * u[5]};
+    Pose34       o;
+    for (int i = 0; i < 3; i++) {
+        double t = 0.0;
+        for (int m = 0; m < 3; m++)
+            t += R[i][m] * (-(double)Pm[m]) + Ri[i][m] * tt[m];
+        t += (double)Qm[i];
+        for (int j = 0; j < 3; j++)
+            o.m[i * 4 + j] = (float)R[i][j];
+        o.m[i * 4 + 3] = (float)t;
+    }
+    return o;
+}
+
+} // namespace smi

@@ -1,0 +1,266 @@
+// sm_linalg.h - small fixed-size FP64 linear algebra of the matching path (normal
+// eigensolve, quaternion averaging, ICP 6x6 solve, pose conversions), shared by the CUDA
+// kernels and the CPU oracle. Only +, -, *, / and sqrt are used, so with FMA contraction
+// off (nvcc --fmad=false, gcc -ffp-contract=off) the results are bit-identical on both.
+//
+// The reference uses Eigen for these steps (util.cpp:262-267 SelfAdjointEigenSolver::
+// computeDirect, util.cpp:563-576 EigenSolver<Matrix4f>, icp.cpp:68 JacobiSVD, type.cpp:
+// 53-59 matrix->AngleAxis/Quaternion); Eigen is not vendored with the reference, so these
+// are written from the textbook methods named at each function and agree with the
+// reference to rounding, not bit-for-bit.
+#pragma once
+
+#include "sm_math.h"
+
+#if defined(__CUDACC__)
+#define SML_HD __host__ __device__ __forceinline__
+#else
+#define SML_HD inline
+#endif
+
+namespace sml {
+
+SML_HD double dsqrt(double a) {
+#if defined(__CUDA_ARCH__)
+    return __dsqrt_rn(a);
+#else
+    return std::sqrt(a);
+#endif
+}
+SML_HD double dabs(double a) { return a < 0.0 ? -a : a; }
+
+// Cyclic Jacobi eigen-decomposition of a symmetric N x N matrix (Golub & Van Loan,
+// "Matrix Computations", 8.5). A is destroyed; d[i] are the eigenvalues, column i of V the
+// matching unit eigenvector. Fixed sweep order, so the result is reproducible.
+template <int N> SML_HD void jacobi_eig(double A[N][N], double V[N][N], double d[N]) {
+    for (int i = 0; i < N; i++)
+        for (int j = 0; j < N; j++)
+            V[i][j] = (i == j) ? 1.0 : 0.0;
+    double scale = 0.0;
+    for (int i = 0; i < N; i++)
+        for (int j = 0; j < N; j++)
+            scale += A[i][j] * A[i][j];
+    for (int sweep = 0; sweep < 60; sweep++) {
+        double off = 0.0;
+        for (int p = 0; p < N - 1; p++)
+            for (int q = p + 1; q < N; q++)
+                off += A[p][q] * A[p][q];
+        if (!(off > scale * 1e-32))
+            break;
+        for (int p = 0; p < N - 1; p++) {
+            for (int q = p + 1; q < N; q++) {
+                const double apq = A[p][q];
+                if (apq == 0.0)
+                    continue;
+                const double theta = (A[q][q] - A[p][p]) / (2.0 * apq);
+                double       t     = 1.0 / (dabs(theta) + dsqrt(theta * theta + 1.0));
+                if (theta < 0.0)
+                    t = -t;
+                const double c = 1.0 / dsqrt(t * t + 1.0);
+                const double s = t * c;
+                for (int k = 0; k < N; k++) {
+                    const double akp = A[k][p], akq = A[k][q];
+                    A[k][p]          = c * akp - s * akq;
+                    A[k][q]          = s * akp + c * akq;
+                }
+                for (int k = 0; k < N; k++) {
+                    const double apk = A[p][k], aqk = A[q][k];
+                    A[p][k]          = c * apk - s * aqk;
+                    A[q][k]          = s * apk + c * aqk;
+                }
+                for (int k = 0; k < N; k++) {
+                    const double vkp = V[k][p], vkq = V[k][q];
+                    V[k][p]          = c * vkp - s * vkq;
+                    V[k][q]          = s * vkp + c * vkq;
+                }
+            }
+        }
+    }
+    for (int i = 0; i < N; i++)
+        d[i] = A[i][i];
+}
+
+// Normal of a 3x3 covariance: the unit eigenvector of the eigenvalue of least magnitude
+// (first such in ascending-eigenvalue order, as util.cpp:264-267 picks it).
+SML_HD void normal_from_cov(const double C[6] /*xx xy xz yy yz zz*/, float out[3]) {
+    double A[3][3] = {{C[0], C[1], C[2]}, {C[1], C[3], C[4]}, {C[2], C[4], C[5]}};
+    double V[3][3], d[3];
+    jacobi_eig<3>(A, V, d);
+    int order[3] = {0, 1, 2};
+    for (int i = 0; i < 3; i++) // ascending eigenvalues, stable
+        for (int j = 0; j < 2 - i; j++)
+            if (d[order[j]] > d[order[j + 1]]) {
+                int t        = order[j];
+                order[j]     = order[j + 1];
+                order[j + 1] = t;
+            }
+    int    best = order[0];
+    double bv   = dabs(d[order[0]]);
+    for (int k = 1; k < 3; k++)
+        if (dabs(d[order[k]]) < bv) {
+            bv   = dabs(d[order[k]]);
+            best = order[k];
+        }
+    double x = V[0][best], y = V[1][best], z = V[2][best];
+    double n = dsqrt(x * x + y * y + z * z);
+    if (n > 0.0) {
+        x /= n;
+        y /= n;
+        z /= n;
+    }
+    out[0] = (float)x;
+    out[1] = (float)y;
+    out[2] = (float)z;
+}
+
+// Markley quaternion average (util.cpp:553-577): eigenvector of the largest eigenvalue of
+// (1/M) sum q q^T, returned as a unit quaternion (w,x,y,z).
+SML_HD void quat_average_from_sum(const double S[10] /*upper triangle of sum q q^T*/, int M,
+                                  double q[4]) {
+    double A[4][4];
+    int    k = 0;
+    for (int i = 0; i < 4; i++)
+        for (int j = i; j < 4; j++) {
+            A[i][j] = S[k] / (double)M;
+            A[j][i] = A[i][j];
+            k++;
+        }
+    double V[4][4], d[4];
+    jacobi_eig<4>(A, V, d);
+    int best = 0;
+    for (int i = 1; i < 4; i++)
+        if (d[i] > d[best])
+            best = i;
+    double n = 0.0;
+    for (int i = 0; i < 4; i++)
+        n += V[i][best] * V[i][best];
+    n = dsqrt(n);
+    for (int i = 0; i < 4; i++)
+        q[i] = (n > 0.0) ? V[i][best] / n : (i == 0 ? 1.0 : 0.0);
+}
+
+// Unit quaternion (w,x,y,z) -> row-major rotation matrix.
+SML_HD void quat_to_mat(const double q[4], double R[9]) {
+    const double w = q[0], x = q[1], y = q[2], z = q[3];
+    const double tx = 2.0 * x, ty = 2.0 * y, tz = 2.0 * z;
+    const double twx = tx * w, twy = ty * w, twz = tz * w;
+    const double txx = tx * x, txy = ty * x, txz = tz * x;
+    const double tyy = ty * y, tyz = tz * y, tzz = tz * z;
+    R[0]             = 1.0 - (tyy + tzz);
+    R[1]             = txy - twz;
+    R[2]             = txz + twy;
+    R[3]             = txy + twz;
+    R[4]             = 1.0 - (txx + tzz);
+    R[5]             = tyz - twx;
+    R[6]             = txz - twy;
+    R[7]             = tyz + twx;
+    R[8]             = 1.0 - (txx + tyy);
+}
+
+// Rotation matrix -> unit quaternion (w,x,y,z), Shepperd's method (largest-pivot branch).
+SML_HD void mat_to_quat(const double R[9], double q[4]) {
+    const double tr = R[0] + R[4] + R[8];
+    if (tr > 0.0) {
+        double t = dsqrt(tr + 1.0);
+        q[0]     = 0.5 * t;
+        t        = 0.5 / t;
+        q[1]     = (R[7] - R[5]) * t;
+        q[2]     = (R[2] - R[6]) * t;
+        q[3]     = (R[3] - R[1]) * t;
+    } else {
+        int i = 0;
+        if (R[4] > R[0])
+            i = 1;
+        if (R[8] > R[i * 4])
+            i = 2;
+        const int j = (i + 1) % 3, k = (j + 1) % 3;
+        double    t = dsqrt(R[i * 4] - R[j * 4] - R[k * 4] + 1.0);
+        double    v[3];
+        v[i] = 0.5 * t;
+        t    = 0.5 / t;
+        q[0] = (R[k * 3 + j] - R[j * 3 + k]) * t;
+        v[j] = (R[j * 3 + i] + R[i * 3 + j]) * t;
+        v[k] = (R[k * 3 + i] + R[i * 3 + k]) * t;
+        q[1] = v[0];
+        q[2] = v[1];
+        q[3] = v[2];
+    }
+}
+
+// Rotation angle in [0, pi] of a unit quaternion: 2 atan2(|v|, |w|) (AngleAxis from
+// quaternion), evaluated with the shared float atan2.
+SML_HD float quat_angle(const double q[4]) {
+    const double n = dsqrt(q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+    if (n == 0.0)
+        return 0.0f;
+    return 2.0f * smm::atan2f_((float)n, (float)dabs(q[0]));
+}
+
+// Solve the symmetric 6x6 system A u = r by Cholesky (A = L L^T). Returns false when a
+// pivot is not positive relative to the matrix scale; the caller then uses the
+// eigen-decomposition pseudo-inverse below.
+SML_HD bool cholesky6(const double A[6][6], const double r[6], double u[6]) {
+    double L[6][6];
+    double dmax = 0.0;
+    for (int i = 0; i < 6; i++)
+        dmax = A[i][i] > dmax ? A[i][i] : dmax;
+    if (!(dmax > 0.0))
+        return false;
+    for (int j = 0; j < 6; j++) {
+        double s = A[j][j];
+        for (int k = 0; k < j; k++)
+            s -= L[j][k] * L[j][k];
+        if (!(s > dmax * 1e-13))
+            return false;
+        const double ljj = dsqrt(s);
+        L[j][j]          = ljj;
+        for (int i = j + 1; i < 6; i++) {
+            double t = A[i][j];
+            for (int k = 0; k < j; k++)
+                t -= L[i][k] * L[j][k];
+            L[i][j] = t / ljj;
+        }
+    }
+    double y[6];
+    for (int i = 0; i < 6; i++) {
+        double t = r[i];
+        for (int k = 0; k < i; k++)
+            t -= L[i][k] * y[k];
+        y[i] = t / L[i][i];
+    }
+    for (int i = 5; i >= 0; i--) {
+        double t = y[i];
+        for (int k = i + 1; k < 6; k++)
+            t -= L[k][i] * u[k];
+        u[i] = t / L[i][i];
+    }
+    return true;
+}
+
+// Least-squares / minimum-norm solve of a symmetric PSD 6x6 system through its
+// eigen-decomposition, discarding eigenvalues below 1e-6 of the largest (rank-deficient
+// cases the reference handles with JacobiSVD, icp.cpp:68).
+SML_HD void pinv6(const double Ain[6][6], const double r[6], double u[6]) {
+    double A[6][6], V[6][6], d[6];
+    for (int i = 0; i < 6; i++)
+        for (int j = 0; j < 6; j++)
+            A[i][j] = Ain[i][j];
+    jacobi_eig<6>(A, V, d);
+    double dmax = 0.0;
+    for (int i = 0; i < 6; i++)
+        dmax = dabs(d[i]) > dmax ? dabs(d[i]) : dmax;
+    for (int i = 0; i < 6; i++)
+        u[i] = 0.0;
+    for (int k = 0; k < 6; k++) {
+        if (!(dabs(d[k]) > dmax * 1e-6))
+            continue;
+        double c = 0.0;
+        for (int i = 0; i < 6; i++)
+            c += V[i][k] * r[i];
+        c /= d[k];
+        for (int i = 0; i < 6; i++)
+            u[i] += c * V[i][k];
+    }
+}
+
+} // namespace sml
