@@ -1,0 +1,180 @@
+/*
+ * surface_match.h - C ABI of the GB300 point-pair-feature matcher (libsurface_match.so).
+ *
+ * This is the drop-in boundary of the reference's ppf::Detector hot path. The reference
+ * (SurfaceMan/surface_match) exports a C++ class only and lists a C API as a TODO
+ * (TODO.md:4, apiExport.h:17-21 defines an unused API_DEMANGLED extern "C"); the entry
+ * points below are that C API: plain pointers and sizes, status codes instead of
+ * exceptions, every buffer owned by the caller. Each function names the reference
+ * interface it replaces.
+ *
+ * Pointers to point data may be host or device (CUDA) pointers; the library detects the
+ * kind and copies host data to the device itself. Coordinates are float32 xyz triples,
+ * normals float32 triples (or NULL when absent).
+ *
+ * Errors map to the reference's exception types: SM_ERR_RANGE <-> std::range_error,
+ * SM_ERR_RUNTIME <-> std::runtime_error (ppf.cpp:39-44,155-168,514-538; type.cpp:79-127).
+ * sm_last_error() returns the message of the last failing call of the calling thread,
+ * worded as the reference's exception message where one exists.
+ */
+#ifndef SURFACE_MATCH_H
+#define SURFACE_MATCH_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SM_API __attribute__((visibility("default")))
+#else
+#define SM_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define SM_OK 0
+#define SM_ERR_RANGE 1    /* std::range_error in the reference */
+#define SM_ERR_RUNTIME 2  /* std::runtime_error in the reference */
+#define SM_ERR_CUDA 3     /* CUDA runtime failure */
+#define SM_ERR_ARG 4      /* NULL handle / bad pointer / bad size */
+#define SM_ERR_NOMEM 5    /* device allocation failed */
+#define SM_ERR_CAPACITY 6 /* an internal capacity was exceeded (reported, never silent) */
+
+typedef struct sm_context_s *sm_context; /* one device + one CUDA stream + workspace */
+typedef struct sm_model_s *sm_model;     /* a trained model resident on the device */
+
+/* ppf::TrainParam (type.h:39-74). */
+typedef struct {
+    float featDistanceStepRel;
+    int   featAngleResolution;
+    float poseRefRelSamplingDistance;
+    int   knnNormal;
+    int   smoothNormal;
+} sm_train_param;
+
+/* ppf::MatchParam (type.h:80-176). */
+typedef struct {
+    int   numMatches;
+    int   knnNormal;
+    int   smoothNormal;
+    int   invertNormal;
+    float maxOverlapDistRel;
+    float maxOverlapDistAbs;
+    int   sparsePoseRefinement;
+    int   densePoseRefinement;
+    int   poseRefNumSteps;
+    float poseRefDistThresholdRel;
+    float poseRefDistThresholdAbs;
+    float poseRefScoringDistRel;
+    float poseRefScoringDistAbs;
+} sm_match_param;
+
+/* Per-call statistics of sm_match (the reference prints these sizes, ppf.cpp:217-220). */
+typedef struct {
+    int64_t n_points;     /* input points */
+    int64_t n_valid;      /* finite points (removeNan, util.cpp:86-105) */
+    int64_t n_sampled;    /* sampled scene points */
+    int64_t n_keypoints;  /* reference (key) points */
+    int64_t n_resampled;  /* dense-refinement scene points */
+    int64_t n_poses;      /* candidate poses from voting */
+    int64_t n_clusters;   /* candidates after clustering */
+    int64_t n_pairs;      /* point pairs evaluated (keypoint x neighbour) */
+    int64_t n_hits;       /* pairs whose key is in the model table */
+    int64_t n_votes;      /* votes cast: matched table entries (ppf.cpp:342-346) */
+    float   ms[8];        /* stage device times: prep, sample+normals, keypoints, vote,
+                             cluster, icp prep, icp, total */
+} sm_match_stats;
+
+/* TrainParam / MatchParam defaults and constructor validation (type.cpp:71-127). */
+SM_API void sm_train_param_default(sm_train_param *p);
+SM_API void sm_match_param_default(sm_match_param *p);
+SM_API int  sm_train_param_check(const sm_train_param *p);
+SM_API int  sm_match_param_check(const sm_match_param *p);
+
+/* Context: device ordinal, optional external cudaStream_t (NULL = the library creates
+ * its own non-blocking stream). Replaces nothing in the reference (its runtime is OpenMP,
+ * ppf.cpp:26-31). */
+SM_API int sm_context_create(int device, void *cuda_stream, sm_context *out);
+SM_API int sm_context_destroy(sm_context ctx);
+SM_API int sm_context_synchronize(sm_context ctx);
+SM_API void *sm_context_stream(sm_context ctx);
+
+/* Model handle (ppf::Detector::IMPL, privateType.h:56-66). */
+SM_API int sm_model_create(sm_context ctx, sm_model *out);
+SM_API int sm_model_destroy(sm_model model);
+
+/* ppf::Detector::trainModel (ppf.h:25-26, ppf.cpp:36-147). xyz/normal: n x 3 floats,
+ * normal may be NULL (normals are then estimated). */
+SM_API int sm_model_train(sm_model model, const float *xyz, const float *normal, int64_t n,
+                          float samplingDistanceRel, const sm_train_param *param);
+
+/* Load a model given as arrays (the state ppf::Detector::load reads, ppf.cpp:529-547):
+ * sampled and resampled clouds with normals, the model box (min xyz, max xyz), and the
+ * hash table as ascending keys, bucket offsets (nkeys + 1) and per-entry reference index
+ * and alpha angle in insertion order. */
+SM_API int sm_model_upload(sm_model model, int64_t n_sampled, const float *sampled_xyz,
+                           const float *sampled_normal, int64_t n_resampled,
+                           const float *resampled_xyz, const float *resampled_normal,
+                           const float *box6, int64_t n_keys, const uint32_t *keys,
+                           const uint32_t *offsets, const uint32_t *refs, const float *alphas,
+                           float samplingDistanceRel, const sm_train_param *param);
+
+/* sizes[4] = {n_sampled, n_resampled, n_keys, n_entries} */
+SM_API int sm_model_sizes(sm_model model, int64_t *sizes);
+/* Copy the model out as arrays (same layout as sm_model_upload; any pointer may be NULL). */
+SM_API int sm_model_download(sm_model model, float *sampled_xyz, float *sampled_normal,
+                             float *resampled_xyz, float *resampled_normal, float *box6,
+                             uint32_t *keys, uint32_t *offsets, uint32_t *refs, float *alphas,
+                             float *samplingDistanceRel, sm_train_param *param);
+
+/* ppf::Detector::save / load (ppf.cpp:512-547, serialize.cpp:5-186): the reference's
+ * little-endian model file (magic 0x7F27F, version 100). */
+SM_API int sm_model_save(sm_model model, const char *path);
+SM_API int sm_model_load(sm_model model, const char *path);
+
+/* ppf::Detector::matchScene (ppf.h:39-42, ppf.cpp:149-510).
+ * xyz/normal: scene points (normal may be NULL: estimated). viewpoint: 3 floats or NULL
+ * (PointCloud::viewPoint, type.h:28; NULL = not set). Results are written sorted by
+ * score: out_pose[i*16..] a row-major 4x4 pose, out_score[i]; *inout_count holds the
+ * capacity on entry and the number of results on return. stats may be NULL. */
+SM_API int sm_match(sm_model model, const float *xyz, const float *normal, int64_t n,
+                    const float *viewpoint, float samplingDistanceRel, float keyPointFraction,
+                    float minScore, const sm_match_param *param, float *out_pose,
+                    float *out_score, int *inout_count, sm_match_stats *stats);
+
+/* Stage entry of the voting step (ppf.cpp:247-409) on caller-supplied scene state:
+ * points/normals (n x 3), keypoint indices, and per-keypoint neighbour lists in search
+ * order (nbr_off: K + 1 offsets into nbr_ids; each list contains the keypoint itself, as
+ * the reference's radius search returns it). Outputs per keypoint: out_stats[K x 8] =
+ * {neighbours, skipped (0 voted, 1 NaN normal, 2 below threshold), hits, votes,
+ * accumulator fingerprint, n candidates, n poses, 0}; out_cands[K x 9] = up to 3
+ * (vote, ref, angle bin) triples (-1 padded); out_poses[K x 3 x 18] (nullable) = pose
+ * 3x4, quaternion wxyz, rotation angle, votes. out_acc (nullable) receives the full
+ * refNum x featAngleResolution accumulators of the first dump_k keypoints. */
+SM_API int sm_vote_stage(sm_model model, const float *points, const float *normals, int64_t n,
+                         const int32_t *keypoints, int64_t K, const int32_t *nbr_off,
+                         const int32_t *nbr_ids, float minScore, int64_t *out_stats,
+                         float *out_cands, float *out_poses, int dump_k, int32_t *out_acc);
+
+/* Intermediate state of the last sm_match on this model's context, for inspection and
+ * parity checks. Fields: 0 sampled ids, 1 keypoint ids, 2 resampled ids (int32);
+ * 3 positions, 4 normals (float x3, after normal estimation); 7 per-keypoint stats
+ * (int64 x8, as sm_vote_stage); 8 candidates (float x9); 9 pose list (float x18);
+ * 10 clustered candidates (float x18); 12 candidate ICP status (int32: 0 accepted,
+ * 1 votes, 2 sparse not converged, 3 sparse score, 4 dense not converged, 5 dense score);
+ * 13 candidate score (float); 14 candidate pose (float x12). */
+SM_API int64_t sm_debug_size(sm_model model, int field);
+SM_API int     sm_debug_get(sm_model model, int field, void *dst);
+
+/* Message of the last failing call on this thread ("" if none). */
+SM_API const char *sm_last_error(void);
+
+/* Library version string. */
+SM_API const char *sm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SURFACE_MATCH_H */

@@ -574,12 +574,10 @@ struct PoseRec {
 };
 
 void pose_update(PoseRec &p) { // Pose::updatePose (type.cpp:53-59)
-    double R[9], q[4];
-    for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 3; j++) R[i * 3 + j] = p.T.m[i * 4 + j];
-    sml::mat_to_quat(R, q);
-    for (int i = 0; i < 4; i++) p.q[i] = (float)q[i];
-    p.angle = sml::quat_angle(q);
+    float rec[smi::kPoseFloats];
+    smi::pose_record(p.T.m, p.votes, rec);
+    memcpy(p.q, rec + 12, 16);
+    p.angle = rec[16];
 }
 
 struct KpOut {
@@ -593,9 +591,11 @@ struct KpOut {
     PoseRec  poses[3];
 };
 
-uint64_t acc_hash(const std::vector<int> &acc) { // FNV-1a over the int32 words
-    uint64_t h = 1469598103934665603ull;
-    for (int v : acc) { h ^= (uint32_t)v; h *= 1099511628211ull; }
+// Order-independent accumulator fingerprint: sum over cells of splitmix64(index, count).
+uint64_t acc_hash(const std::vector<int> &acc) {
+    uint64_t h = 0;
+    for (size_t i = 0; i < acc.size(); i++)
+        if (acc[i]) h += smm::mix64(((uint64_t)i << 32) | (uint32_t)acc[i]);
     return h;
 }
 
@@ -675,30 +675,13 @@ void vote_keypoint(const Model &m, const std::vector<V3> &P, const std::vector<V
         const V3 &pm = m.sp[o.cr[c]], &nm = m.sn[o.cr[c]];
         smm::RT rm = smm::transform_rt(pm.x, pm.y, pm.z, nm.x, nm.y, nm.z);
         float   al = smm::candidate_angle(o.ca[c], A - 1);
-        double  ca = smm::cosf_(al), sa = smm::sinf_(al);
-        // X * RT_m
-        double XM[3][4];
-        for (int j = 0; j < 4; j++) {
-            double r0 = j < 3 ? rm.r[j] : rm.t[0];
-            double r1 = j < 3 ? rm.r[3 + j] : rm.t[1];
-            double r2 = j < 3 ? rm.r[6 + j] : rm.t[2];
-            XM[0][j] = r0;
-            XM[1][j] = ca * r1 - sa * r2;
-            XM[2][j] = sa * r1 + ca * r2;
-        }
-        // RT_s^-1 = [R^T | -R^T t]
+        float   rec[smi::kPoseFloats];
+        smi::candidate_pose(rt, rm, al, o.cv[c], rec);
         PoseRec pr;
-        for (int i = 0; i < 3; i++) {
-            for (int j = 0; j < 4; j++) {
-                double s = 0;
-                for (int k = 0; k < 3; k++) s += (double)rt.r[k * 3 + i] * XM[k][j];
-                if (j == 3)
-                    for (int k = 0; k < 3; k++) s -= (double)rt.r[k * 3 + i] * (double)rt.t[k];
-                pr.T.m[i * 4 + j] = (float)s;
-            }
-        }
-        pr.votes = o.cv[c];
-        pose_update(pr);
+        memcpy(pr.T.m, rec, 48);
+        memcpy(pr.q, rec + 12, 16);
+        pr.angle = rec[16];
+        pr.votes = rec[17];
         o.poses[o.npose++] = pr;
     }
 }

@@ -1,0 +1,1021 @@
+// api.cu - the C ABI (include/surface_match.h) and the host orchestration of the
+// matching path on one device: ppf::Detector::trainModel / matchScene / save / load
+// (ppf.cpp:36-547) over the device stages of prep.cu, vote.cu, cluster.cu and icp.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/surface_match.h"
+#include "sm_icp.h"
+#include "sm_stages.h"
+
+struct sm_context_s {
+    sm::Ctx ctx;
+};
+
+struct sm_model_s {
+    sm_context ctx;
+    sm::Model  m;
+};
+
+namespace sm {
+
+static thread_local std::string g_lastError;
+
+void Model::free_device() {
+    void *ps[] = {sp, sn, rp, rn, hkeys, boff, entries};
+    for (void *p : ps)
+        if (p)
+            cudaFree(p);
+    sp = sn = rp = rn = nullptr;
+    hkeys = boff = nullptr;
+    entries      = nullptr;
+}
+
+namespace {
+
+template <class F> int guarded(F &&f) {
+    try {
+        f();
+        g_lastError.clear();
+        return SM_OK;
+    } catch (const Error &e) {
+        g_lastError = e.what();
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        g_lastError = "host allocation failed";
+        return SM_ERR_NOMEM;
+    } catch (const std::exception &e) {
+        g_lastError = e.what();
+        return SM_ERR_RUNTIME;
+    }
+}
+
+bool is_device_ptr(const void *p) {
+    if (!p)
+        return false;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// Copy n*3 floats to the device unless they already are there.
+const float *to_device(Ctx &c, const float *src, int64_t n, const std::string &tag) {
+    if (!src)
+        return nullptr;
+    if (is_device_ptr(src))
+        return src;
+    float *d = c.arena.get<float>(tag, (size_t)n * 3);
+    SM_CUDA(cudaMemcpyAsync(d, src, (size_t)n * 12, cudaMemcpyHostToDevice, c.stream));
+    return d;
+}
+
+__global__ void k_gather4(const float4 *__restrict__ src, const int *__restrict__ ids, int m,
+                          float4 *__restrict__ dst, int renormalize) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m)
+        return;
+    float4 v = src[ids[i]];
+    if (renormalize) {
+        const float sq = v.x * v.x + (v.y * v.y + v.z * v.z);
+        if (sq > 0.0f) {
+            const float s = smm::fsqrt(sq);
+            v = make_float4(smm::fdiv(v.x, s), smm::fdiv(v.y, s), smm::fdiv(v.z, s), 0.0f);
+        }
+    }
+    dst[i] = v;
+}
+
+__global__ void k_gather_poses(const float *__restrict__ poses, const int *__restrict__ slots,
+                               int m, float *__restrict__ out) {
+    const int i = blockIdx.x;
+    if (i >= m)
+        return;
+    const int s = slots[i];
+    for (int e = threadIdx.x; e < smi::kPoseFloats; e += blockDim.x)
+        out[(size_t)i * smi::kPoseFloats + e] = poses[(size_t)s * smi::kPoseFloats + e];
+}
+
+__global__ void k_f3_to_f4(const float *__restrict__ a, int n, float4 *__restrict__ o) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        o[i] = make_float4(a[3 * (size_t)i], a[3 * (size_t)i + 1], a[3 * (size_t)i + 2], 0.0f);
+}
+
+void check_train_param(const sm_train_param &p) {
+    if (p.featDistanceStepRel > 1 || p.featDistanceStepRel <= 0)
+        throw Error(SM_ERR_RANGE, "Invalid Input: featDistanceStepRel range mismatch in TrainParam()");
+    if (p.featAngleResolution <= 0)
+        throw Error(SM_ERR_RANGE, "Invalid Input: featAngleResolution range mismatch in TrainParam()");
+    if (p.poseRefRelSamplingDistance > 1 || p.poseRefRelSamplingDistance <= 0)
+        throw Error(SM_ERR_RANGE,
+                    "Invalid Input: poseRefRelSamplingDistance range mismatch in TrainParam()");
+}
+
+void check_match_param(const sm_match_param &p) {
+    if (p.numMatches < 1)
+        throw Error(SM_ERR_RANGE, "Invalid Input: numMatches range mismatch in MatchParam()");
+    if (p.maxOverlapDistRel < 0 && p.maxOverlapDistAbs < 0)
+        throw Error(SM_ERR_RANGE, "Invalid Input: maxOverlapDist range mismatch in MatchParam()");
+    if (!p.densePoseRefinement) {
+        if (p.poseRefNumSteps < 1)
+            throw Error(SM_ERR_RANGE, "Invalid Input: poseRefNumSteps range mismatch in MatchParam()");
+        if (p.poseRefDistThresholdRel < 0 && p.poseRefDistThresholdAbs < 0)
+            throw Error(SM_ERR_RANGE,
+                        "Invalid Input: poseRefDistThreshold range mismatch in MatchParam()");
+        if (p.poseRefScoringDistRel < 0 && p.poseRefScoringDistAbs < 0)
+            throw Error(SM_ERR_RANGE, "Invalid Input: poseRefScoringDist range mismatch in MatchParam()");
+    }
+}
+
+// Upload host arrays of a model and build the open-addressed key table.
+void upload_model(Model &m, const std::vector<float> &sp, const std::vector<float> &sn,
+                  const std::vector<float> &rp, const std::vector<float> &rn, const float box[6],
+                  const std::vector<uint32_t> &keys, const std::vector<uint32_t> &offs,
+                  const std::vector<uint32_t> &refs, const std::vector<float> &alphas) {
+    m.free_device();
+    m.ns       = (int)(sp.size() / 3);
+    m.nr       = (int)(rp.size() / 3);
+    m.nkeys    = (int)keys.size();
+    m.nentries = (long long)refs.size();
+    for (int a = 0; a < 3; a++) {
+        m.box.mn[a] = box[a];
+        m.box.mx[a] = box[3 + a];
+    }
+    for (size_t b = 0; b + 1 < offs.size(); b++)
+        if (offs[b + 1] < offs[b] || offs[b + 1] > refs.size())
+            throw Error(SM_ERR_ARG, "model table offsets are not monotone");
+    for (uint32_t r : refs)
+        if ((int)r >= m.ns)
+            throw Error(SM_ERR_ARG, "model table references a point beyond the sampled model");
+    auto up4 = [](const std::vector<float> &v, float4 *&d) {
+        const size_t n = v.size() / 3;
+        std::vector<float4> h(n);
+        for (size_t i = 0; i < n; i++)
+            h[i] = make_float4(v[3 * i], v[3 * i + 1], v[3 * i + 2], 0.0f);
+        SM_CUDA(cudaMalloc(&d, std::max<size_t>(n, 1) * sizeof(float4)));
+        if (n)
+            SM_CUDA(cudaMemcpy(d, h.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+    };
+    up4(sp, m.sp);
+    up4(sn, m.sn);
+    up4(rp, m.rp);
+    up4(rn, m.rn);
+    uint32_t size = 16;
+    while (size < 2u * (uint32_t)m.nkeys)
+        size <<= 1;
+    std::vector<uint4> tab(size, make_uint4(0, 0, 0, 0));
+    for (int b = 0; b < m.nkeys; b++) {
+        uint32_t i = keys[b] & (size - 1);
+        while (tab[i].z != 0)
+            i = (i + 1) & (size - 1);
+        tab[i] = make_uint4(keys[b], offs[b], offs[b + 1] - offs[b], 0);
+    }
+    m.hmask = size - 1;
+    SM_CUDA(cudaMalloc((void **)&m.hkeys, size * sizeof(uint4)));
+    SM_CUDA(cudaMemcpy(m.hkeys, tab.data(), size * sizeof(uint4), cudaMemcpyHostToDevice));
+    std::vector<uint2> ent(std::max<size_t>(refs.size(), 1));
+    for (size_t e = 0; e < refs.size(); e++) {
+        uint32_t ab;
+        memcpy(&ab, &alphas[e], 4);
+        ent[e] = make_uint2(refs[e], ab);
+    }
+    SM_CUDA(cudaMalloc((void **)&m.entries, ent.size() * sizeof(uint2)));
+    SM_CUDA(cudaMemcpy(m.entries, ent.data(), ent.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+    m.h_sp     = sp;
+    m.h_sn     = sn;
+    m.h_rp     = rp;
+    m.h_rn     = rn;
+    m.h_keys   = keys;
+    m.h_offs   = offs;
+    m.h_refs   = refs;
+    m.h_alphas = alphas;
+    m.trained  = true;
+}
+
+std::vector<float> download4(const float4 *d, int n) {
+    std::vector<float4> h(n);
+    if (n)
+        SM_CUDA(cudaMemcpy(h.data(), d, n * sizeof(float4), cudaMemcpyDeviceToHost));
+    std::vector<float> o(3 * (size_t)n);
+    for (int i = 0; i < n; i++) {
+        o[3 * i]     = h[i].x;
+        o[3 * i + 1] = h[i].y;
+        o[3 * i + 2] = h[i].z;
+    }
+    return o;
+}
+
+// trainModel (ppf.cpp:36-147) with the device sampler, normal estimation and pair kernel;
+// the table is grouped by key on the host in pair order, i.e. the reference's
+// single-threaded insertion order (reference point i, then column j).
+void train(Ctx &c, Model &m, const float *xyzIn, const float *nrmIn, int64_t n64, float sdRel,
+           const sm_train_param &tp) {
+    if (sdRel > 1 || sdRel < 0)
+        throw Error(SM_ERR_RANGE, "Invalid Input: samplingDistanceRel range mismatch in trainModel");
+    if (n64 <= 0 || !xyzIn)
+        throw Error(SM_ERR_RUNTIME, "Invalid Input: empty model in trainModel");
+    check_train_param(tp);
+    if (n64 > (1ll << 30))
+        throw Error(SM_ERR_ARG, "model has too many points");
+    const int    n   = (int)n64;
+    const float *xyz = to_device(c, xyzIn, n, "t.xyz");
+    const float *nin = to_device(c, nrmIn, n, "t.nrm");
+    float4      *pos = c.arena.get<float4>("t.pos", n);
+    float4      *nrm = c.arena.get<float4>("t.n4", n);
+    int         *val = c.arena.get<int>("t.valid", n);
+    Box          box;
+    const int    nvalid = prep_points(c, xyz, nin, n, pos, nrm, val, box);
+    if (nvalid == 0)
+        throw Error(SM_ERR_RUNTIME, "Invalid Input: empty model in trainModel");
+    int *valid = c.arena.get<int>("t.vids", n);
+    compact(c, val, n, valid, "t.cv");
+    const float diam         = box.diameter();
+    const float sampleStep   = diam * sdRel;
+    const float reSampleStep = diam * tp.poseRefRelSamplingDistance;
+    int        *idx1         = c.arena.get<int>("t.idx1", n);
+    int        *idx2         = c.arena.get<int>("t.idx2", n);
+    const int   n1 = sample_points(c, pos, n, valid, nvalid, box, sampleStep, idx1, "t.s1");
+    const int   n2 = sample_points(c, pos, n, valid, nvalid, box, reSampleStep, idx2, "t.s2");
+    if (!nrmIn) {
+        float ext[3] = {box.ext(0), box.ext(1), box.ext(2)};
+        Grid  q;
+        build_grid(c, pos, valid, nvalid, box, smg::query_cell(sampleStep * 0.25f, ext), false, q, "t.q");
+        estimate_normals(c, pos, nrm, n, idx1, n1, q, tp.knnNormal, tp.smoothNormal != 0, false,
+                         nullptr, "t.n1");
+        build_grid(c, pos, valid, nvalid, box, smg::query_cell(sampleStep * 0.25f, ext), false, q, "t.q");
+        estimate_normals(c, pos, nrm, n, idx2, n2, q, tp.knnNormal, tp.smoothNormal != 0, false,
+                         nullptr, "t.n2");
+    }
+    float4 *sp = c.arena.get<float4>("t.sp", std::max(n1, 1));
+    float4 *sn = c.arena.get<float4>("t.sn", std::max(n1, 1));
+    float4 *rp = c.arena.get<float4>("t.rp", std::max(n2, 1));
+    float4 *rn = c.arena.get<float4>("t.rn", std::max(n2, 1));
+    if (n1) {
+        k_gather4<<<nblocks(n1, 256), 256, 0, c.stream>>>(pos, idx1, n1, sp, 0);
+        k_gather4<<<nblocks(n1, 256), 256, 0, c.stream>>>(nrm, idx1, n1, sn, 1);
+    }
+    if (n2) {
+        k_gather4<<<nblocks(n2, 256), 256, 0, c.stream>>>(pos, idx2, n2, rp, 0);
+        k_gather4<<<nblocks(n2, 256), 256, 0, c.stream>>>(nrm, idx2, n2, rn, 1);
+    }
+    SM_LAUNCH_CHECK();
+    const int   A         = tp.featAngleResolution;
+    const float angleStep = smm::k2PiF / (float)A;
+    const float distStep  = diam * tp.featDistanceStepRel;
+    const long long npair = (long long)n1 * n1;
+    uint32_t *keys   = c.arena.get<uint32_t>("t.keys", std::max<long long>(npair, 1));
+    float    *alphas = c.arena.get<float>("t.alphas", std::max<long long>(npair, 1));
+    int      *pv     = c.arena.get<int>("t.pv", std::max<long long>(npair, 1));
+    model_pairs(c, sp, sn, n1, angleStep, distStep, keys, alphas, pv);
+    std::vector<uint32_t> hk(npair);
+    std::vector<float>    ha(npair);
+    std::vector<int>      hv(npair);
+    if (npair) {
+        SM_CUDA(cudaMemcpyAsync(hk.data(), keys, npair * 4, cudaMemcpyDeviceToHost, c.stream));
+        SM_CUDA(cudaMemcpyAsync(ha.data(), alphas, npair * 4, cudaMemcpyDeviceToHost, c.stream));
+        SM_CUDA(cudaMemcpyAsync(hv.data(), pv, npair * 4, cudaMemcpyDeviceToHost, c.stream));
+    }
+    std::vector<float> hsp = download4(sp, n1), hsn = download4(sn, n1);
+    std::vector<float> hrp = download4(rp, n2), hrn = download4(rn, n2);
+    c.sync();
+    // group by key, stable in pair order
+    std::vector<uint32_t> order;
+    order.reserve(npair);
+    for (long long t = 0; t < npair; t++)
+        if (hv[t])
+            order.push_back((uint32_t)t);
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return hk[a] < hk[b]; });
+    std::vector<uint32_t> K, O, R;
+    std::vector<float>    AL;
+    R.reserve(order.size());
+    AL.reserve(order.size());
+    for (size_t e = 0; e < order.size(); e++) {
+        const uint32_t t = order[e];
+        if (e == 0 || hk[t] != hk[order[e - 1]]) {
+            K.push_back(hk[t]);
+            O.push_back((uint32_t)e);
+        }
+        R.push_back(t / (uint32_t)n1);
+        AL.push_back(ha[t]);
+    }
+    O.push_back((uint32_t)order.size());
+    const float b6[6] = {box.mn[0], box.mn[1], box.mn[2], box.mx[0], box.mx[1], box.mx[2]};
+    upload_model(m, hsp, hsn, hrp, hrn, b6, K, O, R, AL);
+    m.sdRel = sdRel;
+    m.tp    = tp;
+}
+
+struct MatchOutputs {
+    std::vector<float> pose;  // 12 per result
+    std::vector<float> score;
+};
+
+void record(Ctx &c, int i) { SM_CUDA(cudaEventRecord(c.ev[i], c.stream)); }
+
+// matchScene (ppf.cpp:149-510) on the device.
+void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64_t n64,
+           const float *vp, float sdRel, float kpFrac, float minScore, const sm_match_param &mp,
+           MatchOutputs &res, sm_match_stats *stats) {
+    if (!m.trained)
+        throw Error(SM_ERR_RUNTIME, "No trained model in matchScene");
+    if (sdRel > 1 || sdRel < 0)
+        throw Error(SM_ERR_RANGE, "Invalid Input: samplingDistanceRel range mismatch in matchScene");
+    if (kpFrac > 1 || kpFrac < 0)
+        throw Error(SM_ERR_RANGE, "Invalid Input: keyPointFraction range mismatch in matchScene");
+    if (minScore > 1 || minScore < 0)
+        throw Error(SM_ERR_RANGE, "Invalid Input: minScore range mismatch in matchScene");
+    if (n64 <= 0 || !xyzIn)
+        throw Error(SM_ERR_RUNTIME, "Invalid Input: empty scene in matchScene");
+    check_match_param(mp);
+    if (n64 > (1ll << 30))
+        throw Error(SM_ERR_ARG, "scene has too many points");
+    const int n = (int)n64;
+    c.last.valid = false;
+    record(c, 0);
+    const float *xyz  = to_device(c, xyzIn, n, "m.xyz");
+    const float *nin  = to_device(c, nrmIn, n, "m.nrm");
+    const bool   hasN = nrmIn != nullptr;
+    float4      *pos  = c.arena.get<float4>("m.pos", n);
+    float4      *nrm  = c.arena.get<float4>("m.n4", n);
+    int         *val  = c.arena.get<int>("m.valid", n);
+    Box          box;
+    const int    nvalid = prep_points(c, xyz, nin, n, pos, nrm, val, box);
+    int         *valid  = c.arena.get<int>("m.vids", n);
+    compact(c, val, n, valid, "m.cv");
+    record(c, 1);
+    float ext[3] = {box.ext(0), box.ext(1), box.ext(2)};
+
+    const float diam         = m.box.diameter();
+    const int   A            = m.tp.featAngleResolution;
+    const float angleStep    = smm::k2PiF / (float)A;
+    const float reSampleStep = diam * m.tp.poseRefRelSamplingDistance;
+    const float sampleStep   = diam * sdRel;
+    int        *sampled      = c.arena.get<int>("m.sampled", std::max(n, 1));
+    const int   ns = sample_points(c, pos, n, valid, nvalid, box, sampleStep, sampled, "m.s1");
+    Grid        q;
+    if (!hasN) {
+        build_grid(c, pos, valid, nvalid, box, smg::query_cell(sampleStep * 0.25f, ext), false, q, "m.q");
+        estimate_normals(c, pos, nrm, n, sampled, ns, q, mp.knnNormal, mp.smoothNormal != 0,
+                         mp.invertNormal != 0, vp, "m.n1");
+    }
+    record(c, 2);
+    const float keyStep = smm::fsqrt(1.f / kpFrac) * sampleStep;
+    int        *kp      = c.arena.get<int>("m.kp", std::max(ns, 1));
+    const int   K       = sample_points(c, pos, n, sampled, ns, box, keyStep, kp, "m.s2");
+    record(c, 3);
+    // voting
+    VoteOut vo;
+    vo.stats  = c.arena.get<long long>("m.kstats", (size_t)std::max(K, 1) * 8);
+    vo.cands  = c.arena.get<float>("m.kcands", (size_t)std::max(K, 1) * 9);
+    vo.poses  = c.arena.get<float>("m.kposes", (size_t)std::max(K, 1) * 3 * smi::kPoseFloats);
+    vo.poseOk = c.arena.get<int>("m.kposeok", (size_t)std::max(K, 1) * 3);
+    vo.acc    = nullptr;
+    vote(c, m, pos, nrm, kp, K, nullptr, nullptr, sampled, ns, minScore, vo, 0);
+    int      *slots = c.arena.get<int>("m.slots", (size_t)std::max(K, 1) * 3);
+    const int np    = compact(c, vo.poseOk, K * 3, slots, "m.cp");
+    float    *plist = c.arena.get<float>("m.plist", (size_t)std::max(np, 1) * smi::kPoseFloats);
+    if (np) {
+        k_gather_poses<<<np, 32, 0, c.stream>>>(vo.poses, slots, np, plist);
+        SM_LAUNCH_CHECK();
+    }
+    record(c, 4);
+    float maxOverlap = 0;
+    if (mp.maxOverlapDistRel > 0)
+        maxOverlap = diam * mp.maxOverlapDistRel;
+    if (mp.maxOverlapDistAbs > 0)
+        maxOverlap = mp.maxOverlapDistAbs;
+    float refDist = 0;
+    if (mp.poseRefDistThresholdRel > 0)
+        refDist = diam * mp.poseRefDistThresholdRel;
+    if (mp.poseRefDistThresholdAbs > 0)
+        refDist = mp.poseRefDistThresholdAbs;
+    float scoreDist = 0;
+    if (mp.poseRefScoringDistRel > 0)
+        scoreDist = diam * mp.poseRefScoringDistRel;
+    if (mp.poseRefScoringDistAbs > 0)
+        scoreDist = mp.poseRefScoringDistAbs;
+    const float center[3] = {(m.box.mn[0] + m.box.mx[0]) / 2.f, (m.box.mn[1] + m.box.mx[1]) / 2.f,
+                             (m.box.mn[2] + m.box.mx[2]) / 2.f};
+    float    *cands = c.arena.get<float>("m.cands", (size_t)std::max(np, 1) * smi::kPoseFloats);
+    const int ncand = cluster(c, plist, np, 0.1f * diam, angleStep, center, maxOverlap, cands, "m.cl");
+    record(c, 5);
+    // dense refinement scene
+    int *resampled = c.arena.get<int>("m.resampled", std::max(n, 1));
+    int  nres      = 0;
+    if (mp.densePoseRefinement) {
+        nres = sample_points(c, pos, n, valid, nvalid, box, reSampleStep, resampled, "m.s3");
+        if (!hasN) {
+            build_grid(c, pos, valid, nvalid, box, smg::query_cell(sampleStep * 0.25f, ext), false, q, "m.q");
+            estimate_normals(c, pos, nrm, n, resampled, nres, q, mp.knnNormal, false,
+                             mp.invertNormal != 0, vp, "m.n2");
+        }
+    }
+    IcpScene s;
+    s.pos          = pos;
+    s.nrm          = nrm;
+    const float gs = std::max(sampleStep, refDist / 2.5f);
+    build_grid(c, pos, sampled, ns, box, smg::query_cell(gs, ext), false, s.sampled, "m.gS");
+    const float gr = std::max(2.0f * reSampleStep, refDist / 2.5f);
+    build_grid(c, pos, resampled, nres, box, smg::query_cell(gr, ext), false, s.resampled, "m.gR");
+    const float gf = std::max(scoreDist, sampleStep * 0.25f);
+    build_grid(c, pos, valid, nvalid, box, smg::query_cell(gf, ext), false, s.full, "m.gF");
+    int *rankS = c.arena.get<int>("m.rankS", n);
+    int *rankR = c.arena.get<int>("m.rankR", n);
+    subset_rank(c, sampled, ns, rankS);
+    subset_rank(c, resampled, nres, rankR);
+    s.rankS = rankS;
+    s.rankR = rankR;
+    record(c, 6);
+    IcpParams ip;
+    ip.sparse        = mp.sparsePoseRefinement;
+    ip.dense         = mp.densePoseRefinement;
+    ip.denseSteps    = mp.poseRefNumSteps;
+    ip.rejectDist    = refDist;
+    ip.sampleStep    = sampleStep;
+    ip.reSampleStep  = reSampleStep;
+    ip.scoreDist     = scoreDist;
+    ip.voteThreshold = (float)m.ns * minScore;
+    ip.minScore      = minScore;
+    int   *cstat  = c.arena.get<int>("m.cstat", std::max(ncand, 1));
+    float *cscore = c.arena.get<float>("m.cscore", std::max(ncand, 1));
+    float *cpose  = c.arena.get<float>("m.cpose", (size_t)std::max(ncand, 1) * 12);
+    icp_all(c, m, s, ip, cands, ncand, cstat, cscore, cpose);
+    std::vector<int>   hs(ncand);
+    std::vector<float> hsc(ncand), hp((size_t)ncand * 12);
+    if (ncand) {
+        SM_CUDA(cudaMemcpyAsync(hs.data(), cstat, ncand * 4, cudaMemcpyDeviceToHost, c.stream));
+        SM_CUDA(cudaMemcpyAsync(hsc.data(), cscore, ncand * 4, cudaMemcpyDeviceToHost, c.stream));
+        SM_CUDA(cudaMemcpyAsync(hp.data(), cpose, (size_t)ncand * 48, cudaMemcpyDeviceToHost, c.stream));
+    }
+    record(c, 7);
+    c.sync();
+    // selection walk (ppf.cpp:439-495) and ordering by score (ppf.cpp:498-507)
+    std::vector<int> acc;
+    for (int i = 0; i < ncand; i++) {
+        if (hs[i] != 0)
+            continue;
+        acc.push_back(i);
+        if ((int)acc.size() >= mp.numMatches)
+            break;
+    }
+    std::stable_sort(acc.begin(), acc.end(), [&](int a, int b) { return hsc[a] > hsc[b]; });
+    res.pose.clear();
+    res.score.clear();
+    for (int i : acc) {
+        res.pose.insert(res.pose.end(), hp.begin() + (size_t)i * 12, hp.begin() + (size_t)i * 12 + 12);
+        res.score.push_back(hsc[i]);
+    }
+    c.last.n     = n;
+    c.last.ns    = ns;
+    c.last.nk    = K;
+    c.last.nr    = nres;
+    c.last.np    = np;
+    c.last.ncand = ncand;
+    c.last.valid = true;
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->n_points    = n;
+        stats->n_valid     = nvalid;
+        stats->n_sampled   = ns;
+        stats->n_keypoints = K;
+        stats->n_resampled = nres;
+        stats->n_poses     = np;
+        stats->n_clusters  = ncand;
+        std::vector<long long> st((size_t)K * 8);
+        if (K)
+            SM_CUDA(cudaMemcpy(st.data(), vo.stats, (size_t)K * 64, cudaMemcpyDeviceToHost));
+        for (int k = 0; k < K; k++) {
+            if (st[(size_t)k * 8 + 1] == 0)
+                stats->n_pairs += st[(size_t)k * 8] - 1;
+            stats->n_hits += st[(size_t)k * 8 + 2];
+            stats->n_votes += st[(size_t)k * 8 + 3];
+        }
+        const int stage[8][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 4}, {4, 5}, {5, 6}, {6, 7}, {0, 7}};
+        for (int i = 0; i < 8; i++)
+            SM_CUDA(cudaEventElapsedTime(&stats->ms[i], c.ev[stage[i][0]], c.ev[stage[i][1]]));
+    }
+}
+
+std::string read_all(const std::string &path) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f.is_open())
+        throw Error(SM_ERR_RUNTIME, "failed to open file:" + path);
+    return std::string((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+}
+
+struct Reader {
+    const std::string &s;
+    size_t             p = 0;
+    template <class T> T get() {
+        if (p + sizeof(T) > s.size())
+            throw Error(SM_ERR_RUNTIME, "truncated model file");
+        T v;
+        memcpy(&v, s.data() + p, sizeof(T));
+        p += sizeof(T);
+        return v;
+    }
+    std::vector<float> vec3() {
+        const uint32_t n = get<uint32_t>();
+        if ((size_t)n * 12 > s.size() - p)
+            throw Error(SM_ERR_RUNTIME, "truncated model file");
+        std::vector<float> v((size_t)n * 3);
+        memcpy(v.data(), s.data() + p, (size_t)n * 12);
+        p += (size_t)n * 12;
+        return v;
+    }
+};
+
+constexpr int kMagic   = 0x7F27F; // ppf.cpp:22
+constexpr int kVersion = 100;     // ppf.cpp:21
+
+template <class T> void put(std::string &o, const T &v) { o.append((const char *)&v, sizeof(T)); }
+
+void put_cloud(std::string &o, const std::vector<float> &p, const std::vector<float> &n,
+               const float box[6]) {
+    put<uint32_t>(o, (uint32_t)(p.size() / 3));
+    o.append((const char *)p.data(), p.size() * 4);
+    put<uint32_t>(o, (uint32_t)(n.size() / 3));
+    o.append((const char *)n.data(), n.size() * 4);
+    for (int i = 0; i < 6; i++)
+        put<float>(o, box[i]);
+    const float nanv = NAN;
+    for (int i = 0; i < 3; i++)
+        put<float>(o, nanv); // viewPoint (type.h:28): not set on a model
+}
+
+} // namespace
+} // namespace sm
+
+using namespace sm;
+
+// =======================================================================================
+extern "C" {
+
+SM_API const char *sm_last_error(void) { return g_lastError.c_str(); }
+SM_API const char *sm_version(void) { return "surface_match_gb300 0.1 (sm_103a)"; }
+
+SM_API void sm_train_param_default(sm_train_param *p) {
+    if (p)
+        *p = sm_train_param{0.04f, 30, 0.01f, 10, 1};
+}
+SM_API void sm_match_param_default(sm_match_param *p) {
+    if (p)
+        *p = sm_match_param{1, 10, 1, 0, 0.5f, 0.0f, 1, 1, 5, 0.1f, 0.0f, 0.01f, 0.0f};
+}
+SM_API int sm_train_param_check(const sm_train_param *p) {
+    return guarded([&] {
+        if (!p)
+            throw Error(SM_ERR_ARG, "NULL param");
+        check_train_param(*p);
+    });
+}
+SM_API int sm_match_param_check(const sm_match_param *p) {
+    return guarded([&] {
+        if (!p)
+            throw Error(SM_ERR_ARG, "NULL param");
+        check_match_param(*p);
+    });
+}
+
+SM_API int sm_context_create(int device, void *stream, sm_context *out) {
+    return guarded([&] {
+        if (!out)
+            throw Error(SM_ERR_ARG, "NULL output handle");
+        *out = nullptr;
+        int ndev = 0;
+        SM_CUDA(cudaGetDeviceCount(&ndev));
+        if (device < 0 || device >= ndev)
+            throw Error(SM_ERR_ARG, "no CUDA device " + std::to_string(device));
+        SM_CUDA(cudaSetDevice(device));
+        std::unique_ptr<sm_context_s> c(new sm_context_s());
+        c->ctx.device = device;
+        if (stream) {
+            c->ctx.stream = (cudaStream_t)stream;
+        } else {
+            SM_CUDA(cudaStreamCreateWithFlags(&c->ctx.stream, cudaStreamNonBlocking));
+            c->ctx.ownStream = true;
+        }
+        SM_CUDA(cudaMallocHost((void **)&c->ctx.hostCounts, 64 * sizeof(int)));
+        for (auto &e : c->ctx.ev)
+            SM_CUDA(cudaEventCreate(&e));
+        *out = c.release();
+    });
+}
+
+SM_API int sm_context_destroy(sm_context c) {
+    return guarded([&] {
+        if (!c)
+            return;
+        cudaSetDevice(c->ctx.device);
+        cudaStreamSynchronize(c->ctx.stream);
+        c->ctx.arena.release();
+        for (auto &e : c->ctx.ev)
+            if (e)
+                cudaEventDestroy(e);
+        if (c->ctx.hostCounts)
+            cudaFreeHost(c->ctx.hostCounts);
+        if (c->ctx.ownStream)
+            cudaStreamDestroy(c->ctx.stream);
+        delete c;
+    });
+}
+
+SM_API int sm_context_synchronize(sm_context c) {
+    return guarded([&] {
+        if (!c)
+            throw Error(SM_ERR_ARG, "NULL context");
+        c->ctx.sync();
+    });
+}
+
+SM_API void *sm_context_stream(sm_context c) { return c ? (void *)c->ctx.stream : nullptr; }
+
+SM_API int sm_model_create(sm_context ctx, sm_model *out) {
+    return guarded([&] {
+        if (!ctx || !out)
+            throw Error(SM_ERR_ARG, "NULL handle");
+        sm_model m = new sm_model_s();
+        m->ctx     = ctx;
+        m->m.device = ctx->ctx.device;
+        sm_train_param_default(&m->m.tp);
+        *out = m;
+    });
+}
+
+SM_API int sm_model_destroy(sm_model m) {
+    return guarded([&] {
+        if (!m)
+            return;
+        cudaSetDevice(m->m.device);
+        m->m.free_device();
+        delete m;
+    });
+}
+
+SM_API int sm_model_train(sm_model m, const float *xyz, const float *normal, int64_t n,
+                          float sdRel, const sm_train_param *param) {
+    return guarded([&] {
+        if (!m)
+            throw Error(SM_ERR_ARG, "NULL model");
+        sm_train_param tp;
+        sm_train_param_default(&tp);
+        if (param)
+            tp = *param;
+        SM_CUDA(cudaSetDevice(m->m.device));
+        train(m->ctx->ctx, m->m, xyz, normal, n, sdRel, tp);
+    });
+}
+
+SM_API int sm_model_upload(sm_model m, int64_t ns, const float *sxyz, const float *snrm,
+                           int64_t nr, const float *rxyz, const float *rnrm, const float *box6,
+                           int64_t nk, const uint32_t *keys, const uint32_t *offs,
+                           const uint32_t *refs, const float *alphas, float sdRel,
+                           const sm_train_param *param) {
+    return guarded([&] {
+        if (!m || !box6 || ns < 0 || nr < 0 || nk < 0 || (nk > 0 && (!keys || !offs)))
+            throw Error(SM_ERR_ARG, "invalid model arrays");
+        sm_train_param tp;
+        sm_train_param_default(&tp);
+        if (param)
+            tp = *param;
+        check_train_param(tp);
+        SM_CUDA(cudaSetDevice(m->m.device));
+        const int64_t      ne = nk > 0 ? offs[nk] : 0;
+        std::vector<float> sp(sxyz, sxyz + ns * 3), sn(snrm, snrm + ns * 3);
+        std::vector<float> rp(rxyz, rxyz + nr * 3), rn(rnrm, rnrm + nr * 3);
+        std::vector<uint32_t> K(keys, keys + nk), O(offs, offs + nk + 1), R(refs, refs + ne);
+        std::vector<float>    AL(alphas, alphas + ne);
+        for (int64_t b = 1; b < nk; b++)
+            if (K[b] <= K[b - 1])
+                throw Error(SM_ERR_ARG, "model keys must be strictly ascending");
+        upload_model(m->m, sp, sn, rp, rn, box6, K, O, R, AL);
+        m->m.sdRel = sdRel;
+        m->m.tp    = tp;
+    });
+}
+
+SM_API int sm_model_sizes(sm_model m, int64_t *sizes) {
+    return guarded([&] {
+        if (!m || !sizes)
+            throw Error(SM_ERR_ARG, "NULL argument");
+        sizes[0] = m->m.ns;
+        sizes[1] = m->m.nr;
+        sizes[2] = m->m.nkeys;
+        sizes[3] = m->m.nentries;
+    });
+}
+
+SM_API int sm_model_download(sm_model m, float *sxyz, float *snrm, float *rxyz, float *rnrm,
+                             float *box6, uint32_t *keys, uint32_t *offs, uint32_t *refs,
+                             float *alphas, float *sdRel, sm_train_param *param) {
+    return guarded([&] {
+        if (!m)
+            throw Error(SM_ERR_ARG, "NULL model");
+        if (!m->m.trained)
+            throw Error(SM_ERR_RUNTIME, "No trained model in save");
+        const Model &M = m->m;
+        auto cp = [](void *dst, const void *src, size_t b) {
+            if (dst && b)
+                memcpy(dst, src, b);
+        };
+        cp(sxyz, M.h_sp.data(), M.h_sp.size() * 4);
+        cp(snrm, M.h_sn.data(), M.h_sn.size() * 4);
+        cp(rxyz, M.h_rp.data(), M.h_rp.size() * 4);
+        cp(rnrm, M.h_rn.data(), M.h_rn.size() * 4);
+        if (box6)
+            for (int a = 0; a < 3; a++) {
+                box6[a]     = M.box.mn[a];
+                box6[3 + a] = M.box.mx[a];
+            }
+        cp(keys, M.h_keys.data(), M.h_keys.size() * 4);
+        cp(offs, M.h_offs.data(), M.h_offs.size() * 4);
+        cp(refs, M.h_refs.data(), M.h_refs.size() * 4);
+        cp(alphas, M.h_alphas.data(), M.h_alphas.size() * 4);
+        if (sdRel)
+            *sdRel = M.sdRel;
+        if (param)
+            *param = M.tp;
+    });
+}
+
+// The reference's model file (ppf.cpp:512-547, serialize.cpp): magic, version,
+// samplingDistanceRel, TrainParam field by field, the two clouds, then the hash table as
+// (key, refInd[], alphaAngle[]) buckets.
+SM_API int sm_model_save(sm_model m, const char *path) {
+    return guarded([&] {
+        if (!m || !path)
+            throw Error(SM_ERR_ARG, "NULL argument");
+        std::ofstream f(path, std::ios::out | std::ios::binary);
+        if (!f.is_open())
+            throw Error(SM_ERR_RUNTIME, std::string("failed to open file:") + path);
+        const Model &M = m->m;
+        if (!M.trained)
+            throw Error(SM_ERR_RUNTIME, "No trained model in save");
+        std::string o;
+        put<int>(o, kMagic);
+        put<int>(o, kVersion);
+        put<float>(o, M.sdRel);
+        put<float>(o, M.tp.featDistanceStepRel);
+        put<int>(o, M.tp.featAngleResolution);
+        put<float>(o, M.tp.poseRefRelSamplingDistance);
+        put<int>(o, M.tp.knnNormal);
+        put<uint8_t>(o, (uint8_t)(M.tp.smoothNormal ? 1 : 0));
+        const float b6[6] = {M.box.mn[0], M.box.mn[1], M.box.mn[2], M.box.mx[0], M.box.mx[1], M.box.mx[2]};
+        put_cloud(o, M.h_sp, M.h_sn, b6);
+        put_cloud(o, M.h_rp, M.h_rn, b6);
+        put<uint32_t>(o, (uint32_t)M.h_keys.size());
+        for (size_t b = 0; b < M.h_keys.size(); b++) {
+            const uint32_t o0 = M.h_offs[b], o1 = M.h_offs[b + 1];
+            put<uint32_t>(o, M.h_keys[b]);
+            put<uint32_t>(o, o1 - o0);
+            o.append((const char *)(M.h_refs.data() + o0), (size_t)(o1 - o0) * 4);
+            put<uint32_t>(o, o1 - o0);
+            o.append((const char *)(M.h_alphas.data() + o0), (size_t)(o1 - o0) * 4);
+        }
+        f.write(o.data(), (std::streamsize)o.size());
+        if (!f)
+            throw Error(SM_ERR_RUNTIME, std::string("failed to write file:") + path);
+    });
+}
+
+SM_API int sm_model_load(sm_model m, const char *path) {
+    return guarded([&] {
+        if (!m || !path)
+            throw Error(SM_ERR_ARG, "NULL argument");
+        const std::string s = read_all(path);
+        Reader            r{s};
+        if (r.get<int>() != kMagic)
+            throw Error(SM_ERR_RUNTIME, std::string("unsupported file format:") + path);
+        r.get<int>(); // version
+        const float    sdRel = r.get<float>();
+        sm_train_param tp;
+        tp.featDistanceStepRel        = r.get<float>();
+        tp.featAngleResolution        = r.get<int>();
+        tp.poseRefRelSamplingDistance = r.get<float>();
+        tp.knnNormal                  = r.get<int>();
+        tp.smoothNormal               = r.get<uint8_t>() ? 1 : 0;
+        check_train_param(tp);
+        float              box[6], rbox[6];
+        std::vector<float> sp = r.vec3(), sn = r.vec3();
+        for (float &b : box)
+            b = r.get<float>();
+        for (int i = 0; i < 3; i++)
+            r.get<float>();
+        std::vector<float> rp = r.vec3(), rn = r.vec3();
+        for (float &b : rbox)
+            b = r.get<float>();
+        for (int i = 0; i < 3; i++)
+            r.get<float>();
+        if (sn.size() != sp.size() || rn.size() != rp.size())
+            throw Error(SM_ERR_RUNTIME, std::string("corrupt model file:") + path);
+        const uint32_t nb = r.get<uint32_t>();
+        struct B {
+            uint32_t              key;
+            std::vector<uint32_t> refs;
+            std::vector<float>    al;
+        };
+        std::vector<B> bk(nb);
+        for (uint32_t b = 0; b < nb; b++) {
+            bk[b].key        = r.get<uint32_t>();
+            const uint32_t n1 = r.get<uint32_t>();
+            if ((size_t)n1 * 4 > s.size() - r.p)
+                throw Error(SM_ERR_RUNTIME, "truncated model file");
+            bk[b].refs.resize(n1);
+            memcpy(bk[b].refs.data(), s.data() + r.p, (size_t)n1 * 4);
+            r.p += (size_t)n1 * 4;
+            const uint32_t n2 = r.get<uint32_t>();
+            if (n2 != n1 || (size_t)n2 * 4 > s.size() - r.p)
+                throw Error(SM_ERR_RUNTIME, std::string("corrupt model file:") + path);
+            bk[b].al.resize(n2);
+            memcpy(bk[b].al.data(), s.data() + r.p, (size_t)n2 * 4);
+            r.p += (size_t)n2 * 4;
+        }
+        std::sort(bk.begin(), bk.end(), [](const B &a, const B &b) { return a.key < b.key; });
+        std::vector<uint32_t> K, O, R;
+        std::vector<float>    AL;
+        O.push_back(0);
+        for (size_t b = 0; b < bk.size(); b++) {
+            if (b && bk[b].key == bk[b - 1].key)
+                throw Error(SM_ERR_RUNTIME, std::string("corrupt model file:") + path);
+            K.push_back(bk[b].key);
+            R.insert(R.end(), bk[b].refs.begin(), bk[b].refs.end());
+            AL.insert(AL.end(), bk[b].al.begin(), bk[b].al.end());
+            O.push_back((uint32_t)R.size());
+        }
+        SM_CUDA(cudaSetDevice(m->m.device));
+        upload_model(m->m, sp, sn, rp, rn, box, K, O, R, AL);
+        m->m.sdRel = sdRel;
+        m->m.tp    = tp;
+    });
+}
+
+SM_API int sm_match(sm_model m, const float *xyz, const float *normal, int64_t n,
+                    const float *viewpoint, float sdRel, float kpFrac, float minScore,
+                    const sm_match_param *param, float *outPose, float *outScore, int *inoutCount,
+                    sm_match_stats *stats) {
+    return guarded([&] {
+        if (!m || !inoutCount)
+            throw Error(SM_ERR_ARG, "NULL argument");
+        sm_match_param mp;
+        sm_match_param_default(&mp);
+        if (param)
+            mp = *param;
+        SM_CUDA(cudaSetDevice(m->m.device));
+        MatchOutputs res;
+        match(m->ctx->ctx, m->m, xyz, normal, n, viewpoint, sdRel, kpFrac, minScore, mp, res, stats);
+        const int nres = (int)res.score.size();
+        const int cap  = *inoutCount;
+        *inoutCount    = nres;
+        for (int i = 0; i < nres && i < cap; i++) {
+            if (outPose) {
+                for (int e = 0; e < 12; e++)
+                    outPose[i * 16 + e] = res.pose[(size_t)i * 12 + e];
+                outPose[i * 16 + 12] = 0.f;
+                outPose[i * 16 + 13] = 0.f;
+                outPose[i * 16 + 14] = 0.f;
+                outPose[i * 16 + 15] = 1.f;
+            }
+            if (outScore)
+                outScore[i] = res.score[i];
+        }
+        if (nres > cap)
+            throw Error(SM_ERR_CAPACITY, "more results than the output capacity (" +
+                                             std::to_string(nres) + " > " + std::to_string(cap) + ")");
+    });
+}
+
+SM_API int sm_vote_stage(sm_model m, const float *points, const float *normals, int64_t n,
+                         const int32_t *kp, int64_t K, const int32_t *nbrOff,
+                         const int32_t *nbrIds, float minScore, int64_t *outStats,
+                         float *outCands, float *outPoses, int dumpK, int32_t *outAcc) {
+    return guarded([&] {
+        if (!m || !points || !normals || !kp || !nbrOff || !nbrIds || !outStats || !outCands)
+            throw Error(SM_ERR_ARG, "NULL argument");
+        if (!m->m.trained)
+            throw Error(SM_ERR_RUNTIME, "No trained model in matchScene");
+        Ctx &c = m->ctx->ctx;
+        SM_CUDA(cudaSetDevice(m->m.device));
+        const int    ni = (int)n, Ki = (int)K;
+        const float *p3 = to_device(c, points, n, "v.p3");
+        const float *n3 = to_device(c, normals, n, "v.n3");
+        float4      *pos = c.arena.get<float4>("v.pos", std::max(ni, 1));
+        float4      *nrm = c.arena.get<float4>("v.nrm", std::max(ni, 1));
+        k_f3_to_f4<<<nblocks(ni, 256), 256, 0, c.stream>>>(p3, ni, pos);
+        k_f3_to_f4<<<nblocks(ni, 256), 256, 0, c.stream>>>(n3, ni, nrm);
+        SM_LAUNCH_CHECK();
+        const int64_t tot  = nbrOff[K];
+        int          *dkp  = c.arena.get<int>("v.kp", std::max(Ki, 1));
+        int          *doff = c.arena.get<int>("v.off", Ki + 1);
+        int          *dids = c.arena.get<int>("v.ids", std::max<int64_t>(tot, 1));
+        for (int64_t i = 0; i < tot; i++)
+            if (nbrIds[i] < 0 || nbrIds[i] >= n)
+                throw Error(SM_ERR_ARG, "neighbour index out of range");
+        for (int64_t i = 0; i < K; i++)
+            if (kp[i] < 0 || kp[i] >= n)
+                throw Error(SM_ERR_ARG, "keypoint index out of range");
+        SM_CUDA(cudaMemcpyAsync(dkp, kp, K * 4, cudaMemcpyHostToDevice, c.stream));
+        SM_CUDA(cudaMemcpyAsync(doff, nbrOff, (K + 1) * 4, cudaMemcpyHostToDevice, c.stream));
+        SM_CUDA(cudaMemcpyAsync(dids, nbrIds, tot * 4, cudaMemcpyHostToDevice, c.stream));
+        VoteOut vo;
+        vo.stats  = c.arena.get<long long>("v.stats", (size_t)std::max(Ki, 1) * 8);
+        vo.cands  = c.arena.get<float>("v.cands", (size_t)std::max(Ki, 1) * 9);
+        vo.poses  = c.arena.get<float>("v.poses", (size_t)std::max(Ki, 1) * 3 * smi::kPoseFloats);
+        vo.poseOk = c.arena.get<int>("v.poseok", (size_t)std::max(Ki, 1) * 3);
+        const int dk = std::max(0, std::min(dumpK, Ki));
+        vo.acc = (outAcc && dk) ? c.arena.get<int>("v.acc", (size_t)dk * m->m.ns * m->m.tp.featAngleResolution)
+                                : nullptr;
+        if (vo.acc)
+            SM_CUDA(cudaMemsetAsync(vo.acc, 0, (size_t)dk * m->m.ns * m->m.tp.featAngleResolution * 4, c.stream));
+        vote(c, m->m, pos, nrm, dkp, Ki, doff, dids, nullptr, 0, minScore, vo, dk);
+        SM_CUDA(cudaMemcpyAsync(outStats, vo.stats, (size_t)K * 64, cudaMemcpyDeviceToHost, c.stream));
+        SM_CUDA(cudaMemcpyAsync(outCands, vo.cands, (size_t)K * 36, cudaMemcpyDeviceToHost, c.stream));
+        if (outPoses) {
+            std::vector<float> ps((size_t)K * 3 * smi::kPoseFloats);
+            std::vector<int>   ok((size_t)K * 3);
+            SM_CUDA(cudaMemcpyAsync(ps.data(), vo.poses, ps.size() * 4, cudaMemcpyDeviceToHost, c.stream));
+            SM_CUDA(cudaMemcpyAsync(ok.data(), vo.poseOk, ok.size() * 4, cudaMemcpyDeviceToHost, c.stream));
+            c.sync();
+            for (size_t i = 0; i < ok.size(); i++)
+                for (int e = 0; e < smi::kPoseFloats; e++)
+                    outPoses[i * smi::kPoseFloats + e] = ok[i] ? ps[i * smi::kPoseFloats + e] : 0.f;
+        }
+        if (vo.acc)
+            SM_CUDA(cudaMemcpyAsync(outAcc, vo.acc, (size_t)dk * m->m.ns * m->m.tp.featAngleResolution * 4,
+                                    cudaMemcpyDeviceToHost, c.stream));
+        c.sync();
+    });
+}
+
+// Debug fields of the last sm_match (see the header for the field list).
+static bool debug_field(sm_model m, int field, const void *&src, int64_t &count, size_t &elem) {
+    Ctx &c = m->ctx->ctx;
+    if (!c.last.valid)
+        return false;
+    auto get = [&](const char *name) { return c.arena.get(name, 1); };
+    switch (field) {
+        case 0: src = get("m.sampled"); count = c.last.ns; elem = 4; return true;
+        case 1: src = get("m.kp"); count = c.last.nk; elem = 4; return true;
+        case 2: src = get("m.resampled"); count = c.last.nr; elem = 4; return true;
+        case 3: src = get("m.pos"); count = c.last.n; elem = 16; return true;
+        case 4: src = get("m.n4"); count = c.last.n; elem = 16; return true;
+        case 7: src = get("m.kstats"); count = (int64_t)c.last.nk * 8; elem = 8; return true;
+        case 8: src = get("m.kcands"); count = (int64_t)c.last.nk * 9; elem = 4; return true;
+        case 9: src = get("m.plist"); count = (int64_t)c.last.np * smi::kPoseFloats; elem = 4; return true;
+        case 10: src = get("m.cands"); count = (int64_t)c.last.ncand * smi::kPoseFloats; elem = 4; return true;
+        case 12: src = get("m.cstat"); count = c.last.ncand; elem = 4; return true;
+        case 13: src = get("m.cscore"); count = c.last.ncand; elem = 4; return true;
+        case 14: src = get("m.cpose"); count = (int64_t)c.last.ncand * 12; elem = 4; return true;
+    }
+    return false;
+}
+
+SM_API int64_t sm_debug_size(sm_model m, int field) {
+    if (!m)
+        return -1;
+    const void *src;
+    int64_t     count;
+    size_t      elem;
+    if (!debug_field(m, field, src, count, elem))
+        return -1;
+    return (field == 3 || field == 4) ? count * 3 : count;
+}
+
+SM_API int sm_debug_get(sm_model m, int field, void *dst) {
+    return guarded([&] {
+        if (!m || !dst)
+            throw Error(SM_ERR_ARG, "NULL argument");
+        const void *src;
+        int64_t     count;
+        size_t      elem;
+        if (!debug_field(m, field, src, count, elem))
+            throw Error(SM_ERR_ARG, "no such debug field (or no match yet)");
+        SM_CUDA(cudaSetDevice(m->m.device));
+        m->ctx->ctx.sync();
+        if (field == 3 || field == 4) {
+            std::vector<float4> h(count);
+            SM_CUDA(cudaMemcpy(h.data(), src, count * 16, cudaMemcpyDeviceToHost));
+            float *d = (float *)dst;
+            for (int64_t i = 0; i < count; i++) {
+                d[3 * i]     = h[i].x;
+                d[3 * i + 1] = h[i].y;
+                d[3 * i + 2] = h[i].z;
+            }
+        } else if (count) {
+            SM_CUDA(cudaMemcpy(dst, src, count * elem, cudaMemcpyDeviceToHost));
+        }
+    });
+}
+
+} // extern "C"

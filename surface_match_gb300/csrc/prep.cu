@@ -1,0 +1,741 @@
+// prep.cu - point preparation, scans and compaction, uniform grids, greedy sampling and
+// normal estimation of the matching path.
+//
+// Reference counterparts: removeNan / computeBoundingBox (util.cpp:86-105, 178-207), the
+// k-d tree (kdtree/kdtree.h) replaced by uniform grids, samplePointCloud (util.cpp:107-139),
+// estimateNormal / computeNormal (util.cpp:234-334), normalizeNormal (util.cpp:163-176).
+#include <climits>
+#include <cmath>
+
+#include "sm_icp.h"
+#include "sm_linalg.h"
+#include "sm_stages.h"
+
+namespace sm {
+using namespace smd;
+
+namespace {
+
+constexpr int kScanBs   = 1024;
+constexpr int kScanIpt  = 4;
+constexpr int kScanTile = kScanBs * kScanIpt;
+constexpr int kNoEq     = INT_MIN; // scan raw values instead of (value == eq)
+
+struct GridParams {
+    float org[3], g;
+    int   dim[3];
+};
+
+GridParams grid_params(const Box &b, float g, int dim[3]) {
+    GridParams p;
+    for (int a = 0; a < 3; a++) {
+        p.org[a] = b.mn[a];
+        p.dim[a] = dim[a];
+    }
+    p.g = g;
+    return p;
+}
+
+__device__ __forceinline__ float4 nan4() {
+    const float q = __int_as_float(0x7fc00000);
+    return make_float4(q, q, q, 0.0f);
+}
+
+__device__ __forceinline__ bool finite3(float x, float y, float z) {
+    return isfinite(x) && isfinite(y) && isfinite(z);
+}
+
+// ---------------------------------------------------------------------------------------
+__global__ void k_prep(const float *__restrict__ xyz, const float *__restrict__ nin, int n,
+                       float4 *__restrict__ pos, float4 *__restrict__ nrm, int *__restrict__ valid,
+                       int *__restrict__ bbox, int *__restrict__ nvalid) {
+    __shared__ int smn[3], smx[3], scnt;
+    if (threadIdx.x < 3) {
+        smn[threadIdx.x] = INT_MAX;
+        smx[threadIdx.x] = INT_MIN;
+    }
+    if (threadIdx.x == 0)
+        scnt = 0;
+    __syncthreads();
+    int lmn[3] = {INT_MAX, INT_MAX, INT_MAX}, lmx[3] = {INT_MIN, INT_MIN, INT_MIN}, lc = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float x = xyz[3 * (size_t)i], y = xyz[3 * (size_t)i + 1], z = xyz[3 * (size_t)i + 2];
+        bool        ok = finite3(x, y, z);
+        float4      nn = nan4();
+        if (nin) {
+            float a = nin[3 * (size_t)i], b = nin[3 * (size_t)i + 1], c = nin[3 * (size_t)i + 2];
+            ok      = ok && finite3(a, b, c);
+            const float sq = a * a + (b * b + c * c);
+            if (sq > 0.0f) {
+                const float s = smm::fsqrt(sq);
+                a             = smm::fdiv(a, s);
+                b             = smm::fdiv(b, s);
+                c             = smm::fdiv(c, s);
+            }
+            nn = make_float4(a, b, c, 0.0f);
+        }
+        pos[i]   = make_float4(x, y, z, 0.0f);
+        nrm[i]   = nn;
+        valid[i] = ok ? 1 : 0;
+        if (ok) {
+            const int o[3] = {f2ord(x), f2ord(y), f2ord(z)};
+            for (int a = 0; a < 3; a++) {
+                lmn[a] = min(lmn[a], o[a]);
+                lmx[a] = max(lmx[a], o[a]);
+            }
+            lc++;
+        }
+    }
+    for (int a = 0; a < 3; a++) {
+        lmn[a] = __reduce_min_sync(0xffffffffu, lmn[a]);
+        lmx[a] = __reduce_max_sync(0xffffffffu, lmx[a]);
+    }
+    lc = __reduce_add_sync(0xffffffffu, lc);
+    if ((threadIdx.x & 31) == 0) {
+        for (int a = 0; a < 3; a++) {
+            atomicMin(&smn[a], lmn[a]);
+            atomicMax(&smx[a], lmx[a]);
+        }
+        atomicAdd(&scnt, lc);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int a = 0; a < 3; a++) {
+            atomicMin(&bbox[a], smn[a]);
+            atomicMax(&bbox[3 + a], smx[a]);
+        }
+        atomicAdd(nvalid, scnt);
+    }
+}
+
+__global__ void k_init_bbox(int *bbox, int *nvalid) {
+    if (threadIdx.x < 3) {
+        bbox[threadIdx.x]     = INT_MAX;
+        bbox[3 + threadIdx.x] = INT_MIN;
+    }
+    if (threadIdx.x == 0)
+        *nvalid = 0;
+}
+
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ int scan_val(const int *in, long long i, long long n, int eq) {
+    if (i >= n)
+        return 0;
+    const int v = in[i];
+    return eq == kNoEq ? v : (v == eq ? 1 : 0);
+}
+
+__global__ void k_scan_reduce(const int *__restrict__ in, long long n, int eq, int *part) {
+    __shared__ int sh[33];
+    const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanIpt;
+    int             s    = 0;
+#pragma unroll
+    for (int k = 0; k < kScanIpt; k++)
+        s += scan_val(in, base + k, n, eq);
+    int tot;
+    block_excl_scan(s, sh, &tot);
+    if (threadIdx.x == 0)
+        part[blockIdx.x] = tot;
+}
+
+__global__ void k_scan_parts(int *part, int nparts, int *total) {
+    __shared__ int sh[33];
+    int            carry = 0;
+    for (int b = 0; b < nparts; b += blockDim.x) {
+        const int i = b + threadIdx.x;
+        const int v = i < nparts ? part[i] : 0;
+        int       tot;
+        const int ex = block_excl_scan(v, sh, &tot);
+        if (i < nparts)
+            part[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0 && total)
+        *total = carry;
+}
+
+__global__ void k_scan_apply(const int *__restrict__ in, int *__restrict__ out, long long n, int eq,
+                             const int *__restrict__ part) {
+    __shared__ int  sh[33];
+    const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanIpt;
+    int             v[kScanIpt], s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanIpt; k++) {
+        v[k] = scan_val(in, base + k, n, eq);
+        s += v[k];
+    }
+    int ex = block_excl_scan(s, sh, nullptr) + part[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < kScanIpt; k++) {
+        if (base + k < n)
+            out[base + k] = ex;
+        ex += v[k];
+    }
+}
+
+__global__ void k_scatter_flags(const int *__restrict__ flags, const int *__restrict__ pre, int n,
+                                int eq, int *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const int v = flags[i];
+    if (eq == kNoEq ? v != 0 : v == eq)
+        out[pre[i]] = i;
+}
+
+// ---------------------------------------------------------------------------------------
+__global__ void k_grid_count(const float4 *__restrict__ pos, const int *__restrict__ ids, int m,
+                             GridParams gp, int *__restrict__ cellOf, int *__restrict__ cnt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m)
+        return;
+    const float4 p = pos[ids[i]];
+    const int    cx = smg::coord(p.x, gp.org[0], gp.g, gp.dim[0]);
+    const int    cy = smg::coord(p.y, gp.org[1], gp.g, gp.dim[1]);
+    const int    cz = smg::coord(p.z, gp.org[2], gp.g, gp.dim[2]);
+    const int    c  = (cz * gp.dim[1] + cy) * gp.dim[0] + cx;
+    cellOf[i]       = c;
+    atomicAdd(&cnt[c], 1);
+}
+
+__global__ void k_grid_scatter(const int *__restrict__ ids, const int *__restrict__ cellOf, int m,
+                               int *__restrict__ fill, int *__restrict__ gids) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m)
+        return;
+    const int slot = atomicAdd(&fill[cellOf[i]], 1);
+    gids[slot]     = ids[i];
+}
+
+// Sort the ids of each cell ascending (cells are small; insertion sort per thread).
+__global__ void k_cell_sort(const int *__restrict__ start, long long nc, int *__restrict__ gids) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc)
+        return;
+    const int s = start[c], e = start[c + 1];
+    for (int i = s + 1; i < e; i++) {
+        const int v = gids[i];
+        int       j = i - 1;
+        while (j >= s && gids[j] > v) {
+            gids[j + 1] = gids[j];
+            j--;
+        }
+        gids[j + 1] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+__global__ void k_occ_flags(const int *__restrict__ start, long long nc, int *__restrict__ flag) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < nc)
+        flag[c] = start[c + 1] > start[c] ? 1 : 0;
+}
+
+__global__ void k_occ_rank(const int *__restrict__ occ, int nocc, int *__restrict__ rank, int dim0,
+                           int dim1, int *__restrict__ phaseCnt, int *__restrict__ phaseOf) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nocc)
+        return;
+    const int c  = occ[i];
+    rank[c]      = i;
+    const int cx = c % dim0, cy = (c / dim0) % dim1, cz = c / (dim0 * dim1);
+    const int ph = smg::phase_of(cx, cy, cz);
+    phaseOf[i]   = ph;
+    atomicAdd(&phaseCnt[ph], 1);
+}
+
+__global__ void k_phase_scatter(const int *__restrict__ occ, const int *__restrict__ phaseOf,
+                                int nocc, int *__restrict__ phaseFill, int *__restrict__ lists) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nocc)
+        return;
+    const int slot = atomicAdd(&phaseFill[phaseOf[i]], 1);
+    lists[slot]    = occ[i];
+}
+
+// One warp per occupied cell of the current phase: greedy keep/reject in ascending index
+// order against the kept points of the 26 neighbour cells (all from earlier phases) and
+// the cell's own kept points.
+__global__ void k_sample_phase(const float4 *__restrict__ pos, GridView G,
+                               const int *__restrict__ cells, int ncells,
+                               const int *__restrict__ rank, int *__restrict__ keptCnt,
+                               int *__restrict__ keptIds, int cap, float r2,
+                               int *__restrict__ keptFlag, int *__restrict__ overflow) {
+    const int w    = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= ncells)
+        return;
+    const int cell = cells[w];
+    const int rk   = rank[cell];
+    const int cx = cell % G.dim[0], cy = (cell / G.dim[0]) % G.dim[1],
+              cz = cell / (G.dim[0] * G.dim[1]);
+    const int s = G.start[cell], e = G.start[cell + 1];
+    int      *mine = keptIds + (size_t)rk * cap;
+    int       nk   = 0;
+    for (int base = s; base < e; base += 32) {
+        const int  i   = base + lane;
+        const bool act = i < e;
+        const int  id  = act ? G.ids[i] : 0;
+        float4     q   = act ? pos[id] : make_float4(0.f, 0.f, 0.f, 0.f);
+        bool       ok  = act;
+        for (int dz = -1; dz <= 1; dz++) {
+            const int z = cz + dz;
+            if (z < 0 || z >= G.dim[2])
+                continue;
+            for (int dy = -1; dy <= 1; dy++) {
+                const int y = cy + dy;
+                if (y < 0 || y >= G.dim[1])
+                    continue;
+                for (int dx = -1; dx <= 1; dx++) {
+                    const int x = cx + dx;
+                    if (x < 0 || x >= G.dim[0] || (dx == 0 && dy == 0 && dz == 0))
+                        continue;
+                    const int nr = rank[grid_cell(G, x, y, z)];
+                    if (nr < 0)
+                        continue;
+                    const int  cnt  = keptCnt[nr];
+                    const int *list = keptIds + (size_t)nr * cap;
+                    for (int k = 0; k < cnt && ok; k++) {
+                        const float4 o = pos[list[k]];
+                        if (smm::dist2(o.x, o.y, o.z, q.x, q.y, q.z) < r2)
+                            ok = false;
+                    }
+                }
+            }
+        }
+        for (int k = 0; k < nk && ok; k++) {
+            const float4 o = pos[mine[k]];
+            if (smm::dist2(o.x, o.y, o.z, q.x, q.y, q.z) < r2)
+                ok = false;
+        }
+        unsigned mask = __ballot_sync(0xffffffffu, ok);
+        while (mask) {
+            const int   leader = __ffs(mask) - 1;
+            const int   lid    = __shfl_sync(0xffffffffu, id, leader);
+            const float lx     = __shfl_sync(0xffffffffu, q.x, leader);
+            const float ly     = __shfl_sync(0xffffffffu, q.y, leader);
+            const float lz     = __shfl_sync(0xffffffffu, q.z, leader);
+            if (lane == 0) {
+                if (nk < cap)
+                    mine[nk] = lid;
+                else
+                    atomicExch(overflow, 1);
+            }
+            if (lane == leader) {
+                keptFlag[id] = 1;
+                ok           = false;
+            } else if (ok && lane > leader && smm::dist2(lx, ly, lz, q.x, q.y, q.z) < r2) {
+                ok = false;
+            }
+            nk = min(nk + 1, cap);
+            __syncwarp();
+            mask = __ballot_sync(0xffffffffu, ok);
+        }
+    }
+    if (lane == 0)
+        keptCnt[rk] = nk;
+}
+
+// ---------------------------------------------------------------------------------------
+__global__ void k_mark_todo(const int *__restrict__ ids, int m, const float4 *__restrict__ nrm,
+                            int *__restrict__ need) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m)
+        return;
+    const int id = ids[i];
+    if (!finite3(nrm[id].x, nrm[id].y, nrm[id].z))
+        need[id] = 2;
+}
+
+__global__ void k_knn(const int *__restrict__ list, int nl, GridView G, const float4 *__restrict__ pos,
+                      int k, int *__restrict__ nbr, int *__restrict__ nbrCnt, int markNeighbours,
+                      const float4 *__restrict__ nrm, int *__restrict__ need) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nl)
+        return;
+    const float4 q = pos[list[t]];
+    int          oi[kMaxKnn];
+    float        od[kMaxKnn];
+    const int    n = grid_knn(G, pos, q.x, q.y, q.z, k, oi, od);
+    for (int j = 0; j < k; j++)
+        nbr[(size_t)t * k + j] = j < n ? oi[j] : -1;
+    nbrCnt[t] = n;
+    if (markNeighbours) {
+        for (int j = 0; j < n; j++) {
+            const int id = oi[j];
+            if (need[id] == 0 && !finite3(nrm[id].x, nrm[id].y, nrm[id].z))
+                need[id] = 1;
+        }
+    }
+}
+
+// Phase A: centroid and FP32-Kahan covariance of the neighbourhood, FP64 eigensolve.
+__global__ void k_pca(const int *__restrict__ list, int nl, const int *__restrict__ nbr,
+                      const int *__restrict__ nbrCnt, int k, const float4 *__restrict__ pos,
+                      float4 *__restrict__ cen, float4 *__restrict__ nout) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nl)
+        return;
+    const int  m = nbrCnt[t];
+    const int *L = nbr + (size_t)t * k;
+    if (m < 3) {
+        cen[t]  = make_float4(0.f, 0.f, 0.f, -1.0f); // w < 0: no estimate
+        nout[t] = make_float4(0.f, 0.f, 0.f, -1.0f);
+        return;
+    }
+    smi::KahanF sx, sy, sz;
+    sx.init();
+    sy.init();
+    sz.init();
+    for (int j = 0; j < m; j++) {
+        const float4 p = pos[L[j]];
+        sx.add(p.x);
+        sy.add(p.y);
+        sz.add(p.z);
+    }
+    const float cx = smm::fdiv(sx.value(), (float)m), cy = smm::fdiv(sy.value(), (float)m),
+                cz = smm::fdiv(sz.value(), (float)m);
+    smi::KahanF a[6];
+    for (int e = 0; e < 6; e++)
+        a[e].init();
+    for (int j = 0; j < m; j++) {
+        const float4 p  = pos[L[j]];
+        const float  dx = p.x - cx, dy = p.y - cy, dz = p.z - cz;
+        a[0].add(dx * dx);
+        a[1].add(dx * dy);
+        a[2].add(dx * dz);
+        a[3].add(dy * dy);
+        a[4].add(dy * dz);
+        a[5].add(dz * dz);
+    }
+    double C[6];
+    for (int e = 0; e < 6; e++)
+        C[e] = (double)a[e].value();
+    float n3[3];
+    sml::normal_from_cov(C, n3);
+    cen[t]  = make_float4(cx, cy, cz, 1.0f);
+    nout[t] = make_float4(n3[0], n3[1], n3[2], 1.0f);
+}
+
+__global__ void k_pca_write(const int *__restrict__ list, int nl, const float4 *__restrict__ cen,
+                            const float4 *__restrict__ nin, float4 *__restrict__ pos,
+                            float4 *__restrict__ nrm) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nl || cen[t].w < 0.0f)
+        return;
+    const int id = list[t];
+    pos[id]      = make_float4(cen[t].x, cen[t].y, cen[t].z, 0.0f);
+    nrm[id]      = make_float4(nin[t].x, nin[t].y, nin[t].z, 0.0f);
+}
+
+// Phase B: sign-aligned sum of the raw neighbourhood normals (util.cpp:292-306).
+__global__ void k_smooth(const int *__restrict__ list, int nl, const int *__restrict__ nbr,
+                         const int *__restrict__ nbrCnt, int k, const float4 *__restrict__ nrm,
+                         float4 *__restrict__ out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nl)
+        return;
+    const int m = nbrCnt[t];
+    if (m < 3) {
+        out[t] = make_float4(0.f, 0.f, 0.f, -1.0f);
+        return;
+    }
+    const float4 n0 = nrm[list[t]];
+    float        sx = 0.f, sy = 0.f, sz = 0.f;
+    for (int j = 0; j < m; j++) {
+        const float4 n = nrm[nbr[(size_t)t * k + j]];
+        const float  d = n.x * n0.x + (n.y * n0.y + n.z * n0.z);
+        if (d > 0.0f) {
+            sx = sx + n.x;
+            sy = sy + n.y;
+            sz = sz + n.z;
+        } else {
+            sx = sx - n.x;
+            sy = sy - n.y;
+            sz = sz - n.z;
+        }
+    }
+    const float sq = sx * sx + (sy * sy + sz * sz);
+    if (sq > 0.0f) {
+        const float s = smm::fsqrt(sq);
+        sx            = smm::fdiv(sx, s);
+        sy            = smm::fdiv(sy, s);
+        sz            = smm::fdiv(sz, s);
+    }
+    out[t] = make_float4(sx, sy, sz, 1.0f);
+}
+
+__global__ void k_smooth_write(const int *__restrict__ list, int nl, const float4 *__restrict__ sm,
+                               float4 *__restrict__ nrm) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nl || sm[t].w < 0.0f)
+        return;
+    nrm[list[t]] = make_float4(sm[t].x, sm[t].y, sm[t].z, 0.0f);
+}
+
+// Phase C: orientation toward the viewpoint, or +z (util.cpp:309-333).
+__global__ void k_orient(const int *__restrict__ ids, int m, const float4 *__restrict__ pos,
+                         float4 *__restrict__ nrm, int hasVp, float vx, float vy, float vz,
+                         int invert) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m)
+        return;
+    const int id = ids[i];
+    float4    n  = nrm[id];
+    float     d;
+    if (hasVp) {
+        const float4 p = pos[id];
+        const float  ax = vx - p.x, ay = vy - p.y, az = vz - p.z;
+        d               = n.x * ax + (n.y * ay + n.z * az);
+    } else {
+        d = n.x * 0.0f + (n.y * 0.0f + n.z * 1.0f);
+    }
+    const bool flip = invert ? (d > 0.0f) : (d < 0.0f);
+    if (flip)
+        nrm[id] = make_float4(-n.x, -n.y, -n.z, 0.0f);
+}
+
+__global__ void k_normalize(float4 *__restrict__ nrm, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    float4      v  = nrm[i];
+    const float sq = v.x * v.x + (v.y * v.y + v.z * v.z);
+    if (sq > 0.0f) {
+        const float s = smm::fsqrt(sq);
+        nrm[i]        = make_float4(smm::fdiv(v.x, s), smm::fdiv(v.y, s), smm::fdiv(v.z, s), 0.0f);
+    }
+}
+
+} // namespace
+
+// =======================================================================================
+int prep_points(Ctx &c, const float *xyz, const float *nin, int n, float4 *pos, float4 *nrm,
+                int *validFlag, Box &box) {
+    int *dev = c.arena.get<int>("prep.bbox", 8);
+    k_init_bbox<<<1, 32, 0, c.stream>>>(dev, dev + 6);
+    SM_LAUNCH_CHECK();
+    const int bs = 256;
+    int       nb = std::min(nblocks(n, bs), 152 * 16);
+    if (nb < 1)
+        nb = 1;
+    k_prep<<<nb, bs, 0, c.stream>>>(xyz, nin, n, pos, nrm, validFlag, dev, dev + 6);
+    SM_LAUNCH_CHECK();
+    SM_CUDA(cudaMemcpyAsync(c.hostCounts, dev, 7 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    c.sync();
+    for (int a = 0; a < 3; a++) {
+        box.mn[a] = ord2f(c.hostCounts[a]);
+        box.mx[a] = ord2f(c.hostCounts[3 + a]);
+    }
+    return c.hostCounts[6];
+}
+
+static int scan_impl(Ctx &c, const int *in, int *out, long long n, int eq, const std::string &tag,
+                     bool wantTotal) {
+    const int nparts = (int)((n + kScanTile - 1) / kScanTile);
+    int      *part   = c.arena.get<int>(tag + ".scanpart", nparts + 1);
+    int      *total  = part + nparts;
+    if (nparts > 0) {
+        k_scan_reduce<<<nparts, kScanBs, 0, c.stream>>>(in, n, eq, part);
+        SM_LAUNCH_CHECK();
+    }
+    k_scan_parts<<<1, 1024, 0, c.stream>>>(part, nparts, total);
+    SM_LAUNCH_CHECK();
+    if (nparts > 0) {
+        k_scan_apply<<<nparts, kScanBs, 0, c.stream>>>(in, out, n, eq, part);
+        SM_LAUNCH_CHECK();
+    }
+    if (!wantTotal)
+        return -1;
+    SM_CUDA(cudaMemcpyAsync(c.hostCounts, total, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    c.sync();
+    return c.hostCounts[0];
+}
+
+int scan_excl(Ctx &c, const int *in, int *out, long long n, const std::string &tag, bool wantTotal) {
+    return scan_impl(c, in, out, n, kNoEq, tag, wantTotal);
+}
+
+static int compact_eq(Ctx &c, const int *flags, int n, int eq, int *outIds, const std::string &tag) {
+    if (n <= 0)
+        return 0;
+    int      *pre   = c.arena.get<int>(tag + ".pre", n);
+    const int total = scan_impl(c, flags, pre, n, eq, tag, true);
+    k_scatter_flags<<<nblocks(n, 256), 256, 0, c.stream>>>(flags, pre, n, eq, outIds);
+    SM_LAUNCH_CHECK();
+    return total;
+}
+
+int compact(Ctx &c, const int *flags, int n, int *outIds, const std::string &tag) {
+    return compact_eq(c, flags, n, kNoEq, outIds, tag);
+}
+
+void build_grid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &box, float g,
+                bool sortCells, Grid &G, const std::string &tag) {
+    float ext[3] = {box.ext(0), box.ext(1), box.ext(2)};
+    G.g          = g;
+    for (int a = 0; a < 3; a++) {
+        G.org[a] = box.mn[a];
+        G.dim[a] = smg::dim_of(ext[a], g);
+    }
+    G.nc  = (long long)G.dim[0] * G.dim[1] * G.dim[2];
+    G.m   = m;
+    int *cnt    = c.arena.get<int>(tag + ".cnt", G.nc + 1);
+    G.start     = c.arena.get<int>(tag + ".start", G.nc + 1);
+    G.ids       = c.arena.get<int>(tag + ".ids", std::max(m, 1));
+    int *cellOf = c.arena.get<int>(tag + ".cellOf", std::max(m, 1));
+    SM_CUDA(cudaMemsetAsync(cnt, 0, (G.nc + 1) * sizeof(int), c.stream));
+    GridParams gp = grid_params(box, g, G.dim);
+    if (m > 0) {
+        k_grid_count<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, m, gp, cellOf, cnt);
+        SM_LAUNCH_CHECK();
+    }
+    scan_excl(c, cnt, G.start, G.nc + 1, tag, false);
+    int *fill = cnt; // reuse: fill pointers start at the cell starts
+    SM_CUDA(cudaMemcpyAsync(fill, G.start, G.nc * sizeof(int), cudaMemcpyDeviceToDevice, c.stream));
+    if (m > 0) {
+        k_grid_scatter<<<nblocks(m, 256), 256, 0, c.stream>>>(ids, cellOf, m, fill, G.ids);
+        SM_LAUNCH_CHECK();
+        if (sortCells) {
+            k_cell_sort<<<nblocks(G.nc, 256), 256, 0, c.stream>>>(G.start, G.nc, G.ids);
+            SM_LAUNCH_CHECK();
+        }
+    }
+}
+
+int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m, const Box &box,
+                  float step, int *outIds, const std::string &tag) {
+    if (m <= 0)
+        return 0;
+    float ext[3] = {box.ext(0), box.ext(1), box.ext(2)};
+    const float g = smg::sample_cell(step, ext);
+    Grid        G;
+    build_grid(c, pos, ids, m, box, g, true, G, tag + ".g");
+    int *occFlag = c.arena.get<int>(tag + ".occf", G.nc);
+    k_occ_flags<<<nblocks(G.nc, 256), 256, 0, c.stream>>>(G.start, G.nc, occFlag);
+    SM_LAUNCH_CHECK();
+    int *occ  = c.arena.get<int>(tag + ".occ", std::max<long long>(G.nc, 1));
+    int  nocc = compact(c, occFlag, (int)G.nc, occ, tag + ".occc");
+    int *rank = c.arena.get<int>(tag + ".rank", G.nc);
+    SM_CUDA(cudaMemsetAsync(rank, 0xff, G.nc * sizeof(int), c.stream));
+    int *phaseCnt = c.arena.get<int>(tag + ".phc", 16);
+    SM_CUDA(cudaMemsetAsync(phaseCnt, 0, 16 * sizeof(int), c.stream));
+    int *phaseOf = c.arena.get<int>(tag + ".pho", std::max(nocc, 1));
+    k_occ_rank<<<nblocks(nocc, 256), 256, 0, c.stream>>>(occ, nocc, rank, G.dim[0], G.dim[1],
+                                                         phaseCnt, phaseOf);
+    SM_LAUNCH_CHECK();
+    SM_CUDA(cudaMemcpyAsync(c.hostCounts, phaseCnt, 8 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    c.sync();
+    int off[9];
+    off[0] = 0;
+    for (int p = 0; p < 8; p++)
+        off[p + 1] = off[p] + c.hostCounts[p];
+    int *phaseFill = phaseCnt + 8;
+    SM_CUDA(cudaMemcpyAsync(phaseFill, off, 8 * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    int *lists = c.arena.get<int>(tag + ".phl", std::max(nocc, 1));
+    k_phase_scatter<<<nblocks(nocc, 256), 256, 0, c.stream>>>(occ, phaseOf, nocc, phaseFill, lists);
+    SM_LAUNCH_CHECK();
+    // kept-list capacity: points at pairwise distance >= step inside a cube of side g fit
+    // disjoint balls of radius step/2 inside the cube grown by step/2.
+    const double s   = (double)g / (double)step;
+    const int    cap = (int)std::floor((s + 1.0) * (s + 1.0) * (s + 1.0) / (3.14159265358979 / 6.0)) + 1;
+    int *keptCnt  = c.arena.get<int>(tag + ".kc", std::max(nocc, 1));
+    int *keptIds  = c.arena.get<int>(tag + ".ki", (size_t)std::max(nocc, 1) * cap);
+    int *keptFlag = c.arena.get<int>(tag + ".kf", std::max(npoints, 1) + 1);
+    int *overflow = keptFlag + npoints;
+    SM_CUDA(cudaMemsetAsync(keptCnt, 0, std::max(nocc, 1) * sizeof(int), c.stream));
+    SM_CUDA(cudaMemsetAsync(keptFlag, 0, (npoints + 1) * sizeof(int), c.stream));
+    const float r2 = step * step;
+    for (int p = 0; p < 8; p++) {
+        const int nc = off[p + 1] - off[p];
+        if (nc == 0)
+            continue;
+        k_sample_phase<<<nblocks((long long)nc * 32, 256), 256, 0, c.stream>>>(
+            pos, G.view(), lists + off[p], nc, rank, keptCnt, keptIds, cap, r2, keptFlag, overflow);
+        SM_LAUNCH_CHECK();
+    }
+    const int kept = compact(c, keptFlag, npoints, outIds, tag + ".out");
+    SM_CUDA(cudaMemcpyAsync(c.hostCounts, overflow, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    c.sync();
+    if (c.hostCounts[0])
+        throw Error(SM_ERR_CAPACITY, "sampler: kept-point capacity per cell exceeded");
+    return kept;
+}
+
+void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *ids, int m,
+                      const Grid &query, int k, bool smooth, bool invert, const float *vp,
+                      const std::string &tag) {
+    if (m <= 0)
+        return;
+    if (k < 3)
+        k = 3;
+    if (k > kMaxKnn)
+        throw Error(SM_ERR_RANGE, "knnNormal larger than " + std::to_string(kMaxKnn) + " is not supported");
+    int *need = c.arena.get<int>(tag + ".need", npoints);
+    SM_CUDA(cudaMemsetAsync(need, 0, npoints * sizeof(int), c.stream));
+    k_mark_todo<<<nblocks(m, 256), 256, 0, c.stream>>>(ids, m, nrm, need);
+    SM_LAUNCH_CHECK();
+    int *todo  = c.arena.get<int>(tag + ".todo", m);
+    int  ntodo = compact_eq(c, need, npoints, 2, todo, tag + ".ct");
+    int *nbrT  = c.arena.get<int>(tag + ".nbrT", (size_t)std::max(ntodo, 1) * k);
+    int *cntT  = c.arena.get<int>(tag + ".cntT", std::max(ntodo, 1));
+    if (ntodo > 0) {
+        k_knn<<<nblocks(ntodo, 128), 128, 0, c.stream>>>(todo, ntodo, query.view(), pos, k, nbrT,
+                                                          cntT, smooth ? 1 : 0, nrm, need);
+        SM_LAUNCH_CHECK();
+    }
+    int  nextra = 0;
+    int *extra = nullptr, *nbrE = nullptr, *cntE = nullptr;
+    if (smooth && ntodo > 0) {
+        extra  = c.arena.get<int>(tag + ".extra", npoints);
+        nextra = compact_eq(c, need, npoints, 1, extra, tag + ".ce");
+        nbrE   = c.arena.get<int>(tag + ".nbrE", (size_t)std::max(nextra, 1) * k);
+        cntE   = c.arena.get<int>(tag + ".cntE", std::max(nextra, 1));
+        if (nextra > 0) {
+            k_knn<<<nblocks(nextra, 128), 128, 0, c.stream>>>(extra, nextra, query.view(), pos, k,
+                                                               nbrE, cntE, 0, nrm, need);
+            SM_LAUNCH_CHECK();
+        }
+    }
+    const int nmax = std::max(ntodo, nextra);
+    float4   *cen  = c.arena.get<float4>(tag + ".cen", 2 * (size_t)std::max(nmax, 1));
+    float4   *nn   = c.arena.get<float4>(tag + ".nn", 2 * (size_t)std::max(nmax, 1));
+    if (ntodo > 0) {
+        k_pca<<<nblocks(ntodo, 128), 128, 0, c.stream>>>(todo, ntodo, nbrT, cntT, k, pos, cen, nn);
+        SM_LAUNCH_CHECK();
+    }
+    if (nextra > 0) {
+        k_pca<<<nblocks(nextra, 128), 128, 0, c.stream>>>(extra, nextra, nbrE, cntE, k, pos,
+                                                           cen + nmax, nn + nmax);
+        SM_LAUNCH_CHECK();
+    }
+    if (ntodo > 0) {
+        k_pca_write<<<nblocks(ntodo, 256), 256, 0, c.stream>>>(todo, ntodo, cen, nn, pos, nrm);
+        SM_LAUNCH_CHECK();
+    }
+    if (nextra > 0) {
+        k_pca_write<<<nblocks(nextra, 256), 256, 0, c.stream>>>(extra, nextra, cen + nmax, nn + nmax,
+                                                                 pos, nrm);
+        SM_LAUNCH_CHECK();
+    }
+    if (smooth && ntodo > 0) {
+        k_smooth<<<nblocks(ntodo, 256), 256, 0, c.stream>>>(todo, ntodo, nbrT, cntT, k, nrm, cen);
+        SM_LAUNCH_CHECK();
+        k_smooth_write<<<nblocks(ntodo, 256), 256, 0, c.stream>>>(todo, ntodo, cen, nrm);
+        SM_LAUNCH_CHECK();
+    }
+    const bool hasVp = vp && std::isfinite(vp[0]) && std::isfinite(vp[1]) && std::isfinite(vp[2]);
+    k_orient<<<nblocks(m, 256), 256, 0, c.stream>>>(ids, m, pos, nrm, hasVp ? 1 : 0,
+                                                    hasVp ? vp[0] : 0.f, hasVp ? vp[1] : 0.f,
+                                                    hasVp ? vp[2] : 0.f, invert ? 1 : 0);
+    SM_LAUNCH_CHECK();
+}
+
+void normalize_normals(Ctx &c, float4 *nrm, int n) {
+    if (n <= 0)
+        return;
+    k_normalize<<<nblocks(n, 256), 256, 0, c.stream>>>(nrm, n);
+    SM_LAUNCH_CHECK();
+}
+
+} // namespace sm

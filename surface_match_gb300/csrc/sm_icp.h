@@ -157,4 +157,53 @@ SM_HD Pose34 solve_step(const float sys[kNumSystem], const float Pm[3], const fl
     return o;
 }
 
+// Pose record of one voting candidate: T (3x4), quaternion (w,x,y,z), rotation angle,
+// votes -- 18 floats, the layout of the pose list.
+constexpr int kPoseFloats = 18;
+
+// Pose::updatePose (type.cpp:53-59): quaternion and rotation angle of T's rotation.
+SM_HD void pose_record(const float T[12], float votes, float out[kPoseFloats]) {
+    double R[9], q[4];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+            R[i * 3 + j] = (double)T[i * 4 + j];
+    sml::mat_to_quat(R, q);
+    for (int i = 0; i < 12; i++)
+        out[i] = T[i];
+    for (int i = 0; i < 4; i++)
+        out[12 + i] = (float)q[i];
+    out[16] = sml::quat_angle(q);
+    out[17] = votes;
+}
+
+// Candidate pose of ppf.cpp:393-405: T = RT_s^-1 * Rx(alpha) * RT_m, with the rigid
+// inverse [R^T | -R^T t], cos/sin of the float angle from the shared float functions and
+// the products in FP64.
+SM_HD void candidate_pose(const smm::RT &rs, const smm::RT &rm, float alpha, float votes,
+                          float out[kPoseFloats]) {
+    const double ca = (double)smm::cosf_(alpha), sa = (double)smm::sinf_(alpha);
+    double       XM[3][4];
+    for (int j = 0; j < 4; j++) {
+        const double r0 = j < 3 ? (double)rm.r[j] : (double)rm.t[0];
+        const double r1 = j < 3 ? (double)rm.r[3 + j] : (double)rm.t[1];
+        const double r2 = j < 3 ? (double)rm.r[6 + j] : (double)rm.t[2];
+        XM[0][j]        = r0;
+        XM[1][j]        = ca * r1 - sa * r2;
+        XM[2][j]        = sa * r1 + ca * r2;
+    }
+    float T[12];
+    for (int i = 0; i < 3; i++) {
+        for (int j = 0; j < 4; j++) {
+            double s = 0.0;
+            for (int k = 0; k < 3; k++)
+                s += (double)rs.r[k * 3 + i] * XM[k][j];
+            if (j == 3)
+                for (int k = 0; k < 3; k++)
+                    s -= (double)rs.r[k * 3 + i] * (double)rs.t[k];
+            T[i * 4 + j] = (float)s;
+        }
+    }
+    pose_record(T, votes, out);
+}
+
 } // namespace smi

@@ -251,6 +251,13 @@ SM_HD uint32_t murmur4(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3) {
     return h;
 }
 
+// splitmix64 finaliser (S. Vigna): fingerprint mixing of accumulator cells.
+SM_HD uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
 // float -> uint32 conversion of a non-negative quantised value. NaN (only reachable for a
 // zero-length pair, which two distinct sampled points never form) maps to 0x80000000, the
 // x86 "integer indefinite" value, on both host and device.

@@ -1,0 +1,97 @@
+// sm_stages.h - host entry points of the device stages (implemented in prep.cu, vote.cu,
+// cluster.cu, icp.cu) and the per-context state they share.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "sm_engine.h"
+
+namespace sm {
+
+struct Ctx {
+    int          device    = 0;
+    cudaStream_t stream    = nullptr;
+    bool         ownStream = false;
+    Arena        arena;
+    int         *hostCounts = nullptr; // pinned scratch for small device->host reads
+    cudaEvent_t  ev[10]{};
+    // intermediate state of the last match (device pointers into the arena + sizes)
+    struct Last {
+        int  n = 0, ns = 0, nk = 0, nr = 0, np = 0, nc = 0, ncand = 0;
+        bool valid = false;
+    } last;
+    void sync() { SM_CUDA(cudaStreamSynchronize(stream)); }
+};
+
+// ---- prep.cu ------------------------------------------------------------------------
+// Convert input xyz (+normals) to float4, mark finite points, reduce the bounding box of
+// the valid points. Synchronises; returns the number of valid points.
+int prep_points(Ctx &c, const float *xyz, const float *nrm, int n, float4 *pos, float4 *nrmOut,
+                int *validFlag, Box &box);
+// Exclusive scan of n ints (out may alias nothing); returns the total (synchronises if
+// wantTotal).
+int scan_excl(Ctx &c, const int *in, int *out, long long n, const std::string &tag,
+              bool wantTotal = true);
+// Ascending indices i with flags[i] != 0; returns the count (synchronises).
+int compact(Ctx &c, const int *flags, int n, int *outIds, const std::string &tag);
+// Grid over points ids[0..m) with cell side g over `box`; sortCells orders each cell's
+// ids ascending (needed by the sampler).
+void build_grid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &box, float g,
+                bool sortCells, Grid &G, const std::string &tag);
+// Greedy thinning at `step` in (phase, cell, index) order; writes kept ids ascending,
+// returns their count.
+int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m, const Box &box,
+                  float step, int *outIds, const std::string &tag);
+// Two-phase normal estimation of ids[0..m) (see sm_oracle.cpp estimate_normals).
+void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *ids, int m,
+                      const Grid &query, int k, bool smooth, bool invert, const float *vp,
+                      const std::string &tag);
+// Normalise all normals (normalizeNormal, util.cpp:163-176).
+void normalize_normals(Ctx &c, float4 *nrm, int n);
+
+// ---- vote.cu --------------------------------------------------------------------------
+struct VoteOut {
+    long long *stats;   // K x 8
+    float     *cands;   // K x 9
+    float     *poses;   // K x 3 x 18
+    int       *poseOk;  // K x 3 flags
+    int       *acc;     // dumpK x refNum x A (nullable)
+};
+// Voting for K keypoints with neighbours either given as CSR lists (nbrOff/nbrIds) or, when
+// nbrOff == nullptr, all points of `cand[0..ncand)` within the model diameter in ascending
+// order.
+void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const int *kp, int K,
+          const int *nbrOff, const int *nbrIds, const int *cand, int ncand, float minScore,
+          const VoteOut &out, int dumpK);
+// All ordered model pairs (trainModel's table rows): key and alpha per (i, j).
+void model_pairs(Ctx &c, const float4 *sp, const float4 *sn, int ns, float angleStep,
+                 float distStep, uint32_t *keys, float *alphas, int *valid);
+
+// ---- cluster.cu -----------------------------------------------------------------------
+// Pose clustering (clusterPose, avgClusters, sortPoses, clusterPose2) of np poses
+// (18 floats each, in list order). Writes the ordered candidates (18 floats) and returns
+// their count.
+int cluster(Ctx &c, const float *poses, int np, float distThr, float angThr,
+            const float center[3], float maxOverlap, float *outCands, const std::string &tag);
+
+// ---- icp.cu ---------------------------------------------------------------------------
+struct IcpScene {
+    const float4 *pos, *nrm;
+    Grid          sampled, resampled, full;
+    const int    *rankS, *rankR; // point id -> index in the sampled / resampled subsets
+};
+struct IcpParams {
+    int   sparse, dense, denseSteps;
+    float rejectDist, sampleStep, reSampleStep, scoreDist, voteThreshold, minScore;
+};
+// ICP refinement + scoring of every candidate in parallel. Outputs per candidate: status,
+// score, refined pose (12 floats).
+// rank[ids[i]] = i
+void subset_rank(Ctx &c, const int *ids, int m, int *rank);
+void icp_all(Ctx &c, const Model &m, const IcpScene &s, const IcpParams &p, const float *cands,
+             int ncand, int *status, float *score, float *pose);
+
+} // namespace sm

@@ -1,0 +1,144 @@
+"""Parity of the GPU path with the CPU oracle (run on a GB300: -m gpu).
+
+Bit-exact: sampling, keypoints, normals, PPF keys / hash hits / per-(reference, bin)
+votes, candidates, pose list, clustering and ICP results against the oracle's GPU-order
+mode; and the voting kernel against the oracle's reference-order mode (k-d tree neighbour
+order, i.e. the reference's lane assignment) on identical inputs.
+Tolerance: final poses against the reference-order pipeline within 0.1 degree and
+1e-3 * model diameter.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SD = 0.05
+KP = 0.2
+MS = 0.2
+
+
+@pytest.fixture(scope="module")
+def data():
+    from surface_match_gb300 import synth
+    mc, _, _ = synth.gear_model(8000, seed=5)
+    sc = synth.scene_tiny(seed=3)
+    return mc, sc
+
+
+@pytest.fixture(scope="module")
+def oracle_grid(data):
+    from oracle import MODE_GRID, MatchParam, Oracle
+    mc, sc = data
+    o = Oracle(mode=MODE_GRID, threads=8)
+    m = o.train(mc.xyz, mc.normal, SD)
+    r = o.match(m, sc.cloud.xyz, None, sc.viewpoint, SD, KP, MS, MatchParam(numMatches=8))
+    return m, r
+
+
+@pytest.fixture(scope="module")
+def oracle_ref(data):
+    from oracle import MODE_REF, MatchParam, Oracle
+    mc, sc = data
+    o = Oracle(mode=MODE_REF, threads=8)
+    m = o.train(mc.xyz, mc.normal, SD)
+    r = o.match(m, sc.cloud.xyz, None, sc.viewpoint, SD, KP, MS, MatchParam(numMatches=8),
+                dump_k=6)
+    return m, r
+
+
+@pytest.fixture(scope="module")
+def gpu(data):
+    from surface_match_gb300 import Detector, MatchParam, PointCloud
+    mc, sc = data
+    det = Detector()
+    det.trainModel(PointCloud(mc.xyz, mc.normal), SD)
+    poses, scores = det.matchScene(PointCloud(sc.cloud.xyz, None, sc.viewpoint), SD, KP, MS,
+                                   MatchParam(numMatches=8))
+    return det, poses, scores
+
+
+def test_train_matches_oracle_bit_exact(gpu, oracle_grid):
+    det = gpu[0]
+    m, _ = oracle_grid
+    d = det.download()
+    for k, v in (("sampled", m.sampled), ("sampled_normal", m.sampled_normal),
+                 ("resampled", m.resampled), ("resampled_normal", m.resampled_normal),
+                 ("box", m.box), ("keys", m.keys), ("offsets", m.offsets), ("refs", m.refs)):
+        np.testing.assert_array_equal(d[k], v, err_msg=k)
+    np.testing.assert_array_equal(d["alphas"].view(np.uint32), m.alphas.view(np.uint32))
+
+
+def test_scene_sampling_and_normals_bit_exact(gpu, oracle_grid):
+    det = gpu[0]
+    _, r = oracle_grid
+    np.testing.assert_array_equal(det.debug(0), r.sampled)
+    np.testing.assert_array_equal(det.debug(1), r.keypoints)
+    np.testing.assert_array_equal(det.debug(2), r.resampled)
+    pos, nrm = det.debug(3), det.debug(4)
+    np.testing.assert_array_equal(pos.view(np.uint32), r.positions.view(np.uint32))
+    ok = np.isfinite(r.normals).all(1)
+    np.testing.assert_array_equal(np.isfinite(nrm).all(1), ok)
+    np.testing.assert_array_equal(nrm[ok].view(np.uint32), r.normals[ok].view(np.uint32))
+
+
+def test_votes_keys_and_candidates_bit_exact(gpu, oracle_grid):
+    det = gpu[0]
+    _, r = oracle_grid
+    st = det.debug(7)
+    np.testing.assert_array_equal(st, r.kp_stats)  # neighbours, hits, votes, fingerprint
+    np.testing.assert_array_equal(det.debug(8), r.kp_cands)
+    np.testing.assert_array_equal(det.debug(9).view(np.uint32), r.pose_list.view(np.uint32))
+
+
+def test_clustering_and_icp_bit_exact(gpu, oracle_grid):
+    det, poses, scores = gpu
+    _, r = oracle_grid
+    np.testing.assert_array_equal(det.debug(10).view(np.uint32), r.clustered.view(np.uint32))
+    n = len(r.cand_status)
+    np.testing.assert_array_equal(det.debug(12)[:n], r.cand_status)
+    ok = r.cand_status == 0
+    np.testing.assert_array_equal(det.debug(13)[:n][ok], r.cand_score[ok])
+    np.testing.assert_array_equal(det.debug(14)[:n][ok], r.cand_pose[ok])
+    assert len(scores) == len(r.scores)
+    np.testing.assert_array_equal(scores, r.scores)
+    np.testing.assert_array_equal(poses[:, :3, :].reshape(len(scores), -1),
+                                  r.results[:, :12])
+
+
+def test_vote_kernel_reference_order_bit_exact(oracle_ref):
+    """Voting on the reference-order scene state: the oracle's k-d tree neighbour lists
+    (the reference's unsorted radius-search order, which decides each pair's 8-lane block /
+    scalar-tail rule) and the reference-order model table, uploaded unchanged."""
+    from surface_match_gb300 import Detector, TrainParam
+    m, r = oracle_ref
+    det = Detector()
+    det.upload(m.sampled, m.sampled_normal, m.resampled, m.resampled_normal, m.box, m.keys,
+               m.offsets, m.refs, m.alphas, SD, TrainParam())
+    stats, cands, poses, acc = det.vote_stage(r.positions, r.normals, r.keypoints, r.nbr_off,
+                                              r.nbr_ids, MS, dump_k=6)
+    np.testing.assert_array_equal(stats, r.kp_stats)
+    np.testing.assert_array_equal(cands, r.kp_cands)
+    np.testing.assert_array_equal(acc, r.acc_dump)
+    emitted = poses[stats[:, 6][:, None] > np.arange(3)[None, :]]
+    np.testing.assert_array_equal(emitted.view(np.uint32), r.pose_list.view(np.uint32))
+
+
+def _pose_err(A, B):
+    R = A[:3, :3].astype(np.float64).T @ B[:3, :3].astype(np.float64)
+    ang = np.degrees(np.arccos(np.clip((np.trace(R) - 1) / 2, -1, 1)))
+    return ang, float(np.linalg.norm(A[:3, 3] - B[:3, 3]))
+
+
+def test_poses_within_tolerance_of_reference_order(gpu, oracle_ref, data):
+    """End to end against the reference-order pipeline: same instance count; each GPU
+    pose within 0.1 deg / 1e-3 * diameter of the reference-order pose it matches."""
+    det, poses, scores = gpu
+    m, r = oracle_ref
+    diam = float(np.linalg.norm(m.box[3:] - m.box[:3]))
+    assert len(scores) == len(r.scores)
+    used = set()
+    for P in poses:
+        best = min(((i,) + _pose_err(P, np.vstack([Q, [0, 0, 0, 1]]))
+                    for i, Q in enumerate(r.poses) if i not in used), key=lambda t: t[2])
+        used.add(best[0])
+        assert best[1] < 0.1 and best[2] < 1e-3 * diam, best
