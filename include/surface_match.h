@@ -82,8 +82,8 @@ typedef struct {
     int64_t n_pairs;      /* point pairs evaluated (keypoint x neighbour) */
     int64_t n_hits;       /* pairs whose key is in the model table */
     int64_t n_votes;      /* votes cast: matched table entries (ppf.cpp:342-346) */
-    float   ms[8];        /* stage device times: prep, sample+normals, keypoints, vote,
-                             cluster, icp prep, icp, total */
+    float   ms[8];        /* stage device times (ms): prep, sampling + normals, keypoints,
+                             vote kernel, clustering, refinement prep, refinement, total */
 } sm_match_stats;
 
 /* TrainParam / MatchParam defaults and constructor validation (type.cpp:71-127). */
@@ -163,7 +163,9 @@ SM_API int sm_vote_stage(sm_model model, const float *points, const float *norma
  * (int64 x8, as sm_vote_stage); 8 candidates (float x9); 9 pose list (float x18);
  * 10 clustered candidates (float x18); 12 candidate ICP status (int32: 0 accepted,
  * 1 votes, 2 sparse not converged, 3 sparse score, 4 dense not converged, 5 dense score);
- * 13 candidate score (float); 14 candidate pose (float x12). */
+ * 13 candidate score (float); 14 candidate pose (float x12); 15 ICP trace per candidate
+ * (float x258: sparse then dense stage, 32 iterations x {pairs, mean distance, source
+ * centroid x, step translation x}, then the sparse and dense inlier counts; -1 unused). */
 SM_API int64_t sm_debug_size(sm_model model, int field);
 SM_API int     sm_debug_get(sm_model model, int field, void *dst);
 
@@ -172,6 +174,9 @@ SM_API const char *sm_last_error(void);
 
 /* Library version string. */
 SM_API const char *sm_version(void);
+
+/* Number of CUDA kernels the library has launched so far in this process. */
+SM_API int64_t sm_launch_count(void);
 
 #ifdef __cplusplus
 }

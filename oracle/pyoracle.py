@@ -169,7 +169,7 @@ _FIELDS = {"sampled": (0, np.int32, 1), "keypoints": (1, np.int32, 1),
            "clustered": (10, np.float32, 18), "cluster_sizes": (11, np.int32, 1),
            "cand_status": (12, np.int32, 1), "cand_score": (13, np.float32, 1),
            "cand_pose": (14, np.float32, 12), "results": (15, np.float32, 13),
-           "acc_dump": (16, np.int32, 1)}
+           "acc_dump": (16, np.int32, 1), "cand_trace": (17, np.float32, 258)}
 
 
 class MatchResult:

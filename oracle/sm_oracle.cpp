@@ -181,7 +181,7 @@ struct Grid {
                 od[i] = d;
                 oi[i] = id;
             });
-            float b = smg::ring_bound(s + 1, g);
+            float b = smg::ring_bound(s, g);
             if (n == k && od[k - 1] < b * b)
                 break;
         }
@@ -203,7 +203,7 @@ struct Grid {
                     best = id;
                 }
             });
-            float b = smg::ring_bound(s + 1, g);
+            float b = smg::ring_bound(s, g);
             if (best >= 0 && bd < b * b)
                 break;
             if (b * b > limit2)
@@ -223,7 +223,7 @@ struct Grid {
                 const V3 &p = (*pts)[id];
                 if (smm::dist2(q.x, q.y, q.z, p.x, p.y, p.z) < r2) hit = true;
             });
-            float b = smg::ring_bound(s + 1, g);
+            float b = smg::ring_bound(s, g);
             if (b * b >= r2)
                 break;
         }
@@ -826,7 +826,8 @@ struct StridedSum {
 template <class NN>
 IcpResult icp_regist(const std::vector<V3> &sp, const std::vector<V3> &sn,
                      const std::vector<V3> &P, const std::vector<V3> &N, size_t dstSize,
-                     const smi::Pose34 &init, const IcpCrit &cr, bool fp64, int nthreads, NN &&nn) {
+                     const smi::Pose34 &init, const IcpCrit &cr, bool fp64, int nthreads, NN &&nn,
+                     float *trace = nullptr) {
     IcpResult res;
     res.pose = init;
     const size_t ns = sp.size();
@@ -915,6 +916,15 @@ IcpResult icp_regist(const std::vector<V3> &sp, const std::vector<V3> &sn,
             StridedSum ms(1, fp64);
             for (size_t k = 0; k < cnt; k++) ms.add(pairs[k], &dist[k]);
             mse = ms.result(0) / (float)cnt;
+            if (trace && res.iterations < 32) {
+                trace[res.iterations * 4 + 2] = Pm[0];
+                trace[res.iterations * 4 + 3] = step.m[3];
+            }
+        }
+        if (trace && res.iterations < 32) {
+            trace[res.iterations * 4]     = (float)cnt;
+            trace[res.iterations * 4 + 1] = mse;
+            if (cnt < 6) trace[res.iterations * 4 + 3] = 0.0f;
         }
         // regist loop logic (icp.cpp:233-272)
         bool conv = (cnt > 6) && (mse < cr.mseMax);
@@ -948,6 +958,7 @@ struct MatchOut {
     std::vector<float>   candScore;   // per clustered candidate: final score or -1
     std::vector<int>     candStatus;  // 0 ok, 1 votes, 2 sparse nc, 3 sparse score, 4 dense nc, 5 dense score
     std::vector<PoseRec> candPose;
+    std::vector<float>   candTrace;   // 258 floats per candidate (layout of the GPU trace)
     std::vector<PoseRec> results;     // [score in votes field]
     std::vector<std::vector<int>> accDump; // full accumulators of the first dumpK keypoints
     double               tStage[8] = {0};
@@ -1119,26 +1130,31 @@ MatchOut *match(const Model &m, const float *xyz, const float *nrm, int64_t n, c
         smi::Pose34 pose = c.T;
         float       score = c.votes;
         int         status = 0;
+        std::vector<float> tr(258, -1.0f);
         if (score < voteThreshold) status = 1;
         if (!status && mp.sparsePoseRefinement) {
             if (mode == ORC_MODE_REF) { tree->restore(); tree->reduce(ioi); }
-            auto r = icp_regist(m.sp, m.sn, P, N, o->sampled.size(), pose, sparse, fp64, nthreads, nn_in(gS, &ioi));
+            auto r = icp_regist(m.sp, m.sn, P, N, o->sampled.size(), pose, sparse, fp64, nthreads, nn_in(gS, &ioi), tr.data());
             if (!r.converged) status = 2;
             else {
                 pose = r.pose;
                 if (mode == ORC_MODE_REF) tree->restore();
-                score = std::min(1.f, inliers(m.sp, pose) / float(refNum));
+                int in = inliers(m.sp, pose);
+                tr[256] = (float)in;
+                score = std::min(1.f, in / float(refNum));
                 if (score < minScore) status = 3;
             }
         }
         if (!status && mp.sparsePoseRefinement && mp.densePoseRefinement) {
             if (mode == ORC_MODE_REF) { tree->restore(); tree->reduce(ioi2); }
-            auto r = icp_regist(m.rp, m.rn, P, N, o->resampled.size(), pose, dense, fp64, nthreads, nn_in(gR, &ioi2));
+            auto r = icp_regist(m.rp, m.rn, P, N, o->resampled.size(), pose, dense, fp64, nthreads, nn_in(gR, &ioi2), tr.data() + 128);
             if (!r.converged) status = 4;
             else {
                 pose = r.pose;
                 if (mode == ORC_MODE_REF) tree->restore();
-                score = std::min(1.f, inliers(m.rp, pose) / float(m.rp.size()));
+                int in = inliers(m.rp, pose);
+                tr[257] = (float)in;
+                score = std::min(1.f, in / float(m.rp.size()));
                 if (score < minScore) status = 5;
             }
         }
@@ -1149,6 +1165,7 @@ MatchOut *match(const Model &m, const float *xyz, const float *nrm, int64_t n, c
         o->candStatus.push_back(status);
         o->candScore.push_back(status ? -1.f : score);
         o->candPose.push_back(pr);
+        o->candTrace.insert(o->candTrace.end(), tr.begin(), tr.end());
         if (!status) {
             o->results.push_back(pr);
             if ((int)o->results.size() >= mp.numMatches) break;
@@ -1291,6 +1308,7 @@ int64_t orc_res_size(void *rp, int field) {
         case 14: return r->candPose.size() * 12;
         case 15: return r->results.size() * 13;
         case 16: { int64_t s = 0; for (auto &a : r->accDump) s += a.size(); return s; }
+        case 17: return r->candTrace.size();
     }
     return -1;
 }
@@ -1345,6 +1363,7 @@ void orc_res_get(void *rp, int field, void *dst) {
                 ((float *)dst)[13 * i + 12] = r->results[i].votes;
             }
             break;
+        case 17: memcpy(dst, r->candTrace.data(), r->candTrace.size() * 4); break;
         case 16: {
             int *d = (int *)dst;
             for (auto &a : r->accDump) { memcpy(d, a.data(), a.size() * 4); d += a.size(); }
@@ -1434,5 +1453,30 @@ extern "C" void orc_kd_knn(const float *xyz, int64_t n, const float *box, const 
             idx[(int64_t)k * j + i]  = rs.idx[i];
             dist[(int64_t)k * j + i] = rs.dist[i];
         }
+    }
+}
+
+// Grid-search probe for the exactness tests: k nearest, nearest within a limit and
+// any-within-radius of each query over all points, on a grid of cell side `cell`.
+extern "C" void orc_grid_probe(const float *xyz, int64_t n, const float *qs, int64_t nq,
+                               float cell, int k, float limit2, float r2, int *knnIdx,
+                               float *knnDist, int *nnIdx, float *nnDist, int *within) {
+    std::vector<V3> P(n);
+    for (int64_t i = 0; i < n; i++) P[i] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+    std::vector<int> all(n);
+    std::iota(all.begin(), all.end(), 0);
+    Box b = bbox_of(P, all);
+    Grid G;
+    G.build(P, all, b, cell);
+    for (int64_t j = 0; j < nq; j++) {
+        V3 q{qs[3 * j], qs[3 * j + 1], qs[3 * j + 2]};
+        std::vector<int>   oi(k, -1);
+        std::vector<float> od(k, -1.f);
+        G.knn(q, k, oi.data(), od.data());
+        for (int i = 0; i < k; i++) { knnIdx[j * k + i] = oi[i]; knnDist[j * k + i] = od[i]; }
+        float d;
+        nnIdx[j]  = G.nn(q, limit2, d);
+        nnDist[j] = d;
+        within[j] = G.any_within(q, r2) ? 1 : 0;
     }
 }

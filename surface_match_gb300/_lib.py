@@ -73,6 +73,7 @@ _SIGNATURES = {
     "sm_debug_get": (C.c_int, [_vp, C.c_int, _vp]),
     "sm_last_error": (C.c_char_p, []),
     "sm_version": (C.c_char_p, []),
+    "sm_launch_count": (C.c_int64, []),
 }
 
 

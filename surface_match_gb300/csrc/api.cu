@@ -29,6 +29,7 @@ struct sm_model_s {
 namespace sm {
 
 static thread_local std::string g_lastError;
+long long                       g_launches = 0;
 
 void Model::free_device() {
     void *ps[] = {sp, sn, rp, rn, hkeys, boff, entries};
@@ -217,6 +218,19 @@ std::vector<float> download4(const float4 *d, int n) {
     return o;
 }
 
+// Query-grid cell for k-nearest-neighbour searches: about 1.3x the expected k-NN radius,
+// from the point density the greedy sampling reveals (n_sampled points at `step` cover an
+// area of about n_sampled * step^2 / 0.7). Results do not depend on it, only run time.
+float knn_cell(int nvalid, int nsampled, float step, int k, const float ext[3]) {
+    float g = step * 0.25f;
+    if (nvalid > 0 && nsampled > 0) {
+        const double area = (double)nsampled * step * step / 0.7;
+        const double rk   = std::sqrt((double)std::max(k, 3) * area / (3.14159265 * nvalid));
+        g = (float)std::min<double>(std::max<double>(1.3 * rk, step * 0.1), step);
+    }
+    return smg::query_cell(g, ext);
+}
+
 // trainModel (ppf.cpp:36-147) with the device sampler, normal estimation and pair kernel;
 // the table is grouped by key on the host in pair order, i.e. the reference's
 // single-threaded insertion order (reference point i, then column j).
@@ -251,10 +265,11 @@ void train(Ctx &c, Model &m, const float *xyzIn, const float *nrmIn, int64_t n64
     if (!nrmIn) {
         float ext[3] = {box.ext(0), box.ext(1), box.ext(2)};
         Grid  q;
-        build_grid(c, pos, valid, nvalid, box, smg::query_cell(sampleStep * 0.25f, ext), false, q, "t.q");
+        const float gq = knn_cell(nvalid, n1, sampleStep, tp.knnNormal, ext);
+        build_grid(c, pos, valid, nvalid, box, gq, false, q, "t.q");
         estimate_normals(c, pos, nrm, n, idx1, n1, q, tp.knnNormal, tp.smoothNormal != 0, false,
                          nullptr, "t.n1");
-        build_grid(c, pos, valid, nvalid, box, smg::query_cell(sampleStep * 0.25f, ext), false, q, "t.q");
+        build_grid(c, pos, valid, nvalid, box, gq, false, q, "t.q");
         estimate_normals(c, pos, nrm, n, idx2, n2, q, tp.knnNormal, tp.smoothNormal != 0, false,
                          nullptr, "t.n2");
     }
@@ -365,8 +380,9 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
     int        *sampled      = c.arena.get<int>("m.sampled", std::max(n, 1));
     const int   ns = sample_points(c, pos, n, valid, nvalid, box, sampleStep, sampled, "m.s1");
     Grid        q;
+    const float gq = knn_cell(nvalid, ns, sampleStep, mp.knnNormal, ext);
     if (!hasN) {
-        build_grid(c, pos, valid, nvalid, box, smg::query_cell(sampleStep * 0.25f, ext), false, q, "m.q");
+        build_grid(c, pos, valid, nvalid, box, gq, false, q, "m.q");
         estimate_normals(c, pos, nrm, n, sampled, ns, q, mp.knnNormal, mp.smoothNormal != 0,
                          mp.invertNormal != 0, vp, "m.n1");
     }
@@ -382,7 +398,9 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
     vo.poses  = c.arena.get<float>("m.kposes", (size_t)std::max(K, 1) * 3 * smi::kPoseFloats);
     vo.poseOk = c.arena.get<int>("m.kposeok", (size_t)std::max(K, 1) * 3);
     vo.acc    = nullptr;
+    record(c, 8);
     vote(c, m, pos, nrm, kp, K, nullptr, nullptr, sampled, ns, minScore, vo, 0);
+    record(c, 9);
     int      *slots = c.arena.get<int>("m.slots", (size_t)std::max(K, 1) * 3);
     const int np    = compact(c, vo.poseOk, K * 3, slots, "m.cp");
     float    *plist = c.arena.get<float>("m.plist", (size_t)std::max(np, 1) * smi::kPoseFloats);
@@ -417,7 +435,7 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
     if (mp.densePoseRefinement) {
         nres = sample_points(c, pos, n, valid, nvalid, box, reSampleStep, resampled, "m.s3");
         if (!hasN) {
-            build_grid(c, pos, valid, nvalid, box, smg::query_cell(sampleStep * 0.25f, ext), false, q, "m.q");
+            build_grid(c, pos, valid, nvalid, box, gq, false, q, "m.q");
             estimate_normals(c, pos, nrm, n, resampled, nres, q, mp.knnNormal, false,
                              mp.invertNormal != 0, vp, "m.n2");
         }
@@ -425,11 +443,13 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
     IcpScene s;
     s.pos          = pos;
     s.nrm          = nrm;
-    const float gs = std::max(sampleStep, refDist / 2.5f);
+    // nearest-neighbour grids of the refinement: about half (sparse) or a third (dense) of
+    // the rejection distance, so a query needs few cell shells either way
+    const float gs = std::max(sampleStep, refDist / 2.0f);
     build_grid(c, pos, sampled, ns, box, smg::query_cell(gs, ext), false, s.sampled, "m.gS");
-    const float gr = std::max(2.0f * reSampleStep, refDist / 2.5f);
+    const float gr = std::max(2.0f * reSampleStep, refDist / 3.0f);
     build_grid(c, pos, resampled, nres, box, smg::query_cell(gr, ext), false, s.resampled, "m.gR");
-    const float gf = std::max(scoreDist, sampleStep * 0.25f);
+    const float gf = std::max(scoreDist, gq);
     build_grid(c, pos, valid, nvalid, box, smg::query_cell(gf, ext), false, s.full, "m.gF");
     int *rankS = c.arena.get<int>("m.rankS", n);
     int *rankR = c.arena.get<int>("m.rankR", n);
@@ -451,7 +471,8 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
     int   *cstat  = c.arena.get<int>("m.cstat", std::max(ncand, 1));
     float *cscore = c.arena.get<float>("m.cscore", std::max(ncand, 1));
     float *cpose  = c.arena.get<float>("m.cpose", (size_t)std::max(ncand, 1) * 12);
-    icp_all(c, m, s, ip, cands, ncand, cstat, cscore, cpose);
+    float *ctrace = c.arena.get<float>("m.ctrace", (size_t)std::max(ncand, 1) * kIcpTraceFloats);
+    icp_all(c, m, s, ip, cands, ncand, cstat, cscore, cpose, ctrace);
     std::vector<int>   hs(ncand);
     std::vector<float> hsc(ncand), hp((size_t)ncand * 12);
     if (ncand) {
@@ -502,7 +523,7 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
             stats->n_hits += st[(size_t)k * 8 + 2];
             stats->n_votes += st[(size_t)k * 8 + 3];
         }
-        const int stage[8][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 4}, {4, 5}, {5, 6}, {6, 7}, {0, 7}};
+        const int stage[8][2] = {{0, 1}, {1, 2}, {2, 3}, {8, 9}, {4, 5}, {5, 6}, {6, 7}, {0, 7}};
         for (int i = 0; i < 8; i++)
             SM_CUDA(cudaEventElapsedTime(&stats->ms[i], c.ev[stage[i][0]], c.ev[stage[i][1]]));
     }
@@ -565,6 +586,7 @@ extern "C" {
 
 SM_API const char *sm_last_error(void) { return g_lastError.c_str(); }
 SM_API const char *sm_version(void) { return "surface_match_gb300 0.1 (sm_103a)"; }
+SM_API int64_t     sm_launch_count(void) { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
 
 SM_API void sm_train_param_default(sm_train_param *p) {
     if (p)
@@ -977,6 +999,7 @@ static bool debug_field(sm_model m, int field, const void *&src, int64_t &count,
         case 12: src = get("m.cstat"); count = c.last.ncand; elem = 4; return true;
         case 13: src = get("m.cscore"); count = c.last.ncand; elem = 4; return true;
         case 14: src = get("m.cpose"); count = (int64_t)c.last.ncand * 12; elem = 4; return true;
+        case 15: src = get("m.ctrace"); count = (int64_t)c.last.ncand * kIcpTraceFloats; elem = 4; return true;
     }
     return false;
 }

@@ -2,13 +2,17 @@
 // (icp.cpp:214-278) with findCorresponds (icp.cpp:123-167), the symmetric point-to-plane
 // step (icp.cpp:39-121) and inliner (util.cpp:628-641).
 //
-// Every candidate is independent, so all of them are refined at once: one CTA of
-// kIcpThreads threads per candidate. Per iteration: grid nearest neighbour of each moved
-// model point; per scene point the closest model point wins a 64-bit atomicMin of
-// (distance bits, model index), which reproduces the reference's "first minimum in model
-// order" without its O(n*m) grouping scan; FP32 Kahan sums in a fixed strided layout and
-// tree; FP64 solve on thread 0. The selection walk over the candidates (numMatches) runs
-// on the host afterwards and only reads the per-candidate results.
+// All candidates are refined at once and each candidate's source points are spread over
+// ceil(n / 256) CTAs, so the whole GPU works even for a handful of candidates. One ICP
+// iteration is seven launches: correspondences (grid nearest neighbour, per scene point
+// the closest model point wins a 64-bit atomicMin of (distance bits, model index), which
+// is the reference's "first minimum in model order" without its O(n*m) grouping scan),
+// pair selection, centroids, normal-equation terms, their reduction + FP64 solve,
+// residual distances, their reduction + the convergence logic. Every reduction has the
+// same fixed layout: 256 slots (slot = source index mod 256), each a Kahan sum over its
+// source points in ascending order, merged by a fixed binary tree - the layout the CPU
+// oracle emulates, so poses are bit-identical. The selection walk over the candidates
+// (numMatches) runs on the host afterwards and only reads the per-candidate results.
 #include <cfloat>
 
 #include "sm_icp.h"
@@ -19,294 +23,400 @@ using namespace smd;
 
 namespace {
 
-constexpr int kT = smi::kIcpThreads;
+constexpr int kT = smi::kIcpThreads; // slots per reduction = threads per CTA
 constexpr int kW = kT / 32;
+constexpr int kTraceIters  = 32;
+constexpr int kTraceFloats = 2 * kTraceIters * 4 + 2;
 
-struct IcpArgs {
-    const float4 *sp, *sn, *rp, *rn;
-    int           ns, nr;
-    const float4 *pos, *nrm;
-    GridView      gS, gR, gF;
-    const int    *rankS, *rankR; // point id -> index in the sampled / resampled subset
-    int           nS, nR;
-    IcpParams     p;
-    const float  *cands; // ncand x 18
-    int           wave0, ncand;
-    // per-CTA scratch (indexed by blockIdx.x)
-    int                *nnId;  // maxSrc: scene point id of the pair, -1 none
-    int                *nnR;   // maxSrc: subset rank of that point
-    float4             *x4;    // maxSrc: moved source point, w = squared distance
-    float4             *n4;    // maxSrc: rotated source normal
-    unsigned long long *winS;  // nS
-    unsigned long long *winR;  // nR
-    int                 maxSrc;
-    int                *status;
-    float              *score, *pose;
-};
-
-struct Shared {
-    float       red[kW][smi::kNumSystem][2];
-    smi::Pose34 M, step;
+// Per-candidate state, resident in global memory across the launches of one refinement.
+struct Cand {
+    smi::Pose34 M, keep, step;
     float       Pm[3], Qm[3];
-    float       mse;
-    int         ired[kW];
-    int         cnt;
+    float       resMse, mse, score;
+    int         cnt, iterations, converged, stop, status, active, inl, pad;
 };
 
-// Fixed-layout reduction of W Kahan partials (one per thread): warp shfl_down tree, then
-// warp 0 over the kW warp partials. Result valid on thread 0. Matches the oracle's
-// StridedSum::result.
-template <int W> __device__ void kahan_reduce(smi::KahanF (&v)[W], Shared &S) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+struct Stage {
+    const float4 *src, *srcN; // model points / normals
+    int           n, nb;      // points, CTAs per candidate
+    GridView      G;          // scene subset grid
+    const int    *rank;       // point id -> subset index
+    int           nDst;
+    int           iters;
+    float         mseMin, mseMax, rej2;
+    int           traceOff; // 0 sparse, 1 dense
+};
+
+struct Work {
+    Cand               *cand;
+    const float4       *pos, *nrm;
+    int                *nnId;   // ncand x maxSrc: scene point of the pair (-1 none)
+    int                *nnR;    // ncand x maxSrc: its subset index (-1 none)
+    float4             *x4;     // ncand x maxSrc: moved source point, w = squared distance
+    float4             *n4;     // ncand x maxSrc: rotated source normal
+    float              *terms;  // ncand x 27 x maxSrc (SoA per candidate)
+    unsigned long long *win;    // ncand x maxDst
+    int                 maxSrc, maxDst;
+    float              *trace;  // ncand x kTraceFloats (nullable)
+};
+
+__device__ __forceinline__ unsigned long long win_key(float d, int i) {
+    return ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)i;
+}
+
+__device__ __forceinline__ bool cand_live(const Cand &c, const Stage &s) {
+    return c.active && !c.stop && c.iterations < s.iters;
+}
+
+// K1: correspondences
+__global__ void __launch_bounds__(kT) k_corr(Work w, Stage s) {
+    const int   ci = blockIdx.y;
+    const Cand &C  = w.cand[ci];
+    if (!cand_live(C, s))
+        return;
+    const int i = blockIdx.x * kT + threadIdx.x;
+    if (i >= s.n)
+        return;
+    const size_t o = (size_t)ci * w.maxSrc + i;
+    float4       x, y;
+    smi::pose_apply(C.M, s.src[i].x, s.src[i].y, s.src[i].z, x.x, x.y, x.z);
+    smi::pose_rotate(C.M, s.srcN[i].x, s.srcN[i].y, s.srcN[i].z, y.x, y.y, y.z);
+    float      d;
+    const int  j  = grid_nn(s.G, w.pos, x.x, x.y, x.z, s.rej2, d);
+    const bool ok = j >= 0 && d <= s.rej2;
+    x.w           = d;
+    y.w           = 0.0f;
+    w.x4[o]       = x;
+    w.n4[o]       = y;
+    w.nnId[o]     = ok ? j : -1;
+    const int r   = ok ? s.rank[j] : -1;
+    w.nnR[o]      = r;
+    if (ok)
+        atomicMin(&w.win[(size_t)ci * w.maxDst + r], win_key(d, i));
+}
+
+// K2: keep only the closest source point per scene point
+__global__ void __launch_bounds__(kT) k_pairs(Work w, Stage s) {
+    const int   ci = blockIdx.y;
+    const Cand &C  = w.cand[ci];
+    if (!cand_live(C, s))
+        return;
+    const int i = blockIdx.x * kT + threadIdx.x;
+    if (i >= s.n)
+        return;
+    const size_t o = (size_t)ci * w.maxSrc + i;
+    const int    r = w.nnR[o];
+    if (r < 0)
+        return;
+    if (w.win[(size_t)ci * w.maxDst + r] != win_key(w.x4[o].w, i))
+        w.nnId[o] = -1;
+}
+
+// Fixed-layout reduction of W quantities over the 256 slots: slot t sums, with Kahan, the
+// terms of the pairs i = t, t + 256, ... in ascending order; then the tree (warp
+// shfl_down, then warp 0 over the warp partials). Result valid on thread 0.
+template <int W, class F>
+__device__ void slot_reduce(const Work &w, const Stage &s, int ci, F &&term, smi::KahanF (&v)[W],
+                            float (*red)[W][2]) {
+    const int tid = threadIdx.x;
+    for (int k = 0; k < W; k++)
+        v[k].init();
+    const int *nnId = w.nnId + (size_t)ci * w.maxSrc;
+    for (int i = tid; i < s.n; i += kT) {
+        if (nnId[i] < 0)
+            continue;
+        float t[W];
+        term(i, t);
+        for (int k = 0; k < W; k++)
+            v[k].add(t[k]);
+    }
+    const int lane = tid & 31, wp = tid >> 5;
 #pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) {
-#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1)
         for (int k = 0; k < W; k++) {
             smi::KahanF o;
             o.s = __shfl_down_sync(0xffffffffu, v[k].s, off);
             o.c = __shfl_down_sync(0xffffffffu, v[k].c, off);
             v[k].merge(o);
         }
-    }
     if (lane == 0)
         for (int k = 0; k < W; k++) {
-            S.red[w][k][0] = v[k].s;
-            S.red[w][k][1] = v[k].c;
+            red[wp][k][0] = v[k].s;
+            red[wp][k][1] = v[k].c;
         }
     __syncthreads();
-    if (w == 0) {
+    if (wp == 0) {
         for (int k = 0; k < W; k++) {
-            v[k].s = lane < kW ? S.red[lane][k][0] : 0.f;
-            v[k].c = lane < kW ? S.red[lane][k][1] : 0.f;
+            v[k].s = lane < kW ? red[lane][k][0] : 0.f;
+            v[k].c = lane < kW ? red[lane][k][1] : 0.f;
         }
 #pragma unroll
-        for (int off = kW / 2; off >= 1; off >>= 1) {
-#pragma unroll
+        for (int off = kW / 2; off >= 1; off >>= 1)
             for (int k = 0; k < W; k++) {
                 smi::KahanF o;
                 o.s = __shfl_down_sync(0xffffffffu, v[k].s, off);
                 o.c = __shfl_down_sync(0xffffffffu, v[k].c, off);
                 v[k].merge(o);
             }
-        }
     }
-    __syncthreads();
 }
 
-__device__ int block_sum_int(int v, Shared &S) {
-    v = __reduce_add_sync(0xffffffffu, v);
-    if ((threadIdx.x & 31) == 0)
-        S.ired[threadIdx.x >> 5] = v;
-    __syncthreads();
-    int t = 0;
-    for (int w = 0; w < kW; w++)
-        t += S.ired[w];
-    __syncthreads();
-    return t;
-}
-
-__device__ __forceinline__ unsigned long long win_key(float d, int i) {
-    return ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)i;
-}
-
-// ICP::regist of source (src, srcN, n) against the scene subset of grid G, starting from
-// S.M; returns converged, leaves the refined pose in S.M.
-__device__ bool regist(const IcpArgs &a, Shared &S, const float4 *src, const float4 *srcN, int n,
-                       const GridView &G, const int *rank, unsigned long long *win, int iters,
-                       float mseMin, float mseMax) {
-    const int   tid  = threadIdx.x;
-    int        *nnId = a.nnId + (size_t)blockIdx.x * a.maxSrc;
-    int        *nnR  = a.nnR + (size_t)blockIdx.x * a.maxSrc;
-    float4     *x4   = a.x4 + (size_t)blockIdx.x * a.maxSrc;
-    float4     *n4   = a.n4 + (size_t)blockIdx.x * a.maxSrc;
-    const float rej2 = a.p.rejectDist * a.p.rejectDist;
-    bool        converged = false;
-    float       resMse    = FLT_MAX;
-    int         iterations = 0;
-    while (iterations < iters) {
-        // findCorresponds: nearest scene point, rejection, closest model point per scene point
-        for (int i = tid; i < n; i += kT) {
-            float4 x, y;
-            smi::pose_apply(S.M, src[i].x, src[i].y, src[i].z, x.x, x.y, x.z);
-            smi::pose_rotate(S.M, srcN[i].x, srcN[i].y, srcN[i].z, y.x, y.y, y.z);
-            float     d;
-            const int j  = grid_nn(G, a.pos, x.x, x.y, x.z, rej2, d);
-            const bool ok = j >= 0 && d <= rej2;
-            x.w     = d;
-            x4[i]   = x;
-            n4[i]   = y;
-            nnId[i] = ok ? j : -1;
-            nnR[i]  = ok ? rank[j] : -1;
-            if (ok)
-                atomicMin(&win[nnR[i]], win_key(d, i));
-        }
-        __syncthreads();
-        smi::KahanF mom[6];
-        for (int k = 0; k < 6; k++)
-            mom[k].init();
-        int cnt = 0;
-        for (int i = tid; i < n; i += kT) {
-            const int r = nnR[i];
-            if (r < 0)
-                continue;
-            if (win[r] != win_key(x4[i].w, i)) {
-                nnId[i] = -1; // not the closest source point of its scene point
-                continue;
-            }
-            const float4 q = a.pos[nnId[i]];
-            mom[0].add(x4[i].x);
-            mom[1].add(x4[i].y);
-            mom[2].add(x4[i].z);
-            mom[3].add(q.x);
-            mom[4].add(q.y);
-            mom[5].add(q.z);
-            cnt++;
-        }
-        cnt = block_sum_int(cnt, S);
-        kahan_reduce<6>(mom, S);
-        if (tid == 0) {
-            const float fc = (float)cnt;
-            for (int k = 0; k < 3; k++) {
-                S.Pm[k] = smm::fdiv(mom[k].value(), fc);
-                S.Qm[k] = smm::fdiv(mom[3 + k].value(), fc);
-            }
-        }
-        __syncthreads();
-        float mse = FLT_MAX;
-        if (cnt >= 6) {
-            smi::KahanF sys[smi::kNumSystem];
-            for (int k = 0; k < smi::kNumSystem; k++)
-                sys[k].init();
-            for (int i = tid; i < n; i += kT) {
-                if (nnId[i] < 0)
-                    continue;
-                const float4 q = a.pos[nnId[i]], qn = a.nrm[nnId[i]];
-                float        t[smi::kNumSystem];
-                smi::system_terms(x4[i].x - S.Pm[0], x4[i].y - S.Pm[1], x4[i].z - S.Pm[2],
-                                  q.x - S.Qm[0], q.y - S.Qm[1], q.z - S.Qm[2], n4[i].x + qn.x,
-                                  n4[i].y + qn.y, n4[i].z + qn.z, t);
-                for (int k = 0; k < smi::kNumSystem; k++)
-                    sys[k].add(t[k]);
-            }
-            kahan_reduce<smi::kNumSystem>(sys, S);
-            if (tid == 0) {
-                float v[smi::kNumSystem];
-                for (int k = 0; k < smi::kNumSystem; k++)
-                    v[k] = sys[k].value();
-                S.step = smi::solve_step(v, S.Pm, S.Qm);
-            }
-            __syncthreads();
-            smi::KahanF ms[1];
-            ms[0].init();
-            for (int i = tid; i < n; i += kT) {
-                if (nnId[i] < 0)
-                    continue;
-                float y0, y1, y2, d;
-                smi::pose_apply(S.step, x4[i].x, x4[i].y, x4[i].z, y0, y1, y2);
-                grid_nn(G, a.pos, y0, y1, y2, FLT_MAX, d);
-                ms[0].add(smm::fsqrt(d));
-            }
-            kahan_reduce<1>(ms, S);
-            if (tid == 0)
-                S.mse = smm::fdiv(ms[0].value(), (float)cnt);
-            __syncthreads();
-            mse = S.mse;
-        }
-        // reset the winner slots this iteration used
-        for (int i = tid; i < n; i += kT)
-            if (nnR[i] >= 0)
-                win[nnR[i]] = ~0ull;
-        __syncthreads();
-        // regist loop logic (icp.cpp:233-272), uniform across the CTA
-        if (cnt > 6 && mse < mseMax)
-            converged = true;
-        bool stop = false;
-        if (cnt < 6) {
-            stop = true;
-        } else {
-            if (mse < mseMin)
-                stop = true;
-            const float rate = smm::fdiv(resMse - mse, resMse);
-            if (rate < 0.05f)
-                stop = true;
-            if (iterations++ >= iters)
-                stop = true;
-            if (rate > 0.0f) {
-                resMse = mse;
-                if (tid == 0)
-                    S.M = smi::pose_mul(S.step, S.M);
-            }
-        }
-        __syncthreads();
-        if (stop)
-            break;
-    }
-    return converged;
-}
-
-__device__ int inliers(const IcpArgs &a, Shared &S, const float4 *src, int n) {
-    const float r2 = a.p.scoreDist * a.p.scoreDist;
-    int         c  = 0;
-    for (int i = threadIdx.x; i < n; i += kT) {
-        float x, y, z;
-        smi::pose_apply(S.M, src[i].x, src[i].y, src[i].z, x, y, z);
-        if (grid_any_within(a.gF, a.pos, x, y, z, r2))
-            c++;
-    }
-    return block_sum_int(c, S);
-}
-
-__global__ void __launch_bounds__(kT) k_icp(IcpArgs a) {
-    __shared__ Shared S;
-    const int         ci  = a.wave0 + blockIdx.x;
-    if (ci >= a.ncand)
+// K3: pair count and centroids
+__global__ void __launch_bounds__(kT) k_centroids(Work w, Stage s) {
+    __shared__ float red[kW][6][2];
+    __shared__ int   icnt[kW];
+    const int        ci = blockIdx.x;
+    Cand            &C  = w.cand[ci];
+    if (!cand_live(C, s))
         return;
-    const float *C = a.cands + (size_t)ci * smi::kPoseFloats;
-    if (threadIdx.x == 0)
-        for (int e = 0; e < 12; e++)
-            S.M.m[e] = C[e];
-    __syncthreads();
-    float score  = C[17];
-    int   status = 0;
-    if (score < a.p.voteThreshold)
-        status = 1;
-    smi::Pose34 keep = S.M; // the pose reported when a refinement does not converge
-    if (!status && a.p.sparse) {
-        const bool conv = regist(a, S, a.sp, a.sn, a.ns, a.gS, a.rankS,
-                                 a.winS + (size_t)blockIdx.x * a.nS, 5, a.p.sampleStep * 0.5f,
-                                 a.p.sampleStep);
-        if (!conv) {
-            status = 2;
-        } else {
-            keep = S.M;
-            const int in = inliers(a, S, a.sp, a.ns);
-            score        = fminf(1.0f, smm::fdiv((float)in, (float)a.ns));
-            if (score < a.p.minScore)
-                status = 3;
-        }
-    }
-    if (!status && a.p.sparse && a.p.dense) {
-        const bool conv = regist(a, S, a.rp, a.rn, a.nr, a.gR, a.rankR,
-                                 a.winR + (size_t)blockIdx.x * a.nR, a.p.denseSteps,
-                                 a.p.reSampleStep * 0.5f, a.p.sampleStep);
-        if (!conv) {
-            status = 4;
-        } else {
-            keep = S.M;
-            const int in = inliers(a, S, a.rp, a.nr);
-            score        = fminf(1.0f, smm::fdiv((float)in, (float)a.nr));
-            if (score < a.p.minScore)
-                status = 5;
-        }
-    }
-    if (!status && (a.p.sparse || a.p.dense) && score < a.p.minScore)
-        status = 5;
+    const int *nnId = w.nnId + (size_t)ci * w.maxSrc;
+    int        cnt  = 0;
+    for (int i = threadIdx.x; i < s.n; i += kT)
+        cnt += nnId[i] >= 0 ? 1 : 0;
+    cnt = __reduce_add_sync(0xffffffffu, cnt);
+    if ((threadIdx.x & 31) == 0)
+        icnt[threadIdx.x >> 5] = cnt;
+    const float4 *x4 = w.x4 + (size_t)ci * w.maxSrc;
+    smi::KahanF   v[6];
+    slot_reduce<6>(w, s, ci,
+                   [&](int i, float *t) {
+                       const float4 q = w.pos[nnId[i]];
+                       t[0]           = x4[i].x;
+                       t[1]           = x4[i].y;
+                       t[2]           = x4[i].z;
+                       t[3]           = q.x;
+                       t[4]           = q.y;
+                       t[5]           = q.z;
+                   },
+                   v, red);
     if (threadIdx.x == 0) {
-        a.status[ci] = status;
-        a.score[ci]  = status ? -1.0f : score;
-        for (int e = 0; e < 12; e++)
-            a.pose[(size_t)ci * 12 + e] = keep.m[e];
+        int total = 0;
+        for (int k = 0; k < kW; k++)
+            total += icnt[k];
+        const float fc = (float)total;
+        for (int k = 0; k < 3; k++) {
+            C.Pm[k] = smm::fdiv(v[k].value(), fc);
+            C.Qm[k] = smm::fdiv(v[3 + k].value(), fc);
+        }
+        C.cnt = total;
     }
+}
+
+// K4: normal-equation terms of each pair
+__global__ void __launch_bounds__(kT) k_sys_terms(Work w, Stage s) {
+    const int   ci = blockIdx.y;
+    const Cand &C  = w.cand[ci];
+    if (!cand_live(C, s) || C.cnt < 6)
+        return;
+    const int i = blockIdx.x * kT + threadIdx.x;
+    if (i >= s.n)
+        return;
+    const size_t o  = (size_t)ci * w.maxSrc + i;
+    const int    id = w.nnId[o];
+    if (id < 0)
+        return;
+    const float4 x = w.x4[o], xn = w.n4[o], q = w.pos[id], qn = w.nrm[id];
+    float        t[smi::kNumSystem];
+    smi::system_terms(x.x - C.Pm[0], x.y - C.Pm[1], x.z - C.Pm[2], q.x - C.Qm[0], q.y - C.Qm[1],
+                      q.z - C.Qm[2], xn.x + qn.x, xn.y + qn.y, xn.z + qn.z, t);
+    float *T = w.terms + (size_t)ci * smi::kNumSystem * w.maxSrc;
+    for (int k = 0; k < smi::kNumSystem; k++)
+        T[(size_t)k * w.maxSrc + i] = t[k];
+}
+
+// K5: reduce the normal equations, FP64 solve
+__global__ void __launch_bounds__(kT) k_solve(Work w, Stage s) {
+    __shared__ float red[kW][smi::kNumSystem][2];
+    const int        ci = blockIdx.x;
+    Cand            &C  = w.cand[ci];
+    if (!cand_live(C, s) || C.cnt < 6)
+        return;
+    const float *T = w.terms + (size_t)ci * smi::kNumSystem * w.maxSrc;
+    smi::KahanF  v[smi::kNumSystem];
+    slot_reduce<smi::kNumSystem>(w, s, ci,
+                                 [&](int i, float *t) {
+                                     for (int k = 0; k < smi::kNumSystem; k++)
+                                         t[k] = T[(size_t)k * w.maxSrc + i];
+                                 },
+                                 v, red);
+    if (threadIdx.x == 0) {
+        float sys[smi::kNumSystem];
+        for (int k = 0; k < smi::kNumSystem; k++)
+            sys[k] = v[k].value();
+        C.step = smi::solve_step(sys, C.Pm, C.Qm);
+    }
+}
+
+// K6: residual distance of each pair after the step
+__global__ void __launch_bounds__(kT) k_resid(Work w, Stage s) {
+    const int   ci = blockIdx.y;
+    const Cand &C  = w.cand[ci];
+    if (!cand_live(C, s) || C.cnt < 6)
+        return;
+    const int i = blockIdx.x * kT + threadIdx.x;
+    if (i >= s.n)
+        return;
+    const size_t o = (size_t)ci * w.maxSrc + i;
+    if (w.nnId[o] < 0)
+        return;
+    const float4 x = w.x4[o];
+    float        y0, y1, y2, d;
+    smi::pose_apply(C.step, x.x, x.y, x.z, y0, y1, y2);
+    grid_nn(s.G, w.pos, y0, y1, y2, FLT_MAX, d);
+    w.terms[(size_t)ci * smi::kNumSystem * w.maxSrc + i] = smm::fsqrt(d);
+}
+
+// K7: mean residual, the regist loop logic (icp.cpp:233-272), winner reset
+__global__ void __launch_bounds__(kT) k_update(Work w, Stage s) {
+    __shared__ float red[kW][1][2];
+    const int        ci = blockIdx.x;
+    Cand            &C  = w.cand[ci];
+    if (!cand_live(C, s))
+        return;
+    const int cnt = C.cnt;
+    float     mse = FLT_MAX;
+    if (cnt >= 6) {
+        const float *D = w.terms + (size_t)ci * smi::kNumSystem * w.maxSrc;
+        smi::KahanF  v[1];
+        slot_reduce<1>(w, s, ci, [&](int i, float *t) { t[0] = D[i]; }, v, red);
+        if (threadIdx.x == 0)
+            mse = smm::fdiv(v[0].value(), (float)cnt);
+    }
+    const int *nnR = w.nnR + (size_t)ci * w.maxSrc;
+    for (int i = threadIdx.x; i < s.n; i += kT)
+        if (nnR[i] >= 0)
+            w.win[(size_t)ci * w.maxDst + nnR[i]] = ~0ull;
+    if (threadIdx.x != 0)
+        return;
+    if (w.trace && C.iterations < kTraceIters) {
+        float *t = w.trace + (size_t)ci * kTraceFloats + (s.traceOff * kTraceIters + C.iterations) * 4;
+        t[0]     = (float)cnt;
+        t[1]     = mse;
+        t[2]     = cnt >= 6 ? C.Pm[0] : -1.0f;
+        t[3]     = cnt >= 6 ? C.step.m[3] : 0.0f;
+    }
+    if (cnt > 6 && mse < s.mseMax)
+        C.converged = 1;
+    int stop = 0;
+    if (cnt < 6) {
+        stop = 1;
+    } else {
+        if (mse < s.mseMin)
+            stop = 1;
+        const float rate = smm::fdiv(C.resMse - mse, C.resMse);
+        if (rate < 0.05f)
+            stop = 1;
+        if (C.iterations++ >= s.iters)
+            stop = 1;
+        if (rate > 0.0f) {
+            C.resMse = mse;
+            C.M      = smi::pose_mul(C.step, C.M);
+        }
+    }
+    C.stop = stop;
+}
+
+__global__ void k_init(Work w, const float *__restrict__ cands, int ncand, float voteThreshold,
+                       int sparse) {
+    const int ci = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ci >= ncand)
+        return;
+    Cand        &C = w.cand[ci];
+    const float *P = cands + (size_t)ci * smi::kPoseFloats;
+    for (int e = 0; e < 12; e++)
+        C.M.m[e] = P[e];
+    C.keep   = C.M;
+    C.score  = P[17];
+    C.status = P[17] < voteThreshold ? 1 : 0;
+    C.active = (C.status == 0 && sparse) ? 1 : 0;
+    if (w.trace)
+        for (int e = 0; e < kTraceFloats; e++)
+            w.trace[(size_t)ci * kTraceFloats + e] = -1.0f;
+}
+
+__global__ void k_stage_begin(Work w, int ncand) {
+    const int ci = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ci >= ncand)
+        return;
+    Cand &C      = w.cand[ci];
+    C.resMse     = FLT_MAX;
+    C.iterations = 0;
+    C.converged  = 0;
+    C.stop       = 0;
+    C.inl        = 0;
+}
+
+// After a refinement: failed candidates get their status; converged ones keep the pose.
+__global__ void k_stage_end(Work w, int ncand, int failStatus) {
+    const int ci = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ci >= ncand)
+        return;
+    Cand &C = w.cand[ci];
+    if (!C.active)
+        return;
+    if (!C.converged) {
+        C.status = failStatus;
+        C.active = 0;
+    } else {
+        C.keep = C.M;
+    }
+}
+
+__global__ void __launch_bounds__(kT) k_inliers(Work w, const float4 *__restrict__ src, int n,
+                                                GridView F, float r2) {
+    __shared__ int sc[kW];
+    const int      ci = blockIdx.y;
+    const Cand    &C  = w.cand[ci];
+    if (!C.active)
+        return;
+    const int i = blockIdx.x * kT + threadIdx.x;
+    int       c = 0;
+    if (i < n) {
+        float x, y, z;
+        smi::pose_apply(C.M, src[i].x, src[i].y, src[i].z, x, y, z);
+        c = grid_any_within(F, w.pos, x, y, z, r2) ? 1 : 0;
+    }
+    c = __reduce_add_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31) == 0)
+        sc[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int k = 0; k < kW; k++)
+            t += sc[k];
+        if (t)
+            atomicAdd(&w.cand[ci].inl, t);
+    }
+}
+
+__global__ void k_score(Work w, int ncand, int n, float minScore, int failStatus, int slot) {
+    const int ci = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ci >= ncand)
+        return;
+    Cand &C = w.cand[ci];
+    if (!C.active)
+        return;
+    if (w.trace)
+        w.trace[(size_t)ci * kTraceFloats + 2 * kTraceIters * 4 + slot] = (float)C.inl;
+    C.score = fminf(1.0f, smm::fdiv((float)C.inl, (float)n));
+    if (C.score < minScore) {
+        C.status = failStatus;
+        C.active = 0;
+    }
+}
+
+__global__ void k_finish(Work w, int ncand, int refine, float minScore, int *status, float *score,
+                         float *pose) {
+    const int ci = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ci >= ncand)
+        return;
+    Cand &C = w.cand[ci];
+    if (!C.status && refine && C.score < minScore)
+        C.status = 5;
+    status[ci] = C.status;
+    score[ci]  = C.status ? -1.0f : C.score;
+    for (int e = 0; e < 12; e++)
+        pose[(size_t)ci * 12 + e] = C.keep.m[e];
 }
 
 __global__ void k_rank(const int *__restrict__ ids, int m, int *__restrict__ rank) {
@@ -315,50 +425,79 @@ __global__ void k_rank(const int *__restrict__ ids, int m, int *__restrict__ ran
         rank[ids[i]] = i;
 }
 
-} // namespace
-
-void icp_all(Ctx &c, const Model &m, const IcpScene &s, const IcpParams &p, const float *cands,
-             int ncand, int *status, float *score, float *pose) {
-    if (ncand <= 0)
-        return;
-    IcpArgs a;
-    a.sp    = m.sp;
-    a.sn    = m.sn;
-    a.rp    = m.rp;
-    a.rn    = m.rn;
-    a.ns    = m.ns;
-    a.nr    = m.nr;
-    a.pos   = s.pos;
-    a.nrm   = s.nrm;
-    a.gS    = s.sampled.view();
-    a.gR    = s.resampled.view();
-    a.gF    = s.full.view();
-    a.nS    = std::max(s.sampled.m, 1);
-    a.nR    = std::max(s.resampled.m, 1);
-    a.p     = p;
-    a.cands = cands;
-    a.ncand = ncand;
-    a.status = status;
-    a.score  = score;
-    a.pose   = pose;
-    // point id -> subset rank (the grids' id lists are cell-major, so rank by subset order)
-    a.rankS = s.rankS;
-    a.rankR = s.rankR;
-    a.maxSrc = std::max(m.ns, m.nr);
-    const int wave = std::min(ncand, 2 * 152);
-    a.nnId = c.arena.get<int>("icp.nnId", (size_t)wave * a.maxSrc);
-    a.nnR  = c.arena.get<int>("icp.nnR", (size_t)wave * a.maxSrc);
-    a.x4   = c.arena.get<float4>("icp.x4", (size_t)wave * a.maxSrc);
-    a.n4   = c.arena.get<float4>("icp.n4", (size_t)wave * a.maxSrc);
-    a.winS = c.arena.get<unsigned long long>("icp.winS", (size_t)wave * a.nS);
-    a.winR = c.arena.get<unsigned long long>("icp.winR", (size_t)wave * a.nR);
-    SM_CUDA(cudaMemsetAsync(a.winS, 0xff, (size_t)wave * a.nS * 8, c.stream));
-    SM_CUDA(cudaMemsetAsync(a.winR, 0xff, (size_t)wave * a.nR * 8, c.stream));
-    for (int w0 = 0; w0 < ncand; w0 += wave) {
-        a.wave0 = w0;
-        k_icp<<<std::min(wave, ncand - w0), kT, 0, c.stream>>>(a);
+void run_stage(Ctx &c, Work &w, const Stage &s, int ncand) {
+    const dim3 g2(s.nb, ncand);
+    k_stage_begin<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand);
+    SM_LAUNCH_CHECK();
+    for (int it = 0; it < s.iters; it++) {
+        k_corr<<<g2, kT, 0, c.stream>>>(w, s);
+        SM_LAUNCH_CHECK();
+        k_pairs<<<g2, kT, 0, c.stream>>>(w, s);
+        SM_LAUNCH_CHECK();
+        k_centroids<<<ncand, kT, 0, c.stream>>>(w, s);
+        SM_LAUNCH_CHECK();
+        k_sys_terms<<<g2, kT, 0, c.stream>>>(w, s);
+        SM_LAUNCH_CHECK();
+        k_solve<<<ncand, kT, 0, c.stream>>>(w, s);
+        SM_LAUNCH_CHECK();
+        k_resid<<<g2, kT, 0, c.stream>>>(w, s);
+        SM_LAUNCH_CHECK();
+        k_update<<<ncand, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
     }
+}
+
+} // namespace
+
+void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, const float *cands,
+             int ncand, int *status, float *score, float *pose, float *trace) {
+    if (ncand <= 0)
+        return;
+    Work w;
+    w.pos    = sc.pos;
+    w.nrm    = sc.nrm;
+    w.maxSrc = std::max(std::max(m.ns, m.nr), 1);
+    w.maxDst = std::max(std::max(sc.sampled.m, sc.resampled.m), 1);
+    w.cand   = c.arena.get<Cand>("icp.cand", ncand);
+    w.nnId   = c.arena.get<int>("icp.nnId", (size_t)ncand * w.maxSrc);
+    w.nnR    = c.arena.get<int>("icp.nnR", (size_t)ncand * w.maxSrc);
+    w.x4     = c.arena.get<float4>("icp.x4", (size_t)ncand * w.maxSrc);
+    w.n4     = c.arena.get<float4>("icp.n4", (size_t)ncand * w.maxSrc);
+    w.terms  = c.arena.get<float>("icp.terms", (size_t)ncand * smi::kNumSystem * w.maxSrc);
+    w.win    = c.arena.get<unsigned long long>("icp.win", (size_t)ncand * w.maxDst);
+    w.trace  = trace;
+    SM_CUDA(cudaMemsetAsync(w.win, 0xff, (size_t)ncand * w.maxDst * 8, c.stream));
+    k_init<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, cands, ncand, p.voteThreshold, p.sparse);
+    SM_LAUNCH_CHECK();
+    const float rej2 = p.rejectDist * p.rejectDist;
+    const float sc2  = p.scoreDist * p.scoreDist;
+    if (p.sparse) {
+        Stage s{m.sp, m.sn, m.ns, nblocks(m.ns, kT), sc.sampled.view(), sc.rankS,
+                sc.sampled.m, 5, p.sampleStep * 0.5f, p.sampleStep, rej2, 0};
+        run_stage(c, w, s, ncand);
+        k_stage_end<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, 2);
+        SM_LAUNCH_CHECK();
+        k_inliers<<<dim3(nblocks(m.ns, kT), ncand), kT, 0, c.stream>>>(w, m.sp, m.ns,
+                                                                       sc.full.view(), sc2);
+        SM_LAUNCH_CHECK();
+        k_score<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, m.ns, p.minScore, 3, 0);
+        SM_LAUNCH_CHECK();
+        if (p.dense) {
+            Stage d{m.rp, m.rn, m.nr, nblocks(m.nr, kT), sc.resampled.view(), sc.rankR,
+                    sc.resampled.m, p.denseSteps, p.reSampleStep * 0.5f, p.sampleStep, rej2, 1};
+            run_stage(c, w, d, ncand);
+            k_stage_end<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, 4);
+            SM_LAUNCH_CHECK();
+            k_inliers<<<dim3(nblocks(m.nr, kT), ncand), kT, 0, c.stream>>>(w, m.rp, m.nr,
+                                                                           sc.full.view(), sc2);
+            SM_LAUNCH_CHECK();
+            k_score<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, m.nr, p.minScore, 5, 1);
+            SM_LAUNCH_CHECK();
+        }
+    }
+    k_finish<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, (p.sparse || p.dense) ? 1 : 0,
+                                                         p.minScore, status, score, pose);
+    SM_LAUNCH_CHECK();
 }
 
 void subset_rank(Ctx &c, const int *ids, int m, int *rank) {

@@ -85,7 +85,7 @@ __device__ __forceinline__ int grid_knn(const GridView &G, const float4 *__restr
             od[i] = d;
             oi[i] = id;
         });
-        const float b = smg::ring_bound(s + 1, G.g);
+        const float b = smg::ring_bound(s, G.g);
         if (n == k && od[k - 1] < b * b)
             break;
     }
@@ -110,7 +110,7 @@ __device__ __forceinline__ int grid_nn(const GridView &G, const float4 *__restri
                 best = id;
             }
         });
-        const float b = smg::ring_bound(s + 1, G.g);
+        const float b = smg::ring_bound(s, G.g);
         if (best >= 0 && bd < b * b)
             break;
         if (b * b > limit2)
@@ -136,7 +136,7 @@ __device__ __forceinline__ bool grid_any_within(const GridView &G, const float4 
         });
         if (hit)
             return true;
-        const float b = smg::ring_bound(s + 1, G.g);
+        const float b = smg::ring_bound(s, G.g);
         if (b * b >= r2)
             break;
     }

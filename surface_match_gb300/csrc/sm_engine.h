@@ -27,7 +27,13 @@ struct Error : std::runtime_error {
             throw ::sm::Error(SM_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));   \
     } while (0)
 
-#define SM_LAUNCH_CHECK() SM_CUDA(cudaGetLastError())
+// Kernel launches issued by the library (all contexts); read by sm_launch_count().
+extern long long g_launches;
+#define SM_LAUNCH_CHECK()                                                                      \
+    do {                                                                                       \
+        __atomic_add_fetch(&::sm::g_launches, 1, __ATOMIC_RELAXED);                            \
+        SM_CUDA(cudaGetLastError());                                                           \
+    } while (0)
 
 inline int nblocks(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 

@@ -54,8 +54,9 @@ SM_HD int coord(float x, float origin, float g, int dim) {
 
 SM_HD int phase_of(int cx, int cy, int cz) { return (cx & 1) | ((cy & 1) << 1) | ((cz & 1) << 2); }
 
-// Lower bound (with a 1% cell margin for rounding) of the distance from a query in cell
-// `c` to any point outside the block of cells within Chebyshev radius s of it.
+// After the cells within Chebyshev radius s of the query's cell have been searched, every
+// other point lies at least s cells' width away from the query: lower bound s * g, less a
+// 1% cell margin for the rounding of cell coordinates.
 SM_HD float ring_bound(int s, float g) { return s <= 0 ? 0.0f : ((float)s - 0.01f) * g; }
 
 } // namespace smg

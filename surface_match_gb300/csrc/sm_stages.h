@@ -92,6 +92,7 @@ struct IcpParams {
 // rank[ids[i]] = i
 void subset_rank(Ctx &c, const int *ids, int m, int *rank);
 void icp_all(Ctx &c, const Model &m, const IcpScene &s, const IcpParams &p, const float *cands,
-             int ncand, int *status, float *score, float *pose);
+             int ncand, int *status, float *score, float *pose, float *trace = nullptr);
+constexpr int kIcpTraceFloats = 2 * 32 * 4 + 2; // per candidate, see icp.cu
 
 } // namespace sm

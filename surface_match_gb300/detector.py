@@ -291,7 +291,7 @@ class Detector:
     _DEBUG = {0: (np.int32, 1), 1: (np.int32, 1), 2: (np.int32, 1), 3: (np.float32, 3),
               4: (np.float32, 3), 7: (np.int64, 8), 8: (np.float32, 9), 9: (np.float32, 18),
               10: (np.float32, 18), 12: (np.int32, 1), 13: (np.float32, 1),
-              14: (np.float32, 12)}
+              14: (np.float32, 12), 15: (np.float32, 258)}
 
     def debug(self, field_id: int):
         """Intermediate state of the last matchScene (field ids as sm_debug_get)."""

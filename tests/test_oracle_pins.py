@@ -179,3 +179,38 @@ def test_oracle_reproduces_committed_stage_goldens(tag):
     np.testing.assert_array_equal(r.kp_stats, g[f"{tag}_kp_stats"])
     np.testing.assert_array_equal(r.kp_cands, g[f"{tag}_kp_cands"])
     np.testing.assert_array_equal(r.results, g[f"{tag}_results"])
+
+
+@pytest.mark.parametrize("cell", [0.05, 0.13, 0.5, 2.0])
+def test_grid_searches_are_exact_for_any_cell_size(oracle_lib, cell):
+    """k nearest (ties by index), nearest within a limit and any-within-radius on the
+    uniform grid equal brute force, whatever the cell size (the GPU uses the same
+    search-termination rule)."""
+    L = oracle_lib
+    L.orc_grid_probe.argtypes = [f32p, C.c_int64, f32p, C.c_int64, C.c_float, C.c_int,
+                                 C.c_float, C.c_float, i32p, f32p, i32p, f32p, i32p]
+    rng = np.random.default_rng(5)
+    P = np.ascontiguousarray(np.concatenate([rng.uniform(-1, 1, (3000, 3)),
+                                             np.round(rng.uniform(-1, 1, (500, 3)) * 4) / 4])
+                             .astype(np.float32))
+    Q = np.ascontiguousarray(np.concatenate([P[rng.integers(len(P), size=200)] +
+                                             rng.normal(0, 0.05, (200, 3)),
+                                             rng.uniform(-1.5, 1.5, (100, 3))])
+                             .astype(np.float32))
+    k, lim2, r2 = 10, np.float32(0.3 ** 2), np.float32(0.07 ** 2)
+    ki, kd = np.zeros((len(Q), k), np.int32), np.zeros((len(Q), k), np.float32)
+    ni, nd = np.zeros(len(Q), np.int32), np.zeros(len(Q), np.float32)
+    wi = np.zeros(len(Q), np.int32)
+    L.orc_grid_probe(P.ctypes.data_as(f32p), len(P), Q.ctypes.data_as(f32p), len(Q), cell, k,
+                     lim2, r2, ki.ctypes.data_as(i32p), kd.ctypes.data_as(f32p),
+                     ni.ctypes.data_as(i32p), nd.ctypes.data_as(f32p), wi.ctypes.data_as(i32p))
+    d = Q[:, None, :] - P[None, :, :]  # same float formula: ((d0^2 + d1^2) + d2^2)
+    d2 = (d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1]) + d[..., 2] * d[..., 2]
+    order = np.lexsort((np.broadcast_to(np.arange(len(P)), d2.shape), d2), axis=1)
+    np.testing.assert_array_equal(ki, order[:, :k])
+    np.testing.assert_array_equal(kd, np.take_along_axis(d2, order[:, :k], 1))
+    best = order[:, 0]
+    bd = d2[np.arange(len(Q)), best]
+    inlim = bd <= lim2
+    np.testing.assert_array_equal(ni[inlim], best[inlim])
+    np.testing.assert_array_equal(wi, (d2 < r2).any(1).astype(np.int32))
