@@ -157,6 +157,24 @@ SM_API int sm_vote_stage(sm_model model, const float *points, const float *norma
                          const int32_t *nbr_ids, float minScore, int64_t *out_stats,
                          float *out_cands, float *out_poses, int dump_k, int32_t *out_acc);
 
+/* sm_vote_stage for callers that cannot allocate device memory: a plugin inside a host
+ * framework that owns all device memory and forbids allocation while its work runs, or a
+ * latency-critical loop that cannot take cudaMalloc's implicit synchronisation. No
+ * counterpart in the reference (its voting loop, ppf.cpp:247-409, allocates per call).
+ * Same arguments, meaning and results as sm_vote_stage, except that every pointer is a
+ * DEVICE pointer owned by the caller (nbr_ids holding nbr_off[K] entries), and out_poses
+ * is required. The call allocates nothing: its staging lives in a fixed array in the
+ * library's device image (about 4.8 MiB, held on every GPU that loads the library until
+ * the process exits), which limits a call to n <= 131072 points and K <= 65536 keypoints;
+ * larger sizes return SM_ERR_CAPACITY. The first call on a device resolves that array's
+ * address, so make it before any stream capture. All calls share the array: calls whose
+ * GPU work overlaps race on it. Returns after the results are written. */
+SM_API int sm_vote_stage_noalloc(sm_model model, const float *points, const float *normals,
+                                 int64_t n, const int32_t *keypoints, int64_t K,
+                                 const int32_t *nbr_off, const int32_t *nbr_ids, float minScore,
+                                 int64_t *out_stats, float *out_cands, float *out_poses,
+                                 int dump_k, int32_t *out_acc);
+
 /* Intermediate state of the last sm_match on this model's context, for inspection and
  * parity checks. Fields: 0 sampled ids, 1 keypoint ids, 2 resampled ids (int32);
  * 3 positions, 4 normals (float x3, after normal estimation); 7 per-keypoint stats

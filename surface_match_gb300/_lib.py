@@ -69,6 +69,8 @@ _SIGNATURES = {
                            C.POINTER(MatchStatsC)]),
     "sm_vote_stage": (C.c_int, [_vp, _f32p, _f32p, C.c_int64, _i32p, C.c_int64, _i32p, _i32p,
                                 C.c_float, _i64p, _f32p, _f32p, C.c_int, _i32p]),
+    "sm_vote_stage_noalloc": (C.c_int, [_vp, _vp, _vp, C.c_int64, _vp, C.c_int64, _vp, _vp,
+                                        C.c_float, _vp, _vp, _vp, C.c_int, _vp]),
     "sm_debug_size": (C.c_int64, [_vp, C.c_int]),
     "sm_debug_get": (C.c_int, [_vp, C.c_int, _vp]),
     "sm_last_error": (C.c_char_p, []),

@@ -577,6 +577,11 @@ void put_cloud(std::string &o, const std::vector<float> &p, const std::vector<fl
 }
 
 } // namespace
+
+Model *model_core(sm_model m) { return &m->m; }
+Ctx   *model_ctx(sm_model m) { return &m->ctx->ctx; }
+int    run_guarded(const std::function<void()> &f) { return guarded(f); }
+
 } // namespace sm
 
 using namespace sm;

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -94,5 +95,11 @@ void subset_rank(Ctx &c, const int *ids, int m, int *rank);
 void icp_all(Ctx &c, const Model &m, const IcpScene &s, const IcpParams &p, const float *cands,
              int ncand, int *status, float *score, float *pose, float *trace = nullptr);
 constexpr int kIcpTraceFloats = 2 * 32 * 4 + 2; // per candidate, see icp.cu
+
+// Access to a model handle's engine state and the C ABI's error handling, for entry points
+// defined outside api.cu.
+Model *model_core(sm_model m);
+Ctx   *model_ctx(sm_model m);
+int    run_guarded(const std::function<void()> &f);
 
 } // namespace sm
