@@ -221,14 +221,14 @@ std::vector<float> download4(const float4 *d, int n) {
 // Query-grid cell for k-nearest-neighbour searches: about 1.3x the expected k-NN radius,
 // from the point density the greedy sampling reveals (n_sampled points at `step` cover an
 // area of about n_sampled * step^2 / 0.7). Results do not depend on it, only run time.
-float knn_cell(int nvalid, int nsampled, float step, int k, const float ext[3]) {
+float knn_cell(int nvalid, int nsampled, float step, int k) {
     float g = step * 0.25f;
     if (nvalid > 0 && nsampled > 0) {
         const double area = (double)nsampled * step * step / 0.7;
         const double rk   = std::sqrt((double)std::max(k, 3) * area / (3.14159265 * nvalid));
         g = (float)std::min<double>(std::max<double>(1.3 * rk, step * 0.1), step);
     }
-    return smg::query_cell(g, ext);
+    return g;
 }
 
 // trainModel (ppf.cpp:36-147) with the device sampler, normal estimation and pair kernel;
@@ -263,13 +263,12 @@ void train(Ctx &c, Model &m, const float *xyzIn, const float *nrmIn, int64_t n64
     const int   n1 = sample_points(c, pos, n, valid, nvalid, box, sampleStep, idx1, "t.s1");
     const int   n2 = sample_points(c, pos, n, valid, nvalid, box, reSampleStep, idx2, "t.s2");
     if (!nrmIn) {
-        float ext[3] = {box.ext(0), box.ext(1), box.ext(2)};
-        Grid  q;
-        const float gq = knn_cell(nvalid, n1, sampleStep, tp.knnNormal, ext);
-        build_grid(c, pos, valid, nvalid, box, gq, false, q, "t.q");
+        HGrid q;
+        const float gq = knn_cell(nvalid, n1, sampleStep, tp.knnNormal);
+        build_hgrid(c, pos, valid, nvalid, box, gq, q, "t.q");
         estimate_normals(c, pos, nrm, n, idx1, n1, q, tp.knnNormal, tp.smoothNormal != 0, false,
                          nullptr, "t.n1");
-        build_grid(c, pos, valid, nvalid, box, gq, false, q, "t.q");
+        build_hgrid(c, pos, valid, nvalid, box, gq, q, "t.q");
         estimate_normals(c, pos, nrm, n, idx2, n2, q, tp.knnNormal, tp.smoothNormal != 0, false,
                          nullptr, "t.n2");
     }
@@ -379,10 +378,10 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
     const float sampleStep   = diam * sdRel;
     int        *sampled      = c.arena.get<int>("m.sampled", std::max(n, 1));
     const int   ns = sample_points(c, pos, n, valid, nvalid, box, sampleStep, sampled, "m.s1");
-    Grid        q;
-    const float gq = knn_cell(nvalid, ns, sampleStep, mp.knnNormal, ext);
+    HGrid       q;
+    const float gq = knn_cell(nvalid, ns, sampleStep, mp.knnNormal);
     if (!hasN) {
-        build_grid(c, pos, valid, nvalid, box, gq, false, q, "m.q");
+        build_hgrid(c, pos, valid, nvalid, box, gq, q, "m.q");
         estimate_normals(c, pos, nrm, n, sampled, ns, q, mp.knnNormal, mp.smoothNormal != 0,
                          mp.invertNormal != 0, vp, "m.n1");
     }
@@ -435,7 +434,7 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
     if (mp.densePoseRefinement) {
         nres = sample_points(c, pos, n, valid, nvalid, box, reSampleStep, resampled, "m.s3");
         if (!hasN) {
-            build_grid(c, pos, valid, nvalid, box, gq, false, q, "m.q");
+            build_hgrid(c, pos, valid, nvalid, box, gq, q, "m.q");
             estimate_normals(c, pos, nrm, n, resampled, nres, q, mp.knnNormal, false,
                              mp.invertNormal != 0, vp, "m.n2");
         }
@@ -443,14 +442,13 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
     IcpScene s;
     s.pos          = pos;
     s.nrm          = nrm;
-    // nearest-neighbour grids of the refinement: about half (sparse) or a third (dense) of
-    // the rejection distance, so a query needs few cell shells either way
-    const float gs = std::max(sampleStep, refDist / 2.0f);
-    build_grid(c, pos, sampled, ns, box, smg::query_cell(gs, ext), false, s.sampled, "m.gS");
-    const float gr = std::max(2.0f * reSampleStep, refDist / 3.0f);
-    build_grid(c, pos, resampled, nres, box, smg::query_cell(gr, ext), false, s.resampled, "m.gR");
-    const float gf = std::max(scoreDist, gq);
-    build_grid(c, pos, valid, nvalid, box, smg::query_cell(gf, ext), false, s.full, "m.gF");
+    // Nearest-neighbour grids of the refinement: cells of about a third of the rejection
+    // distance (never finer than the subset's spacing), so three cell shells always cover
+    // it. The inlier grid's cell just exceeds the scoring distance, so two shells decide.
+    build_hgrid(c, pos, sampled, ns, box, std::max(sampleStep, refDist / 2.98f), s.sampled, "m.gS");
+    build_hgrid(c, pos, resampled, nres, box, std::max(2.0f * reSampleStep, refDist / 2.98f),
+                s.resampled, "m.gR");
+    build_hgrid(c, pos, valid, nvalid, box, std::max(scoreDist * 1.02f, gq), s.full, "m.gF");
     int *rankS = c.arena.get<int>("m.rankS", n);
     int *rankR = c.arena.get<int>("m.rankR", n);
     subset_rank(c, sampled, ns, rankS);

@@ -39,7 +39,7 @@ struct Cand {
 struct Stage {
     const float4 *src, *srcN; // model points / normals
     int           n, nb;      // points, CTAs per candidate
-    GridView      G;          // scene subset grid
+    HGridView     G;          // scene subset grid
     const int    *rank;       // point id -> subset index
     int           nDst;
     int           iters;
@@ -68,31 +68,33 @@ __device__ __forceinline__ bool cand_live(const Cand &c, const Stage &s) {
     return c.active && !c.stop && c.iterations < s.iters;
 }
 
-// K1: correspondences
+// K1: correspondences, one warp per source point (warp-cooperative grid search)
 __global__ void __launch_bounds__(kT) k_corr(Work w, Stage s) {
     const int   ci = blockIdx.y;
     const Cand &C  = w.cand[ci];
     if (!cand_live(C, s))
         return;
-    const int i = blockIdx.x * kT + threadIdx.x;
-    if (i >= s.n)
-        return;
-    const size_t o = (size_t)ci * w.maxSrc + i;
-    float4       x, y;
-    smi::pose_apply(C.M, s.src[i].x, s.src[i].y, s.src[i].z, x.x, x.y, x.z);
-    smi::pose_rotate(C.M, s.srcN[i].x, s.srcN[i].y, s.srcN[i].z, y.x, y.y, y.z);
-    float      d;
-    const int  j  = grid_nn(s.G, w.pos, x.x, x.y, x.z, s.rej2, d);
-    const bool ok = j >= 0 && d <= s.rej2;
-    x.w           = d;
-    y.w           = 0.0f;
-    w.x4[o]       = x;
-    w.n4[o]       = y;
-    w.nnId[o]     = ok ? j : -1;
-    const int r   = ok ? s.rank[j] : -1;
-    w.nnR[o]      = r;
-    if (ok)
-        atomicMin(&w.win[(size_t)ci * w.maxDst + r], win_key(d, i));
+    const int lane = threadIdx.x & 31;
+    for (int i = blockIdx.x * kW + (threadIdx.x >> 5); i < s.n; i += gridDim.x * kW) {
+        const size_t o = (size_t)ci * w.maxSrc + i;
+        float4       x, y;
+        smi::pose_apply(C.M, s.src[i].x, s.src[i].y, s.src[i].z, x.x, x.y, x.z);
+        smi::pose_rotate(C.M, s.srcN[i].x, s.srcN[i].y, s.srcN[i].z, y.x, y.y, y.z);
+        float      d;
+        const int  j  = warp_nn(s.G, w.pos, x.x, x.y, x.z, s.rej2, d);
+        const bool ok = j >= 0 && d <= s.rej2;
+        if (lane == 0) {
+            x.w       = d;
+            y.w       = 0.0f;
+            w.x4[o]   = x;
+            w.n4[o]   = y;
+            w.nnId[o] = ok ? j : -1;
+            const int r = ok ? s.rank[j] : -1;
+            w.nnR[o]    = r;
+            if (ok)
+                atomicMin(&w.win[(size_t)ci * w.maxDst + r], win_key(d, i));
+        }
+    }
 }
 
 // K2: keep only the closest source point per scene point
@@ -247,23 +249,23 @@ __global__ void __launch_bounds__(kT) k_solve(Work w, Stage s) {
     }
 }
 
-// K6: residual distance of each pair after the step
+// K6: residual distance of each pair after the step, one warp per pair
 __global__ void __launch_bounds__(kT) k_resid(Work w, Stage s) {
     const int   ci = blockIdx.y;
     const Cand &C  = w.cand[ci];
     if (!cand_live(C, s) || C.cnt < 6)
         return;
-    const int i = blockIdx.x * kT + threadIdx.x;
-    if (i >= s.n)
-        return;
-    const size_t o = (size_t)ci * w.maxSrc + i;
-    if (w.nnId[o] < 0)
-        return;
-    const float4 x = w.x4[o];
-    float        y0, y1, y2, d;
-    smi::pose_apply(C.step, x.x, x.y, x.z, y0, y1, y2);
-    grid_nn(s.G, w.pos, y0, y1, y2, FLT_MAX, d);
-    w.terms[(size_t)ci * smi::kNumSystem * w.maxSrc + i] = smm::fsqrt(d);
+    for (int i = blockIdx.x * kW + (threadIdx.x >> 5); i < s.n; i += gridDim.x * kW) {
+        const size_t o = (size_t)ci * w.maxSrc + i;
+        if (w.nnId[o] < 0)
+            continue;
+        const float4 x = w.x4[o];
+        float        y0, y1, y2, d;
+        smi::pose_apply(C.step, x.x, x.y, x.z, y0, y1, y2);
+        warp_nn(s.G, w.pos, y0, y1, y2, FLT_MAX, d);
+        if ((threadIdx.x & 31) == 0)
+            w.terms[(size_t)ci * smi::kNumSystem * w.maxSrc + i] = smm::fsqrt(d);
+    }
 }
 
 // K7: mean residual, the regist loop logic (icp.cpp:233-272), winner reset
@@ -363,7 +365,7 @@ __global__ void k_stage_end(Work w, int ncand, int failStatus) {
 }
 
 __global__ void __launch_bounds__(kT) k_inliers(Work w, const float4 *__restrict__ src, int n,
-                                                GridView F, float r2) {
+                                                HGridView F, float r2) {
     __shared__ int sc[kW];
     const int      ci = blockIdx.y;
     const Cand    &C  = w.cand[ci];
@@ -427,10 +429,11 @@ __global__ void k_rank(const int *__restrict__ ids, int m, int *__restrict__ ran
 
 void run_stage(Ctx &c, Work &w, const Stage &s, int ncand) {
     const dim3 g2(s.nb, ncand);
+    const dim3 gw(std::max(1, nblocks(s.n, kW * 4)), ncand); // warp kernels: 4 points per warp
     k_stage_begin<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand);
     SM_LAUNCH_CHECK();
     for (int it = 0; it < s.iters; it++) {
-        k_corr<<<g2, kT, 0, c.stream>>>(w, s);
+        k_corr<<<gw, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
         k_pairs<<<g2, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
@@ -440,7 +443,7 @@ void run_stage(Ctx &c, Work &w, const Stage &s, int ncand) {
         SM_LAUNCH_CHECK();
         k_solve<<<ncand, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
-        k_resid<<<g2, kT, 0, c.stream>>>(w, s);
+        k_resid<<<gw, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
         k_update<<<ncand, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
@@ -472,8 +475,8 @@ void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, con
     const float rej2 = p.rejectDist * p.rejectDist;
     const float sc2  = p.scoreDist * p.scoreDist;
     if (p.sparse) {
-        Stage s{m.sp, m.sn, m.ns, nblocks(m.ns, kT), sc.sampled.view(), sc.rankS,
-                sc.sampled.m, 5, p.sampleStep * 0.5f, p.sampleStep, rej2, 0};
+        Stage s{m.sp, m.sn, m.ns, nblocks(m.ns, kT), sc.sampled.view(), sc.rankS, sc.sampled.m, 5,
+                p.sampleStep * 0.5f, p.sampleStep, rej2, 0};
         run_stage(c, w, s, ncand);
         k_stage_end<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, 2);
         SM_LAUNCH_CHECK();

@@ -347,26 +347,92 @@ __global__ void k_mark_todo(const int *__restrict__ ids, int m, const float4 *__
         need[id] = 2;
 }
 
-__global__ void k_knn(const int *__restrict__ list, int nl, GridView G, const float4 *__restrict__ pos,
+template <int K>
+__global__ void k_knn(const int *__restrict__ list, int nl, HGridView G, const float4 *__restrict__ pos,
                       int k, int *__restrict__ nbr, int *__restrict__ nbrCnt, int markNeighbours,
                       const float4 *__restrict__ nrm, int *__restrict__ need) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nl)
         return;
     const float4 q = pos[list[t]];
-    int          oi[kMaxKnn];
-    float        od[kMaxKnn];
-    const int    n = grid_knn(G, pos, q.x, q.y, q.z, k, oi, od);
-    for (int j = 0; j < k; j++)
-        nbr[(size_t)t * k + j] = j < n ? oi[j] : -1;
+    int          oi[K];
+    float        od[K];
+    const int    n = grid_knn<K>(G, pos, q.x, q.y, q.z, k, oi, od);
+#pragma unroll
+    for (int j = 0; j < K; j++)
+        if (j < k)
+            nbr[(size_t)t * k + j] = j < n ? oi[j] : -1;
     nbrCnt[t] = n;
     if (markNeighbours) {
-        for (int j = 0; j < n; j++) {
+#pragma unroll
+        for (int j = 0; j < K; j++) {
+            if (j >= n)
+                break;
             const int id = oi[j];
             if (need[id] == 0 && !finite3(nrm[id].x, nrm[id].y, nrm[id].z))
                 need[id] = 1;
         }
     }
+}
+
+void launch_knn(cudaStream_t st, const int *list, int nl, const HGridView &G, const float4 *pos,
+                int k, int *nbr, int *cnt, int mark, const float4 *nrm, int *need) {
+    if (nl <= 0)
+        return;
+    if (k <= 10)
+        k_knn<10><<<nblocks(nl, 128), 128, 0, st>>>(list, nl, G, pos, k, nbr, cnt, mark, nrm, need);
+    else if (k <= 16)
+        k_knn<16><<<nblocks(nl, 128), 128, 0, st>>>(list, nl, G, pos, k, nbr, cnt, mark, nrm, need);
+    else
+        k_knn<kMaxKnn><<<nblocks(nl, 128), 128, 0, st>>>(list, nl, G, pos, k, nbr, cnt, mark, nrm, need);
+    SM_LAUNCH_CHECK();
+}
+
+// ---- hashed grid build -----------------------------------------------------------------
+__device__ __forceinline__ unsigned long long hkey(const float4 &p, const GridParams &gp) {
+    const int cx = smg::coord(p.x, gp.org[0], gp.g, gp.dim[0]);
+    const int cy = smg::coord(p.y, gp.org[1], gp.g, gp.dim[1]);
+    const int cz = smg::coord(p.z, gp.org[2], gp.g, gp.dim[2]);
+    return ((unsigned long long)cz * (unsigned)gp.dim[1] + (unsigned)cy) * (unsigned)gp.dim[0] +
+           (unsigned)cx;
+}
+
+__global__ void k_hg_insert(const float4 *__restrict__ pos, const int *__restrict__ ids, int m,
+                            GridParams gp, unsigned long long *__restrict__ keys, uint32_t mask,
+                            int *__restrict__ slotOf, int *__restrict__ cnt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m)
+        return;
+    const unsigned long long key = hkey(pos[ids[i]], gp);
+    uint32_t                 h   = (uint32_t)smm::mix64(key) & mask;
+    for (uint32_t p = 0; p <= mask; p++) {
+        const unsigned long long prev = atomicCAS(&keys[h], ~0ull, key);
+        if (prev == ~0ull || prev == key) {
+            slotOf[i] = (int)h;
+            atomicAdd(&cnt[h], 1);
+            return;
+        }
+        h = (h + 1) & mask;
+    }
+}
+
+__global__ void k_hg_scatter(const int *__restrict__ ids, const int *__restrict__ slotOf, int m,
+                             int *__restrict__ fill, int *__restrict__ gids) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m)
+        return;
+    gids[atomicAdd(&fill[slotOf[i]], 1)] = ids[i];
+}
+
+__global__ void k_hg_pack_from_start(const unsigned long long *__restrict__ keys,
+                                     const int *__restrict__ start, uint32_t T,
+                                     uint4 *__restrict__ slot) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T)
+        return;
+    const unsigned long long k = keys[t];
+    slot[t] = make_uint4((uint32_t)k, (uint32_t)(k >> 32), (uint32_t)start[t],
+                         (uint32_t)(start[t + 1] - start[t]));
 }
 
 // Phase A: centroid and FP32-Kahan covariance of the neighbourhood, FP64 eigensolve.
@@ -603,6 +669,47 @@ void build_grid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &box
     }
 }
 
+void build_hgrid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &box, float g,
+                 HGrid &H, const std::string &tag) {
+    // cells per axis stay below 2^20 so that cell keys fit 60 bits (coarser cells if needed)
+    while (smg::dim_of(box.ext(0), g) >= (1 << 20) || smg::dim_of(box.ext(1), g) >= (1 << 20) ||
+           smg::dim_of(box.ext(2), g) >= (1 << 20))
+        g = g * 2.0f;
+    H.g = g;
+    for (int a = 0; a < 3; a++) {
+        H.org[a] = box.mn[a];
+        H.dim[a] = smg::dim_of(box.ext(a), g);
+    }
+    uint32_t T = 1024;
+    while (T < 2u * (uint32_t)std::max(m, 1))
+        T <<= 1;
+    H.mask = T - 1;
+    H.m    = m;
+    auto *keys   = c.arena.get<unsigned long long>(tag + ".keys", T);
+    int  *cnt    = c.arena.get<int>(tag + ".cnt", T + 1);
+    int  *start  = c.arena.get<int>(tag + ".start", T + 1);
+    int  *slotOf = c.arena.get<int>(tag + ".slotOf", std::max(m, 1));
+    H.ids        = c.arena.get<int>(tag + ".ids", std::max(m, 1));
+    H.slot       = c.arena.get<uint4>(tag + ".slot", T);
+    SM_CUDA(cudaMemsetAsync(keys, 0xff, (size_t)T * 8, c.stream));
+    SM_CUDA(cudaMemsetAsync(cnt, 0, (size_t)(T + 1) * 4, c.stream));
+    GridParams gp = grid_params(box, g, H.dim);
+    if (m > 0) {
+        k_hg_insert<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, m, gp, keys, H.mask, slotOf, cnt);
+        SM_LAUNCH_CHECK();
+    }
+    scan_excl(c, cnt, start, (long long)T + 1, tag, false);
+    int *fill = cnt;
+    SM_CUDA(cudaMemcpyAsync(fill, start, (size_t)T * 4, cudaMemcpyDeviceToDevice, c.stream));
+    if (m > 0) {
+        k_hg_scatter<<<nblocks(m, 256), 256, 0, c.stream>>>(ids, slotOf, m, fill, H.ids);
+        SM_LAUNCH_CHECK();
+    }
+    // counts again for the packed table: start[t+1] - start[t]
+    k_hg_pack_from_start<<<nblocks(T, 256), 256, 0, c.stream>>>(keys, start, T, H.slot);
+    SM_LAUNCH_CHECK();
+}
+
 int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m, const Box &box,
                   float step, int *outIds, const std::string &tag) {
     if (m <= 0)
@@ -663,7 +770,7 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
 }
 
 void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *ids, int m,
-                      const Grid &query, int k, bool smooth, bool invert, const float *vp,
+                      const HGrid &query, int k, bool smooth, bool invert, const float *vp,
                       const std::string &tag) {
     if (m <= 0)
         return;
@@ -679,11 +786,7 @@ void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *
     int  ntodo = compact_eq(c, need, npoints, 2, todo, tag + ".ct");
     int *nbrT  = c.arena.get<int>(tag + ".nbrT", (size_t)std::max(ntodo, 1) * k);
     int *cntT  = c.arena.get<int>(tag + ".cntT", std::max(ntodo, 1));
-    if (ntodo > 0) {
-        k_knn<<<nblocks(ntodo, 128), 128, 0, c.stream>>>(todo, ntodo, query.view(), pos, k, nbrT,
-                                                          cntT, smooth ? 1 : 0, nrm, need);
-        SM_LAUNCH_CHECK();
-    }
+    launch_knn(c.stream, todo, ntodo, query.view(), pos, k, nbrT, cntT, smooth ? 1 : 0, nrm, need);
     int  nextra = 0;
     int *extra = nullptr, *nbrE = nullptr, *cntE = nullptr;
     if (smooth && ntodo > 0) {
@@ -691,11 +794,7 @@ void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *
         nextra = compact_eq(c, need, npoints, 1, extra, tag + ".ce");
         nbrE   = c.arena.get<int>(tag + ".nbrE", (size_t)std::max(nextra, 1) * k);
         cntE   = c.arena.get<int>(tag + ".cntE", std::max(nextra, 1));
-        if (nextra > 0) {
-            k_knn<<<nblocks(nextra, 128), 128, 0, c.stream>>>(extra, nextra, query.view(), pos, k,
-                                                               nbrE, cntE, 0, nrm, need);
-            SM_LAUNCH_CHECK();
-        }
+        launch_knn(c.stream, extra, nextra, query.view(), pos, k, nbrE, cntE, 0, nrm, need);
     }
     const int nmax = std::max(ntodo, nextra);
     float4   *cen  = c.arena.get<float4>(tag + ".cen", 2 * (size_t)std::max(nmax, 1));

@@ -12,97 +12,159 @@ namespace smd {
 
 constexpr int kMaxKnn = 32; // largest supported knnNormal
 
-// Device view of a uniform grid over a subset of points: cells are stored cell-major as a
-// CSR (start[cell] .. start[cell+1] into ids).
+// Device view of a dense uniform grid over a subset of points: cells are stored cell-major
+// as a CSR (start[cell] .. start[cell+1] into ids). Used where per-cell state is needed
+// (the sampler).
 struct GridView {
     float      org[3];
     float      g;
     int        dim[3];
     const int *start;
     const int *ids;
+    __device__ __forceinline__ void range(int x, int y, int z, int &s, int &e) const {
+        const int c = (z * dim[1] + y) * dim[0] + x;
+        s           = start[c];
+        e           = start[c + 1];
+    }
 };
 
-__device__ __forceinline__ void grid_cc(const GridView &G, float x, float y, float z, int c[3]) {
-    c[0] = smg::coord(x, G.org[0], G.g, G.dim[0]);
-    c[1] = smg::coord(y, G.org[1], G.g, G.dim[1]);
-    c[2] = smg::coord(z, G.org[2], G.g, G.dim[2]);
+// Device view of a hashed uniform grid: only occupied cells are stored, in an
+// open-addressed table of uint4 {key low, key high, first point, point count} (count 0 =
+// empty slot), so cells can be as fine as the queries want whatever the scene's extent,
+// and the table stays small enough to live in L2.
+struct HGridView {
+    float       org[3];
+    float       g;
+    int         dim[3];
+    const uint4 *slot;
+    uint32_t    mask;
+    const int  *ids;
+    __device__ __forceinline__ void range(int x, int y, int z, int &s, int &e) const {
+        const unsigned long long key =
+            ((unsigned long long)z * (unsigned)dim[1] + (unsigned)y) * (unsigned)dim[0] + (unsigned)x;
+        uint32_t h = (uint32_t)smm::mix64(key) & mask;
+        for (uint32_t p = 0; p <= mask; p++) {
+            const uint4 v = slot[h];
+            if (v.w == 0u)
+                break;
+            if (v.x == (uint32_t)key && v.y == (uint32_t)(key >> 32)) {
+                s = (int)v.z;
+                e = (int)(v.z + v.w);
+                return;
+            }
+            h = (h + 1) & mask;
+        }
+        s = e = 0;
+    }
+};
+
+template <class G> __device__ __forceinline__ void grid_cc(const G &g, float x, float y, float z, int c[3]) {
+    c[0] = smg::coord(x, g.org[0], g.g, g.dim[0]);
+    c[1] = smg::coord(y, g.org[1], g.g, g.dim[1]);
+    c[2] = smg::coord(z, g.org[2], g.g, g.dim[2]);
 }
 
 __device__ __forceinline__ int grid_cell(const GridView &G, int x, int y, int z) {
     return (z * G.dim[1] + y) * G.dim[0] + x;
 }
 
-__device__ __forceinline__ int grid_max_shell(const GridView &G, const int c[3]) {
+template <class G> __device__ __forceinline__ int grid_max_shell(const G &g, const int c[3]) {
     int m = 0;
     for (int a = 0; a < 3; a++) {
-        const int lo = c[a], hi = G.dim[a] - 1 - c[a];
+        const int lo = c[a], hi = g.dim[a] - 1 - c[a];
         m          = max(m, max(lo, hi));
     }
     return m;
 }
 
 // Visit every point of the cells at Chebyshev distance exactly s from cell c.
-template <class F>
-__device__ __forceinline__ void grid_shell(const GridView &G, const int c[3], int s, F &&f) {
-    const int z0 = max(c[2] - s, 0), z1 = min(c[2] + s, G.dim[2] - 1);
-    const int y0 = max(c[1] - s, 0), y1 = min(c[1] + s, G.dim[1] - 1);
+template <class G, class F>
+__device__ __forceinline__ void grid_shell(const G &g, const int c[3], int s, F &&f) {
+    const int z0 = max(c[2] - s, 0), z1 = min(c[2] + s, g.dim[2] - 1);
+    const int y0 = max(c[1] - s, 0), y1 = min(c[1] + s, g.dim[1] - 1);
     for (int z = z0; z <= z1; z++) {
         for (int y = y0; y <= y1; y++) {
             const bool face = (z == c[2] - s || z == c[2] + s || y == c[1] - s || y == c[1] + s);
             const int  step = face ? 1 : 2 * s;
             for (int x = c[0] - s; x <= c[0] + s; x += (step > 0 ? step : 1)) {
-                if (x < 0 || x >= G.dim[0])
+                if (x < 0 || x >= g.dim[0])
                     continue;
-                const int cell = grid_cell(G, x, y, z);
-                const int e    = G.start[cell + 1];
-                for (int k = G.start[cell]; k < e; k++)
-                    f(G.ids[k]);
+                int b, e;
+                g.range(x, y, z, b, e);
+                for (int k = b; k < e; k++)
+                    f(g.ids[k]);
             }
         }
     }
 }
 
 // k nearest neighbours of q by (squared distance, index); returns how many were found.
-__device__ __forceinline__ int grid_knn(const GridView &G, const float4 *__restrict__ pos,
-                                        float qx, float qy, float qz, int k, int *oi,
-                                        float *od) {
+// K is the capacity of the (register-resident when K is small) candidate lists.
+template <int K, class G>
+__device__ __forceinline__ int grid_knn(const G &g, const float4 *__restrict__ pos, float qx,
+                                        float qy, float qz, int k, int *oi, float *od) {
     int c[3];
-    grid_cc(G, qx, qy, qz, c);
-    int       n  = 0;
-    const int ms = grid_max_shell(G, c);
+    grid_cc(g, qx, qy, qz, c);
+    int   n = 0;
+    int   li[K];
+    float ld[K];
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+        li[j] = 0x7fffffff;
+        ld[j] = 3.402823466e+38f;
+    }
+    const int ms = grid_max_shell(g, c);
     for (int s = 0; s <= ms; s++) {
-        grid_shell(G, c, s, [&](int id) {
+        grid_shell(g, c, s, [&](int id) {
             const float4 p = pos[id];
             const float  d = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
-            if (n == k && !(d < od[k - 1] || (d == od[k - 1] && id < oi[k - 1])))
+            // insert (d, id) into the sorted lists, capacity k (k <= K)
+            if (!(d < ld[k - 1] || (d == ld[k - 1] && id < li[k - 1])))
                 return;
-            int i = (n < k) ? n++ : k - 1;
-            while (i > 0 && (od[i - 1] > d || (od[i - 1] == d && oi[i - 1] > id))) {
-                od[i] = od[i - 1];
-                oi[i] = oi[i - 1];
-                i--;
+            float cd = d;
+            int   ci = id;
+#pragma unroll
+            for (int j = 0; j < K; j++) {
+                if (j < k && (cd < ld[j] || (cd == ld[j] && ci < li[j]))) {
+                    const float td = ld[j];
+                    const int   ti = li[j];
+                    ld[j]          = cd;
+                    li[j]          = ci;
+                    cd             = td;
+                    ci             = ti;
+                }
             }
-            od[i] = d;
-            oi[i] = id;
+            if (n < k)
+                n++;
         });
-        const float b = smg::ring_bound(s, G.g);
-        if (n == k && od[k - 1] < b * b)
+        const float b = smg::ring_bound(s, g.g);
+        if (n == k && ld[k - 1] < b * b)
             break;
     }
+#pragma unroll
+    for (int j = 0; j < K; j++)
+        if (j < k) {
+            oi[j] = li[j];
+            od[j] = ld[j];
+        }
     return n;
 }
 
 // Nearest neighbour by (squared distance, index), searched until the ring bound passes
-// `limit2`; returns -1 when the grid is empty.
-__device__ __forceinline__ int grid_nn(const GridView &G, const float4 *__restrict__ pos,
-                                       float qx, float qy, float qz, float limit2, float &outd) {
+// `limit2` (or `maxShell` shells); returns -1 when none was found. `exact` is set when the
+// result is the true nearest point or provably no point lies within limit2.
+template <class G>
+__device__ __forceinline__ int grid_nn(const G &g, const float4 *__restrict__ pos, float qx,
+                                       float qy, float qz, float limit2, float &outd,
+                                       int maxShell = 0x7fffffff, bool *exact = nullptr) {
     int c[3];
-    grid_cc(G, qx, qy, qz, c);
+    grid_cc(g, qx, qy, qz, c);
     int       best = -1;
     float     bd   = 3.402823466e+38f;
-    const int ms   = grid_max_shell(G, c);
+    const int ms   = min(grid_max_shell(g, c), maxShell);
+    bool      done = false;
     for (int s = 0; s <= ms; s++) {
-        grid_shell(G, c, s, [&](int id) {
+        grid_shell(g, c, s, [&](int id) {
             const float4 p = pos[id];
             const float  d = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
             if (d < bd || (d == bd && id < best)) {
@@ -110,24 +172,98 @@ __device__ __forceinline__ int grid_nn(const GridView &G, const float4 *__restri
                 best = id;
             }
         });
-        const float b = smg::ring_bound(s, G.g);
-        if (best >= 0 && bd < b * b)
+        const float b = smg::ring_bound(s, g.g);
+        if ((best >= 0 && bd < b * b) || b * b > limit2) {
+            done = true;
             break;
-        if (b * b > limit2)
-            break;
+        }
     }
+    if (ms == grid_max_shell(g, c))
+        done = true;
+    if (exact)
+        *exact = done;
     outd = bd;
     return best;
 }
 
-__device__ __forceinline__ bool grid_any_within(const GridView &G, const float4 *__restrict__ pos,
-                                                float qx, float qy, float qz, float r2) {
+// Exact nearest neighbour through a fine grid first (cheap when a point is close) and a
+// coarse grid over the same points when the fine grid's first shells cannot decide.
+template <class G>
+__device__ __forceinline__ int grid_nn2(const G &fine, const G &coarse, int fineShells,
+                                        const float4 *__restrict__ pos, float qx, float qy,
+                                        float qz, float limit2, float &outd) {
+    bool      exact = false;
+    const int j     = grid_nn(fine, pos, qx, qy, qz, limit2, outd, fineShells, &exact);
+    if (exact)
+        return j;
+    return grid_nn(coarse, pos, qx, qy, qz, limit2, outd);
+}
+
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(0xffffffffu, v, o);
+        v                          = t < v ? t : v;
+    }
+    return v;
+}
+
+// Warp-cooperative exact nearest neighbour: all 32 lanes call it with the same query; the
+// cells of each shell are split over the lanes and the (distance bits, index) minimum is
+// taken across the warp, so near and far queries cost the warp the same work pattern. Same
+// result and termination rule as grid_nn.
+template <class G>
+__device__ __forceinline__ int warp_nn(const G &g, const float4 *__restrict__ pos, float qx,
+                                       float qy, float qz, float limit2, float &outd) {
+    const int lane = threadIdx.x & 31;
+    int       c[3];
+    grid_cc(g, qx, qy, qz, c);
+    unsigned long long best = ~0ull;
+    const int          ms   = grid_max_shell(g, c);
+    for (int s = 0; s <= ms; s++) {
+        const int w = 2 * s + 1, cube = w * w * w;
+        for (int t = lane; t < cube; t += 32) {
+            const int dx = t % w - s, dy = (t / w) % w - s, dz = t / (w * w) - s;
+            if (max(abs(dx), max(abs(dy), abs(dz))) != s)
+                continue;
+            const int x = c[0] + dx, y = c[1] + dy, z = c[2] + dz;
+            if (x < 0 || y < 0 || z < 0 || x >= g.dim[0] || y >= g.dim[1] || z >= g.dim[2])
+                continue;
+            int b, e;
+            g.range(x, y, z, b, e);
+            for (int k = b; k < e; k++) {
+                const int    id = g.ids[k];
+                const float4 p  = pos[id];
+                const float  d  = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
+                const unsigned long long key =
+                    ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)id;
+                best = key < best ? key : best;
+            }
+        }
+        best          = warp_min_u64(best);
+        const float b = smg::ring_bound(s, g.g);
+        if (best != ~0ull && __uint_as_float((unsigned)(best >> 32)) < b * b)
+            break;
+        if (b * b > limit2)
+            break;
+    }
+    if (best == ~0ull) {
+        outd = 3.402823466e+38f;
+        return -1;
+    }
+    outd = __uint_as_float((unsigned)(best >> 32));
+    return (int)(unsigned)(best & 0xffffffffu);
+}
+
+template <class G>
+__device__ __forceinline__ bool grid_any_within(const G &g, const float4 *__restrict__ pos, float qx,
+                                                float qy, float qz, float r2) {
     int c[3];
-    grid_cc(G, qx, qy, qz, c);
-    const int ms = grid_max_shell(G, c);
+    grid_cc(g, qx, qy, qz, c);
+    const int ms = grid_max_shell(g, c);
     for (int s = 0; s <= ms; s++) {
         bool hit = false;
-        grid_shell(G, c, s, [&](int id) {
+        grid_shell(g, c, s, [&](int id) {
             if (hit)
                 return;
             const float4 p = pos[id];
@@ -136,7 +272,7 @@ __device__ __forceinline__ bool grid_any_within(const GridView &G, const float4 
         });
         if (hit)
             return true;
-        const float b = smg::ring_bound(s, G.g);
+        const float b = smg::ring_bound(s, g.g);
         if (b * b >= r2)
             break;
     }

@@ -103,6 +103,29 @@ struct Grid {
     }
 };
 
+// A hashed grid built on the device over a subset of points (see smd::HGridView).
+struct HGrid {
+    float     org[3] = {0, 0, 0};
+    float     g      = 1;
+    int       dim[3] = {1, 1, 1};
+    uint4    *slot   = nullptr;
+    uint32_t  mask   = 0;
+    int      *ids    = nullptr;
+    int       m      = 0;
+    smd::HGridView view() const {
+        smd::HGridView v;
+        for (int a = 0; a < 3; a++) {
+            v.org[a] = org[a];
+            v.dim[a] = dim[a];
+        }
+        v.g    = g;
+        v.slot = slot;
+        v.mask = mask;
+        v.ids  = ids;
+        return v;
+    }
+};
+
 struct Box {
     float mn[3], mx[3];
     float ext(int a) const { return mx[a] - mn[a]; }

@@ -42,13 +42,16 @@ int compact(Ctx &c, const int *flags, int n, int *outIds, const std::string &tag
 // ids ascending (needed by the sampler).
 void build_grid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &box, float g,
                 bool sortCells, Grid &G, const std::string &tag);
+// Hashed grid over points ids[0..m) with cell side g (fine cells at any scene extent).
+void build_hgrid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &box, float g,
+                 HGrid &H, const std::string &tag);
 // Greedy thinning at `step` in (phase, cell, index) order; writes kept ids ascending,
 // returns their count.
 int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m, const Box &box,
                   float step, int *outIds, const std::string &tag);
 // Two-phase normal estimation of ids[0..m) (see sm_oracle.cpp estimate_normals).
 void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *ids, int m,
-                      const Grid &query, int k, bool smooth, bool invert, const float *vp,
+                      const HGrid &query, int k, bool smooth, bool invert, const float *vp,
                       const std::string &tag);
 // Normalise all normals (normalizeNormal, util.cpp:163-176).
 void normalize_normals(Ctx &c, float4 *nrm, int n);
@@ -81,7 +84,7 @@ int cluster(Ctx &c, const float *poses, int np, float distThr, float angThr,
 // ---- icp.cu ---------------------------------------------------------------------------
 struct IcpScene {
     const float4 *pos, *nrm;
-    Grid          sampled, resampled, full;
+    HGrid         sampled, resampled, full;
     const int    *rankS, *rankR; // point id -> index in the sampled / resampled subsets
 };
 struct IcpParams {
