@@ -43,6 +43,7 @@ extern "C" {
 
 typedef struct sm_context_s *sm_context; /* one device + one CUDA stream + workspace */
 typedef struct sm_model_s *sm_model;     /* a trained model resident on the device */
+typedef struct sm_server_s *sm_server;   /* a matchScene serving loop on one device */
 
 /* ppf::TrainParam (type.h:39-74). */
 typedef struct {
@@ -142,6 +143,45 @@ SM_API int sm_match(sm_model model, const float *xyz, const float *normal, int64
                     const float *viewpoint, float samplingDistanceRel, float keyPointFraction,
                     float minScore, const sm_match_param *param, float *out_pose,
                     float *out_score, int *inout_count, sm_match_stats *stats);
+
+/* Batched ppf::Detector::matchScene (ppf.cpp:149-510) over njobs (scene, model) jobs of
+ * uneven size: job j matches scene xyz[j] (n[j] points; normals[j] or NULL, normals may be
+ * NULL as a whole; viewpoints[3*j] or viewpoints NULL) against models[j] (all on one
+ * device). Up to `concurrency` jobs run at once, each on its own stream and workspace, so
+ * their kernels overlap; results equal sm_match's for the same job. Outputs: out_pose
+ * [njobs x max_results x 16], out_score [njobs x max_results], out_count[njobs],
+ * out_status[njobs] (nullable, per-job status code), stats[njobs] (nullable). Returns
+ * SM_OK, or the first failing job's status with its message in sm_last_error(). */
+SM_API int sm_match_batch(int njobs, const sm_model *models, const float *const *xyz,
+                          const float *const *normals, const int64_t *n,
+                          const float *viewpoints, float samplingDistanceRel,
+                          float keyPointFraction, float minScore, const sm_match_param *param,
+                          int max_results, float *out_pose, float *out_score, int *out_count,
+                          int *out_status, int concurrency, sm_match_stats *stats);
+
+/* Serving (no counterpart in the reference, which matches one scene per call on the host).
+ * A server keeps `slots` workers (each a CUDA stream + workspace) over resident models and
+ * admits queued requests in arrival order as soon as a slot is free and the request's
+ * estimated device footprint (64 MiB + 512 B per point) fits in hbm_budget_bytes next to
+ * the requests in flight (a request larger than the budget runs alone). Admitted requests
+ * run concurrently; each result equals sm_match's for the same scene and model. */
+SM_API int sm_server_create(int device, int slots, int64_t hbm_budget_bytes, sm_server *out);
+/* Finishes the queued and running requests, then stops the workers. */
+SM_API int sm_server_destroy(sm_server server);
+/* Queue a matchScene request; host inputs are copied (the caller may free them on return),
+ * device inputs are read when the request runs and must stay valid until it is polled. */
+SM_API int sm_server_submit(sm_server server, sm_model model, const float *xyz,
+                            const float *normal, int64_t n, const float *viewpoint,
+                            float samplingDistanceRel, float keyPointFraction, float minScore,
+                            const sm_match_param *param, int64_t *out_request_id);
+/* Collect up to max_requests finished requests (waiting up to wait_ms for the first):
+ * ids, status codes, result counts, poses [k x max_results x 16], scores [k x max_results],
+ * times_ms [k x 3] = queue, service and total milliseconds. *n_out = requests returned. */
+SM_API int sm_server_poll(sm_server server, int max_requests, int max_results, int wait_ms,
+                          int64_t *ids, int *status, int *counts, float *poses, float *scores,
+                          double *times_ms, int *n_out);
+/* out6 = {queued, running, completed, estimated bytes in flight, peak, budget} */
+SM_API int sm_server_status(sm_server server, int64_t *out6);
 
 /* Stage entry of the voting step (ppf.cpp:247-409) on caller-supplied scene state:
  * points/normals (n x 3), keypoint indices, and per-keypoint neighbour lists in search

@@ -69,6 +69,16 @@ _SIGNATURES = {
                            C.POINTER(MatchStatsC)]),
     "sm_vote_stage": (C.c_int, [_vp, _f32p, _f32p, C.c_int64, _i32p, C.c_int64, _i32p, _i32p,
                                 C.c_float, _i64p, _f32p, _f32p, C.c_int, _i32p]),
+    "sm_match_batch": (C.c_int, [C.c_int, _vp, _vp, _vp, _i64p, _f32p, C.c_float, C.c_float,
+                                 C.c_float, C.POINTER(MatchParamC), C.c_int, _f32p, _f32p,
+                                 _i32p, _i32p, C.c_int, C.POINTER(MatchStatsC)]),
+    "sm_server_create": (C.c_int, [C.c_int, C.c_int, C.c_int64, C.POINTER(_vp)]),
+    "sm_server_destroy": (C.c_int, [_vp]),
+    "sm_server_submit": (C.c_int, [_vp, _vp, _f32p, _f32p, C.c_int64, _f32p, C.c_float,
+                                   C.c_float, C.c_float, C.POINTER(MatchParamC), _i64p]),
+    "sm_server_poll": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _i64p, _i32p, _i32p, _f32p,
+                                 _f32p, C.POINTER(C.c_double), _i32p]),
+    "sm_server_status": (C.c_int, [_vp, _i64p]),
     "sm_vote_stage_noalloc": (C.c_int, [_vp, _vp, _vp, C.c_int64, _vp, C.c_int64, _vp, _vp,
                                         C.c_float, _vp, _vp, _vp, C.c_int, _vp]),
     "sm_debug_size": (C.c_int64, [_vp, C.c_int]),

@@ -19,7 +19,7 @@ BUILD = os.path.join(HERE, "_build")
 INCLUDE = os.path.abspath(os.path.join(HERE, "..", "include"))
 LIB = os.path.join(HERE, "libsurface_match.so")
 
-CU_SOURCES = ["prep.cu", "vote.cu", "cluster.cu", "icp.cu", "api.cu", "noalloc.cu"]
+CU_SOURCES = ["prep.cu", "vote.cu", "cluster.cu", "icp.cu", "api.cu", "noalloc.cu", "batch.cu", "server.cu"]
 CPP_SOURCES: list = []
 HEADERS = ["sm_math.h", "sm_linalg.h", "sm_icp.h", "sm_grid.h", "sm_device.cuh",
            "sm_engine.h", "sm_stages.h"]

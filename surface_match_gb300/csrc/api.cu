@@ -576,6 +576,16 @@ void put_cloud(std::string &o, const std::vector<float> &p, const std::vector<fl
 
 } // namespace
 
+void match_into(Ctx &c, const Model &m, const float *xyz, const float *nrm, int64_t n,
+                const float *vp, float sdRel, float kpFrac, float minScore,
+                const sm_match_param &mp, std::vector<float> &pose, std::vector<float> &score,
+                sm_match_stats *stats) {
+    MatchOutputs res;
+    match(c, m, xyz, nrm, n, vp, sdRel, kpFrac, minScore, mp, res, stats);
+    pose  = std::move(res.pose);
+    score = std::move(res.score);
+}
+
 Model *model_core(sm_model m) { return &m->m; }
 Ctx   *model_ctx(sm_model m) { return &m->ctx->ctx; }
 int    run_guarded(const std::function<void()> &f) { return guarded(f); }

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <functional>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -98,6 +99,15 @@ void subset_rank(Ctx &c, const int *ids, int m, int *rank);
 void icp_all(Ctx &c, const Model &m, const IcpScene &s, const IcpParams &p, const float *cands,
              int ncand, int *status, float *score, float *pose, float *trace = nullptr);
 constexpr int kIcpTraceFloats = 2 * 32 * 4 + 2; // per candidate, see icp.cu
+
+// matchScene on one context (api.cu), and the per-device pool of worker contexts that the
+// batch and serving entry points run jobs on (batch.cu).
+void match_into(Ctx &c, const Model &m, const float *xyz, const float *nrm, int64_t n,
+                const float *vp, float sdRel, float kpFrac, float minScore,
+                const sm_match_param &mp, std::vector<float> &pose, std::vector<float> &score,
+                sm_match_stats *stats);
+std::unique_ptr<Ctx> acquire_worker(int device);
+void                 release_worker(int device, std::unique_ptr<Ctx> c);
 
 // Access to a model handle's engine state and the C ABI's error handling, for entry points
 // defined outside api.cu.

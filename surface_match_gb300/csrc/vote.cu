@@ -83,16 +83,61 @@ __device__ __forceinline__ uint32_t probe(const uint4 *__restrict__ tab, uint32_
     return 0;
 }
 
+constexpr int kRowBuf = 2048; // rows buffered per processing round
+
+// Votes of the hits hOff/hCnt/hAs/hAsT[0..nHits) (prefix hPre, total V) into the shared
+// accumulator. Each warp takes a contiguous range of votes and walks the hit list forward,
+// so a lane finds its hit in a step or two instead of a binary search per vote.
+__device__ __forceinline__ void cast_votes(const VoteArgs &a, uint32_t *acc, const int *hOff,
+                                           const int *hCnt, const float *hAs, const float *hAsT,
+                                           const int *hPre, int nHits, int V, int r0, int r1) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = kVoteBs / 32;
+    const int per  = (V + nw - 1) / nw;
+    const int v0 = w * per, v1 = min(V, v0 + per);
+    if (v0 >= v1)
+        return;
+    int lo = 0, hi = nHits - 1; // last hit with hPre <= v0
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (hPre[mid] <= v0)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    int h = lo;
+    for (int base = v0; base < v1; base += 32) {
+        const int v = base + lane;
+        int       hv = h;
+        if (v < v1) {
+            while (hPre[hv + 1] <= v)
+                hv++;
+            const int   e   = v - hPre[hv];
+            const int   B   = hCnt[hv];
+            const uint2 ent = a.entries[hOff[hv] + e];
+            const int   ref = (int)ent.x;
+            if (ref >= r0 && ref < r1) {
+                uint32_t bin = smm::vote_bin(e < B - B % smm::kLanes, __uint_as_float(ent.y),
+                                             hAs[hv], hAsT[hv], a.smax);
+                if (bin > (uint32_t)(a.A - 1))
+                    bin = a.A - 1; // unreachable; keeps the index in range
+                atomicAdd(&acc[(ref - r0) * a.A + bin], 1u);
+            }
+        }
+        h = __shfl_sync(0xffffffffu, hv, 31);
+    }
+}
+
 template <bool CSR> __global__ void __launch_bounds__(kVoteBs) k_vote(VoteArgs a) {
     extern __shared__ uint32_t acc[];
-    __shared__ int       hOff[kVoteBs], hCnt[kVoteBs], hPre[kVoteBs + 1];
-    __shared__ float     hAs[kVoteBs], hAsT[kVoteBs];
+    __shared__ int       rows[kRowBuf];
+    __shared__ int       hOff[kRowBuf], hCnt[kRowBuf], hPre[kRowBuf + 1];
+    __shared__ float     hAs[kRowBuf], hAsT[kRowBuf];
     __shared__ int       sh[33];
     __shared__ smm::RT   rt;
     __shared__ Cand      wc[kVoteBs / 32][3];
     __shared__ long long sstat[4];
     __shared__ unsigned long long shash;
-    __shared__ int       sRows, sSearched;
+    __shared__ int       sRows, sSearched, sHits;
 
     const int c   = blockIdx.x;
     const int tid = threadIdx.x;
@@ -160,49 +205,68 @@ template <bool CSR> __global__ void __launch_bounds__(kVoteBs) k_vote(VoteArgs a
         const int nb = (r1 - r0) * A;
         for (int i = tid; i < nb; i += kVoteBs)
             acc[i] = 0u;
-        __syncthreads();
-        int rowBase = 0;
-        for (int base = 0; base < listLen; base += kVoteBs) {
-            const int i   = base + tid;
-            int       id  = -1;
-            bool      row = false;
-            float4    q   = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (i < listLen) {
-                id = CSR ? a.nbrIds[listBeg + i] : a.cand[i];
-                q  = a.pos[id];
-                row = id != pid &&
-                      (CSR || smm::dist2(p1.x, p1.y, p1.z, q.x, q.y, q.z) < a.sqDiam);
+        int rowBase = 0, nBuf = 0;
+        for (int base = 0; base < listLen || nBuf > 0; base += kVoteBs) {
+            // gather the next tile's rows (in list order) into the buffer
+            if (base < listLen) {
+                const int i   = base + tid;
+                int       id  = -1;
+                bool      row = false;
+                if (i < listLen) {
+                    id = CSR ? a.nbrIds[listBeg + i] : a.cand[i];
+                    if (id != pid) {
+                        if (CSR) {
+                            row = true;
+                        } else {
+                            const float4 q = a.pos[id];
+                            row = smm::dist2(p1.x, p1.y, p1.z, q.x, q.y, q.z) < a.sqDiam;
+                        }
+                    }
+                }
+                int       nRows;
+                const int rp = block_excl_scan(row ? 1 : 0, sh, &nRows);
+                if (row)
+                    rows[nBuf + rp] = id;
+                nBuf += nRows;
             }
-            int       nRows;
-            const int rpos = rowBase + block_excl_scan(row ? 1 : 0, sh, &nRows);
-            rowBase += nRows;
-            bool     hit = false;
-            uint32_t off = 0, cnt = 0;
-            float    as = 0.f;
-            if (row) {
+            const bool last = base + kVoteBs >= listLen;
+            if (nBuf + kVoteBs <= kRowBuf && !last)
+                continue;
+            // process the buffered rows: keys, alphas, probes; hits in any order
+            if (tid == 0)
+                sHits = 0;
+            __syncthreads();
+            for (int k = tid; k < nBuf; k += kVoteBs) {
+                const int    id  = rows[k];
+                const int    rpos = rowBase + k;
                 const bool   blk = rpos < vecR;
+                const float4 q   = a.pos[id];
                 const float4 n2  = a.nrm[id];
                 const uint32_t key = smm::ppf_key(blk, p1.x, p1.y, p1.z, n1.x, n1.y, n1.z, q.x, q.y,
                                                   q.z, n2.x, n2.y, n2.z, a.angleStep, a.distStep);
-                as = smm::alpha_of(blk, rt, q.x, q.y, q.z);
-                if (!smm::fisnan(as)) {
-                    cnt = probe(a.htab, a.hmask, key, off);
-                    hit = cnt > 0;
+                const float as = smm::alpha_of(blk, rt, q.x, q.y, q.z);
+                if (smm::fisnan(as))
+                    continue;
+                uint32_t  off = 0;
+                const int cnt = (int)probe(a.htab, a.hmask, key, off);
+                if (cnt > 0) {
+                    const int hp = atomicAdd(&sHits, 1);
+                    hOff[hp]     = (int)off;
+                    hCnt[hp]     = cnt;
+                    hAs[hp]      = as;
+                    hAsT[hp]     = smm::alpha_tail_shift(as);
                 }
             }
-            int       nHits;
-            const int hpos = block_excl_scan(hit ? 1 : 0, sh, &nHits);
-            if (hit) {
-                hOff[hpos] = (int)off;
-                hCnt[hpos] = (int)cnt;
-                hAs[hpos]  = as;
-                hAsT[hpos] = smm::alpha_tail_shift(as);
-            }
             __syncthreads();
-            int       V;
-            const int pre = block_excl_scan(tid < nHits ? hCnt[tid] : 0, sh, &V);
-            if (tid < nHits)
-                hPre[tid] = pre;
+            const int nHits = sHits;
+            int       V     = 0;
+            for (int h0 = 0; h0 < nHits; h0 += kVoteBs) {
+                int       tot;
+                const int pre = block_excl_scan(h0 + tid < nHits ? hCnt[h0 + tid] : 0, sh, &tot);
+                if (h0 + tid < nHits)
+                    hPre[h0 + tid] = V + pre;
+                V += tot;
+            }
             if (tid == 0) {
                 hPre[nHits] = V;
                 if (r0 == 0) {
@@ -211,28 +275,11 @@ template <bool CSR> __global__ void __launch_bounds__(kVoteBs) k_vote(VoteArgs a
                 }
             }
             __syncthreads();
-            for (int v = tid; v < V; v += kVoteBs) {
-                int lo = 0, hi = nHits - 1; // last h with hPre[h] <= v
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (hPre[mid] <= v)
-                        lo = mid;
-                    else
-                        hi = mid - 1;
-                }
-                const int   e   = v - hPre[lo];
-                const int   B   = hCnt[lo];
-                const uint2 ent = a.entries[hOff[lo] + e];
-                const int   ref = (int)ent.x;
-                if (ref >= r0 && ref < r1) {
-                    uint32_t bin = smm::vote_bin(e < B - B % smm::kLanes, __uint_as_float(ent.y),
-                                                 hAs[lo], hAsT[lo], a.smax);
-                    if (bin > (uint32_t)(A - 1))
-                        bin = A - 1; // unreachable; keeps the index in range
-                    atomicAdd(&acc[(ref - r0) * A + bin], 1u);
-                }
-            }
+            if (nHits > 0)
+                cast_votes(a, acc, hOff, hCnt, hAs, hAsT, hPre, nHits, V, r0, r1);
             __syncthreads();
+            rowBase += nBuf;
+            nBuf = 0;
         }
         // peaks of this reference-point chunk (ppf.cpp:363-389)
         const float thre = a.voteThreshold / 2.0f;
@@ -389,7 +436,7 @@ void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const in
     a.dumpK         = out.acc ? dumpK : 0;
     int maxSmem = 0;
     SM_CUDA(cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));
-    const int staticSmem = 24 * 1024;
+    const int staticSmem = 24 * (int)kRowBuf + 8 * 1024;
     int       budget     = maxSmem - staticSmem;
     a.refChunk = std::max(1, std::min(m.ns, budget / (int)(a.A * sizeof(uint32_t))));
     const size_t smem = (size_t)a.refChunk * a.A * sizeof(uint32_t);

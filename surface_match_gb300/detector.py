@@ -304,3 +304,119 @@ class Detector:
         if n:
             _check(L.sm_debug_get(self.model, field_id, a.ctypes.data_as(C.c_void_p)))
         return a.reshape(-1, w) if w > 1 else a
+
+
+def match_batch(jobs, samplingDistanceRel=0.04, keyPointFraction=0.2, minScore=0.2,
+                param: MatchParam | None = None, concurrency=4):
+    """Batched matchScene (sm_match_batch). jobs: list of (Detector, PointCloud). Returns a
+    list of (poses (k, 4, 4), scores (k,)) per job, in job order, and per-job statistics."""
+    param = param or MatchParam()
+    L = _lib.load()
+    nj = len(jobs)
+    maxr = max(1, param.numMatches)
+    models = (C.c_void_p * nj)(*[d.model.value for d, _ in jobs])
+    keep, xs, ns_ = [], [], []
+    nrm_any = any(pc.normal is not None for _, pc in jobs)
+    nrms = []
+    vps = np.zeros((nj, 3), np.float32)
+    have_vp = all(pc.viewPoint is not None for _, pc in jobs)
+    for j, (_, pc) in enumerate(jobs):
+        p, k = _ptr(pc.point)
+        keep.append(k)
+        xs.append(C.cast(p, C.c_void_p))
+        ns_.append(_len(pc.point))
+        if nrm_any:
+            q, k2 = _ptr(pc.normal)
+            keep.append(k2)
+            nrms.append(C.cast(q, C.c_void_p) if q is not None else None)
+        if have_vp:
+            vps[j] = np.asarray(pc.viewPoint, np.float32)
+    xarr = (C.c_void_p * nj)(*xs)
+    narr = (C.c_void_p * nj)(*nrms) if nrm_any else None
+    n64 = np.asarray(ns_, np.int64)
+    poses = np.zeros((nj, maxr, 4, 4), np.float32)
+    scores = np.zeros((nj, maxr), np.float32)
+    count = np.zeros(nj, np.int32)
+    status = np.zeros(nj, np.int32)
+    stats = (MatchStatsC * nj)()
+    f32 = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
+    i32 = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))  # noqa: E731
+    rc = L.sm_match_batch(nj, C.cast(models, C.c_void_p), C.cast(xarr, C.c_void_p),
+                          C.cast(narr, C.c_void_p) if narr is not None else None,
+                          n64.ctypes.data_as(C.POINTER(C.c_int64)),
+                          f32(vps) if have_vp else None, samplingDistanceRel, keyPointFraction,
+                          minScore, C.byref(param.c()), maxr, f32(poses), f32(scores),
+                          i32(count), i32(status), concurrency, stats)
+    _check(rc)
+    out = [(poses[j, :count[j]], scores[j, :count[j]]) for j in range(nj)]
+    st = [{f: getattr(s, f) for f, _ in MatchStatsC._fields_ if f != "ms"} | {"ms": list(s.ms)}
+          for s in stats]
+    return out, st
+
+
+class Server:
+    """Serving loop over resident models (sm_server_*): submit scenes as they arrive, poll
+    finished requests with their queue / service / total latencies."""
+
+    def __init__(self, device=0, slots=4, hbm_budget_bytes=64 << 30):
+        h = C.c_void_p()
+        _check(_lib.load().sm_server_create(device, slots, hbm_budget_bytes, C.byref(h)))
+        self.handle = h
+
+    def submit(self, detector: "Detector", scene: PointCloud, samplingDistanceRel=0.04,
+               keyPointFraction=0.2, minScore=0.2, param: MatchParam | None = None) -> int:
+        param = param or MatchParam()
+        p, k1 = _ptr(scene.point)
+        q, k2 = _ptr(scene.normal)
+        vp = None
+        if scene.viewPoint is not None:
+            vpa = np.ascontiguousarray(scene.viewPoint, np.float32)
+            vp = vpa.ctypes.data_as(C.POINTER(C.c_float))
+        rid = C.c_int64()
+        _check(_lib.load().sm_server_submit(self.handle, detector.model, p, q,
+                                            _len(scene.point), vp, samplingDistanceRel,
+                                            keyPointFraction, minScore, C.byref(param.c()),
+                                            C.byref(rid)))
+        return rid.value
+
+    def poll(self, max_requests=64, max_results=16, wait_ms=0):
+        """Finished requests: list of dicts {id, status, poses, scores, queue_ms, service_ms,
+        total_ms}."""
+        ids = np.zeros(max_requests, np.int64)
+        st = np.zeros(max_requests, np.int32)
+        cnt = np.zeros(max_requests, np.int32)
+        poses = np.zeros((max_requests, max_results, 4, 4), np.float32)
+        scores = np.zeros((max_requests, max_results), np.float32)
+        times = np.zeros((max_requests, 3), np.float64)
+        n = C.c_int()
+        _check(_lib.load().sm_server_poll(
+            self.handle, max_requests, max_results, wait_ms,
+            ids.ctypes.data_as(C.POINTER(C.c_int64)), st.ctypes.data_as(C.POINTER(C.c_int32)),
+            cnt.ctypes.data_as(C.POINTER(C.c_int32)), poses.ctypes.data_as(C.POINTER(C.c_float)),
+            scores.ctypes.data_as(C.POINTER(C.c_float)),
+            times.ctypes.data_as(C.POINTER(C.c_double)), C.byref(n)))
+        out = []
+        for i in range(n.value):
+            k = min(int(cnt[i]), max_results)
+            out.append({"id": int(ids[i]), "status": int(st[i]), "poses": poses[i, :k].copy(),
+                        "scores": scores[i, :k].copy(), "queue_ms": float(times[i, 0]),
+                        "service_ms": float(times[i, 1]), "total_ms": float(times[i, 2])})
+        return out
+
+    def status(self):
+        v = np.zeros(6, np.int64)
+        _check(_lib.load().sm_server_status(self.handle, v.ctypes.data_as(C.POINTER(C.c_int64))))
+        return dict(zip(["queued", "running", "completed", "bytes_in_flight", "peak_bytes",
+                         "budget"], (int(x) for x in v)))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _lib.load().sm_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+

@@ -422,3 +422,64 @@ def scene_tiny(seed=3, model=None, n_inst=2, pts=6000, noise=0.2):
                       points_per_instance=pts, plane=(220.0, 0.0), plane_points=pts,
                       clutter_frac=0.05, clutter="uniform", noise=noise,
                       model_centers={"gear": c})
+
+
+def scene_random(seed, n_target, surfaces, centers, noise, clutter_frac, n_inst,
+                 box=((-200, -200, 0), (200, 200, 200))):
+    """A scene of about n_target points: n_inst instances of one model, clutter of random
+    boxes and spheres, noise, viewpoint culling (batching / serving workloads)."""
+    name = list(surfaces)[0]
+    # about half of each instance's surface faces the viewer; clutter adds its fraction
+    per = max(200, int(n_target * (1 - clutter_frac) * 2.0 / max(1, n_inst)))
+    return make_scene(seed, {name: surfaces[name]}, n_inst, box, points_per_instance=per,
+                      clutter_frac=clutter_frac, clutter="shapes", noise=noise,
+                      model_centers={name: centers[name]})
+
+
+def batch_models(seed=11):
+    """The three procedural models of the batching workload, each sampled at 20k-40k
+    points: name -> (Cloud, surface, centre)."""
+    rng = np.random.default_rng(seed)
+    out = {}
+    for k, name in enumerate(["gear", "bracket", "torus"]):
+        out[name] = model_cloud(name, int(rng.integers(20000, 40001)), seed + k)
+    return out
+
+
+def batch_scenes(n_scenes=64, seed=21, models=None, n_min=50_000, n_max=2_000_000):
+    """The batching workload: scenes with log-uniform point counts in [n_min, n_max], 1-12
+    instances of one of the models (drawn per scene), noise sigma U(0.2, 0.5) mm and
+    clutter U(10%, 40%), all from the seed. Returns [(model name, Scene)]."""
+    models = models or batch_models()
+    rng = np.random.default_rng(seed)
+    names = sorted(models)
+    out = []
+    for i in range(n_scenes):
+        name = names[int(rng.integers(len(names)))]
+        n = int(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        sc = scene_random(int(rng.integers(1 << 30)), n, {name: models[name][1]},
+                          {name: models[name][2]}, float(rng.uniform(0.2, 0.5)),
+                          float(rng.uniform(0.10, 0.40)), int(rng.integers(1, 13)))
+        out.append((name, sc))
+    return out
+
+
+def serving_models(seed=31):
+    """Eight resident models: gear, L-bracket, torus, plus five gears and brackets with a
+    random tooth count (12-40) or plate size (30-80 mm)."""
+    rng = np.random.default_rng(seed)
+    surfs = {"gear": gear_surface(), "bracket": bracket_surface(), "torus": torus_surface()}
+    for k in range(5):
+        if k % 2 == 0:
+            teeth = int(rng.integers(12, 41))
+            r_out = float(rng.uniform(30, 60))
+            surfs[f"gear{teeth}"] = gear_surface(teeth=teeth, r_out=r_out, r_root=r_out * 0.84,
+                                                 bore=r_out * 0.2, thickness=float(rng.uniform(10, 25)))
+        else:
+            w, d = (float(x) for x in rng.uniform(30, 80, 2))
+            surfs[f"bracket{int(w)}x{int(d)}"] = bracket_surface(width=w, depth=d,
+                                                                thick=float(rng.uniform(5, 10)))
+    out = {}
+    for k, (name, s) in enumerate(surfs.items()):
+        out[name] = model_cloud(name, 20000, seed + k, surface=s)
+    return out
