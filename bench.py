@@ -49,6 +49,10 @@ WORKLOADS = {
     "serve": (None, 0.04, 0.2,
               "serving: Poisson arrivals of scenes (100k-3M points, log-uniform) against 8 "
               "resident models; rates 10..2000 scenes/s; matchScene(0.04, 0.2, 0.2, 16)"),
+    "precision": (None, 0.04, 0.2,
+                  "precision: scenes of 2M points with gears and L-brackets, sigma 0.5 mm, "
+                  "normals estimated (k=10), dense ICP 30 iterations; GPU FP32 + Kahan vs "
+                  "the CPU restatement with FP64 accumulation, same search orders"),
     "small": ("scene_small", 0.04, 0.1,
               "small scene: 3 gears over a 400x400 mm plane, 10% uniform clutter, sigma 0.2 mm, "
               "normals estimated; trainModel(gear 20k pts, 0.04), "
@@ -279,6 +283,119 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+def _rot_err_deg(A, B):
+    import numpy as np
+    R = A[:3, :3].astype(np.float64).T @ B[:3, :3].astype(np.float64)
+    return float(np.degrees(np.arccos(np.clip((np.trace(R) - 1) / 2, -1, 1))))
+
+
+def _precision_scene(o64, models, name, seed, npts, noise, n_inst):
+    """One scene of the precision study: GPU (FP32 + Kahan) against the oracle with FP64
+    accumulation, both with the GPU's search orders, so that only the accumulation differs."""
+    import numpy as np
+    from oracle import MatchParam as OMP
+    from surface_match_gb300 import Detector, MatchParam, PointCloud, synth
+    cloud, surf, ctr = models[name]
+    sc = synth.scene_random(seed, npts, {name: surf}, {name: ctr}, noise, 0.2, n_inst)
+    det = Detector()
+    det.trainModel(PointCloud(cloud.xyz, cloud.normal), SD)
+    poses, scores = det.matchScene(PointCloud(sc.cloud.xyz, None, sc.viewpoint), SD, KP, MS,
+                                   MatchParam(numMatches=NUM_MATCHES, poseRefNumSteps=30))
+    nrm32, sampled = det.debug(4), det.debug(0)
+    m64 = o64.train(cloud.xyz, cloud.normal, SD)
+    r64 = o64.match(m64, sc.cloud.xyz, None, sc.viewpoint, SD, KP, MS,
+                    OMP(numMatches=NUM_MATCHES, poseRefNumSteps=30))
+    common = np.intersect1d(sampled, r64.sampled)
+    a, b = nrm32[common].astype(np.float64), r64.normals[common].astype(np.float64)
+    cosang = np.abs(np.sum(a * b, 1)) / np.maximum(np.linalg.norm(a, axis=1) *
+                                                   np.linalg.norm(b, axis=1), 1e-30)
+    nerr = np.degrees(np.arccos(np.clip(cosang, -1, 1)))
+    diam = float(np.linalg.norm(np.ptp(cloud.xyz.astype(np.float64), axis=0)))
+    inst, used = [], set()
+    for P, s in zip(poses, scores):
+        best = None
+        for j, Q in enumerate(r64.poses):
+            if j in used:
+                continue
+            dt = float(np.linalg.norm(P[:3, 3].astype(np.float64) - Q[:, 3]))
+            if best is None or dt < best[1]:
+                best = (j, dt)
+        if best is None or best[1] > 0.1 * diam:
+            continue
+        used.add(best[0])
+        Q = np.vstack([r64.poses[best[0]], [0, 0, 0, 1]])
+        inst.append({"rot_err_deg": _rot_err_deg(P, Q), "trans_err_mm": best[1],
+                     "score_fp32": float(s), "score_fp64": float(r64.scores[best[0]])})
+    return {"model": name, "noise_mm": noise, "points": int(len(sc.cloud.xyz)),
+            "sampled": int(len(common)),
+            "instances_fp32": int(len(scores)), "instances_fp64": int(len(r64.scores)),
+            "normal_err_deg": {"median": float(np.median(nerr)) if len(nerr) else None,
+                               "p99": float(np.percentile(nerr, 99)) if len(nerr) else None,
+                               "max": float(nerr.max()) if len(nerr) else None,
+                               "bit_equal_frac": float(np.mean(
+                                   (nrm32[common] == r64.normals[common]).all(1)))},
+            "instances": inst}
+
+
+def run_precision(args):
+    """FP32 + Kahan accumulation (GPU) against FP64 accumulation (oracle, GPU search
+    orders): normal angle error of every sampled scene point, and rotation / translation
+    error of every matched instance. The study's scenes (2M points, noise 0.5 mm) are
+    followed by a supplement of sparser, less noisy scenes, where instances are found and
+    poses compared."""
+    import numpy as np
+    from oracle import MODE_GRID, Oracle
+    from surface_match_gb300 import synth
+    models = {name: synth.model_cloud(name, 20000, 50 + k)
+              for k, name in enumerate(["gear", "bracket"])}
+    rng = np.random.default_rng(91)
+    o64 = Oracle(mode=MODE_GRID, threads=os.cpu_count() or 8, fp64=True)
+    plan = [(0.5, args.precision_points, i) for i in range(args.precision_scenes)]
+    plan += [(args.precision_supplement_noise, args.precision_supplement_points, i)
+             for i in range(args.precision_supplement)]
+    rows = []
+    for noise, npts, i in plan:
+        r = _precision_scene(o64, models, ["gear", "bracket"][i % 2],
+                             int(rng.integers(1 << 30)), npts, noise, int(rng.integers(3, 9)))
+        rows.append(r)
+        print(json.dumps({"scene": len(rows) - 1, **{k: v for k, v in r.items()
+                                                      if k != "instances"},
+                          "n_inst_compared": len(r["instances"])}), file=sys.stderr, flush=True)
+    allr = [x["rot_err_deg"] for r in rows for x in r["instances"]]
+    allt = [x["trans_err_mm"] for r in rows for x in r["instances"]]
+    nmax = [r["normal_err_deg"]["max"] for r in rows if r["normal_err_deg"]["max"] is not None]
+    line = {"metric": "precision: FP32+Kahan vs FP64 accumulation", "workload": "precision",
+            "config": {"workload": WORKLOADS["precision"][3],
+                       "scenes": args.precision_scenes,
+                       "supplement": {"scenes": args.precision_supplement,
+                                      "noise_mm": args.precision_supplement_noise,
+                                      "points_per_scene": args.precision_supplement_points},
+                       "points_per_scene": args.precision_points, "sd_rel": SD, "kp": KP},
+            "same_instance_count": all(r["instances_fp32"] == r["instances_fp64"]
+                                       for r in rows),
+            "instances_compared": len(allr),
+            "max_rot_err_deg": max(allr) if allr else None,
+            "max_trans_err_mm": max(allt) if allt else None,
+            "max_normal_err_deg": max(nmax) if nmax else None,
+            "median_normal_err_deg": float(np.median([r["normal_err_deg"]["median"]
+                                                      for r in rows])),
+            "scenes": rows}
+    print(json.dumps(line), flush=True)
+
+
+def vote_traffic():
+    """DRAM bytes (read + write) of one k_vote launch of this workload, from the ncu capture
+    summarised in profiles/k_vote_<workload>.md (its line "dram_bytes_per_launch = N");
+    None when no capture of this workload exists."""
+    import re
+    try:
+        txt = open(os.path.join(ROOT, "profiles", f"k_vote_{WL}.md")).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_launch\s*=\s*([0-9]+)", txt)
+    return int(m.group(1)) if m else None
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -294,6 +411,11 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=32.0)
     ap.add_argument("--serve-requests", type=int, default=120)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[10, 50, 200, 1000, 2000])
+    ap.add_argument("--precision-scenes", type=int, default=16)
+    ap.add_argument("--precision-points", type=int, default=2_000_000)
+    ap.add_argument("--precision-supplement", type=int, default=6)
+    ap.add_argument("--precision-supplement-noise", type=float, default=0.2)
+    ap.add_argument("--precision-supplement-points", type=int, default=300_000)
     args = ap.parse_args()
     global WL, SD, KP
     WL = args.workload
@@ -302,6 +424,8 @@ def main():
         return run_batch(args)
     if WL == "serve" and args.impl != "reference":
         return run_serve(args)
+    if WL == "precision":
+        return run_precision(args)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -394,13 +518,7 @@ def main():
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     alg_bytes = 8 * votes + 32 * pairs  # bucket entries read + neighbour rows read
     achieved = alg_bytes / (vk / 1000.0) / 1e9
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "vote_traffic.json")
-    if os.path.exists(tf):
-        try:
-            traffic = json.load(open(tf)).get("dram_bytes_per_launch")
-        except Exception:
-            traffic = None
+    traffic = vote_traffic()
     line = {"metric": METRIC, "value": value, "unit": "scenes/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",

@@ -145,7 +145,7 @@ extern "C" SM_API int sm_vote_stage_noalloc(sm_model m, const float *points, con
         vo.poses  = outPoses;
         vo.poseOk = ok;
         vo.acc    = dk ? outAcc : nullptr;
-        vote(c, M, P, N, kp, Ki, nbrOff, nbrIds, nullptr, 0, minScore, vo, dk);
+        vote_fused(c, M, P, N, kp, Ki, nbrOff, nbrIds, minScore, vo, dk);
         k_clear_unemitted<<<Ki * 3, 32, 0, c.stream>>>(ok, Ki * 3, outPoses);
         SM_LAUNCH_CHECK();
         SM_CUDA(cudaStreamSynchronize(c.stream));

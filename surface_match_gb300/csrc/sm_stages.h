@@ -71,6 +71,10 @@ struct VoteOut {
 void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const int *kp, int K,
           const int *nbrOff, const int *nbrIds, const int *cand, int ncand, float minScore,
           const VoteOut &out, int dumpK);
+// The same from CSR lists in a single kernel that needs no workspace (same results).
+void vote_fused(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const int *kp,
+                int K, const int *nbrOff, const int *nbrIds, float minScore, const VoteOut &out,
+                int dumpK);
 // All ordered model pairs (trainModel's table rows): key and alpha per (i, j).
 void model_pairs(Ctx &c, const float4 *sp, const float4 *sn, int ns, float angleStep,
                  float distStep, uint32_t *keys, float *alphas, int *valid);

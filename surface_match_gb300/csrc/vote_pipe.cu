@@ -1,0 +1,427 @@
+// vote_pipe.cu - the voting stage of matchScene (ppf.cpp:247-409) as a pipeline of
+// kernels, each shaped for what it spends its time on.
+//
+//  1. k_kp_radius / k_kp_csr: per keypoint its neighbour count, its rows (neighbours other
+//     than itself) and the list position of its first "tail" row - the reference computes
+//     a keypoint's rows in 8-lane blocks and the last (rows mod 8) one by one, with
+//     different float rounding. In radius mode (all candidates within the model diameter,
+//     in ascending order) the rows are kept as a bitmask over the candidate list, computed
+//     from candidate tiles staged in shared memory and shared by eight keypoints.
+//  2. A prefix sum over the rows gives every keypoint a segment of the row list.
+//  3. k_rows_fill writes (keypoint, point, lane rule) per row into its segment.
+//  4. k_ppf: one thread per row at full occupancy - quantised PPF key, scene alpha, model
+//     table probe; a hit (bucket, count, alpha) is appended to the keypoint's segment.
+//  5. k_lpt: keypoints ordered by their vote count, largest first, so the heaviest
+//     accumulators start first and the tail of the next kernel stays short.
+//  6. k_vote_acc: one CTA per keypoint votes its hits into a shared-memory (reference
+//     point x angle bin) accumulator - 16-bit counters when the keypoint's vote count
+//     allows - then extracts peaks, the top three candidates and their poses.
+#include "sm_stages.h"
+#include "sm_vote.cuh"
+
+namespace sm {
+using namespace smd;
+using namespace vt;
+
+void fill_vote_model(const Model &m, float minScore, VoteArgs &a);
+
+namespace {
+
+constexpr int kKpWarps   = 8;    // keypoints per CTA of the radius kernel
+constexpr int kTile      = 1024; // candidates per shared-memory tile
+constexpr int kAccBs     = 512;
+constexpr int kHitChunk  = 1024; // hits staged in shared memory per round
+constexpr int kLptBins   = 40;
+
+struct PipeBufs {
+    int4               *info;    // K: {searched, rows voted (0 when skipped), first tail row, flags}
+    smm::RT            *rt;      // K: transform of the keypoint
+    uint32_t           *mask;    // K x words: row bits over the candidate list (radius mode)
+    int                 words;
+    int                *rowOff;  // K + 1
+    int2               *rows;    // rows: {keypoint, point * 2 + block lane}
+    int4               *hits;    // per row segment: {bucket offset, count, alpha bits, 0}
+    int                *hitCnt;  // K
+    unsigned long long *votes;   // K
+    int                *order;   // K
+};
+
+// flags: bit 0 = keypoint votes, bit 1 = its normal is not finite
+__device__ __forceinline__ int4 kp_info(const VoteArgs &a, int searched, int R, int tail,
+                                        const float4 &n1) {
+    const bool nanN   = !(isfinite(n1.x) && isfinite(n1.y) && isfinite(n1.z));
+    const bool active = !nanN && !((float)searched < a.voteThreshold);
+    return make_int4(searched, active ? R : 0, tail, (active ? 1 : 0) | (nanN ? 2 : 0));
+}
+
+// Position of the first of the last `need` set bits of the warp's mask words [0, nw) (the
+// first tail row); `n` when need == 0. All lanes return the same value.
+__device__ __forceinline__ int tail_from_mask(const uint32_t *m, int nw, int need, int n) {
+    const int lane  = threadIdx.x & 31;
+    int       found = n;
+    for (int base = nw - 1; base >= 0 && need > 0; base -= 32) {
+        const int      wi = base - lane; // lane 0 = last word
+        const uint32_t wv = wi >= 0 ? m[wi] : 0u;
+        const int      k  = __popc(wv);
+        // rows in words after this lane's word (lanes before it in this round)
+        int incl = k;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o)
+                incl += t;
+        }
+        const int      excl = incl - k;
+        const bool     mine = excl < need && incl >= need;
+        const uint32_t who  = __ballot_sync(0xffffffffu, mine);
+        if (who) {
+            const int src = __ffs(who) - 1;
+            int       pos = 0;
+            if (lane == src) {
+                uint32_t b = wv; // the (need - excl)-th highest set bit of wv
+                for (int t = 1; t < need - excl; t++)
+                    b &= ~(0x80000000u >> __clz(b));
+                pos = wi * 32 + (31 - __clz(b));
+            }
+            found = __shfl_sync(0xffffffffu, pos, src);
+            need  = 0;
+        } else {
+            need -= __shfl_sync(0xffffffffu, incl, 31);
+        }
+    }
+    return found;
+}
+
+// Radius mode: eight keypoints per CTA, one per warp, over shared-memory tiles of the
+// candidates' positions.
+__global__ void __launch_bounds__(kKpWarps * 32) k_kp_radius(VoteArgs a, PipeBufs b) {
+    __shared__ float4 tp[kTile];
+    __shared__ int    tid_[kTile];
+    const int   lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int   c    = blockIdx.x * kKpWarps + w;
+    const bool  live = c < a.K;
+    const int   pid  = live ? a.kp[c] : -1;
+    float4      p1   = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (live)
+        p1 = a.pos[pid];
+    uint32_t *mrow = b.mask + (size_t)(live ? c : 0) * b.words;
+    int       S = 0, R = 0;
+    for (int t0 = 0; t0 < a.ncand; t0 += kTile) {
+        const int tn = min(kTile, a.ncand - t0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < tn; i += blockDim.x) {
+            const int id = a.cand[t0 + i];
+            tid_[i]      = id;
+            tp[i]        = a.pos[id];
+        }
+        __syncthreads();
+        if (!live)
+            continue;
+        for (int j = 0; j < tn; j += 32) {
+            const int  i   = j + lane;
+            bool       in  = false;
+            bool       row = false;
+            if (i < tn) {
+                const float4 q = tp[i];
+                in             = smm::dist2(p1.x, p1.y, p1.z, q.x, q.y, q.z) < a.sqDiam;
+                row            = in && tid_[i] != pid;
+            }
+            const uint32_t bi = __ballot_sync(0xffffffffu, in);
+            const uint32_t br = __ballot_sync(0xffffffffu, row);
+            S += __popc(bi);
+            R += __popc(br);
+            if (lane == 0)
+                mrow[(t0 + j) >> 5] = br;
+        }
+    }
+    if (!live)
+        return;
+    __syncwarp();
+    const int tail = tail_from_mask(mrow, b.words, R % smm::kLanes, a.ncand);
+    if (lane == 0) {
+        const float4 n1 = a.nrm[pid];
+        b.info[c]       = kp_info(a, S, R, tail, n1);
+        b.rt[c]         = smm::transform_rt(p1.x, p1.y, p1.z, n1.x, n1.y, n1.z);
+    }
+}
+
+// CSR mode: one warp per keypoint over its list.
+__global__ void k_kp_csr(VoteArgs a, PipeBufs b) {
+    const int lane = threadIdx.x & 31;
+    const int c    = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (c >= a.K)
+        return;
+    const int  pid = a.kp[c];
+    const int  beg = a.nbrOff[c], len = a.nbrOff[c + 1] - beg;
+    const int *L   = a.nbrIds + beg;
+    int        R   = 0;
+    for (int i = lane; i < len; i += 32)
+        R += L[i] != pid ? 1 : 0;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1)
+        R += __shfl_xor_sync(0xffffffffu, R, o);
+    int need = R % smm::kLanes, found = len;
+    for (int end = len; end > 0 && need > 0; end -= 32) {
+        const int i = end - 1 - lane;
+        uint32_t  m = __ballot_sync(0xffffffffu, i >= 0 && L[i] != pid);
+        const int k = __popc(m);
+        if (k >= need) {
+            for (int t = 1; t < need; t++)
+                m &= m - 1;
+            found = end - 1 - (__ffs(m) - 1);
+            need  = 0;
+        } else {
+            need -= k;
+        }
+    }
+    if (lane == 0) {
+        const float4 p1 = a.pos[pid], n1 = a.nrm[pid];
+        b.info[c]       = kp_info(a, len, R, found, n1);
+        b.rt[c]         = smm::transform_rt(p1.x, p1.y, p1.z, n1.x, n1.y, n1.z);
+    }
+}
+
+__global__ void k_rows_count(const int4 *__restrict__ info, int K, int *__restrict__ cnt) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < K)
+        cnt[c] = info[c].y;
+}
+
+// The rows of keypoint blockIdx.x into its segment (any order within it).
+__global__ void k_rows_fill(VoteArgs a, PipeBufs b, int csr) {
+    __shared__ int sN;
+    const int  c    = blockIdx.x;
+    const int4 info = b.info[c];
+    if (info.y == 0)
+        return;
+    if (threadIdx.x == 0)
+        sN = 0;
+    __syncthreads();
+    int2     *out  = b.rows + b.rowOff[c];
+    const int pid  = a.kp[c];
+    const int lane = threadIdx.x & 31;
+    if (!csr) {
+        const uint32_t *m = b.mask + (size_t)c * b.words;
+        for (int wi = threadIdx.x; wi < b.words; wi += blockDim.x) {
+            uint32_t wv = m[wi];
+            if (!wv)
+                continue;
+            int p = atomicAdd(&sN, __popc(wv));
+            while (wv) {
+                const int bit = __ffs(wv) - 1;
+                wv &= wv - 1;
+                const int i = wi * 32 + bit;
+                out[p++]    = make_int2(c, a.cand[i] * 2 + (i < info.z ? 1 : 0));
+            }
+        }
+        return;
+    }
+    const int  beg = a.nbrOff[c], len = a.nbrOff[c + 1] - beg;
+    const int *L   = a.nbrIds + beg;
+    for (int i0 = 0; i0 < len; i0 += blockDim.x) {
+        const int      i     = i0 + threadIdx.x;
+        const int      id    = i < len ? L[i] : -1;
+        const bool     row   = i < len && id != pid;
+        const uint32_t m     = __ballot_sync(0xffffffffu, row);
+        int            wbase = 0;
+        if (lane == 0 && m)
+            wbase = atomicAdd(&sN, __popc(m));
+        wbase = __shfl_sync(0xffffffffu, wbase, 0);
+        if (row)
+            out[wbase + __popc(m & ((1u << lane) - 1u))] = make_int2(c, id * 2 + (i < info.z ? 1 : 0));
+    }
+}
+
+// One thread per row: PPF key and scene alpha with the row's lane rule, then the model
+// table probe; hits go to the keypoint's segment.
+__global__ void k_ppf(VoteArgs a, PipeBufs b, const int *__restrict__ total) {
+    const int n = *total;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const int2     row = b.rows[r];
+        const int      c   = row.x;
+        const int      id  = row.y >> 1;
+        const bool     blk = (row.y & 1) != 0;
+        const int      pid = a.kp[c];
+        const float4   p1 = a.pos[pid], n1 = a.nrm[pid];
+        const float4   q = a.pos[id], n2 = a.nrm[id];
+        const smm::RT  rt  = b.rt[c];
+        const uint32_t key = smm::ppf_key(blk, p1.x, p1.y, p1.z, n1.x, n1.y, n1.z, q.x, q.y, q.z,
+                                          n2.x, n2.y, n2.z, a.angleStep, a.distStep);
+        const float as = smm::alpha_of(blk, rt, q.x, q.y, q.z);
+        if (smm::fisnan(as))
+            continue;
+        uint32_t  off = 0;
+        const int cnt = (int)probe(a.htab, a.hmask, key, off);
+        if (cnt > 0) {
+            const int slot               = atomicAdd(&b.hitCnt[c], 1);
+            b.hits[b.rowOff[c] + slot]   = make_int4((int)off, cnt, __float_as_int(as), 0);
+            atomicAdd(&b.votes[c], (unsigned long long)cnt);
+        }
+    }
+}
+
+__device__ __forceinline__ int lpt_bin(unsigned long long v) {
+    return v == 0 ? 0 : min(kLptBins - 1, 64 - __clzll((long long)v));
+}
+
+// Keypoints by vote count, largest first (binned by powers of two).
+__global__ void k_lpt(const unsigned long long *__restrict__ votes, int K, int *__restrict__ order) {
+    __shared__ int hist[kLptBins], start[kLptBins];
+    if (threadIdx.x < kLptBins)
+        hist[threadIdx.x] = 0;
+    __syncthreads();
+    for (int c = threadIdx.x; c < K; c += blockDim.x)
+        atomicAdd(&hist[lpt_bin(votes[c])], 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int s = 0;
+        for (int k = kLptBins - 1; k >= 0; k--) {
+            start[k] = s;
+            s += hist[k];
+        }
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < K; c += blockDim.x)
+        order[atomicAdd(&start[lpt_bin(votes[c])], 1)] = c;
+}
+
+__global__ void __launch_bounds__(kAccBs, 2) k_vote_acc(VoteArgs a, PipeBufs b) {
+    extern __shared__ uint32_t acc[];
+    __shared__ int       hOff[kHitChunk], hCnt[kHitChunk], cPre[kHitChunk + 1];
+    __shared__ float     hAs[kHitChunk], hAsT[kHitChunk];
+    __shared__ int       sh[33];
+    __shared__ Cand      wc[kAccBs / 32][3];
+    __shared__ unsigned long long shash;
+
+    const int  c    = b.order[blockIdx.x];
+    const int  tid  = threadIdx.x;
+    const int4 info = b.info[c];
+    if (!(info.w & 1)) {
+        skip_keypoint(a, c, info.x, (info.w & 2) != 0);
+        return;
+    }
+    if (tid == 0)
+        shash = 0;
+    const long long V      = (long long)b.votes[c];
+    const int       nH     = b.hitCnt[c];
+    const int4     *H      = b.hits + b.rowOff[c];
+    const bool      narrow = V <= kNarrowMax;
+    const int       chunk  = narrow ? a.refChunk : a.refChunkWide;
+    Cand            top[3];
+    for (int t = 0; t < 3; t++)
+        top[t] = Cand{-1.0f, INT_MAX, 0};
+    unsigned long long myHash = 0;
+    for (int r0 = 0; r0 < a.ns; r0 += chunk) {
+        const int r1     = min(r0 + chunk, a.ns);
+        const int nElem  = (r1 - r0) * a.A;
+        const int nWords = narrow ? (nElem + 1) >> 1 : nElem;
+        for (int i = tid; i < nWords; i += kAccBs)
+            acc[i] = 0u;
+        for (int h0 = 0; h0 < nH; h0 += kHitChunk) {
+            const int n = min(kHitChunk, nH - h0);
+            __syncthreads();
+            int T = 0;
+            for (int j0 = 0; j0 < n; j0 += kAccBs) {
+                const int j   = j0 + tid;
+                int       nit = 0;
+                if (j < n) {
+                    const int4 hv = H[h0 + j];
+                    hOff[j]       = hv.x;
+                    hCnt[j]       = hv.y;
+                    hAs[j]        = __int_as_float(hv.z);
+                    hAsT[j]       = smm::alpha_tail_shift(__int_as_float(hv.z));
+                    nit           = (hv.y + kItem - 1) / kItem;
+                }
+                int       tot;
+                const int pre = block_excl_scan(nit, sh, &tot);
+                if (j < n)
+                    cPre[j] = T + pre;
+                T += tot;
+            }
+            if (tid == 0)
+                cPre[n] = T;
+            __syncthreads();
+            cast_votes(a, acc, hOff, hCnt, hAs, hAsT, cPre, n, T, r0, r1, narrow);
+        }
+        __syncthreads();
+        peaks_chunk(a, acc, narrow, r0, r1, top, myHash);
+        dump_chunk(a, c, acc, narrow, r0, r1);
+        __syncthreads();
+    }
+    finish_keypoint(a, c, b.rt[c], top, myHash, info.x, nH, V, wc, &shash);
+}
+
+} // namespace
+
+void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const int *kp, int K,
+          const int *nbrOff, const int *nbrIds, const int *cand, int ncand, float minScore,
+          const VoteOut &out, int dumpK) {
+    if (K <= 0)
+        return;
+    VoteArgs a{};
+    fill_vote_model(m, minScore, a);
+    a.pos    = pos;
+    a.nrm    = nrm;
+    a.kp     = kp;
+    a.K      = K;
+    a.nbrOff = nbrOff;
+    a.nbrIds = nbrIds;
+    a.cand   = cand;
+    a.ncand  = ncand;
+    a.stats  = out.stats;
+    a.cands  = out.cands;
+    a.poses  = out.poses;
+    a.poseOk = out.poseOk;
+    a.acc    = out.acc;
+    a.dumpK  = out.acc ? dumpK : 0;
+    const bool csr = nbrOff != nullptr;
+
+    int optin = 0, perSM = 0;
+    SM_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));
+    SM_CUDA(cudaDeviceGetAttribute(&perSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c.device));
+    cudaFuncAttributes fa;
+    SM_CUDA(cudaFuncGetAttributes(&fa, k_vote_acc));
+    const size_t smem = acc_sizing(a.ns, a.A, (long long)fa.sharedSizeBytes, optin, perSM,
+                                   &a.refChunk, &a.refChunkWide);
+    if (!smem)
+        throw Error(SM_ERR_CAPACITY, "featAngleResolution too large for the vote accumulator");
+
+    PipeBufs b{};
+    b.info   = c.arena.get<int4>("v.info", K);
+    b.rt     = c.arena.get<smm::RT>("v.rt", K);
+    b.words  = csr ? 0 : (ncand + 31) / 32;
+    b.mask   = csr ? nullptr : c.arena.get<uint32_t>("v.mask", (size_t)K * std::max(b.words, 1));
+    b.rowOff = c.arena.get<int>("v.rowoff", (size_t)K + 1);
+    b.hitCnt = c.arena.get<int>("v.hitcnt", K);
+    b.votes  = c.arena.get<unsigned long long>("v.votes", K);
+    b.order  = c.arena.get<int>("v.order", K);
+    int *cnt = c.arena.get<int>("v.rowcnt", (size_t)K + 1);
+    if (csr) {
+        k_kp_csr<<<nblocks((long long)K * 32, 256), 256, 0, c.stream>>>(a, b);
+    } else {
+        k_kp_radius<<<nblocks(K, kKpWarps), kKpWarps * 32, 0, c.stream>>>(a, b);
+    }
+    SM_LAUNCH_CHECK();
+    k_rows_count<<<nblocks(K, 256), 256, 0, c.stream>>>(b.info, K, cnt);
+    SM_LAUNCH_CHECK();
+    SM_CUDA(cudaMemsetAsync(cnt + K, 0, sizeof(int), c.stream));
+    const int rtot = scan_excl(c, cnt, b.rowOff, (long long)K + 1, "v.scan", true);
+    b.rows = c.arena.get<int2>("v.rows", std::max(rtot, 1));
+    b.hits = c.arena.get<int4>("v.hits", std::max(rtot, 1));
+    SM_CUDA(cudaMemsetAsync(b.hitCnt, 0, (size_t)K * sizeof(int), c.stream));
+    SM_CUDA(cudaMemsetAsync(b.votes, 0, (size_t)K * sizeof(unsigned long long), c.stream));
+    k_rows_fill<<<K, 256, 0, c.stream>>>(a, b, csr ? 1 : 0);
+    SM_LAUNCH_CHECK();
+    if (rtot > 0) {
+        const int g = (int)std::min<long long>(nblocks(rtot, 256), 152LL * 8);
+        k_ppf<<<g, 256, 0, c.stream>>>(a, b, b.rowOff + K);
+        SM_LAUNCH_CHECK();
+    }
+    k_lpt<<<1, 1024, 0, c.stream>>>(b.votes, K, b.order);
+    SM_LAUNCH_CHECK();
+    SM_CUDA(cudaFuncSetAttribute(k_vote_acc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_vote_acc<<<K, kAccBs, smem, c.stream>>>(a, b);
+    SM_LAUNCH_CHECK();
+}
+
+} // namespace sm

@@ -71,3 +71,35 @@ def test_serving_mix_equals_alone_and_respects_budget(setup):
         if budget == 1:  # every request exceeds the budget: admitted only when alone
             assert st["peak_bytes"] == max(64 * (1 << 20) + 512 * len(pc.point)
                                            for _, pc in jobs)
+
+
+def test_precision_fp32_kahan_vs_fp64_accumulation():
+    """The GPU's FP32 + Kahan accumulation (normals' covariance, ICP normal equations)
+    against the oracle with FP64 accumulation (same search orders): sampled normals within a
+    small angle, the same instance count, every instance pose within 0.1 deg and
+    1e-3 * diameter."""
+    from oracle import MODE_GRID, MatchParam as OMP, Oracle
+    from surface_match_gb300 import Detector, MatchParam, PointCloud, synth
+    cloud, surf, ctr = synth.model_cloud("gear", 8000, 60)
+    sc = synth.scene_random(17, 80000, {"gear": surf}, {"gear": ctr}, 0.2, 0.2, 3,
+                            box=((-120, -120, 0), (120, 120, 120)))
+    det = Detector()
+    det.trainModel(PointCloud(cloud.xyz, cloud.normal), SD)
+    poses, scores = det.matchScene(PointCloud(sc.cloud.xyz, None, sc.viewpoint), SD, KP, MS,
+                                   MatchParam(numMatches=8, poseRefNumSteps=30))
+    o = Oracle(mode=MODE_GRID, threads=8, fp64=True)
+    m = o.train(cloud.xyz, cloud.normal, SD)
+    r = o.match(m, sc.cloud.xyz, None, sc.viewpoint, SD, KP, MS,
+                OMP(numMatches=8, poseRefNumSteps=30))
+    ids = np.intersect1d(det.debug(0), r.sampled)
+    a, b = det.debug(4)[ids].astype(np.float64), r.normals[ids].astype(np.float64)
+    ang = np.degrees(np.arccos(np.clip(np.abs((a * b).sum(1)), 0, 1)))
+    assert np.median(ang) < 1e-3 and np.percentile(ang, 99) < 0.1, (np.median(ang), ang.max())
+    diam = float(np.linalg.norm(np.ptp(cloud.xyz, axis=0)))
+    assert len(scores) == len(r.scores) and len(scores) > 0
+    for P in poses:
+        j = int(np.argmin([np.linalg.norm(P[:3, 3] - Q[:, 3]) for Q in r.poses]))
+        Q = r.poses[j]
+        R = P[:3, :3].astype(np.float64).T @ Q[:, :3].astype(np.float64)
+        rot = np.degrees(np.arccos(np.clip((np.trace(R) - 1) / 2, -1, 1)))
+        assert rot < 0.1 and np.linalg.norm(P[:3, 3] - Q[:, 3]) < 1e-3 * diam

@@ -124,6 +124,37 @@ def test_vote_kernel_reference_order_bit_exact(oracle_ref):
     np.testing.assert_array_equal(emitted.view(np.uint32), r.pose_list.view(np.uint32))
 
 
+@pytest.mark.parametrize("dist_rel,angles", [(0.25, 12), (0.04, 360)])
+def test_vote_kernel_counter_widths_and_passes(data, dist_rel, angles):
+    """The accumulator's other regimes, bit-exact against the oracle: coarse distance
+    steps make buckets so large that keypoints cast more than 65535 votes (16-bit counters
+    give way to 32-bit ones), and 360 angle bins make the accumulator larger than one CTA's
+    shared memory (several reference-point passes)."""
+    from oracle import MODE_REF, MatchParam, Oracle, TrainParam as OTP
+    from surface_match_gb300 import Detector, TrainParam
+    mc, sc = data
+    o = Oracle(mode=MODE_REF, threads=8)
+    m = o.train(mc.xyz, mc.normal, SD, OTP(featDistanceStepRel=dist_rel,
+                                           featAngleResolution=angles))
+    r = o.match(m, sc.cloud.xyz, None, sc.viewpoint, SD, KP, MS, MatchParam(numMatches=8),
+                dump_k=4)
+    if dist_rel > 0.2:
+        assert r.kp_stats[:, 3].max() > 65535
+    if angles == 360:
+        assert len(m.sampled) * angles * 2 > 200 * 1024
+    det = Detector()
+    det.upload(m.sampled, m.sampled_normal, m.resampled, m.resampled_normal, m.box, m.keys,
+               m.offsets, m.refs, m.alphas, SD,
+               TrainParam(featDistanceStepRel=dist_rel, featAngleResolution=angles))
+    stats, cands, poses, acc = det.vote_stage(r.positions, r.normals, r.keypoints, r.nbr_off,
+                                              r.nbr_ids, MS, dump_k=4)
+    np.testing.assert_array_equal(stats, r.kp_stats)
+    np.testing.assert_array_equal(cands, r.kp_cands)
+    np.testing.assert_array_equal(acc, r.acc_dump)
+    emitted = poses[stats[:, 6][:, None] > np.arange(3)[None, :]]
+    np.testing.assert_array_equal(emitted.view(np.uint32), r.pose_list.view(np.uint32))
+
+
 def gear_symmetries(teeth=24):
     """Rotations mapping the procedural spur gear onto itself (model frame): turns about z
     by a tooth pitch, and half-turns about the in-plane axes through tooth and gap
