@@ -218,15 +218,16 @@ std::vector<float> download4(const float4 *d, int n) {
     return o;
 }
 
-// Query-grid cell for k-nearest-neighbour searches: about 1.3x the expected k-NN radius,
+// Query-grid cell for k-nearest-neighbour searches: about 1.6x the expected k-NN radius,
 // from the point density the greedy sampling reveals (n_sampled points at `step` cover an
-// area of about n_sampled * step^2 / 0.7). Results do not depend on it, only run time.
+// area of about n_sampled * step^2 / 0.7), so that the query's cell and its 26 neighbours
+// decide nearly every query. Results do not depend on it, only run time.
 float knn_cell(int nvalid, int nsampled, float step, int k) {
     float g = step * 0.25f;
     if (nvalid > 0 && nsampled > 0) {
         const double area = (double)nsampled * step * step / 0.7;
         const double rk   = std::sqrt((double)std::max(k, 3) * area / (3.14159265 * nvalid));
-        g = (float)std::min<double>(std::max<double>(1.3 * rk, step * 0.1), step);
+        g = (float)std::min<double>(std::max<double>(1.6 * rk, step * 0.1), step);
     }
     return g;
 }

@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(kT) k_corr(Work w, Stage s) {
         smi::pose_apply(C.M, s.src[i].x, s.src[i].y, s.src[i].z, x.x, x.y, x.z);
         smi::pose_rotate(C.M, s.srcN[i].x, s.srcN[i].y, s.srcN[i].z, y.x, y.y, y.z);
         float      d;
-        const int  j  = warp_nn(s.G, w.pos, x.x, x.y, x.z, s.rej2, d);
+        const int  j  = warp_nn(s.G, x.x, x.y, x.z, s.rej2, d);
         const bool ok = j >= 0 && d <= s.rej2;
         if (lane == 0) {
             x.w       = d;
@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(kT) k_resid(Work w, Stage s) {
         const float4 x = w.x4[o];
         float        y0, y1, y2, d;
         smi::pose_apply(C.step, x.x, x.y, x.z, y0, y1, y2);
-        warp_nn(s.G, w.pos, y0, y1, y2, FLT_MAX, d);
+        warp_nn(s.G, y0, y1, y2, FLT_MAX, d);
         if ((threadIdx.x & 31) == 0)
             w.terms[(size_t)ci * smi::kNumSystem * w.maxSrc + i] = smm::fsqrt(d);
     }
@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(kT) k_inliers(Work w, const float4 *__restrict
     if (i < n) {
         float x, y, z;
         smi::pose_apply(C.M, src[i].x, src[i].y, src[i].z, x, y, z);
-        c = grid_any_within(F, w.pos, x, y, z, r2) ? 1 : 0;
+        c = grid_any_within(F, x, y, z, r2) ? 1 : 0;
     }
     c = __reduce_add_sync(0xffffffffu, c);
     if ((threadIdx.x & 31) == 0)

@@ -347,45 +347,102 @@ __global__ void k_mark_todo(const int *__restrict__ ids, int m, const float4 *__
         need[id] = 2;
 }
 
+// Neighbours of one query (slots [K-k, K) of li, ascending): the lists, and for smoothing the
+// marking of neighbours that still need a normal.
 template <int K>
-__global__ void k_knn(const int *__restrict__ list, int nl, HGridView G, const float4 *__restrict__ pos,
-                      int k, int *__restrict__ nbr, int *__restrict__ nbrCnt, int markNeighbours,
-                      const float4 *__restrict__ nrm, int *__restrict__ need) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nl)
-        return;
-    const float4 q = pos[list[t]];
-    int          oi[K];
-    float        od[K];
-    const int    n = grid_knn<K>(G, pos, q.x, q.y, q.z, k, oi, od);
+__device__ __forceinline__ void knn_store(int t, int k, int n, const int (&li)[K],
+                                          int *__restrict__ nbr, int *__restrict__ nbrCnt,
+                                          int markNeighbours, const float4 *__restrict__ nrm,
+                                          int *__restrict__ need) {
+    int *out = nbr + (size_t)t * k - (K - k);
 #pragma unroll
     for (int j = 0; j < K; j++)
-        if (j < k)
-            nbr[(size_t)t * k + j] = j < n ? oi[j] : -1;
+        if (j >= K - k)
+            out[j] = j - (K - k) < n ? li[j] : -1;
     nbrCnt[t] = n;
     if (markNeighbours) {
 #pragma unroll
         for (int j = 0; j < K; j++) {
-            if (j >= n)
-                break;
-            const int id = oi[j];
+            if (j < K - k || j - (K - k) >= n)
+                continue;
+            const int id = li[j];
             if (need[id] == 0 && !finite3(nrm[id].x, nrm[id].y, nrm[id].z))
                 need[id] = 1;
         }
     }
 }
 
+// One warp per query over the query's cell and its 26 neighbours (the query grid's cell is
+// chosen so that this decides almost every query); undecided queries are queued for
+// k_knn_warp.
+template <int K>
+__global__ void k_knn(const int *__restrict__ list, int nl, HGridView G, const float4 *__restrict__ pos,
+                      int k, int *__restrict__ nbr, int *__restrict__ nbrCnt, int markNeighbours,
+                      const float4 *__restrict__ nrm, int *__restrict__ need,
+                      int *__restrict__ pend, int *__restrict__ npend) {
+    const int lane = threadIdx.x & 31;
+    const int t    = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (t >= nl)
+        return;
+    const float4 q = pos[list[t]];
+    int          li[K];
+    float        ld[K];
+    bool         done = false;
+    const int    n    = warp_knn1<K>(G, q.x, q.y, q.z, k, li, ld, &done);
+    if (lane != 0)
+        return;
+    if (!done) {
+        pend[atomicAdd(npend, 1)] = t;
+        return;
+    }
+    knn_store<K>(t, k, n, li, nbr, nbrCnt, markNeighbours, nrm, need);
+}
+
+// The queued queries, one warp each: the lanes split each shell's cells (same result as the
+// thread search run to the end).
+template <int K>
+__global__ void k_knn_warp(const int *__restrict__ list, const int *__restrict__ pend,
+                           const int *__restrict__ npend, HGridView G,
+                           const float4 *__restrict__ pos, int k, int *__restrict__ nbr,
+                           int *__restrict__ nbrCnt, int markNeighbours,
+                           const float4 *__restrict__ nrm, int *__restrict__ need) {
+    const int lane = threadIdx.x & 31;
+    const int np   = *npend;
+    for (int w = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5); w < np;
+         w += (gridDim.x * blockDim.x) >> 5) {
+        const int    t = pend[w];
+        const float4 q = pos[list[t]];
+        int          li[K];
+        float        ld[K];
+        const int    n = warp_knn<K>(G, q.x, q.y, q.z, k, li, ld);
+        if (lane == 0)
+            knn_store<K>(t, k, n, li, nbr, nbrCnt, markNeighbours, nrm, need);
+    }
+}
+
+template <int K>
+void launch_knn_k(cudaStream_t st, const int *list, int nl, const HGridView &G, const float4 *pos,
+                  int k, int *nbr, int *cnt, int mark, const float4 *nrm, int *need, int *pend,
+                  int *npend) {
+    SM_CUDA(cudaMemsetAsync(npend, 0, sizeof(int), st));
+    k_knn<K><<<nblocks((long long)nl * 32, 256), 256, 0, st>>>(list, nl, G, pos, k, nbr, cnt, mark,
+                                                                nrm, need, pend, npend);
+    SM_LAUNCH_CHECK();
+    k_knn_warp<K><<<152 * 4, 256, 0, st>>>(list, pend, npend, G, pos, k, nbr, cnt, mark, nrm, need);
+    SM_LAUNCH_CHECK();
+}
+
 void launch_knn(cudaStream_t st, const int *list, int nl, const HGridView &G, const float4 *pos,
-                int k, int *nbr, int *cnt, int mark, const float4 *nrm, int *need) {
+                int k, int *nbr, int *cnt, int mark, const float4 *nrm, int *need, int *pend,
+                int *npend) {
     if (nl <= 0)
         return;
     if (k <= 10)
-        k_knn<10><<<nblocks(nl, 128), 128, 0, st>>>(list, nl, G, pos, k, nbr, cnt, mark, nrm, need);
+        launch_knn_k<10>(st, list, nl, G, pos, k, nbr, cnt, mark, nrm, need, pend, npend);
     else if (k <= 16)
-        k_knn<16><<<nblocks(nl, 128), 128, 0, st>>>(list, nl, G, pos, k, nbr, cnt, mark, nrm, need);
+        launch_knn_k<16>(st, list, nl, G, pos, k, nbr, cnt, mark, nrm, need, pend, npend);
     else
-        k_knn<kMaxKnn><<<nblocks(nl, 128), 128, 0, st>>>(list, nl, G, pos, k, nbr, cnt, mark, nrm, need);
-    SM_LAUNCH_CHECK();
+        launch_knn_k<kMaxKnn>(st, list, nl, G, pos, k, nbr, cnt, mark, nrm, need, pend, npend);
 }
 
 // ---- hashed grid build -----------------------------------------------------------------
@@ -416,12 +473,17 @@ __global__ void k_hg_insert(const float4 *__restrict__ pos, const int *__restric
     }
 }
 
-__global__ void k_hg_scatter(const int *__restrict__ ids, const int *__restrict__ slotOf, int m,
-                             int *__restrict__ fill, int *__restrict__ gids) {
+__global__ void k_hg_scatter(const float4 *__restrict__ pos, const int *__restrict__ ids,
+                             const int *__restrict__ slotOf, int m, int *__restrict__ fill,
+                             int *__restrict__ gids, float4 *__restrict__ pts) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m)
         return;
-    gids[atomicAdd(&fill[slotOf[i]], 1)] = ids[i];
+    const int    id = ids[i];
+    const float4 p  = pos[id];
+    const int    k  = atomicAdd(&fill[slotOf[i]], 1);
+    gids[k]         = id;
+    pts[k]          = make_float4(p.x, p.y, p.z, __int_as_float(id));
 }
 
 __global__ void k_hg_pack_from_start(const unsigned long long *__restrict__ keys,
@@ -433,6 +495,22 @@ __global__ void k_hg_pack_from_start(const unsigned long long *__restrict__ keys
     const unsigned long long k = keys[t];
     slot[t] = make_uint4((uint32_t)k, (uint32_t)(k >> 32), (uint32_t)start[t],
                          (uint32_t)(start[t + 1] - start[t]));
+}
+
+// Query lists in the query grid's cell order: a warp then searches 32 neighbouring queries
+// (similar cells, shared cache lines, little divergence). flags[k] = need[gids[k]] == eq.
+__global__ void k_flags_grid_order(const int *__restrict__ gids, int m, const int *__restrict__ need,
+                                   int eq, int *__restrict__ flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m)
+        flags[i] = need[gids[i]] == eq ? 1 : 0;
+}
+
+__global__ void k_map_ids(const int *__restrict__ idx, int n, const int *__restrict__ gids,
+                          int *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        out[i] = gids[idx[i]];
 }
 
 // Phase A: centroid and FP32-Kahan covariance of the neighbourhood, FP64 eigensolve.
@@ -636,6 +714,23 @@ int compact(Ctx &c, const int *flags, int n, int *outIds, const std::string &tag
     return compact_eq(c, flags, n, kNoEq, outIds, tag);
 }
 
+// The points p of grid H with need[p] == eq, in H's cell order.
+static int compact_grid_order(Ctx &c, const HGrid &H, const int *need, int eq, int *out,
+                              const std::string &tag) {
+    if (H.m <= 0)
+        return 0;
+    int *flags = c.arena.get<int>(tag + ".gf", H.m);
+    int *idx   = c.arena.get<int>(tag + ".gi", H.m);
+    k_flags_grid_order<<<nblocks(H.m, 256), 256, 0, c.stream>>>(H.ids, H.m, need, eq, flags);
+    SM_LAUNCH_CHECK();
+    const int n = compact(c, flags, H.m, idx, tag + ".gc");
+    if (n > 0) {
+        k_map_ids<<<nblocks(n, 256), 256, 0, c.stream>>>(idx, n, H.ids, out);
+        SM_LAUNCH_CHECK();
+    }
+    return n;
+}
+
 void build_grid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &box, float g,
                 bool sortCells, Grid &G, const std::string &tag) {
     float ext[3] = {box.ext(0), box.ext(1), box.ext(2)};
@@ -690,6 +785,7 @@ void build_hgrid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &bo
     int  *start  = c.arena.get<int>(tag + ".start", T + 1);
     int  *slotOf = c.arena.get<int>(tag + ".slotOf", std::max(m, 1));
     H.ids        = c.arena.get<int>(tag + ".ids", std::max(m, 1));
+    H.pts        = c.arena.get<float4>(tag + ".pts", std::max(m, 1));
     H.slot       = c.arena.get<uint4>(tag + ".slot", T);
     SM_CUDA(cudaMemsetAsync(keys, 0xff, (size_t)T * 8, c.stream));
     SM_CUDA(cudaMemsetAsync(cnt, 0, (size_t)(T + 1) * 4, c.stream));
@@ -702,7 +798,7 @@ void build_hgrid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &bo
     int *fill = cnt;
     SM_CUDA(cudaMemcpyAsync(fill, start, (size_t)T * 4, cudaMemcpyDeviceToDevice, c.stream));
     if (m > 0) {
-        k_hg_scatter<<<nblocks(m, 256), 256, 0, c.stream>>>(ids, slotOf, m, fill, H.ids);
+        k_hg_scatter<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, slotOf, m, fill, H.ids, H.pts);
         SM_LAUNCH_CHECK();
     }
     // counts again for the packed table: start[t+1] - start[t]
@@ -783,18 +879,22 @@ void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *
     k_mark_todo<<<nblocks(m, 256), 256, 0, c.stream>>>(ids, m, nrm, need);
     SM_LAUNCH_CHECK();
     int *todo  = c.arena.get<int>(tag + ".todo", m);
-    int  ntodo = compact_eq(c, need, npoints, 2, todo, tag + ".ct");
+    int  ntodo = compact_grid_order(c, query, need, 2, todo, tag + ".ct");
     int *nbrT  = c.arena.get<int>(tag + ".nbrT", (size_t)std::max(ntodo, 1) * k);
     int *cntT  = c.arena.get<int>(tag + ".cntT", std::max(ntodo, 1));
-    launch_knn(c.stream, todo, ntodo, query.view(), pos, k, nbrT, cntT, smooth ? 1 : 0, nrm, need);
+    int *pend  = c.arena.get<int>(tag + ".pend", (size_t)npoints + 1);
+    int *npend = pend + npoints;
+    launch_knn(c.stream, todo, ntodo, query.view(), pos, k, nbrT, cntT, smooth ? 1 : 0, nrm, need,
+               pend, npend);
     int  nextra = 0;
     int *extra = nullptr, *nbrE = nullptr, *cntE = nullptr;
     if (smooth && ntodo > 0) {
         extra  = c.arena.get<int>(tag + ".extra", npoints);
-        nextra = compact_eq(c, need, npoints, 1, extra, tag + ".ce");
+        nextra = compact_grid_order(c, query, need, 1, extra, tag + ".ce");
         nbrE   = c.arena.get<int>(tag + ".nbrE", (size_t)std::max(nextra, 1) * k);
         cntE   = c.arena.get<int>(tag + ".cntE", std::max(nextra, 1));
-        launch_knn(c.stream, extra, nextra, query.view(), pos, k, nbrE, cntE, 0, nrm, need);
+        launch_knn(c.stream, extra, nextra, query.view(), pos, k, nbrE, cntE, 0, nrm, need, pend,
+                   npend);
     }
     const int nmax = std::max(ntodo, nextra);
     float4   *cen  = c.arena.get<float4>(tag + ".cen", 2 * (size_t)std::max(nmax, 1));

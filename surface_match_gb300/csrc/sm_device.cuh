@@ -31,14 +31,16 @@ struct GridView {
 // Device view of a hashed uniform grid: only occupied cells are stored, in an
 // open-addressed table of uint4 {key low, key high, first point, point count} (count 0 =
 // empty slot), so cells can be as fine as the queries want whatever the scene's extent,
-// and the table stays small enough to live in L2.
+// and the table stays small enough to live in L2. The points of a cell are contiguous in
+// `pts` (position, point index in w), so a search reads them without an indirection.
 struct HGridView {
-    float       org[3];
-    float       g;
-    int         dim[3];
-    const uint4 *slot;
-    uint32_t    mask;
-    const int  *ids;
+    float         org[3];
+    float         g;
+    int           dim[3];
+    const uint4  *slot;
+    uint32_t      mask;
+    const int    *ids;
+    const float4 *pts;
     __device__ __forceinline__ void range(int x, int y, int z, int &s, int &e) const {
         const unsigned long long key =
             ((unsigned long long)z * (unsigned)dim[1] + (unsigned)y) * (unsigned)dim[0] + (unsigned)x;
@@ -77,7 +79,8 @@ template <class G> __device__ __forceinline__ int grid_max_shell(const G &g, con
     return m;
 }
 
-// Visit every point of the cells at Chebyshev distance exactly s from cell c.
+// Visit every point (position, index in w) of the cells at Chebyshev distance exactly s from
+// cell c.
 template <class G, class F>
 __device__ __forceinline__ void grid_shell(const G &g, const int c[3], int s, F &&f) {
     const int z0 = max(c[2] - s, 0), z1 = min(c[2] + s, g.dim[2] - 1);
@@ -92,40 +95,47 @@ __device__ __forceinline__ void grid_shell(const G &g, const int c[3], int s, F 
                 int b, e;
                 g.range(x, y, z, b, e);
                 for (int k = b; k < e; k++)
-                    f(g.ids[k]);
+                    f(g.pts[k]);
             }
         }
     }
 }
 
-// k nearest neighbours of q by (squared distance, index); returns how many were found.
-// K is the capacity of the (register-resident when K is small) candidate lists.
+// k nearest neighbours of q by (squared distance, index), k <= K; returns how many were
+// found. The lists li/ld have the fixed capacity K: slots [0, K-k) hold sentinels smaller
+// than any point and the neighbours fill [K-k, K) in ascending order, so every index is a
+// compile-time constant and the lists stay in registers. The search stops after `maxShell`
+// shells when that does not decide it; *done then says whether the result is final.
 template <int K, class G>
-__device__ __forceinline__ int grid_knn(const G &g, const float4 *__restrict__ pos, float qx,
-                                        float qy, float qz, int k, int *oi, float *od) {
+__device__ __forceinline__ int grid_knn(const G &g, float qx, float qy, float qz, int k,
+                                        int (&li)[K], float (&ld)[K], int maxShell = 0x7fffffff,
+                                        bool *done = nullptr) {
     int c[3];
     grid_cc(g, qx, qy, qz, c);
-    int   n = 0;
-    int   li[K];
-    float ld[K];
+    bool fin = false;
+    int  n   = 0;
 #pragma unroll
     for (int j = 0; j < K; j++) {
-        li[j] = 0x7fffffff;
-        ld[j] = 3.402823466e+38f;
+        const bool sent = j < K - k;
+        li[j]           = sent ? -1 : 0x7fffffff;
+        ld[j]           = sent ? -1.0f : 3.402823466e+38f;
     }
     const int ms = grid_max_shell(g, c);
     for (int s = 0; s <= ms; s++) {
-        grid_shell(g, c, s, [&](int id) {
-            const float4 p = pos[id];
-            const float  d = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
-            // insert (d, id) into the sorted lists, capacity k (k <= K)
-            if (!(d < ld[k - 1] || (d == ld[k - 1] && id < li[k - 1])))
+        if (s > maxShell)
+            break;
+        if (s == ms)
+            fin = true;
+        grid_shell(g, c, s, [&](const float4 p) {
+            const int   id = __float_as_int(p.w);
+            const float d  = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
+            if (!(d < ld[K - 1] || (d == ld[K - 1] && id < li[K - 1])))
                 return;
             float cd = d;
             int   ci = id;
 #pragma unroll
             for (int j = 0; j < K; j++) {
-                if (j < k && (cd < ld[j] || (cd == ld[j] && ci < li[j]))) {
+                if (cd < ld[j] || (cd == ld[j] && ci < li[j])) {
                     const float td = ld[j];
                     const int   ti = li[j];
                     ld[j]          = cd;
@@ -138,15 +148,13 @@ __device__ __forceinline__ int grid_knn(const G &g, const float4 *__restrict__ p
                 n++;
         });
         const float b = smg::ring_bound(s, g.g);
-        if (n == k && ld[k - 1] < b * b)
+        if (n == k && ld[K - 1] < b * b) {
+            fin = true;
             break;
-    }
-#pragma unroll
-    for (int j = 0; j < K; j++)
-        if (j < k) {
-            oi[j] = li[j];
-            od[j] = ld[j];
         }
+    }
+    if (done)
+        *done = fin;
     return n;
 }
 
@@ -154,7 +162,7 @@ __device__ __forceinline__ int grid_knn(const G &g, const float4 *__restrict__ p
 // `limit2` (or `maxShell` shells); returns -1 when none was found. `exact` is set when the
 // result is the true nearest point or provably no point lies within limit2.
 template <class G>
-__device__ __forceinline__ int grid_nn(const G &g, const float4 *__restrict__ pos, float qx,
+__device__ __forceinline__ int grid_nn(const G &g, float qx,
                                        float qy, float qz, float limit2, float &outd,
                                        int maxShell = 0x7fffffff, bool *exact = nullptr) {
     int c[3];
@@ -164,9 +172,9 @@ __device__ __forceinline__ int grid_nn(const G &g, const float4 *__restrict__ po
     const int ms   = min(grid_max_shell(g, c), maxShell);
     bool      done = false;
     for (int s = 0; s <= ms; s++) {
-        grid_shell(g, c, s, [&](int id) {
-            const float4 p = pos[id];
-            const float  d = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
+        grid_shell(g, c, s, [&](const float4 p) {
+            const int   id = __float_as_int(p.w);
+            const float d  = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
             if (d < bd || (d == bd && id < best)) {
                 bd   = d;
                 best = id;
@@ -186,17 +194,15 @@ __device__ __forceinline__ int grid_nn(const G &g, const float4 *__restrict__ po
     return best;
 }
 
-// Exact nearest neighbour through a fine grid first (cheap when a point is close) and a
-// coarse grid over the same points when the fine grid's first shells cannot decide.
-template <class G>
-__device__ __forceinline__ int grid_nn2(const G &fine, const G &coarse, int fineShells,
-                                        const float4 *__restrict__ pos, float qx, float qy,
-                                        float qz, float limit2, float &outd) {
-    bool      exact = false;
-    const int j     = grid_nn(fine, pos, qx, qy, qz, limit2, outd, fineShells, &exact);
-    if (exact)
-        return j;
-    return grid_nn(coarse, pos, qx, qy, qz, limit2, outd);
+__device__ __forceinline__ int warp_incl_scan(int v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o)
+            v += t;
+    }
+    return v;
 }
 
 __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
@@ -208,12 +214,31 @@ __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v)
     return v;
 }
 
+// The m-th smallest key (m >= 1) over the warp's fixed-capacity lists T (removing the m
+// smallest from T); ~0 when the warp holds fewer than m keys.
+template <int K>
+__device__ __forceinline__ unsigned long long warp_kth(unsigned long long (&T)[K], int m) {
+    unsigned long long r = ~0ull;
+    for (int round = 0; round < m; round++) {
+        unsigned long long mine = ~0ull;
+#pragma unroll
+        for (int j = 0; j < K; j++)
+            mine = T[j] < mine ? T[j] : mine;
+        r = warp_min_u64(mine);
+#pragma unroll
+        for (int j = 0; j < K; j++)
+            if (T[j] == r)
+                T[j] = ~0ull;
+    }
+    return r;
+}
+
 // Warp-cooperative exact nearest neighbour: all 32 lanes call it with the same query; the
 // cells of each shell are split over the lanes and the (distance bits, index) minimum is
 // taken across the warp, so near and far queries cost the warp the same work pattern. Same
 // result and termination rule as grid_nn.
 template <class G>
-__device__ __forceinline__ int warp_nn(const G &g, const float4 *__restrict__ pos, float qx,
+__device__ __forceinline__ int warp_nn(const G &g, float qx,
                                        float qy, float qz, float limit2, float &outd) {
     const int lane = threadIdx.x & 31;
     int       c[3];
@@ -232,8 +257,8 @@ __device__ __forceinline__ int warp_nn(const G &g, const float4 *__restrict__ po
             int b, e;
             g.range(x, y, z, b, e);
             for (int k = b; k < e; k++) {
-                const int    id = g.ids[k];
-                const float4 p  = pos[id];
+                const float4 p  = g.pts[k];
+                const int    id = __float_as_int(p.w);
                 const float  d  = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
                 const unsigned long long key =
                     ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)id;
@@ -255,18 +280,191 @@ __device__ __forceinline__ int warp_nn(const G &g, const float4 *__restrict__ po
     return (int)(unsigned)(best & 0xffffffffu);
 }
 
+// Warp-cooperative exact k nearest neighbours: all 32 lanes call it with the same query; the
+// cells of each shell are split over the lanes, each lane keeps its k best keys (distance
+// bits, index, plus one; fixed capacity K with zero sentinels in front as in grid_knn), and
+// the warp's k-th best decides termination with grid_knn's rule, so the result is
+// grid_knn's. For queries far from their neighbours (many shells). Returns the count found;
+// every lane gets the neighbours in li/ld slots [K-k, K) like grid_knn.
+template <int K, class G>
+__device__ __forceinline__ int warp_knn(const G &g, float qx, float qy, float qz, int k,
+                                        int (&li)[K], float (&ld)[K]) {
+    const int lane = threadIdx.x & 31;
+    int       c[3];
+    grid_cc(g, qx, qy, qz, c);
+    unsigned long long L[K];
+#pragma unroll
+    for (int j = 0; j < K; j++)
+        L[j] = j < K - k ? 0ull : ~0ull;
+    int       seen = 0;
+    const int ms   = grid_max_shell(g, c);
+    for (int s = 0; s <= ms; s++) {
+        const int w = 2 * s + 1, cube = w * w * w;
+        for (int t = lane; t < cube; t += 32) {
+            const int dx = t % w - s, dy = (t / w) % w - s, dz = t / (w * w) - s;
+            if (max(abs(dx), max(abs(dy), abs(dz))) != s)
+                continue;
+            const int x = c[0] + dx, y = c[1] + dy, z = c[2] + dz;
+            if (x < 0 || y < 0 || z < 0 || x >= g.dim[0] || y >= g.dim[1] || z >= g.dim[2])
+                continue;
+            int b, e;
+            g.range(x, y, z, b, e);
+            for (int q = b; q < e; q++) {
+                const float4 p  = g.pts[q];
+                const int    id = __float_as_int(p.w);
+                const float  d  = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
+                unsigned long long key =
+                    (((unsigned long long)__float_as_uint(d) << 32) | (unsigned)id) + 1ull;
+                seen++;
+                if (!(key < L[K - 1]))
+                    continue;
+#pragma unroll
+                for (int j = 0; j < K; j++) {
+                    if (key < L[j]) {
+                        const unsigned long long t2 = L[j];
+                        L[j]                        = key;
+                        key                         = t2;
+                    }
+                }
+            }
+        }
+        int tot = seen;
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1)
+            tot += __shfl_xor_sync(0xffffffffu, tot, o);
+        if (s == 0 || tot < k)
+            continue; // a shell-0 search never decides (its ring bound is 0)
+        unsigned long long T[K];
+#pragma unroll
+        for (int j = 0; j < K; j++)
+            T[j] = j < K - k ? ~0ull : L[j];
+        const unsigned long long m   = warp_kth<K>(T, k);
+        const float              bnd = smg::ring_bound(s, g.g);
+        if (__uint_as_float((unsigned)((m - 1ull) >> 32)) < bnd * bnd)
+            break;
+    }
+    unsigned long long T[K];
+#pragma unroll
+    for (int j = 0; j < K; j++)
+        T[j] = j < K - k ? ~0ull : L[j];
+    int n = 0;
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+        li[j] = -1;
+        ld[j] = -1.0f;
+    }
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+        if (j < K - k)
+            continue;
+        const unsigned long long m = warp_kth<K>(T, 1);
+        if (m == ~0ull) {
+            li[j] = 0x7fffffff;
+            ld[j] = 3.402823466e+38f;
+            continue;
+        }
+        li[j] = (int)(unsigned)((m - 1ull) & 0xffffffffu);
+        ld[j] = __uint_as_float((unsigned)((m - 1ull) >> 32));
+        n++;
+    }
+    return n;
+}
+
+// grid_knn(..., maxShell = 1) by a warp: lane l < 27 probes the l-th cell of the query's
+// 3x3x3 block, a prefix sum over the cells' point counts flattens their points, and the
+// lanes take 32 points per round into lane-local fixed-capacity lists (keys as in
+// warp_knn), merged at the end. Same neighbours and *done as the thread search; every lane
+// gets li/ld like grid_knn.
+template <int K>
+__device__ __forceinline__ int warp_knn1(const HGridView &g, float qx, float qy, float qz, int k,
+                                         int (&li)[K], float (&ld)[K], bool *done) {
+    const int lane = threadIdx.x & 31;
+    int       c[3];
+    grid_cc(g, qx, qy, qz, c);
+    int b = 0, e = 0;
+    if (lane < 27) {
+        const int x = c[0] + lane % 3 - 1, y = c[1] + (lane / 3) % 3 - 1, z = c[2] + lane / 9 - 1;
+        if (x >= 0 && y >= 0 && z >= 0 && x < g.dim[0] && y < g.dim[1] && z < g.dim[2])
+            g.range(x, y, z, b, e);
+    }
+    const int cnt  = e - b;
+    const int incl = warp_incl_scan(cnt);
+    const int excl = incl - cnt;
+    const int T    = __shfl_sync(0xffffffffu, incl, 31);
+    unsigned long long L[K];
+#pragma unroll
+    for (int j = 0; j < K; j++)
+        L[j] = j < K - k ? 0ull : ~0ull;
+    for (int base = 0; base < T; base += 32) {
+        const int r = base + lane;
+        // the cell holding candidate r: last lane j with excl_j <= r
+        int lo = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const int mid = lo + step;
+            const int ev  = __shfl_sync(0xffffffffu, excl, mid & 31);
+            if (mid < 27 && ev <= r)
+                lo = mid;
+        }
+        const int bj = __shfl_sync(0xffffffffu, b, lo);
+        const int ej = __shfl_sync(0xffffffffu, excl, lo);
+        if (r >= T)
+            continue;
+        const float4 p  = g.pts[bj + (r - ej)];
+        const float  d  = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
+        unsigned long long key =
+            (((unsigned long long)__float_as_uint(d) << 32) | (unsigned)__float_as_int(p.w)) + 1ull;
+        if (!(key < L[K - 1]))
+            continue;
+#pragma unroll
+        for (int j = 0; j < K; j++) {
+            if (key < L[j]) {
+                const unsigned long long t2 = L[j];
+                L[j]                        = key;
+                key                         = t2;
+            }
+        }
+    }
+    unsigned long long Tq[K];
+#pragma unroll
+    for (int j = 0; j < K; j++)
+        Tq[j] = j < K - k ? ~0ull : L[j];
+    int n = 0;
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+        li[j] = -1;
+        ld[j] = -1.0f;
+    }
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+        if (j < K - k)
+            continue;
+        const unsigned long long m = warp_kth<K>(Tq, 1);
+        if (m == ~0ull) {
+            li[j] = 0x7fffffff;
+            ld[j] = 3.402823466e+38f;
+            continue;
+        }
+        li[j] = (int)(unsigned)((m - 1ull) & 0xffffffffu);
+        ld[j] = __uint_as_float((unsigned)((m - 1ull) >> 32));
+        n++;
+    }
+    const float bnd = smg::ring_bound(1, g.g);
+    *done           = (n == k && ld[K - 1] < bnd * bnd) || grid_max_shell(g, c) <= 1;
+    return n;
+}
+
 template <class G>
-__device__ __forceinline__ bool grid_any_within(const G &g, const float4 *__restrict__ pos, float qx,
+__device__ __forceinline__ bool grid_any_within(const G &g, float qx,
                                                 float qy, float qz, float r2) {
     int c[3];
     grid_cc(g, qx, qy, qz, c);
     const int ms = grid_max_shell(g, c);
     for (int s = 0; s <= ms; s++) {
         bool hit = false;
-        grid_shell(g, c, s, [&](int id) {
+        grid_shell(g, c, s, [&](const float4 p) {
             if (hit)
                 return;
-            const float4 p = pos[id];
             if (smm::dist2(qx, qy, qz, p.x, p.y, p.z) < r2)
                 hit = true;
         });
@@ -295,16 +493,6 @@ __host__ __device__ __forceinline__ float ord2f(int i) {
 #endif
 }
 
-__device__ __forceinline__ int warp_incl_scan(int v) {
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o)
-            v += t;
-    }
-    return v;
-}
 
 // Block-wide exclusive scan of one int per thread (blockDim.x <= 1024, multiple of 32).
 // `sh` needs 33 ints. Returns the exclusive prefix; *total gets the block sum.

@@ -111,6 +111,7 @@ struct HGrid {
     uint4    *slot   = nullptr;
     uint32_t  mask   = 0;
     int      *ids    = nullptr;
+    float4   *pts    = nullptr; // positions in cell order, point index in w (bit pattern)
     int       m      = 0;
     smd::HGridView view() const {
         smd::HGridView v;
@@ -122,6 +123,7 @@ struct HGrid {
         v.slot = slot;
         v.mask = mask;
         v.ids  = ids;
+        v.pts  = pts;
         return v;
     }
 };
