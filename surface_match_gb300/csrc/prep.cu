@@ -253,15 +253,31 @@ __global__ void k_phase_scatter(const int *__restrict__ occ, const int *__restri
     lists[slot]    = occ[i];
 }
 
-// One warp per occupied cell of the current phase: greedy keep/reject in ascending index
-// order against the kept points of the 26 neighbour cells (all from earlier phases) and
-// the cell's own kept points.
-__global__ void k_sample_phase(const float4 *__restrict__ pos, GridView G,
-                               const int *__restrict__ cells, int ncells,
-                               const int *__restrict__ rank, int *__restrict__ keptCnt,
-                               int *__restrict__ keptIds, int cap, float r2,
-                               int *__restrict__ keptFlag, int *__restrict__ overflow) {
-    const int w    = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+constexpr int kSpWarps = 4;   // warps (cells) per CTA of the phase kernel
+constexpr int kSpIds   = 384; // cell sizes held in shared memory
+constexpr int kSpStage = 384; // neighbours' kept points staged in shared memory
+
+// One warp per occupied cell of the current phase. The sequential greedy visits the cell's
+// points by ascending index and keeps a point unless a kept point lies within the step;
+// the kept points of the 26 neighbour cells (earlier phases) are fixed, so the warp first
+// drops every point within the step of one of them (order-free), then repeats "keep the
+// smallest surviving index, drop the survivors within the step of it" - the same kept set
+// as the sequential visit, at (kept points x cell size / 32) work and without sorting.
+// Kept points are recorded as positions (keptPos, `cap` per cell). The neighbours' kept
+// points and the cell's points are staged in shared memory; cells too large for the
+// staging buffers take the same steps in global memory (`alive` flags in aliveTmp).
+__global__ void __launch_bounds__(kSpWarps * 32)
+    k_sample_phase(const float4 *__restrict__ pos, GridView G, const int *__restrict__ cells,
+                   int ncells, const int *__restrict__ rank, int *__restrict__ keptCnt,
+                   float4 *__restrict__ keptPos, int cap, float r2, int *__restrict__ keptFlag,
+                   int *__restrict__ overflow, int *__restrict__ aliveTmp) {
+    __shared__ float4 stage[kSpWarps][kSpStage];
+    __shared__ float4 cpos[kSpWarps][kSpIds];
+    __shared__ int    cid[kSpWarps][kSpIds];
+    __shared__ int    calive[kSpWarps][kSpIds];
+    __shared__ int    snr[kSpWarps][26], scnt[kSpWarps][26];
+    const int wl   = threadIdx.x >> 5;
+    const int w    = blockIdx.x * kSpWarps + wl;
     const int lane = threadIdx.x & 31;
     if (w >= ncells)
         return;
@@ -269,68 +285,107 @@ __global__ void k_sample_phase(const float4 *__restrict__ pos, GridView G,
     const int rk   = rank[cell];
     const int cx = cell % G.dim[0], cy = (cell / G.dim[0]) % G.dim[1],
               cz = cell / (G.dim[0] * G.dim[1]);
-    const int s = G.start[cell], e = G.start[cell + 1];
-    int      *mine = keptIds + (size_t)rk * cap;
-    int       nk   = 0;
-    for (int base = s; base < e; base += 32) {
-        const int  i   = base + lane;
-        const bool act = i < e;
-        const int  id  = act ? G.ids[i] : 0;
-        float4     q   = act ? pos[id] : make_float4(0.f, 0.f, 0.f, 0.f);
-        bool       ok  = act;
-        for (int dz = -1; dz <= 1; dz++) {
-            const int z = cz + dz;
-            if (z < 0 || z >= G.dim[2])
-                continue;
-            for (int dy = -1; dy <= 1; dy++) {
-                const int y = cy + dy;
-                if (y < 0 || y >= G.dim[1])
-                    continue;
-                for (int dx = -1; dx <= 1; dx++) {
-                    const int x = cx + dx;
-                    if (x < 0 || x >= G.dim[0] || (dx == 0 && dy == 0 && dz == 0))
-                        continue;
-                    const int nr = rank[grid_cell(G, x, y, z)];
-                    if (nr < 0)
-                        continue;
-                    const int  cnt  = keptCnt[nr];
-                    const int *list = keptIds + (size_t)nr * cap;
-                    for (int k = 0; k < cnt && ok; k++) {
-                        const float4 o = pos[list[k]];
-                        if (smm::dist2(o.x, o.y, o.z, q.x, q.y, q.z) < r2)
-                            ok = false;
-                    }
+    const int s = G.start[cell], e = G.start[cell + 1], n = e - s;
+    // neighbour l (lane < 26) of the 3x3x3 block without its centre
+    int nr = -1, cnt = 0;
+    if (lane < 26) {
+        const int o = lane < 13 ? lane : lane + 1;
+        const int x = cx + o % 3 - 1, y = cy + (o / 3) % 3 - 1, z = cz + o / 9 - 1;
+        if (x >= 0 && y >= 0 && z >= 0 && x < G.dim[0] && y < G.dim[1] && z < G.dim[2]) {
+            nr  = rank[grid_cell(G, x, y, z)];
+            cnt = nr >= 0 ? keptCnt[nr] : 0;
+        }
+        snr[wl][lane]  = nr;
+        scnt[wl][lane] = cnt;
+    }
+    __syncwarp();
+    const int  incl    = warp_incl_scan(cnt);
+    const int  excl    = incl - cnt;
+    const int  NK      = __shfl_sync(0xffffffffu, incl, 31);
+    const bool stageNb = NK <= kSpStage;
+    const bool stageC  = n <= kSpIds;
+    float4    *st      = stage[wl];
+    if (stageNb) {
+        for (int base = 0; base < NK; base += 32) {
+            const int t  = base + lane;
+            int       lo = 0;
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+                const int mid = lo + step;
+                const int ev  = __shfl_sync(0xffffffffu, excl, mid & 31);
+                if (mid < 26 && ev <= t)
+                    lo = mid;
+            }
+            const int nj = __shfl_sync(0xffffffffu, nr, lo);
+            const int ej = __shfl_sync(0xffffffffu, excl, lo);
+            if (t < NK)
+                st[t] = keptPos[(size_t)nj * cap + (t - ej)];
+        }
+    }
+    int *alive = stageC ? calive[wl] : aliveTmp + s;
+    // survivors of the neighbours' kept points
+    for (int i = lane; i < n; i += 32) {
+        const int    id = G.ids[s + i];
+        const float4 q  = pos[id];
+        bool         ok = true;
+        if (stageNb) {
+            for (int k = 0; k < NK && ok; k++) {
+                const float4 o = st[k];
+                if (smm::dist2(o.x, o.y, o.z, q.x, q.y, q.z) < r2)
+                    ok = false;
+            }
+        } else {
+            for (int j = 0; j < 26 && ok; j++) {
+                const int nj = snr[wl][j], cj = scnt[wl][j];
+                for (int k = 0; k < cj && ok; k++) {
+                    const float4 o = keptPos[(size_t)nj * cap + k];
+                    if (smm::dist2(o.x, o.y, o.z, q.x, q.y, q.z) < r2)
+                        ok = false;
                 }
             }
         }
-        for (int k = 0; k < nk && ok; k++) {
-            const float4 o = pos[mine[k]];
-            if (smm::dist2(o.x, o.y, o.z, q.x, q.y, q.z) < r2)
-                ok = false;
+        alive[i] = ok ? 1 : 0;
+        if (stageC) {
+            cid[wl][i]  = id;
+            cpos[wl][i] = q;
         }
-        unsigned mask = __ballot_sync(0xffffffffu, ok);
-        while (mask) {
-            const int   leader = __ffs(mask) - 1;
-            const int   lid    = __shfl_sync(0xffffffffu, id, leader);
-            const float lx     = __shfl_sync(0xffffffffu, q.x, leader);
-            const float ly     = __shfl_sync(0xffffffffu, q.y, leader);
-            const float lz     = __shfl_sync(0xffffffffu, q.z, leader);
-            if (lane == 0) {
-                if (nk < cap)
-                    mine[nk] = lid;
-                else
-                    atomicExch(overflow, 1);
+    }
+    __syncwarp();
+    // keep the smallest surviving index, drop the survivors within the step, repeat
+    float4 *mine = keptPos + (size_t)rk * cap;
+    int     nk   = 0;
+    for (;;) {
+        int myMin = INT_MAX;
+        for (int i = lane; i < n; i += 32)
+            if (alive[i]) {
+                const int id = stageC ? cid[wl][i] : G.ids[s + i];
+                myMin        = min(myMin, id);
             }
-            if (lane == leader) {
-                keptFlag[id] = 1;
-                ok           = false;
-            } else if (ok && lane > leader && smm::dist2(lx, ly, lz, q.x, q.y, q.z) < r2) {
-                ok = false;
-            }
-            nk = min(nk + 1, cap);
-            __syncwarp();
-            mask = __ballot_sync(0xffffffffu, ok);
+        int m = myMin;
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1)
+            m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (m == INT_MAX)
+            break;
+        const float4 kp4 = pos[m];
+        const float4 kp  = make_float4(kp4.x, kp4.y, kp4.z, 0.0f);
+        if (lane == 0) {
+            keptFlag[m] = 1;
+            if (nk < cap)
+                mine[nk] = kp;
+            else
+                atomicExch(overflow, 1);
         }
+        nk = min(nk + 1, cap);
+        for (int i = lane; i < n; i += 32) {
+            if (!alive[i])
+                continue;
+            const int    id = stageC ? cid[wl][i] : G.ids[s + i];
+            const float4 q  = stageC ? cpos[wl][i] : pos[id];
+            if (id == m || smm::dist2(kp.x, kp.y, kp.z, q.x, q.y, q.z) < r2)
+                alive[i] = 0;
+        }
+        __syncwarp();
     }
     if (lane == 0)
         keptCnt[rk] = nk;
@@ -813,7 +868,7 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
     float ext[3] = {box.ext(0), box.ext(1), box.ext(2)};
     const float g = smg::sample_cell(step, ext);
     Grid        G;
-    build_grid(c, pos, ids, m, box, g, true, G, tag + ".g");
+    build_grid(c, pos, ids, m, box, g, false, G, tag + ".g");
     int *occFlag = c.arena.get<int>(tag + ".occf", G.nc);
     k_occ_flags<<<nblocks(G.nc, 256), 256, 0, c.stream>>>(G.start, G.nc, occFlag);
     SM_LAUNCH_CHECK();
@@ -843,7 +898,8 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
     const double s   = (double)g / (double)step;
     const int    cap = (int)std::floor((s + 1.0) * (s + 1.0) * (s + 1.0) / (3.14159265358979 / 6.0)) + 1;
     int *keptCnt  = c.arena.get<int>(tag + ".kc", std::max(nocc, 1));
-    int *keptIds  = c.arena.get<int>(tag + ".ki", (size_t)std::max(nocc, 1) * cap);
+    float4 *keptPos = c.arena.get<float4>(tag + ".kp", (size_t)std::max(nocc, 1) * cap);
+    int    *aliveTmp = c.arena.get<int>(tag + ".al", std::max(m, 1));
     int *keptFlag = c.arena.get<int>(tag + ".kf", std::max(npoints, 1) + 1);
     int *overflow = keptFlag + npoints;
     SM_CUDA(cudaMemsetAsync(keptCnt, 0, std::max(nocc, 1) * sizeof(int), c.stream));
@@ -853,8 +909,9 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
         const int nc = off[p + 1] - off[p];
         if (nc == 0)
             continue;
-        k_sample_phase<<<nblocks((long long)nc * 32, 256), 256, 0, c.stream>>>(
-            pos, G.view(), lists + off[p], nc, rank, keptCnt, keptIds, cap, r2, keptFlag, overflow);
+        k_sample_phase<<<nblocks(nc, kSpWarps), kSpWarps * 32, 0, c.stream>>>(
+            pos, G.view(), lists + off[p], nc, rank, keptCnt, keptPos, cap, r2, keptFlag, overflow,
+            aliveTmp);
         SM_LAUNCH_CHECK();
     }
     const int kept = compact(c, keptFlag, npoints, outIds, tag + ".out");
