@@ -1,11 +1,21 @@
 // cluster.cu - pose clustering of matchScene (ppf.cpp:414-418): sortPoses, clusterPose,
 // avgClusters, sortPoses, clusterPose2 (util.cpp:486-601).
 //
-// One CTA. The sorts are stable rank-by-counting sorts on (votes desc, list position).
-// The two greedy first-fit clusterings are sequential by definition (a pose joins the
-// first earlier cluster head it is compatible with); warp 0 walks the poses in order and
-// tests the current heads 32 at a time with a ballot. Sums run in member order, so the
-// result is identical to the oracle's sequential restatement.
+// Three kernels. k_cluster_a (one CTA): stable rank-by-counting sort on (votes desc, list
+// position), then clusterPose, a greedy first-fit clustering (a pose joins the first
+// earlier head it is compatible with). Its compatibility of every pose with every earlier
+// pose is evaluated in parallel into a bit matrix in shared memory; heads are then
+// resolved in parallel rounds (a pose compatible with a head is a member, one whose
+// compatible earlier poses are all members is a head), which reproduces the sequential
+// decisions, and a member's cluster is its lowest compatible head - the first in creation
+// order. Larger pose lists walk the poses with one warp instead. k_cluster_avg: one block
+// per cluster sums its members in pose order (FP32 translation, FP64 quaternion moments)
+// and averages them, so the clusters' FP64 work spreads over the SMs. k_cluster_b (one
+// CTA): the second sort and clusterPose2. Results are identical to the oracle's
+// sequential restatement.
+#include <cmath>
+#include <cstring>
+
 #include "sm_icp.h"
 #include "sm_stages.h"
 
@@ -13,76 +23,187 @@ namespace sm {
 
 namespace {
 
-constexpr int kClBs = 1024;
-constexpr int PF    = smi::kPoseFloats;
+constexpr int kClBs   = 1024;
+constexpr int PF      = smi::kPoseFloats;
+constexpr int kClMaxC = 1024; // poses for which the compatibility bits are precomputed
 
-__device__ __forceinline__ float norm3(float x, float y, float z) {
-    return smm::fsqrt(x * x + (y * y + z * z));
-}
-
-// out[rank(i)] = in[i] for the stable sort by votes (float 17) descending.
-__device__ void stable_sort_votes(const float *in, int n, float *out) {
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const float v    = in[(size_t)i * PF + 17];
-        int         rank = 0;
-        for (int j = 0; j < n; j++) {
-            const float u = in[(size_t)j * PF + 17];
-            rank += (u > v || (u == v && j < i)) ? 1 : 0;
-        }
-        for (int e = 0; e < PF; e++)
-            out[(size_t)rank * PF + e] = in[(size_t)i * PF + e];
-    }
-}
+// Shared-memory bytes per pose of k_cluster_a: sort key (float4), votes and one int list.
+constexpr int kClPerPose = 16 + 2 * 4;
 
 struct ClArgs {
     const float *poses;
     int          np;
-    float        distThr, angThr, cx, cy, cz, thr2;
-    float       *sorted;  // np x PF
-    int         *clu, *next, *tail, *heads; // np each
-    float       *avg;     // np x PF (cluster creation order)
-    float       *avgSorted;
-    float4      *tr;      // np
-    int         *lead2;   // np
-    float       *out;     // np x PF
+    float        sqThr, angThr, cx, cy, cz, thr2;
+    float       *sorted;    // np x PF
+    float       *avg;       // np x PF (cluster creation order)
+    float       *avgSorted; // np x PF
+    float4      *tr;        // np
+    float       *out;       // np x PF
     int         *outCount;
+    float4      *gbuf4;     // np float4 when the per-pose state does not fit shared memory
+    int         *gbuf;      // 2 np ints, likewise
+    float4      *tv, *qv;   // np each: sorted {tx, ty, tz, votes} and quaternions
+    int         *clu;       // np: cluster number per sorted pose
+    int         *heads;     // np: pose index of each cluster head
+    int         *nhOut;     // cluster count
+    int          smemState; // per-pose state in shared memory
+    int          useBits;   // compatibility bits in shared memory
 };
 
-__global__ void __launch_bounds__(kClBs) k_cluster(ClArgs a) {
-    __shared__ int sNh, sNout;
+// out[rank(i)] = in[i] for the stable sort by votes (float 17) descending; `votes` holds
+// the n vote counts. With `key`, also the sorted {tx, ty, tz, angle}, {tx, ty, tz, votes}
+// and quaternion of each pose.
+__device__ void stable_sort_votes(const float *in, const float *votes, int n, float *out,
+                                  float4 *key, float4 *tv, float4 *qv) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const float v    = votes[i];
+        int         rank = 0;
+        for (int j = 0; j < n; j++) {
+            const float u = votes[j];
+            rank += (u > v || (u == v && j < i)) ? 1 : 0;
+        }
+        const float *P = in + (size_t)i * PF;
+        for (int e = 0; e < PF; e++)
+            out[(size_t)rank * PF + e] = P[e];
+        if (key) {
+            key[rank] = make_float4(P[3], P[7], P[11], P[16]);
+            tv[rank]  = make_float4(P[3], P[7], P[11], P[17]);
+            qv[rank]  = make_float4(P[12], P[13], P[14], P[15]);
+        }
+    }
+}
+
+// clusterPose compatibility of pose a with head b (util.cpp:499-520); the distance test
+// sqrt(v) < distThr is evaluated as v < sqThr (exact: see sqrt_lt_bound).
+__device__ __forceinline__ bool compat(const float4 &a, const float4 &b, float sqThr, float angThr) {
+    const float x = a.x - b.x, y = a.y - b.y, z = a.z - b.z;
+    return x * x + (y * y + z * z) < sqThr && smm::fabs_(a.w - b.w) < angThr;
+}
+
+__global__ void __launch_bounds__(kClBs) k_cluster_a(ClArgs a) {
+    extern __shared__ float4 dsm4[];
+    __shared__ int sNh;
     const int      tid = threadIdx.x, lane = tid & 31;
     const int      np  = a.np;
-    stable_sort_votes(a.poses, np, a.sorted);
+    float4        *key   = a.smemState ? dsm4 : a.gbuf4;
+    int           *ib    = a.smemState ? (int *)(dsm4 + np) : a.gbuf;
+    float         *votes = (float *)ib;
+    int           *tail  = ib + np;
+    const int      W     = (np + 31) >> 5;
+    uint32_t      *bits  = (uint32_t *)(ib + 2 * np); // W x np (word-major), when useBits
+    uint32_t      *headB = bits + (size_t)W * np;     // W
+    uint32_t      *unkB  = headB + W;                 // W
+    uint32_t      *newH  = unkB + W;                  // W
+    uint32_t      *newM  = newH + W;                  // W
+    int           *hpre  = (int *)(newM + W);         // W + 1
+    for (int i = tid; i < np; i += kClBs)
+        votes[i] = a.poses[(size_t)i * PF + 17];
     __syncthreads();
-    // clusterPose: warp 0 walks the poses in sorted order
-    if (tid < 32) {
+    stable_sort_votes(a.poses, votes, np, a.sorted, key, a.tv, a.qv);
+    __syncthreads();
+    if (a.useBits) {
+        // word w of row i (stored at bits[w * np + i]), bit b: pose i is compatible with the
+        // earlier pose 32 w + b
+        for (int idx = tid; idx < np * W; idx += kClBs) {
+            const int    w = idx / np, i = idx % np;
+            const float4 P = key[i];
+            uint32_t     m = 0;
+            if (w * 32 < i) {
+                for (int b = 0; b < 32; b++) {
+                    const int j = w * 32 + b;
+                    if (j < i && compat(P, key[j], a.sqThr, a.angThr))
+                        m |= 1u << b;
+                }
+            }
+            bits[idx] = m;
+        }
+        for (int w = tid; w < W; w += kClBs) {
+            headB[w] = 0u;
+            const int rem = np - w * 32;
+            unkB[w]       = rem >= 32 ? 0xffffffffu : ((1u << rem) - 1u);
+        }
+        __syncthreads();
+        // Heads by rounds: an undecided pose compatible with a head is a member; one whose
+        // compatible earlier poses are all decided members is a head. The smallest undecided
+        // pose is decided in every round, and each decision is the sequential one.
+        for (;;) {
+            for (int w = tid; w < W; w += kClBs) {
+                newH[w] = 0u;
+                newM[w] = 0u;
+            }
+            __syncthreads();
+            bool any = false;
+            for (int i = tid; i < np; i += kClBs) {
+                if (!((unkB[i >> 5] >> (i & 31)) & 1u))
+                    continue;
+                any            = true;
+                bool hitHead   = false, hitUnk = false;
+                const int wmax = i >> 5;
+                for (int w = 0; w <= wmax; w++) {
+                    const uint32_t r = bits[(size_t)w * np + i];
+                    hitHead          = hitHead || (r & headB[w]) != 0u;
+                    hitUnk           = hitUnk || (r & unkB[w]) != 0u;
+                }
+                if (hitHead)
+                    atomicOr(&newM[i >> 5], 1u << (i & 31));
+                else if (!hitUnk)
+                    atomicOr(&newH[i >> 5], 1u << (i & 31));
+            }
+            if (!__syncthreads_or(any))
+                break;
+            for (int w = tid; w < W; w += kClBs) {
+                headB[w] |= newH[w];
+                unkB[w] &= ~(newH[w] | newM[w]);
+            }
+            __syncthreads();
+        }
+        // cluster numbers: heads in pose order; a member joins its lowest compatible head
+        if (tid == 0) {
+            int s = 0;
+            for (int w = 0; w < W; w++) {
+                hpre[w] = s;
+                s += __popc(headB[w]);
+            }
+            hpre[W] = s;
+            sNh     = s;
+        }
+        __syncthreads();
+        for (int i = tid; i < np; i += kClBs) {
+            const uint32_t hb = headB[i >> 5];
+            if ((hb >> (i & 31)) & 1u) {
+                const int h = hpre[i >> 5] + __popc(hb & ((1u << (i & 31)) - 1u));
+                a.clu[i]    = h;
+                a.heads[h]  = i;
+                continue;
+            }
+            for (int w = 0; w <= (i >> 5); w++) {
+                const uint32_t r = bits[(size_t)w * np + i] & headB[w];
+                if (r) {
+                    const int b = __ffs(r) - 1;
+                    a.clu[i]    = hpre[w] + __popc(headB[w] & ((1u << b) - 1u));
+                    break;
+                }
+            }
+        }
+    } else if (tid < 32) {
+        // clusterPose: warp 0 walks the poses in sorted order, 32 heads per step
         int nh = 0;
         for (int i = 0; i < np; i++) {
-            const float *P     = a.sorted + (size_t)i * PF;
-            const float  tx = P[3], ty = P[7], tz = P[11], an = P[16];
+            const float4 P     = key[i];
             int          found = -1;
             for (int h0 = 0; h0 < nh && found < 0; h0 += 32) {
-                const int h  = h0 + lane;
-                bool      ok = false;
-                if (h < nh) {
-                    const float *H = a.sorted + (size_t)a.heads[h] * PF;
-                    const float  d = norm3(tx - H[3], ty - H[7], tz - H[11]);
-                    ok             = d < a.distThr && smm::fabs_(an - H[16]) < a.angThr;
-                }
-                const unsigned m = __ballot_sync(0xffffffffu, ok);
+                const int      h  = h0 + lane;
+                const bool     ok = h < nh && compat(P, key[a.heads[h]], a.sqThr, a.angThr);
+                const unsigned m  = __ballot_sync(0xffffffffu, ok);
                 if (m)
                     found = h0 + __ffs(m) - 1;
             }
             if (lane == 0) {
-                a.next[i] = -1;
                 if (found < 0) {
                     a.heads[nh] = i;
                     a.clu[i]    = nh;
-                    a.tail[nh]  = i;
                 } else {
-                    a.clu[i]              = found;
-                    a.next[a.tail[found]] = i;
-                    a.tail[found]         = i;
+                    a.clu[i] = found;
                 }
             }
             if (found < 0)
@@ -93,27 +214,47 @@ __global__ void __launch_bounds__(kClBs) k_cluster(ClArgs a) {
             sNh = nh;
     }
     __syncthreads();
-    const int nh = sNh;
-    // avgClusters: mean translation, summed votes, Markley quaternion average
-    for (int h = tid; h < nh; h += kClBs) {
-        float  px = 0.f, py = 0.f, pz = 0.f, votes = 0.f;
-        double S[10];
+    if (tid == 0)
+        *a.nhOut = sNh;
+    (void)tail;
+}
+
+// avgClusters: one block per cluster (grid-stride); the warp finds the members in pose
+// order 32 at a time, lane 0 sums them in that order (mean translation, summed votes,
+// Markley quaternion average in FP64).
+__global__ void k_cluster_avg(ClArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int nh   = *a.nhOut;
+    for (int h = blockIdx.x; h < nh; h += gridDim.x) {
+        const int head = a.heads[h];
+        float     px = 0.f, py = 0.f, pz = 0.f, vs = 0.f;
+        double    S[10];
         for (int e = 0; e < 10; e++)
             S[e] = 0.0;
         int cnt = 0;
-        for (int i = a.heads[h]; i >= 0; i = a.next[i]) {
-            const float *P = a.sorted + (size_t)i * PF;
-            px             = px + P[3];
-            py             = py + P[7];
-            pz             = pz + P[11];
-            votes          = votes + P[17];
-            const double v[4] = {P[12], P[13], P[14], P[15]};
-            int          k    = 0;
-            for (int r = 0; r < 4; r++)
-                for (int s = r; s < 4; s++)
-                    S[k++] += v[r] * v[s];
-            cnt++;
+        for (int base = head; base < a.np; base += 32) {
+            const int      i   = base + lane;
+            const bool     mem = i < a.np && a.clu[i] == h;
+            const uint32_t m   = __ballot_sync(0xffffffffu, mem);
+            if (lane == 0) {
+                for (uint32_t r = m; r; r &= r - 1) {
+                    const int    k  = base + __ffs(r) - 1;
+                    const float4 t = a.tv[k], q4 = a.qv[k];
+                    px             = px + t.x;
+                    py             = py + t.y;
+                    pz             = pz + t.z;
+                    vs             = vs + t.w;
+                    const double v[4] = {q4.x, q4.y, q4.z, q4.w};
+                    int          e    = 0;
+                    for (int rr = 0; rr < 4; rr++)
+                        for (int ss = rr; ss < 4; ss++)
+                            S[e++] += v[rr] * v[ss];
+                    cnt++;
+                }
+            }
         }
+        if (lane != 0)
+            continue;
         double q[4], R[9];
         sml::quat_average_from_sum(S, cnt, q);
         sml::quat_to_mat(q, R);
@@ -128,12 +269,22 @@ __global__ void __launch_bounds__(kClBs) k_cluster(ClArgs a) {
         for (int r = 0; r < 4; r++)
             O[12 + r] = (float)q[r];
         O[16] = sml::quat_angle(q);
-        O[17] = votes;
+        O[17] = vs;
     }
+}
+
+// sortPoses of the averaged clusters and clusterPose2 (overlap of the transformed model-box
+// centres); one block.
+__global__ void __launch_bounds__(kClBs) k_cluster_b(ClArgs a) {
+    __shared__ int sNout;
+    const int      tid = threadIdx.x, lane = tid & 31;
+    const int      nh  = *a.nhOut;
+    float         *votes = (float *)a.gbuf;
+    for (int h = tid; h < nh; h += kClBs)
+        votes[h] = a.avg[(size_t)h * PF + 17];
     __syncthreads();
-    stable_sort_votes(a.avg, nh, a.avgSorted);
+    stable_sort_votes(a.avg, votes, nh, a.avgSorted, nullptr, nullptr, nullptr);
     __syncthreads();
-    // clusterPose2: overlap of the transformed model-box centres
     for (int h = tid; h < nh; h += kClBs) {
         smi::Pose34 T;
         for (int e = 0; e < 12; e++)
@@ -183,6 +334,26 @@ __global__ void __launch_bounds__(kClBs) k_cluster(ClArgs a) {
         *a.outCount = sNout;
 }
 
+// Smallest float v >= 0 with sqrtf(v) >= t (IEEE square root is correctly rounded and
+// monotone, so sqrtf(v) < t <=> v < this bound, NaN included).
+float sqrt_lt_bound(float t) {
+    if (!(t > 0.0f))
+        return 0.0f;
+    uint32_t lo = 0, hi = 0x7f800000u; // +0 .. +inf
+    while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        float          v;
+        memcpy(&v, &mid, 4);
+        if (std::sqrt(v) >= t)
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    float r;
+    memcpy(&r, &lo, 4);
+    return r;
+}
+
 } // namespace
 
 int cluster(Ctx &c, const float *poses, int np, float distThr, float angThr, const float center[3],
@@ -192,25 +363,41 @@ int cluster(Ctx &c, const float *poses, int np, float distThr, float angThr, con
     ClArgs a;
     a.poses     = poses;
     a.np        = np;
-    a.distThr   = distThr;
+    a.sqThr     = sqrt_lt_bound(distThr);
     a.angThr    = angThr;
     a.cx        = center[0];
     a.cy        = center[1];
     a.cz        = center[2];
     a.thr2      = maxOverlap * maxOverlap;
     a.sorted    = c.arena.get<float>(tag + ".sorted", (size_t)np * PF);
-    int *ib     = c.arena.get<int>(tag + ".ints", (size_t)np * 5 + 1);
-    a.clu       = ib;
-    a.next      = ib + np;
-    a.tail      = ib + 2 * np;
-    a.heads     = ib + 3 * np;
-    a.lead2     = ib + 4 * np;
-    a.outCount  = ib + 5 * np;
     a.avg       = c.arena.get<float>(tag + ".avg", (size_t)np * PF);
     a.avgSorted = c.arena.get<float>(tag + ".avgs", (size_t)np * PF);
     a.tr        = c.arena.get<float4>(tag + ".tr", np);
     a.out       = outCands;
-    k_cluster<<<1, kClBs, 0, c.stream>>>(a);
+    a.outCount  = c.arena.get<int>(tag + ".count", 1);
+    a.gbuf4     = c.arena.get<float4>(tag + ".g4", np);
+    a.gbuf      = c.arena.get<int>(tag + ".gi", (size_t)np * 2);
+    a.tv        = c.arena.get<float4>(tag + ".tv", np);
+    a.qv        = c.arena.get<float4>(tag + ".qv", np);
+    int *ints   = c.arena.get<int>(tag + ".ints", (size_t)np * 2 + 1);
+    a.clu       = ints;
+    a.heads     = ints + np;
+    a.nhOut     = ints + 2 * (size_t)np;
+    int optin = 0;
+    SM_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));
+    const size_t W     = ((size_t)np + 31) / 32;
+    const size_t state = (size_t)np * kClPerPose;
+    const size_t bitsB = ((size_t)np * W + 6 * W + 1) * 4;
+    a.smemState        = state + 1024 <= (size_t)optin ? 1 : 0;
+    a.useBits          = a.smemState && np <= kClMaxC && state + bitsB + 1024 <= (size_t)optin ? 1 : 0;
+    const size_t smem  = a.smemState ? state + (a.useBits ? bitsB : 0) : 0;
+    if (smem)
+        SM_CUDA(cudaFuncSetAttribute(k_cluster_a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_cluster_a<<<1, kClBs, smem, c.stream>>>(a);
+    SM_LAUNCH_CHECK();
+    k_cluster_avg<<<std::min(np, 152 * 8), 32, 0, c.stream>>>(a);
+    SM_LAUNCH_CHECK();
+    k_cluster_b<<<1, kClBs, 0, c.stream>>>(a);
     SM_LAUNCH_CHECK();
     SM_CUDA(cudaMemcpyAsync(c.hostCounts, a.outCount, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     c.sync();
