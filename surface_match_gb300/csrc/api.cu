@@ -8,7 +8,9 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -590,6 +592,23 @@ void match_into(Ctx &c, const Model &m, const float *xyz, const float *nrm, int6
 Model *model_core(sm_model m) { return &m->m; }
 Ctx   *model_ctx(sm_model m) { return &m->ctx->ctx; }
 int    run_guarded(const std::function<void()> &f) { return guarded(f); }
+
+size_t allow_dynamic_smem(const void *kernel, int device) {
+    static std::mutex                                mu;
+    static std::map<std::pair<const void *, int>, size_t> done;
+    std::lock_guard<std::mutex>                      lk(mu);
+    auto                                             it = done.find({kernel, device});
+    if (it != done.end())
+        return it->second;
+    int optin = 0;
+    SM_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+    cudaFuncAttributes fa;
+    SM_CUDA(cudaFuncGetAttributes(&fa, kernel));
+    const size_t avail = (size_t)optin - fa.sharedSizeBytes;
+    SM_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)avail));
+    done[{kernel, device}] = avail;
+    return avail;
+}
 
 } // namespace sm
 

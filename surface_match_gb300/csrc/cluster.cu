@@ -391,8 +391,8 @@ int cluster(Ctx &c, const float *poses, int np, float distThr, float angThr, con
     a.smemState        = state + 1024 <= (size_t)optin ? 1 : 0;
     a.useBits          = a.smemState && np <= kClMaxC && state + bitsB + 1024 <= (size_t)optin ? 1 : 0;
     const size_t smem  = a.smemState ? state + (a.useBits ? bitsB : 0) : 0;
-    if (smem)
-        SM_CUDA(cudaFuncSetAttribute(k_cluster_a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (smem > allow_dynamic_smem((const void *)k_cluster_a, c.device))
+        throw Error(SM_ERR_CAPACITY, "shared-memory request above the device limit");
     k_cluster_a<<<1, kClBs, smem, c.stream>>>(a);
     SM_LAUNCH_CHECK();
     k_cluster_avg<<<std::min(np, 152 * 8), 32, 0, c.stream>>>(a);

@@ -30,8 +30,12 @@ SML_HD double dsqrt(double a) {
 SML_HD double dabs(double a) { return a < 0.0 ? -a : a; }
 
 // Cyclic Jacobi eigen-decomposition of a symmetric N x N matrix (Golub & Van Loan,
-// "Matrix Computations", 8.5). A is destroyed; d[i] are the eigenvalues, column i of V the
-// matching unit eigenvector. Fixed sweep order, so the result is reproducible.
+// "Matrix Computations", 8.5): each rotation zeroes a_pq and, by symmetry, updates only the
+// diagonal pair and the off-diagonal entries of rows p and q. Sweeps stop once the
+// off-diagonal mass falls below 1e-24 of the matrix's (relative size 1e-12, far below the
+// float precision of every result taken from it). A is destroyed (its upper triangle holds
+// the state); d[i] are the eigenvalues, column i of V the matching unit eigenvector. Fixed
+// sweep order, so the result is reproducible.
 template <int N> SML_HD void jacobi_eig(double A[N][N], double V[N][N], double d[N]) {
     for (int i = 0; i < N; i++)
         for (int j = 0; j < N; j++)
@@ -45,7 +49,7 @@ template <int N> SML_HD void jacobi_eig(double A[N][N], double V[N][N], double d
         for (int p = 0; p < N - 1; p++)
             for (int q = p + 1; q < N; q++)
                 off += A[p][q] * A[p][q];
-        if (!(off > scale * 1e-32))
+        if (!(off > scale * 1e-24))
             break;
         for (int p = 0; p < N - 1; p++) {
             for (int q = p + 1; q < N; q++) {
@@ -58,15 +62,18 @@ template <int N> SML_HD void jacobi_eig(double A[N][N], double V[N][N], double d
                     t = -t;
                 const double c = 1.0 / dsqrt(t * t + 1.0);
                 const double s = t * c;
-                for (int k = 0; k < N; k++) {
-                    const double akp = A[k][p], akq = A[k][q];
-                    A[k][p]          = c * akp - s * akq;
-                    A[k][q]          = s * akp + c * akq;
-                }
-                for (int k = 0; k < N; k++) {
-                    const double apk = A[p][k], aqk = A[q][k];
-                    A[p][k]          = c * apk - s * aqk;
-                    A[q][k]          = s * apk + c * aqk;
+                A[p][p]        = A[p][p] - t * apq;
+                A[q][q]        = A[q][q] + t * apq;
+                A[p][q]        = 0.0;
+                for (int r = 0; r < N; r++) {
+                    if (r == p || r == q)
+                        continue;
+                    // a_rp, a_rq in the upper triangle
+                    double &arp = r < p ? A[r][p] : A[p][r];
+                    double &arq = r < q ? A[r][q] : A[q][r];
+                    const double g = arp, h = arq;
+                    arp            = c * g - s * h;
+                    arq            = s * g + c * h;
                 }
                 for (int k = 0; k < N; k++) {
                     const double vkp = V[k][p], vkq = V[k][q];

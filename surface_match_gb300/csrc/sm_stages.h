@@ -113,6 +113,11 @@ void match_into(Ctx &c, const Model &m, const float *xyz, const float *nrm, int6
 std::unique_ptr<Ctx> acquire_worker(int device);
 void                 release_worker(int device, std::unique_ptr<Ctx> c);
 
+// Raise a kernel's dynamic shared-memory limit to the device maximum, once per kernel and
+// device (the attribute is per function and process-wide: setting it to each launch's own
+// size would race between concurrent worker threads). Returns the usable bytes.
+size_t allow_dynamic_smem(const void *kernel, int device);
+
 // Access to a model handle's engine state and the C ABI's error handling, for entry points
 // defined outside api.cu.
 Model *model_core(sm_model m);

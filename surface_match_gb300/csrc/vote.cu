@@ -249,7 +249,8 @@ void vote_fused(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, co
                                    &a.refChunk, &a.refChunkWide);
     if (!smem)
         throw Error(SM_ERR_CAPACITY, "featAngleResolution too large for the vote accumulator");
-    SM_CUDA(cudaFuncSetAttribute(k_vote_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (smem > allow_dynamic_smem((const void *)k_vote_fused, c.device))
+        throw Error(SM_ERR_CAPACITY, "shared-memory request above the device limit");
     k_vote_fused<<<K, kVoteBs, smem, c.stream>>>(a);
     SM_LAUNCH_CHECK();
 }

@@ -419,7 +419,8 @@ void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const in
     }
     k_lpt<<<1, 1024, 0, c.stream>>>(b.votes, K, b.order);
     SM_LAUNCH_CHECK();
-    SM_CUDA(cudaFuncSetAttribute(k_vote_acc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (smem > allow_dynamic_smem((const void *)k_vote_acc, c.device))
+        throw Error(SM_ERR_CAPACITY, "shared-memory request above the device limit");
     k_vote_acc<<<K, kAccBs, smem, c.stream>>>(a, b);
     SM_LAUNCH_CHECK();
 }
