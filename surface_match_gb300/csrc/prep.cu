@@ -543,13 +543,15 @@ __global__ void k_hg_scatter(const float4 *__restrict__ pos, const int *__restri
 
 __global__ void k_hg_pack_from_start(const unsigned long long *__restrict__ keys,
                                      const int *__restrict__ start, uint32_t T,
-                                     uint4 *__restrict__ slot) {
+                                     uint4 *__restrict__ slot, uint32_t *__restrict__ occ) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= T)
         return;
-    const unsigned long long k = keys[t];
-    slot[t] = make_uint4((uint32_t)k, (uint32_t)(k >> 32), (uint32_t)start[t],
-                         (uint32_t)(start[t + 1] - start[t]));
+    const unsigned long long k   = keys[t];
+    const uint32_t           cnt = (uint32_t)(start[t + 1] - start[t]);
+    slot[t] = make_uint4((uint32_t)k, (uint32_t)(k >> 32), (uint32_t)start[t], cnt);
+    if (occ && cnt)
+        atomicOr(&occ[k >> 5], 1u << (k & 31));
 }
 
 // Query lists in the query grid's cell order: a warp then searches 32 neighbouring queries
@@ -856,8 +858,16 @@ void build_hgrid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &bo
         k_hg_scatter<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, slotOf, m, fill, H.ids, H.pts);
         SM_LAUNCH_CHECK();
     }
+    // occupancy bits over the cell box, when it has at most 2^28 cells (32 MB)
+    const unsigned long long ncell = (unsigned long long)H.dim[0] * H.dim[1] * H.dim[2];
+    H.occ = nullptr;
+    if (ncell <= (1ull << 28)) {
+        const size_t words = (size_t)((ncell + 31) / 32);
+        H.occ              = c.arena.get<uint32_t>(tag + ".occ", words);
+        SM_CUDA(cudaMemsetAsync(H.occ, 0, words * 4, c.stream));
+    }
     // counts again for the packed table: start[t+1] - start[t]
-    k_hg_pack_from_start<<<nblocks(T, 256), 256, 0, c.stream>>>(keys, start, T, H.slot);
+    k_hg_pack_from_start<<<nblocks(T, 256), 256, 0, c.stream>>>(keys, start, T, H.slot, H.occ);
     SM_LAUNCH_CHECK();
 }
 

@@ -32,7 +32,8 @@ struct GridView {
 // open-addressed table of uint4 {key low, key high, first point, point count} (count 0 =
 // empty slot), so cells can be as fine as the queries want whatever the scene's extent,
 // and the table stays small enough to live in L2. The points of a cell are contiguous in
-// `pts` (position, point index in w), so a search reads them without an indirection.
+// `pts` (position, point index in w), so a search reads them without an indirection, and
+// an occupancy bitmap over the cell box lets searches skip empty cells without a probe.
 struct HGridView {
     float         org[3];
     float         g;
@@ -41,9 +42,14 @@ struct HGridView {
     uint32_t      mask;
     const int    *ids;
     const float4 *pts;
+    const uint32_t *occ; // one bit per cell of the dim box (nullptr: not built)
     __device__ __forceinline__ void range(int x, int y, int z, int &s, int &e) const {
         const unsigned long long key =
             ((unsigned long long)z * (unsigned)dim[1] + (unsigned)y) * (unsigned)dim[0] + (unsigned)x;
+        if (occ && !((occ[key >> 5] >> (key & 31)) & 1u)) {
+            s = e = 0; // empty cell: no table probe
+            return;
+        }
         uint32_t h = (uint32_t)smm::mix64(key) & mask;
         for (uint32_t p = 0; p <= mask; p++) {
             const uint4 v = slot[h];

@@ -112,6 +112,7 @@ struct HGrid {
     uint32_t  mask   = 0;
     int      *ids    = nullptr;
     float4   *pts    = nullptr; // positions in cell order, point index in w (bit pattern)
+    uint32_t *occ    = nullptr; // occupancy bit per cell (nullptr when the cell box is too large)
     int       m      = 0;
     smd::HGridView view() const {
         smd::HGridView v;
@@ -124,6 +125,7 @@ struct HGrid {
         v.mask = mask;
         v.ids  = ids;
         v.pts  = pts;
+        v.occ  = occ;
         return v;
     }
 };
