@@ -84,7 +84,9 @@ typedef struct {
     int64_t n_hits;       /* pairs whose key is in the model table */
     int64_t n_votes;      /* votes cast: matched table entries (ppf.cpp:342-346) */
     float   ms[8];        /* stage device times (ms): prep, sampling + normals, keypoints,
-                             vote kernel, clustering, refinement prep, refinement, total */
+                             voting, clustering, refinement prep, refinement, total */
+    float   vote_ms[2];   /* device times (ms) of the voting stage's two main kernels: pair
+                             features + table probes, shared-memory accumulation + peaks */
 } sm_match_stats;
 
 /* TrainParam / MatchParam defaults and constructor validation (type.cpp:71-127). */

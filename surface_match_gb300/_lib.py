@@ -31,7 +31,8 @@ class MatchStatsC(C.Structure):
     _fields_ = [("n_points", C.c_int64), ("n_valid", C.c_int64), ("n_sampled", C.c_int64),
                 ("n_keypoints", C.c_int64), ("n_resampled", C.c_int64),
                 ("n_poses", C.c_int64), ("n_clusters", C.c_int64), ("n_pairs", C.c_int64),
-                ("n_hits", C.c_int64), ("n_votes", C.c_int64), ("ms", C.c_float * 8)]
+                ("n_hits", C.c_int64), ("n_votes", C.c_int64), ("ms", C.c_float * 8),
+                ("vote_ms", C.c_float * 2)]
 
 
 _lock = threading.Lock()

@@ -527,6 +527,10 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
         const int stage[8][2] = {{0, 1}, {1, 2}, {2, 3}, {8, 9}, {4, 5}, {5, 6}, {6, 7}, {0, 7}};
         for (int i = 0; i < 8; i++)
             SM_CUDA(cudaEventElapsedTime(&stats->ms[i], c.ev[stage[i][0]], c.ev[stage[i][1]]));
+        if (K > 0) {
+            SM_CUDA(cudaEventElapsedTime(&stats->vote_ms[0], c.ev[10], c.ev[11]));
+            SM_CUDA(cudaEventElapsedTime(&stats->vote_ms[1], c.ev[12], c.ev[13]));
+        }
     }
 }
 

@@ -19,7 +19,7 @@ struct Ctx {
     bool         ownStream = false;
     Arena        arena;
     int         *hostCounts = nullptr; // pinned scratch for small device->host reads
-    cudaEvent_t  ev[10]{};
+    cudaEvent_t  ev[14]{}; // stage timing (api.cu), vote-kernel timing 10..13 (vote_pipe.cu)
     // intermediate state of the last match (device pointers into the arena + sizes)
     struct Last {
         int  n = 0, ns = 0, nk = 0, nr = 0, np = 0, nc = 0, ncand = 0;

@@ -412,17 +412,21 @@ void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const in
     SM_CUDA(cudaMemsetAsync(b.votes, 0, (size_t)K * sizeof(unsigned long long), c.stream));
     k_rows_fill<<<K, 256, 0, c.stream>>>(a, b, csr ? 1 : 0);
     SM_LAUNCH_CHECK();
+    SM_CUDA(cudaEventRecord(c.ev[10], c.stream));
     if (rtot > 0) {
         const int g = (int)std::min<long long>(nblocks(rtot, 256), 152LL * 8);
         k_ppf<<<g, 256, 0, c.stream>>>(a, b, b.rowOff + K);
         SM_LAUNCH_CHECK();
     }
+    SM_CUDA(cudaEventRecord(c.ev[11], c.stream));
     k_lpt<<<1, 1024, 0, c.stream>>>(b.votes, K, b.order);
     SM_LAUNCH_CHECK();
+    SM_CUDA(cudaEventRecord(c.ev[12], c.stream));
     if (smem > allow_dynamic_smem((const void *)k_vote_acc, c.device))
         throw Error(SM_ERR_CAPACITY, "shared-memory request above the device limit");
     k_vote_acc<<<K, kAccBs, smem, c.stream>>>(a, b);
     SM_LAUNCH_CHECK();
+    SM_CUDA(cudaEventRecord(c.ev[13], c.stream));
 }
 
 } // namespace sm

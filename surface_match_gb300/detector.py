@@ -195,8 +195,10 @@ class Detector:
                                     scores.ctypes.data_as(C.POINTER(C.c_float)), C.byref(count),
                                     C.byref(st)))
         k = count.value
-        self.last_stats = {f: getattr(st, f) for f, _ in MatchStatsC._fields_ if f != "ms"}
+        self.last_stats = {f: getattr(st, f) for f, _ in MatchStatsC._fields_
+                           if f not in ("ms", "vote_ms")}
         self.last_stats["ms"] = list(st.ms)
+        self.last_stats["vote_ms"] = list(st.vote_ms)
         if matchResult is not None:
             pos = self.debug(3)
             nrm_ = self.debug(4)
@@ -349,7 +351,8 @@ def match_batch(jobs, samplingDistanceRel=0.04, keyPointFraction=0.2, minScore=0
                           i32(count), i32(status), concurrency, stats)
     _check(rc)
     out = [(poses[j, :count[j]], scores[j, :count[j]]) for j in range(nj)]
-    st = [{f: getattr(s, f) for f, _ in MatchStatsC._fields_ if f != "ms"} | {"ms": list(s.ms)}
+    st = [{f: getattr(s, f) for f, _ in MatchStatsC._fields_ if f not in ("ms", "vote_ms")} |
+          {"ms": list(s.ms), "vote_ms": list(s.vote_ms)}
           for s in stats]
     return out, st
 
