@@ -402,102 +402,34 @@ __global__ void k_mark_todo(const int *__restrict__ ids, int m, const float4 *__
         need[id] = 2;
 }
 
-// Neighbours of one query (slots [K-k, K) of li, ascending): the lists, and for smoothing the
-// marking of neighbours that still need a normal.
-template <int K>
-__device__ __forceinline__ void knn_store(int t, int k, int n, const int (&li)[K],
-                                          int *__restrict__ nbr, int *__restrict__ nbrCnt,
-                                          int markNeighbours, const float4 *__restrict__ nrm,
-                                          int *__restrict__ need) {
-    int *out = nbr + (size_t)t * k - (K - k);
-#pragma unroll
-    for (int j = 0; j < K; j++)
-        if (j >= K - k)
-            out[j] = j - (K - k) < n ? li[j] : -1;
-    nbrCnt[t] = n;
-    if (markNeighbours) {
-#pragma unroll
-        for (int j = 0; j < K; j++) {
-            if (j < K - k || j - (K - k) >= n)
-                continue;
-            const int id = li[j];
-            if (need[id] == 0 && !finite3(nrm[id].x, nrm[id].y, nrm[id].z))
-                need[id] = 1;
-        }
-    }
-}
-
-// One warp per query over the query's cell and its 26 neighbours (the query grid's cell is
-// chosen so that this decides almost every query); undecided queries are queued for
-// k_knn_warp.
-template <int K>
+// One warp per query (exact k nearest neighbours, sm_device.cuh warp_knn_sorted); lane j
+// writes the j-th neighbour, and with smoothing marks it when it still needs a normal.
 __global__ void k_knn(const int *__restrict__ list, int nl, HGridView G, const float4 *__restrict__ pos,
                       int k, int *__restrict__ nbr, int *__restrict__ nbrCnt, int markNeighbours,
-                      const float4 *__restrict__ nrm, int *__restrict__ need,
-                      int *__restrict__ pend, int *__restrict__ npend) {
+                      const float4 *__restrict__ nrm, int *__restrict__ need) {
     const int lane = threadIdx.x & 31;
     const int t    = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     if (t >= nl)
         return;
     const float4 q = pos[list[t]];
-    int          li[K];
-    float        ld[K];
-    bool         done = false;
-    const int    n    = warp_knn1<K>(G, q.x, q.y, q.z, k, li, ld, &done);
-    if (lane != 0)
-        return;
-    if (!done) {
-        pend[atomicAdd(npend, 1)] = t;
-        return;
-    }
-    knn_store<K>(t, k, n, li, nbr, nbrCnt, markNeighbours, nrm, need);
-}
-
-// The queued queries, one warp each: the lanes split each shell's cells (same result as the
-// thread search run to the end).
-template <int K>
-__global__ void k_knn_warp(const int *__restrict__ list, const int *__restrict__ pend,
-                           const int *__restrict__ npend, HGridView G,
-                           const float4 *__restrict__ pos, int k, int *__restrict__ nbr,
-                           int *__restrict__ nbrCnt, int markNeighbours,
-                           const float4 *__restrict__ nrm, int *__restrict__ need) {
-    const int lane = threadIdx.x & 31;
-    const int np   = *npend;
-    for (int w = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5); w < np;
-         w += (gridDim.x * blockDim.x) >> 5) {
-        const int    t = pend[w];
-        const float4 q = pos[list[t]];
-        int          li[K];
-        float        ld[K];
-        const int    n = warp_knn<K>(G, q.x, q.y, q.z, k, li, ld);
-        if (lane == 0)
-            knn_store<K>(t, k, n, li, nbr, nbrCnt, markNeighbours, nrm, need);
-    }
-}
-
-template <int K>
-void launch_knn_k(cudaStream_t st, const int *list, int nl, const HGridView &G, const float4 *pos,
-                  int k, int *nbr, int *cnt, int mark, const float4 *nrm, int *need, int *pend,
-                  int *npend) {
-    SM_CUDA(cudaMemsetAsync(npend, 0, sizeof(int), st));
-    k_knn<K><<<nblocks((long long)nl * 32, 256), 256, 0, st>>>(list, nl, G, pos, k, nbr, cnt, mark,
-                                                                nrm, need, pend, npend);
-    SM_LAUNCH_CHECK();
-    k_knn_warp<K><<<152 * 4, 256, 0, st>>>(list, pend, npend, G, pos, k, nbr, cnt, mark, nrm, need);
-    SM_LAUNCH_CHECK();
+    int          id;
+    float        d;
+    const int    n = warp_knn_sorted(G, q.x, q.y, q.z, k, &id, &d);
+    if (lane < k)
+        nbr[(size_t)t * k + lane] = lane < n ? id : -1;
+    if (lane == 0)
+        nbrCnt[t] = n;
+    if (markNeighbours && lane < n && need[id] == 0 && !finite3(nrm[id].x, nrm[id].y, nrm[id].z))
+        need[id] = 1;
 }
 
 void launch_knn(cudaStream_t st, const int *list, int nl, const HGridView &G, const float4 *pos,
-                int k, int *nbr, int *cnt, int mark, const float4 *nrm, int *need, int *pend,
-                int *npend) {
+                int k, int *nbr, int *cnt, int mark, const float4 *nrm, int *need) {
     if (nl <= 0)
         return;
-    if (k <= 10)
-        launch_knn_k<10>(st, list, nl, G, pos, k, nbr, cnt, mark, nrm, need, pend, npend);
-    else if (k <= 16)
-        launch_knn_k<16>(st, list, nl, G, pos, k, nbr, cnt, mark, nrm, need, pend, npend);
-    else
-        launch_knn_k<kMaxKnn>(st, list, nl, G, pos, k, nbr, cnt, mark, nrm, need, pend, npend);
+    k_knn<<<nblocks((long long)nl * 32, 256), 256, 0, st>>>(list, nl, G, pos, k, nbr, cnt, mark,
+                                                            nrm, need);
+    SM_LAUNCH_CHECK();
 }
 
 // ---- hashed grid build -----------------------------------------------------------------
@@ -949,10 +881,7 @@ void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *
     int  ntodo = compact_grid_order(c, query, need, 2, todo, tag + ".ct");
     int *nbrT  = c.arena.get<int>(tag + ".nbrT", (size_t)std::max(ntodo, 1) * k);
     int *cntT  = c.arena.get<int>(tag + ".cntT", std::max(ntodo, 1));
-    int *pend  = c.arena.get<int>(tag + ".pend", (size_t)npoints + 1);
-    int *npend = pend + npoints;
-    launch_knn(c.stream, todo, ntodo, query.view(), pos, k, nbrT, cntT, smooth ? 1 : 0, nrm, need,
-               pend, npend);
+    launch_knn(c.stream, todo, ntodo, query.view(), pos, k, nbrT, cntT, smooth ? 1 : 0, nrm, need);
     int  nextra = 0;
     int *extra = nullptr, *nbrE = nullptr, *cntE = nullptr;
     if (smooth && ntodo > 0) {
@@ -960,8 +889,7 @@ void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *
         nextra = compact_grid_order(c, query, need, 1, extra, tag + ".ce");
         nbrE   = c.arena.get<int>(tag + ".nbrE", (size_t)std::max(nextra, 1) * k);
         cntE   = c.arena.get<int>(tag + ".cntE", std::max(nextra, 1));
-        launch_knn(c.stream, extra, nextra, query.view(), pos, k, nbrE, cntE, 0, nrm, need, pend,
-                   npend);
+        launch_knn(c.stream, extra, nextra, query.view(), pos, k, nbrE, cntE, 0, nrm, need);
     }
     const int nmax = std::max(ntodo, nextra);
     float4   *cen  = c.arena.get<float4>(tag + ".cen", 2 * (size_t)std::max(nmax, 1));

@@ -376,87 +376,105 @@ __device__ __forceinline__ int warp_knn(const G &g, float qx, float qy, float qz
     return n;
 }
 
-// grid_knn(..., maxShell = 1) by a warp: lane l < 27 probes the l-th cell of the query's
-// 3x3x3 block, a prefix sum over the cells' point counts flattens their points, and the
-// lanes take 32 points per round into lane-local fixed-capacity lists (keys as in
-// warp_knn), merged at the end. Same neighbours and *done as the thread search; every lane
-// gets li/ld like grid_knn.
-template <int K>
-__device__ __forceinline__ int warp_knn1(const HGridView &g, float qx, float qy, float qz, int k,
-                                         int (&li)[K], float (&ld)[K], bool *done) {
+// Ascending bitonic sort of one 64-bit key per lane across the warp.
+__device__ __forceinline__ unsigned long long warp_bitonic_sort(unsigned long long key) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const unsigned long long o  = __shfl_xor_sync(0xffffffffu, key, j);
+            const bool               up = (lane & k) == 0, lower = (lane & j) == 0;
+            key = (lower == up) ? (o < key ? o : key) : (o > key ? o : key);
+        }
+    }
+    return key;
+}
+
+// The 32 smallest of two ascending warp-wide lists (one key per lane), ascending.
+__device__ __forceinline__ unsigned long long warp_merge_low(unsigned long long r,
+                                                             unsigned long long sorted) {
+    const int                lane = threadIdx.x & 31;
+    const unsigned long long rev  = __shfl_sync(0xffffffffu, sorted, 31 - lane);
+    unsigned long long       m    = rev < r ? rev : r; // bitonic, holds the 32 smallest
+#pragma unroll
+    for (int j = 16; j > 0; j >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, m, j);
+        m                          = (lane & j) == 0 ? (o < m ? o : m) : (o > m ? o : m);
+    }
+    return m;
+}
+
+// Exact k nearest neighbours (k <= 32) of q by (squared distance, index), one warp per
+// query. Shell by shell, the lanes probe 32 cells at a time (occupancy bit, table), a prefix
+// sum flattens the probed cells' points, and each round of 32 points is sorted across the
+// lanes and merged into the running 32 best (lane j holds the j-th smallest key: distance
+// bits, index); rounds with no point below the current k-th best are skipped. Termination
+// is grid_knn's rule (after shell s, the k-th distance below the ring bound), so the result
+// is grid_knn's. Returns the number found (<= k); lane j < that count gets the j-th
+// neighbour's index in *id and squared distance in *d.
+template <class G>
+__device__ __forceinline__ int warp_knn_sorted(const G &g, float qx, float qy, float qz, int k,
+                                               int *id, float *d) {
     const int lane = threadIdx.x & 31;
     int       c[3];
     grid_cc(g, qx, qy, qz, c);
-    int b = 0, e = 0;
-    if (lane < 27) {
-        const int x = c[0] + lane % 3 - 1, y = c[1] + (lane / 3) % 3 - 1, z = c[2] + lane / 9 - 1;
-        if (x >= 0 && y >= 0 && z >= 0 && x < g.dim[0] && y < g.dim[1] && z < g.dim[2])
-            g.range(x, y, z, b, e);
-    }
-    const int cnt  = e - b;
-    const int incl = warp_incl_scan(cnt);
-    const int excl = incl - cnt;
-    const int T    = __shfl_sync(0xffffffffu, incl, 31);
-    unsigned long long L[K];
+    unsigned long long best = ~0ull; // lane j: j-th smallest so far
+    int                seen = 0;
+    const int          ms   = max(grid_max_shell(g, c), 1);
+    // shells 0 and 1 together: the query's 3x3x3 block (no decision is possible at shell 0)
+    for (int s = 1; s <= ms; s++) {
+        const int lo = s == 1 ? 0 : s, w = 2 * s + 1, cube = w * w * w;
+        for (int t0 = 0; t0 < cube; t0 += 32) {
+            const int t  = t0 + lane;
+            int       b = 0, e = 0;
+            if (t < cube) {
+                const int dx = t % w - s, dy = (t / w) % w - s, dz = t / (w * w) - s;
+                const int r  = max(abs(dx), max(abs(dy), abs(dz)));
+                const int x = c[0] + dx, y = c[1] + dy, z = c[2] + dz;
+                if (r >= lo && x >= 0 && y >= 0 && z >= 0 && x < g.dim[0] && y < g.dim[1] &&
+                    z < g.dim[2])
+                    g.range(x, y, z, b, e);
+            }
+            const int cnt  = e - b;
+            const int incl = warp_incl_scan(cnt);
+            const int excl = incl - cnt;
+            const int T    = __shfl_sync(0xffffffffu, incl, 31);
+            seen += T;
+            for (int base = 0; base < T; base += 32) {
+                const int r  = base + lane;
+                int       lo2 = 0; // the lane whose cell holds point r: last lane with excl <= r
 #pragma unroll
-    for (int j = 0; j < K; j++)
-        L[j] = j < K - k ? 0ull : ~0ull;
-    for (int base = 0; base < T; base += 32) {
-        const int r = base + lane;
-        // the cell holding candidate r: last lane j with excl_j <= r
-        int lo = 0;
-#pragma unroll
-        for (int step = 16; step >= 1; step >>= 1) {
-            const int mid = lo + step;
-            const int ev  = __shfl_sync(0xffffffffu, excl, mid & 31);
-            if (mid < 27 && ev <= r)
-                lo = mid;
-        }
-        const int bj = __shfl_sync(0xffffffffu, b, lo);
-        const int ej = __shfl_sync(0xffffffffu, excl, lo);
-        if (r >= T)
-            continue;
-        const float4 p  = g.pts[bj + (r - ej)];
-        const float  d  = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
-        unsigned long long key =
-            (((unsigned long long)__float_as_uint(d) << 32) | (unsigned)__float_as_int(p.w)) + 1ull;
-        if (!(key < L[K - 1]))
-            continue;
-#pragma unroll
-        for (int j = 0; j < K; j++) {
-            if (key < L[j]) {
-                const unsigned long long t2 = L[j];
-                L[j]                        = key;
-                key                         = t2;
+                for (int step = 16; step >= 1; step >>= 1) {
+                    const int mid = lo2 + step;
+                    const int ev  = __shfl_sync(0xffffffffu, excl, mid);
+                    if (ev <= r)
+                        lo2 = mid;
+                }
+                const int bj = __shfl_sync(0xffffffffu, b, lo2);
+                const int ej = __shfl_sync(0xffffffffu, excl, lo2);
+                unsigned long long key = ~0ull;
+                if (r < T) {
+                    const float4 p  = g.pts[bj + (r - ej)];
+                    const float  dd = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
+                    key = ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)__float_as_int(p.w);
+                }
+                const unsigned long long kth = __shfl_sync(0xffffffffu, best, k - 1);
+                if (!__any_sync(0xffffffffu, key < kth))
+                    continue;
+                best = warp_merge_low(best, warp_bitonic_sort(key));
             }
         }
-    }
-    unsigned long long Tq[K];
-#pragma unroll
-    for (int j = 0; j < K; j++)
-        Tq[j] = j < K - k ? ~0ull : L[j];
-    int n = 0;
-#pragma unroll
-    for (int j = 0; j < K; j++) {
-        li[j] = -1;
-        ld[j] = -1.0f;
-    }
-#pragma unroll
-    for (int j = 0; j < K; j++) {
-        if (j < K - k)
-            continue;
-        const unsigned long long m = warp_kth<K>(Tq, 1);
-        if (m == ~0ull) {
-            li[j] = 0x7fffffff;
-            ld[j] = 3.402823466e+38f;
-            continue;
+        if (seen >= k) {
+            const unsigned long long kth = __shfl_sync(0xffffffffu, best, k - 1);
+            const float              bnd = smg::ring_bound(s, g.g);
+            if (__uint_as_float((unsigned)(kth >> 32)) < bnd * bnd)
+                break;
         }
-        li[j] = (int)(unsigned)((m - 1ull) & 0xffffffffu);
-        ld[j] = __uint_as_float((unsigned)((m - 1ull) >> 32));
-        n++;
     }
-    const float bnd = smg::ring_bound(1, g.g);
-    *done           = (n == k && ld[K - 1] < bnd * bnd) || grid_max_shell(g, c) <= 1;
+    const int n = min(seen, k);
+    *id         = (int)(unsigned)(best & 0xffffffffu);
+    *d          = __uint_as_float((unsigned)(best >> 32));
     return n;
 }
 
