@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(kT) k_corr(Work w, Stage s) {
         smi::pose_apply(C.M, s.src[i].x, s.src[i].y, s.src[i].z, x.x, x.y, x.z);
         smi::pose_rotate(C.M, s.srcN[i].x, s.srcN[i].y, s.srcN[i].z, y.x, y.y, y.z);
         float      d;
-        const int  j  = warp_nn(s.G, x.x, x.y, x.z, s.rej2, d);
+        const int  j  = warp_nn_walk(s.G, x.x, x.y, x.z, s.rej2, d);
         const bool ok = j >= 0 && d <= s.rej2;
         if (lane == 0) {
             x.w       = d;
@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(kT) k_resid(Work w, Stage s) {
         const float4 x = w.x4[o];
         float        y0, y1, y2, d;
         smi::pose_apply(C.step, x.x, x.y, x.z, y0, y1, y2);
-        warp_nn(s.G, y0, y1, y2, FLT_MAX, d);
+        warp_nn_walk(s.G, y0, y1, y2, FLT_MAX, d);
         if ((threadIdx.x & 31) == 0)
             w.terms[(size_t)ci * smi::kNumSystem * w.maxSrc + i] = smm::fsqrt(d);
     }
@@ -364,6 +364,8 @@ __global__ void k_stage_end(Work w, int ncand, int failStatus) {
     }
 }
 
+// Inliers of each candidate: source points with a scene point closer than the scoring
+// distance, one warp per point (warp_any_within).
 __global__ void __launch_bounds__(kT) k_inliers(Work w, const float4 *__restrict__ src, int n,
                                                 HGridView F, float r2) {
     __shared__ int sc[kW];
@@ -371,15 +373,14 @@ __global__ void __launch_bounds__(kT) k_inliers(Work w, const float4 *__restrict
     const Cand    &C  = w.cand[ci];
     if (!C.active)
         return;
-    const int i = blockIdx.x * kT + threadIdx.x;
-    int       c = 0;
-    if (i < n) {
+    const int lane = threadIdx.x & 31;
+    int       c    = 0;
+    for (int i = blockIdx.x * kW + (threadIdx.x >> 5); i < n; i += gridDim.x * kW) {
         float x, y, z;
         smi::pose_apply(C.M, src[i].x, src[i].y, src[i].z, x, y, z);
-        c = grid_any_within(F, x, y, z, r2) ? 1 : 0;
+        c += warp_any_within(F, x, y, z, r2) ? 1 : 0;
     }
-    c = __reduce_add_sync(0xffffffffu, c);
-    if ((threadIdx.x & 31) == 0)
+    if (lane == 0)
         sc[threadIdx.x >> 5] = c;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -480,8 +481,8 @@ void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, con
         run_stage(c, w, s, ncand);
         k_stage_end<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, 2);
         SM_LAUNCH_CHECK();
-        k_inliers<<<dim3(nblocks(m.ns, kT), ncand), kT, 0, c.stream>>>(w, m.sp, m.ns,
-                                                                       sc.full.view(), sc2);
+        k_inliers<<<dim3(std::max(1, nblocks(m.ns, kW * 4)), ncand), kT, 0, c.stream>>>(
+            w, m.sp, m.ns, sc.full.view(), sc2);
         SM_LAUNCH_CHECK();
         k_score<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, m.ns, p.minScore, 3, 0);
         SM_LAUNCH_CHECK();
@@ -491,8 +492,8 @@ void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, con
             run_stage(c, w, d, ncand);
             k_stage_end<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, 4);
             SM_LAUNCH_CHECK();
-            k_inliers<<<dim3(nblocks(m.nr, kT), ncand), kT, 0, c.stream>>>(w, m.rp, m.nr,
-                                                                           sc.full.view(), sc2);
+            k_inliers<<<dim3(std::max(1, nblocks(m.nr, kW * 4)), ncand), kT, 0, c.stream>>>(
+                w, m.rp, m.nr, sc.full.view(), sc2);
             SM_LAUNCH_CHECK();
             k_score<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, m.nr, p.minScore, 5, 1);
             SM_LAUNCH_CHECK();

@@ -405,28 +405,25 @@ __device__ __forceinline__ unsigned long long warp_merge_low(unsigned long long 
     return m;
 }
 
-// Exact k nearest neighbours (k <= 32) of q by (squared distance, index), one warp per
-// query. Shell by shell, the lanes probe 32 cells at a time (occupancy bit, table), a prefix
-// sum flattens the probed cells' points, and each round of 32 points is sorted across the
-// lanes and merged into the running 32 best (lane j holds the j-th smallest key: distance
-// bits, index); rounds with no point below the current k-th best are skipped. Termination
-// is grid_knn's rule (after shell s, the k-th distance below the ring bound), so the result
-// is grid_knn's. Returns the number found (<= k); lane j < that count gets the j-th
-// neighbour's index in *id and squared distance in *d.
-template <class G>
-__device__ __forceinline__ int warp_knn_sorted(const G &g, float qx, float qy, float qz, int k,
-                                               int *id, float *d) {
+// Warp-cooperative walk over the points around q, shell by shell (shells 0 and 1 together:
+// the 3x3x3 block; no search can stop after shell 0, whose ring bound is 0). The lanes probe
+// 32 cells at a time (occupancy bit, table), a prefix sum flattens the probed cells' points,
+// and visit(p, valid) is called by all lanes for each round of 32 points (p = position with
+// the point index in w; valid false on idle lanes). After each shell, stop(s) - evaluated by
+// all lanes, warp-uniform - ends the walk. Every point of shells 1..s is visited exactly once
+// before stop(s), so a search written on it sees the same points as one that walks the
+// cells one by one.
+template <class G, class V, class S>
+__device__ __forceinline__ void warp_walk(const G &g, float qx, float qy, float qz, V &&visit,
+                                          S &&stop) {
     const int lane = threadIdx.x & 31;
     int       c[3];
     grid_cc(g, qx, qy, qz, c);
-    unsigned long long best = ~0ull; // lane j: j-th smallest so far
-    int                seen = 0;
-    const int          ms   = max(grid_max_shell(g, c), 1);
-    // shells 0 and 1 together: the query's 3x3x3 block (no decision is possible at shell 0)
+    const int ms = max(grid_max_shell(g, c), 1);
     for (int s = 1; s <= ms; s++) {
         const int lo = s == 1 ? 0 : s, w = 2 * s + 1, cube = w * w * w;
         for (int t0 = 0; t0 < cube; t0 += 32) {
-            const int t  = t0 + lane;
+            const int t = t0 + lane;
             int       b = 0, e = 0;
             if (t < cube) {
                 const int dx = t % w - s, dy = (t / w) % w - s, dz = t / (w * w) - s;
@@ -440,42 +437,112 @@ __device__ __forceinline__ int warp_knn_sorted(const G &g, float qx, float qy, f
             const int incl = warp_incl_scan(cnt);
             const int excl = incl - cnt;
             const int T    = __shfl_sync(0xffffffffu, incl, 31);
-            seen += T;
             for (int base = 0; base < T; base += 32) {
-                const int r  = base + lane;
-                int       lo2 = 0; // the lane whose cell holds point r: last lane with excl <= r
+                const int r   = base + lane;
+                int       own = 0; // the lane whose cell holds point r: last lane with excl <= r
 #pragma unroll
                 for (int step = 16; step >= 1; step >>= 1) {
-                    const int mid = lo2 + step;
-                    const int ev  = __shfl_sync(0xffffffffu, excl, mid);
-                    if (ev <= r)
-                        lo2 = mid;
+                    const int mid = own + step;
+                    if (__shfl_sync(0xffffffffu, excl, mid) <= r)
+                        own = mid;
                 }
-                const int bj = __shfl_sync(0xffffffffu, b, lo2);
-                const int ej = __shfl_sync(0xffffffffu, excl, lo2);
-                unsigned long long key = ~0ull;
-                if (r < T) {
-                    const float4 p  = g.pts[bj + (r - ej)];
-                    const float  dd = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
-                    key = ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)__float_as_int(p.w);
-                }
-                const unsigned long long kth = __shfl_sync(0xffffffffu, best, k - 1);
-                if (!__any_sync(0xffffffffu, key < kth))
-                    continue;
-                best = warp_merge_low(best, warp_bitonic_sort(key));
+                const int bj = __shfl_sync(0xffffffffu, b, own);
+                const int ej = __shfl_sync(0xffffffffu, excl, own);
+                const bool   valid = r < T;
+                const float4 p     = valid ? g.pts[bj + (r - ej)] : make_float4(0.f, 0.f, 0.f, 0.f);
+                visit(p, valid);
             }
         }
-        if (seen >= k) {
+        if (stop(s))
+            return;
+    }
+}
+
+// Exact k nearest neighbours (k <= 32) of q by (squared distance, index), one warp per
+// query, on warp_walk: each round of 32 points is sorted across the lanes and merged into
+// the running 32 best (lane j holds the j-th smallest key: distance bits, index); rounds with
+// no point below the current k-th best are skipped. Termination is grid_knn's rule (after
+// shell s, the k-th distance below the ring bound), so the result is grid_knn's. Returns the
+// number found (<= k); lane j < that count gets the j-th neighbour's index in *id and squared
+// distance in *d.
+template <class G>
+__device__ __forceinline__ int warp_knn_sorted(const G &g, float qx, float qy, float qz, int k,
+                                               int *id, float *d) {
+    unsigned long long best = ~0ull; // lane j: j-th smallest so far
+    int                seen = 0;
+    warp_walk(
+        g, qx, qy, qz,
+        [&](const float4 &p, bool valid) {
+            seen += __popc(__ballot_sync(0xffffffffu, valid));
+            unsigned long long key = ~0ull;
+            if (valid) {
+                const float dd = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
+                key = ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)__float_as_int(p.w);
+            }
+            const unsigned long long kth = __shfl_sync(0xffffffffu, best, k - 1);
+            if (__any_sync(0xffffffffu, key < kth))
+                best = warp_merge_low(best, warp_bitonic_sort(key));
+        },
+        [&](int s) {
+            if (seen < k)
+                return false;
             const unsigned long long kth = __shfl_sync(0xffffffffu, best, k - 1);
             const float              bnd = smg::ring_bound(s, g.g);
-            if (__uint_as_float((unsigned)(kth >> 32)) < bnd * bnd)
-                break;
-        }
-    }
+            return __uint_as_float((unsigned)(kth >> 32)) < bnd * bnd;
+        });
     const int n = min(seen, k);
     *id         = (int)(unsigned)(best & 0xffffffffu);
     *d          = __uint_as_float((unsigned)(best >> 32));
     return n;
+}
+
+// Nearest point by (squared distance, index) on warp_walk, searched until the nearest is
+// below the ring bound or the ring bound passes limit2 (grid_nn's rule); -1 when none was
+// found. All lanes return the result.
+template <class G>
+__device__ __forceinline__ int warp_nn_walk(const G &g, float qx, float qy, float qz,
+                                            float limit2, float &outd) {
+    unsigned long long best = ~0ull;
+    warp_walk(
+        g, qx, qy, qz,
+        [&](const float4 &p, bool valid) {
+            if (valid) {
+                const float dd = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
+                const unsigned long long key =
+                    ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)__float_as_int(p.w);
+                best = key < best ? key : best;
+            }
+        },
+        [&](int s) {
+            best          = warp_min_u64(best);
+            const float b = smg::ring_bound(s, g.g);
+            return (best != ~0ull && __uint_as_float((unsigned)(best >> 32)) < b * b) ||
+                   b * b > limit2;
+        });
+    best = warp_min_u64(best);
+    if (best == ~0ull) {
+        outd = 3.402823466e+38f;
+        return -1;
+    }
+    outd = __uint_as_float((unsigned)(best >> 32));
+    return (int)(unsigned)(best & 0xffffffffu);
+}
+
+// Whether any point lies closer than sqrt(r2) to q (grid_any_within's rule), by a warp.
+template <class G>
+__device__ __forceinline__ bool warp_any_within(const G &g, float qx, float qy, float qz, float r2) {
+    bool hit = false;
+    warp_walk(
+        g, qx, qy, qz,
+        [&](const float4 &p, bool valid) {
+            const bool h = valid && smm::dist2(qx, qy, qz, p.x, p.y, p.z) < r2;
+            hit          = hit || __any_sync(0xffffffffu, h);
+        },
+        [&](int s) {
+            const float b = smg::ring_bound(s, g.g);
+            return hit || b * b >= r2;
+        });
+    return hit;
 }
 
 template <class G>
