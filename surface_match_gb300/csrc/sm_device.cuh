@@ -85,121 +85,6 @@ template <class G> __device__ __forceinline__ int grid_max_shell(const G &g, con
     return m;
 }
 
-// Visit every point (position, index in w) of the cells at Chebyshev distance exactly s from
-// cell c.
-template <class G, class F>
-__device__ __forceinline__ void grid_shell(const G &g, const int c[3], int s, F &&f) {
-    const int z0 = max(c[2] - s, 0), z1 = min(c[2] + s, g.dim[2] - 1);
-    const int y0 = max(c[1] - s, 0), y1 = min(c[1] + s, g.dim[1] - 1);
-    for (int z = z0; z <= z1; z++) {
-        for (int y = y0; y <= y1; y++) {
-            const bool face = (z == c[2] - s || z == c[2] + s || y == c[1] - s || y == c[1] + s);
-            const int  step = face ? 1 : 2 * s;
-            for (int x = c[0] - s; x <= c[0] + s; x += (step > 0 ? step : 1)) {
-                if (x < 0 || x >= g.dim[0])
-                    continue;
-                int b, e;
-                g.range(x, y, z, b, e);
-                for (int k = b; k < e; k++)
-                    f(g.pts[k]);
-            }
-        }
-    }
-}
-
-// k nearest neighbours of q by (squared distance, index), k <= K; returns how many were
-// found. The lists li/ld have the fixed capacity K: slots [0, K-k) hold sentinels smaller
-// than any point and the neighbours fill [K-k, K) in ascending order, so every index is a
-// compile-time constant and the lists stay in registers. The search stops after `maxShell`
-// shells when that does not decide it; *done then says whether the result is final.
-template <int K, class G>
-__device__ __forceinline__ int grid_knn(const G &g, float qx, float qy, float qz, int k,
-                                        int (&li)[K], float (&ld)[K], int maxShell = 0x7fffffff,
-                                        bool *done = nullptr) {
-    int c[3];
-    grid_cc(g, qx, qy, qz, c);
-    bool fin = false;
-    int  n   = 0;
-#pragma unroll
-    for (int j = 0; j < K; j++) {
-        const bool sent = j < K - k;
-        li[j]           = sent ? -1 : 0x7fffffff;
-        ld[j]           = sent ? -1.0f : 3.402823466e+38f;
-    }
-    const int ms = grid_max_shell(g, c);
-    for (int s = 0; s <= ms; s++) {
-        if (s > maxShell)
-            break;
-        if (s == ms)
-            fin = true;
-        grid_shell(g, c, s, [&](const float4 p) {
-            const int   id = __float_as_int(p.w);
-            const float d  = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
-            if (!(d < ld[K - 1] || (d == ld[K - 1] && id < li[K - 1])))
-                return;
-            float cd = d;
-            int   ci = id;
-#pragma unroll
-            for (int j = 0; j < K; j++) {
-                if (cd < ld[j] || (cd == ld[j] && ci < li[j])) {
-                    const float td = ld[j];
-                    const int   ti = li[j];
-                    ld[j]          = cd;
-                    li[j]          = ci;
-                    cd             = td;
-                    ci             = ti;
-                }
-            }
-            if (n < k)
-                n++;
-        });
-        const float b = smg::ring_bound(s, g.g);
-        if (n == k && ld[K - 1] < b * b) {
-            fin = true;
-            break;
-        }
-    }
-    if (done)
-        *done = fin;
-    return n;
-}
-
-// Nearest neighbour by (squared distance, index), searched until the ring bound passes
-// `limit2` (or `maxShell` shells); returns -1 when none was found. `exact` is set when the
-// result is the true nearest point or provably no point lies within limit2.
-template <class G>
-__device__ __forceinline__ int grid_nn(const G &g, float qx,
-                                       float qy, float qz, float limit2, float &outd,
-                                       int maxShell = 0x7fffffff, bool *exact = nullptr) {
-    int c[3];
-    grid_cc(g, qx, qy, qz, c);
-    int       best = -1;
-    float     bd   = 3.402823466e+38f;
-    const int ms   = min(grid_max_shell(g, c), maxShell);
-    bool      done = false;
-    for (int s = 0; s <= ms; s++) {
-        grid_shell(g, c, s, [&](const float4 p) {
-            const int   id = __float_as_int(p.w);
-            const float d  = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
-            if (d < bd || (d == bd && id < best)) {
-                bd   = d;
-                best = id;
-            }
-        });
-        const float b = smg::ring_bound(s, g.g);
-        if ((best >= 0 && bd < b * b) || b * b > limit2) {
-            done = true;
-            break;
-        }
-    }
-    if (ms == grid_max_shell(g, c))
-        done = true;
-    if (exact)
-        *exact = done;
-    outd = bd;
-    return best;
-}
-
 __device__ __forceinline__ int warp_incl_scan(int v) {
     const int lane = threadIdx.x & 31;
 #pragma unroll
@@ -218,162 +103,6 @@ __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v)
         v                          = t < v ? t : v;
     }
     return v;
-}
-
-// The m-th smallest key (m >= 1) over the warp's fixed-capacity lists T (removing the m
-// smallest from T); ~0 when the warp holds fewer than m keys.
-template <int K>
-__device__ __forceinline__ unsigned long long warp_kth(unsigned long long (&T)[K], int m) {
-    unsigned long long r = ~0ull;
-    for (int round = 0; round < m; round++) {
-        unsigned long long mine = ~0ull;
-#pragma unroll
-        for (int j = 0; j < K; j++)
-            mine = T[j] < mine ? T[j] : mine;
-        r = warp_min_u64(mine);
-#pragma unroll
-        for (int j = 0; j < K; j++)
-            if (T[j] == r)
-                T[j] = ~0ull;
-    }
-    return r;
-}
-
-// Warp-cooperative exact nearest neighbour: all 32 lanes call it with the same query; the
-// cells of each shell are split over the lanes and the (distance bits, index) minimum is
-// taken across the warp, so near and far queries cost the warp the same work pattern. Same
-// result and termination rule as grid_nn.
-template <class G>
-__device__ __forceinline__ int warp_nn(const G &g, float qx,
-                                       float qy, float qz, float limit2, float &outd) {
-    const int lane = threadIdx.x & 31;
-    int       c[3];
-    grid_cc(g, qx, qy, qz, c);
-    unsigned long long best = ~0ull;
-    const int          ms   = grid_max_shell(g, c);
-    for (int s = 0; s <= ms; s++) {
-        const int w = 2 * s + 1, cube = w * w * w;
-        for (int t = lane; t < cube; t += 32) {
-            const int dx = t % w - s, dy = (t / w) % w - s, dz = t / (w * w) - s;
-            if (max(abs(dx), max(abs(dy), abs(dz))) != s)
-                continue;
-            const int x = c[0] + dx, y = c[1] + dy, z = c[2] + dz;
-            if (x < 0 || y < 0 || z < 0 || x >= g.dim[0] || y >= g.dim[1] || z >= g.dim[2])
-                continue;
-            int b, e;
-            g.range(x, y, z, b, e);
-            for (int k = b; k < e; k++) {
-                const float4 p  = g.pts[k];
-                const int    id = __float_as_int(p.w);
-                const float  d  = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
-                const unsigned long long key =
-                    ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)id;
-                best = key < best ? key : best;
-            }
-        }
-        best          = warp_min_u64(best);
-        const float b = smg::ring_bound(s, g.g);
-        if (best != ~0ull && __uint_as_float((unsigned)(best >> 32)) < b * b)
-            break;
-        if (b * b > limit2)
-            break;
-    }
-    if (best == ~0ull) {
-        outd = 3.402823466e+38f;
-        return -1;
-    }
-    outd = __uint_as_float((unsigned)(best >> 32));
-    return (int)(unsigned)(best & 0xffffffffu);
-}
-
-// Warp-cooperative exact k nearest neighbours: all 32 lanes call it with the same query; the
-// cells of each shell are split over the lanes, each lane keeps its k best keys (distance
-// bits, index, plus one; fixed capacity K with zero sentinels in front as in grid_knn), and
-// the warp's k-th best decides termination with grid_knn's rule, so the result is
-// grid_knn's. For queries far from their neighbours (many shells). Returns the count found;
-// every lane gets the neighbours in li/ld slots [K-k, K) like grid_knn.
-template <int K, class G>
-__device__ __forceinline__ int warp_knn(const G &g, float qx, float qy, float qz, int k,
-                                        int (&li)[K], float (&ld)[K]) {
-    const int lane = threadIdx.x & 31;
-    int       c[3];
-    grid_cc(g, qx, qy, qz, c);
-    unsigned long long L[K];
-#pragma unroll
-    for (int j = 0; j < K; j++)
-        L[j] = j < K - k ? 0ull : ~0ull;
-    int       seen = 0;
-    const int ms   = grid_max_shell(g, c);
-    for (int s = 0; s <= ms; s++) {
-        const int w = 2 * s + 1, cube = w * w * w;
-        for (int t = lane; t < cube; t += 32) {
-            const int dx = t % w - s, dy = (t / w) % w - s, dz = t / (w * w) - s;
-            if (max(abs(dx), max(abs(dy), abs(dz))) != s)
-                continue;
-            const int x = c[0] + dx, y = c[1] + dy, z = c[2] + dz;
-            if (x < 0 || y < 0 || z < 0 || x >= g.dim[0] || y >= g.dim[1] || z >= g.dim[2])
-                continue;
-            int b, e;
-            g.range(x, y, z, b, e);
-            for (int q = b; q < e; q++) {
-                const float4 p  = g.pts[q];
-                const int    id = __float_as_int(p.w);
-                const float  d  = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
-                unsigned long long key =
-                    (((unsigned long long)__float_as_uint(d) << 32) | (unsigned)id) + 1ull;
-                seen++;
-                if (!(key < L[K - 1]))
-                    continue;
-#pragma unroll
-                for (int j = 0; j < K; j++) {
-                    if (key < L[j]) {
-                        const unsigned long long t2 = L[j];
-                        L[j]                        = key;
-                        key                         = t2;
-                    }
-                }
-            }
-        }
-        int tot = seen;
-#pragma unroll
-        for (int o = 16; o >= 1; o >>= 1)
-            tot += __shfl_xor_sync(0xffffffffu, tot, o);
-        if (s == 0 || tot < k)
-            continue; // a shell-0 search never decides (its ring bound is 0)
-        unsigned long long T[K];
-#pragma unroll
-        for (int j = 0; j < K; j++)
-            T[j] = j < K - k ? ~0ull : L[j];
-        const unsigned long long m   = warp_kth<K>(T, k);
-        const float              bnd = smg::ring_bound(s, g.g);
-        if (__uint_as_float((unsigned)((m - 1ull) >> 32)) < bnd * bnd)
-            break;
-    }
-    unsigned long long T[K];
-#pragma unroll
-    for (int j = 0; j < K; j++)
-        T[j] = j < K - k ? ~0ull : L[j];
-    int n = 0;
-#pragma unroll
-    for (int j = 0; j < K; j++) {
-        li[j] = -1;
-        ld[j] = -1.0f;
-    }
-#pragma unroll
-    for (int j = 0; j < K; j++) {
-        if (j < K - k)
-            continue;
-        const unsigned long long m = warp_kth<K>(T, 1);
-        if (m == ~0ull) {
-            li[j] = 0x7fffffff;
-            ld[j] = 3.402823466e+38f;
-            continue;
-        }
-        li[j] = (int)(unsigned)((m - 1ull) & 0xffffffffu);
-        ld[j] = __uint_as_float((unsigned)((m - 1ull) >> 32));
-        n++;
-    }
-    return n;
 }
 
 // Ascending bitonic sort of one 64-bit key per lane across the warp.
@@ -461,10 +190,10 @@ __device__ __forceinline__ void warp_walk(const G &g, float qx, float qy, float 
 // Exact k nearest neighbours (k <= 32) of q by (squared distance, index), one warp per
 // query, on warp_walk: each round of 32 points is sorted across the lanes and merged into
 // the running 32 best (lane j holds the j-th smallest key: distance bits, index); rounds with
-// no point below the current k-th best are skipped. Termination is grid_knn's rule (after
-// shell s, the k-th distance below the ring bound), so the result is grid_knn's. Returns the
-// number found (<= k); lane j < that count gets the j-th neighbour's index in *id and squared
-// distance in *d.
+// no point below the current k-th best are skipped. The search ends after shell s once k
+// points were seen and the k-th distance is below the ring bound of s (every unvisited point
+// is farther), so the result is the exact k nearest. Returns the number found (<= k); lane
+// j < that count gets the j-th neighbour's index in *id and squared distance in *d.
 template <class G>
 __device__ __forceinline__ int warp_knn_sorted(const G &g, float qx, float qy, float qz, int k,
                                                int *id, float *d) {
@@ -497,8 +226,8 @@ __device__ __forceinline__ int warp_knn_sorted(const G &g, float qx, float qy, f
 }
 
 // Nearest point by (squared distance, index) on warp_walk, searched until the nearest is
-// below the ring bound or the ring bound passes limit2 (grid_nn's rule); -1 when none was
-// found. All lanes return the result.
+// below the ring bound or the ring bound passes limit2; -1 when none was found. All lanes
+// return the result.
 template <class G>
 __device__ __forceinline__ int warp_nn_walk(const G &g, float qx, float qy, float qz,
                                             float limit2, float &outd) {
@@ -528,7 +257,8 @@ __device__ __forceinline__ int warp_nn_walk(const G &g, float qx, float qy, floa
     return (int)(unsigned)(best & 0xffffffffu);
 }
 
-// Whether any point lies closer than sqrt(r2) to q (grid_any_within's rule), by a warp.
+// Whether any point lies closer than sqrt(r2) to q, by a warp: stops at a hit or after the
+// shell whose ring bound reaches sqrt(r2).
 template <class G>
 __device__ __forceinline__ bool warp_any_within(const G &g, float qx, float qy, float qz, float r2) {
     bool hit = false;
@@ -543,29 +273,6 @@ __device__ __forceinline__ bool warp_any_within(const G &g, float qx, float qy, 
             return hit || b * b >= r2;
         });
     return hit;
-}
-
-template <class G>
-__device__ __forceinline__ bool grid_any_within(const G &g, float qx,
-                                                float qy, float qz, float r2) {
-    int c[3];
-    grid_cc(g, qx, qy, qz, c);
-    const int ms = grid_max_shell(g, c);
-    for (int s = 0; s <= ms; s++) {
-        bool hit = false;
-        grid_shell(g, c, s, [&](const float4 p) {
-            if (hit)
-                return;
-            if (smm::dist2(qx, qy, qz, p.x, p.y, p.z) < r2)
-                hit = true;
-        });
-        if (hit)
-            return true;
-        const float b = smg::ring_bound(s, g.g);
-        if (b * b >= r2)
-            break;
-    }
-    return false;
 }
 
 // Order-preserving float <-> int mapping for atomicMin/atomicMax on floats.
