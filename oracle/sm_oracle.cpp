@@ -784,17 +784,18 @@ struct IcpCrit {
     float rejectDist, mseMin, mseMax, tolerance;
 };
 
-// FP32 Kahan partials over kIcpThreads strided slots, merged by the GPU's fixed tree.
+// FP32 Kahan partials over kIcpSlots strided slots, merged by the GPU's fixed trees (32
+// slots of a warp, the warps of a block, then the blocks; sm_icp.h).
 struct StridedSum {
     int         width;
     bool        fp64;
     std::vector<smi::KahanF> part;
     std::vector<double>      dpart;
-    explicit StridedSum(int w, bool f64) : width(w), fp64(f64), part(smi::kIcpThreads * w), dpart(w, 0.0) {
+    explicit StridedSum(int w, bool f64) : width(w), fp64(f64), part(smi::kIcpSlots * w), dpart(w, 0.0) {
         for (auto &k : part) k.init();
     }
     void add(int i, const float *v) {
-        int t = i % smi::kIcpThreads;
+        int t = i % smi::kIcpSlots;
         for (int c = 0; c < width; c++) {
             part[t * width + c].add(v[c]);
             dpart[c] += (double)v[c];
@@ -806,20 +807,24 @@ struct StridedSum {
     }
     float result(int c) const {
         if (fp64) return (float)dpart[c];
-        smi::KahanF lane[smi::kIcpThreads];
-        for (int t = 0; t < smi::kIcpThreads; t++) lane[t] = part[t * width + c];
-        const int W = 32, NW = smi::kIcpThreads / 32;
-        smi::KahanF ws[NW];
-        for (int w = 0; w < NW; w++) {
-            smi::KahanF a[32];
-            for (int l = 0; l < 32; l++) a[l] = lane[w * 32 + l];
-            for (int off = W / 2; off >= 1; off /= 2)
-                for (int l = 0; l < off; l++) a[l].merge(a[l + off]);
-            ws[w] = a[0];
+        const int   NW = smi::kIcpThreads / 32, NB = smi::kIcpBlocks;
+        smi::KahanF bs[NB];
+        for (int b = 0; b < NB; b++) {
+            smi::KahanF ws[NW];
+            for (int w = 0; w < NW; w++) {
+                smi::KahanF a[32];
+                for (int l = 0; l < 32; l++) a[l] = part[(b * smi::kIcpThreads + w * 32 + l) * width + c];
+                for (int off = 16; off >= 1; off /= 2)
+                    for (int l = 0; l < off; l++) a[l].merge(a[l + off]);
+                ws[w] = a[0];
+            }
+            for (int off = NW / 2; off >= 1; off /= 2)
+                for (int l = 0; l < off; l++) ws[l].merge(ws[l + off]);
+            bs[b] = ws[0];
         }
-        for (int off = NW / 2; off >= 1; off /= 2)
-            for (int l = 0; l < off; l++) ws[l].merge(ws[l + off]);
-        return ws[0].value();
+        for (int off = NB / 2; off >= 1; off /= 2)
+            for (int l = 0; l < off; l++) bs[l].merge(bs[l + off]);
+        return bs[0].value();
     }
 };
 

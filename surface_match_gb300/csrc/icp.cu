@@ -54,7 +54,9 @@ struct Work {
     int                *nnR;    // ncand x maxSrc: its subset index (-1 none)
     float4             *x4;     // ncand x maxSrc: moved source point, w = squared distance
     float4             *n4;     // ncand x maxSrc: rotated source normal
-    float              *terms;  // ncand x 27 x maxSrc (SoA per candidate)
+    float              *resid;  // ncand x maxSrc: residual distance of each pair
+    float2             *part;   // ncand x kIcpBlocks x 27: block partials {sum, compensation}
+    int                *ctr;    // ncand: blocks of the current reduction that are done
     unsigned long long *win;    // ncand x maxDst
     int                 maxSrc, maxDst;
     float              *trace;  // ncand x kTraceFloats (nullable)
@@ -114,17 +116,20 @@ __global__ void __launch_bounds__(kT) k_pairs(Work w, Stage s) {
         w.nnId[o] = -1;
 }
 
-// Fixed-layout reduction of W quantities over the 256 slots: slot t sums, with Kahan, the
-// terms of the pairs i = t, t + 256, ... in ascending order; then the tree (warp
-// shfl_down, then warp 0 over the warp partials). Result valid on thread 0.
+// Fixed-layout reduction of W quantities (sm_icp.h): block b of candidate ci holds slots
+// b * 256 + tid; slot t sums, with Kahan, the terms of the pairs i = t, t + kIcpSlots, ...
+// in ascending order; the block merges its slots by the tree (warp shfl_down, then warp 0
+// over the warp partials) and publishes the result; the last block of the candidate to
+// finish merges the kIcpBlocks partials by the block tree. Returns true on that block, whose
+// thread 0 then holds the total in v.
 template <int W, class F>
-__device__ void slot_reduce(const Work &w, const Stage &s, int ci, F &&term, smi::KahanF (&v)[W],
-                            float (*red)[W][2]) {
+__device__ bool slot_reduce(const Work &w, const Stage &s, int ci, F &&term, smi::KahanF (&v)[W],
+                            float (*red)[W][2], int *flag) {
     const int tid = threadIdx.x;
     for (int k = 0; k < W; k++)
         v[k].init();
     const int *nnId = w.nnId + (size_t)ci * w.maxSrc;
-    for (int i = tid; i < s.n; i += kT) {
+    for (int i = blockIdx.x * kT + tid; i < s.n; i += smi::kIcpSlots) {
         if (nnId[i] < 0)
             continue;
         float t[W];
@@ -161,40 +166,83 @@ __device__ void slot_reduce(const Work &w, const Stage &s, int ci, F &&term, smi
                 v[k].merge(o);
             }
     }
+    // publish the block's partial; the last block of the candidate merges them all
+    float2 *P = w.part + ((size_t)ci * smi::kIcpBlocks) * smi::kNumSystem;
+    if (tid == 0) {
+        for (int k = 0; k < W; k++)
+            P[(size_t)blockIdx.x * smi::kNumSystem + k] = make_float2(v[k].s, v[k].c);
+        __threadfence();
+        const int done = atomicAdd(&w.ctr[ci], 1);
+        *flag          = done == smi::kIcpBlocks - 1;
+    }
+    __syncthreads();
+    if (!*flag)
+        return false;
+    __threadfence();
+    if (wp == 0) {
+        for (int k = 0; k < W; k++) {
+            const float2 pb = lane < smi::kIcpBlocks
+                                  ? __ldcg(&P[(size_t)lane * smi::kNumSystem + k])
+                                  : make_float2(0.f, 0.f);
+            v[k].s = pb.x;
+            v[k].c = pb.y;
+        }
+#pragma unroll
+        for (int off = smi::kIcpBlocks / 2; off >= 1; off >>= 1)
+            for (int k = 0; k < W; k++) {
+                smi::KahanF o;
+                o.s = __shfl_down_sync(0xffffffffu, v[k].s, off);
+                o.c = __shfl_down_sync(0xffffffffu, v[k].c, off);
+                v[k].merge(o);
+            }
+        if (lane == 0)
+            w.ctr[ci] = 0; // ready for the next reduction of this candidate
+    }
+    return true;
 }
 
 // K3: pair count and centroids
 __global__ void __launch_bounds__(kT) k_centroids(Work w, Stage s) {
     __shared__ float red[kW][6][2];
     __shared__ int   icnt[kW];
-    const int        ci = blockIdx.x;
+    __shared__ int   flag;
+    const int        ci = blockIdx.y;
     Cand            &C  = w.cand[ci];
     if (!cand_live(C, s))
         return;
     const int *nnId = w.nnId + (size_t)ci * w.maxSrc;
     int        cnt  = 0;
-    for (int i = threadIdx.x; i < s.n; i += kT)
+    for (int i = blockIdx.x * kT + threadIdx.x; i < s.n; i += smi::kIcpSlots)
         cnt += nnId[i] >= 0 ? 1 : 0;
     cnt = __reduce_add_sync(0xffffffffu, cnt);
     if ((threadIdx.x & 31) == 0)
         icnt[threadIdx.x >> 5] = cnt;
     const float4 *x4 = w.x4 + (size_t)ci * w.maxSrc;
     smi::KahanF   v[6];
-    slot_reduce<6>(w, s, ci,
-                   [&](int i, float *t) {
-                       const float4 q = w.pos[nnId[i]];
-                       t[0]           = x4[i].x;
-                       t[1]           = x4[i].y;
-                       t[2]           = x4[i].z;
-                       t[3]           = q.x;
-                       t[4]           = q.y;
-                       t[5]           = q.z;
-                   },
-                   v, red);
-    if (threadIdx.x == 0) {
-        int total = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) { // the block's pair count rides in the spare partial slot 26
+        int t = 0;
         for (int k = 0; k < kW; k++)
-            total += icnt[k];
+            t += icnt[k];
+        w.part[((size_t)ci * smi::kIcpBlocks + blockIdx.x) * smi::kNumSystem + 26] =
+            make_float2(__int_as_float(t), 0.f);
+    }
+    const bool last = slot_reduce<6>(w, s, ci,
+                                     [&](int i, float *t) {
+                                         const float4 q = w.pos[nnId[i]];
+                                         t[0]           = x4[i].x;
+                                         t[1]           = x4[i].y;
+                                         t[2]           = x4[i].z;
+                                         t[3]           = q.x;
+                                         t[4]           = q.y;
+                                         t[5]           = q.z;
+                                     },
+                                     v, red, &flag);
+    if (last && threadIdx.x == 0) {
+        int total = 0;
+        for (int b = 0; b < smi::kIcpBlocks; b++)
+            total += __float_as_int(
+                __ldcg(&w.part[((size_t)ci * smi::kIcpBlocks + b) * smi::kNumSystem + 26]).x);
         const float fc = (float)total;
         for (int k = 0; k < 3; k++) {
             C.Pm[k] = smm::fdiv(v[k].value(), fc);
@@ -204,48 +252,36 @@ __global__ void __launch_bounds__(kT) k_centroids(Work w, Stage s) {
     }
 }
 
-// K4: normal-equation terms of each pair
-__global__ void __launch_bounds__(kT) k_sys_terms(Work w, Stage s) {
-    const int   ci = blockIdx.y;
-    const Cand &C  = w.cand[ci];
-    if (!cand_live(C, s) || C.cnt < 6)
-        return;
-    const int i = blockIdx.x * kT + threadIdx.x;
-    if (i >= s.n)
-        return;
-    const size_t o  = (size_t)ci * w.maxSrc + i;
-    const int    id = w.nnId[o];
-    if (id < 0)
-        return;
-    const float4 x = w.x4[o], xn = w.n4[o], q = w.pos[id], qn = w.nrm[id];
-    float        t[smi::kNumSystem];
-    smi::system_terms(x.x - C.Pm[0], x.y - C.Pm[1], x.z - C.Pm[2], q.x - C.Qm[0], q.y - C.Qm[1],
-                      q.z - C.Qm[2], xn.x + qn.x, xn.y + qn.y, xn.z + qn.z, t);
-    float *T = w.terms + (size_t)ci * smi::kNumSystem * w.maxSrc;
-    for (int k = 0; k < smi::kNumSystem; k++)
-        T[(size_t)k * w.maxSrc + i] = t[k];
-}
-
-// K5: reduce the normal equations, FP64 solve
+// K5: the normal-equation terms of the pairs (computed in place), reduced; FP64 solve
 __global__ void __launch_bounds__(kT) k_solve(Work w, Stage s) {
     __shared__ float red[kW][smi::kNumSystem][2];
-    const int        ci = blockIdx.x;
+    __shared__ int   flag;
+    const int        ci = blockIdx.y;
     Cand            &C  = w.cand[ci];
     if (!cand_live(C, s) || C.cnt < 6)
         return;
-    const float *T = w.terms + (size_t)ci * smi::kNumSystem * w.maxSrc;
+    const float Pm0 = C.Pm[0], Pm1 = C.Pm[1], Pm2 = C.Pm[2];
+    const float Qm0 = C.Qm[0], Qm1 = C.Qm[1], Qm2 = C.Qm[2];
+    const size_t o0 = (size_t)ci * w.maxSrc;
     smi::KahanF  v[smi::kNumSystem];
-    slot_reduce<smi::kNumSystem>(w, s, ci,
-                                 [&](int i, float *t) {
-                                     for (int k = 0; k < smi::kNumSystem; k++)
-                                         t[k] = T[(size_t)k * w.maxSrc + i];
-                                 },
-                                 v, red);
-    if (threadIdx.x == 0) {
+    const bool   last = slot_reduce<smi::kNumSystem>(
+        w, s, ci,
+        [&](int i, float *t) {
+            const int    id = w.nnId[o0 + i];
+            const float4 x = w.x4[o0 + i], xn = w.n4[o0 + i], q = w.pos[id], qn = w.nrm[id];
+            smi::system_terms(x.x - Pm0, x.y - Pm1, x.z - Pm2, q.x - Qm0, q.y - Qm1, q.z - Qm2,
+                              xn.x + qn.x, xn.y + qn.y, xn.z + qn.z, t);
+        },
+        v, red, &flag);
+    if (last && threadIdx.x < 32) {
+        // the totals are on thread 0; warp 0 solves with one row of the system per lane
         float sys[smi::kNumSystem];
         for (int k = 0; k < smi::kNumSystem; k++)
-            sys[k] = v[k].value();
-        C.step = smi::solve_step(sys, C.Pm, C.Qm);
+            sys[k] = __shfl_sync(0xffffffffu, v[k].value(), 0);
+        const float       pm[3] = {C.Pm[0], C.Pm[1], C.Pm[2]}, qm[3] = {C.Qm[0], C.Qm[1], C.Qm[2]};
+        const smi::Pose34 st    = smi::solve_step_warp(sys, pm, qm);
+        if (threadIdx.x == 0)
+            C.step = st;
     }
 }
 
@@ -264,30 +300,34 @@ __global__ void __launch_bounds__(kT) k_resid(Work w, Stage s) {
         smi::pose_apply(C.step, x.x, x.y, x.z, y0, y1, y2);
         warp_nn_walk(s.G, y0, y1, y2, FLT_MAX, d);
         if ((threadIdx.x & 31) == 0)
-            w.terms[(size_t)ci * smi::kNumSystem * w.maxSrc + i] = smm::fsqrt(d);
+            w.resid[(size_t)ci * w.maxSrc + i] = smm::fsqrt(d);
     }
 }
 
 // K7: mean residual, the regist loop logic (icp.cpp:233-272), winner reset
 __global__ void __launch_bounds__(kT) k_update(Work w, Stage s) {
     __shared__ float red[kW][1][2];
-    const int        ci = blockIdx.x;
+    __shared__ int   flag;
+    const int        ci = blockIdx.y;
     Cand            &C  = w.cand[ci];
     if (!cand_live(C, s))
         return;
+    const int *nnR = w.nnR + (size_t)ci * w.maxSrc;
+    for (int i = blockIdx.x * kT + threadIdx.x; i < s.n; i += smi::kIcpSlots)
+        if (nnR[i] >= 0)
+            w.win[(size_t)ci * w.maxDst + nnR[i]] = ~0ull;
     const int cnt = C.cnt;
     float     mse = FLT_MAX;
     if (cnt >= 6) {
-        const float *D = w.terms + (size_t)ci * smi::kNumSystem * w.maxSrc;
+        const float *D = w.resid + (size_t)ci * w.maxSrc;
         smi::KahanF  v[1];
-        slot_reduce<1>(w, s, ci, [&](int i, float *t) { t[0] = D[i]; }, v, red);
+        if (!slot_reduce<1>(w, s, ci, [&](int i, float *t) { t[0] = D[i]; }, v, red, &flag))
+            return;
         if (threadIdx.x == 0)
             mse = smm::fdiv(v[0].value(), (float)cnt);
+    } else if (blockIdx.x != 0) {
+        return;
     }
-    const int *nnR = w.nnR + (size_t)ci * w.maxSrc;
-    for (int i = threadIdx.x; i < s.n; i += kT)
-        if (nnR[i] >= 0)
-            w.win[(size_t)ci * w.maxDst + nnR[i]] = ~0ull;
     if (threadIdx.x != 0)
         return;
     if (w.trace && C.iterations < kTraceIters) {
@@ -430,6 +470,7 @@ __global__ void k_rank(const int *__restrict__ ids, int m, int *__restrict__ ran
 
 void run_stage(Ctx &c, Work &w, const Stage &s, int ncand) {
     const dim3 g2(s.nb, ncand);
+    const dim3 gr(smi::kIcpBlocks, ncand);                    // reductions
     const dim3 gw(std::max(1, nblocks(s.n, kW * 4)), ncand); // warp kernels: 4 points per warp
     k_stage_begin<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand);
     SM_LAUNCH_CHECK();
@@ -438,15 +479,13 @@ void run_stage(Ctx &c, Work &w, const Stage &s, int ncand) {
         SM_LAUNCH_CHECK();
         k_pairs<<<g2, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
-        k_centroids<<<ncand, kT, 0, c.stream>>>(w, s);
+        k_centroids<<<gr, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
-        k_sys_terms<<<g2, kT, 0, c.stream>>>(w, s);
-        SM_LAUNCH_CHECK();
-        k_solve<<<ncand, kT, 0, c.stream>>>(w, s);
+        k_solve<<<gr, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
         k_resid<<<gw, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
-        k_update<<<ncand, kT, 0, c.stream>>>(w, s);
+        k_update<<<gr, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
     }
 }
@@ -467,7 +506,10 @@ void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, con
     w.nnR    = c.arena.get<int>("icp.nnR", (size_t)ncand * w.maxSrc);
     w.x4     = c.arena.get<float4>("icp.x4", (size_t)ncand * w.maxSrc);
     w.n4     = c.arena.get<float4>("icp.n4", (size_t)ncand * w.maxSrc);
-    w.terms  = c.arena.get<float>("icp.terms", (size_t)ncand * smi::kNumSystem * w.maxSrc);
+    w.resid  = c.arena.get<float>("icp.resid", (size_t)ncand * w.maxSrc);
+    w.part   = c.arena.get<float2>("icp.part", (size_t)ncand * smi::kIcpBlocks * smi::kNumSystem);
+    w.ctr    = c.arena.get<int>("icp.ctr", ncand);
+    SM_CUDA(cudaMemsetAsync(w.ctr, 0, (size_t)ncand * sizeof(int), c.stream));
     w.win    = c.arena.get<unsigned long long>("icp.win", (size_t)ncand * w.maxDst);
     w.trace  = trace;
     SM_CUDA(cudaMemsetAsync(w.win, 0xff, (size_t)ncand * w.maxDst * 8, c.stream));

@@ -5,8 +5,10 @@
 // util.cpp:209-232 (transformPointCloud). Precision design: the 21 + 6 entries of the
 // normal equations and the centroid sums are accumulated in FP32 with Kahan compensation;
 // only the 6x6 solve and the pose composition run in FP64. Both sides use the same
-// summation layout (kIcpThreads strided partial sums merged by a fixed binary tree), so
-// the GPU and the oracle produce bit-identical poses.
+// summation layout, so the GPU and the oracle produce bit-identical poses: kIcpSlots
+// strided partial sums (slot = source index mod kIcpSlots, ascending within a slot), merged
+// by fixed binary trees - within each group of 32 slots (offsets 16..1), over the
+// kIcpThreads / 32 groups of a block (offsets 4..1), then over the kIcpBlocks blocks.
 #pragma once
 
 #include "sm_linalg.h"
@@ -14,7 +16,9 @@
 
 namespace smi {
 
-constexpr int kIcpThreads = 256; // ICP CTA size; also the oracle's emulated partial count
+constexpr int kIcpThreads = 256;                       // ICP CTA size
+constexpr int kIcpBlocks  = 8;                         // CTAs per candidate and reduction
+constexpr int kIcpSlots   = kIcpThreads * kIcpBlocks;  // strided partial sums
 
 // Kahan-compensated FP32 accumulator; value() = s - c.
 struct KahanF {
@@ -105,51 +109,94 @@ SM_HD void system_terms(float px, float py, float pz, float qx, float qy, float 
 // (icp.cpp:68-86): theta = atan(|a~|) with sin/cos taken exactly as |a~|/sqrt(1+|a~|^2) and
 // 1/sqrt(1+|a~|^2), R_i = I + sin W + (1-cos) W^2, R = R_i^2,
 // t = R_i^2 (-Pmean) + R_i (cos * t~) + Qmean.
-SM_HD Pose34 solve_step(const float sys[kNumSystem], const float Pm[3], const float Qm[3]) {
-    double A[6][6], r[6], u[6];
-    int    k = 0;
+SM_HD void system_matrix(const float sys[kNumSystem], double A[6][6], double r[6]) {
+    int k = 0;
+    SML_UNROLL
     for (int i = 0; i < 6; i++)
+        SML_UNROLL
         for (int j = i; j < 6; j++) {
             A[i][j] = (double)sys[k];
             A[j][i] = A[i][j];
             k++;
         }
+    SML_UNROLL
     for (int i = 0; i < 6; i++)
         r[i] = -(double)sys[21 + i];
-    if (!sml::cholesky6(A, r, u))
-        sml::pinv6(A, r, u);
+}
+
+// The step's pose from the solution u = (rotation vector a~, translation) of the system.
+SM_HD Pose34 step_pose(const double u[6], const float Pm[3], const float Qm[3]);
+
+SM_HD Pose34 solve_step(const float sys[kNumSystem], const float Pm[3], const float Qm[3]) {
+    double A[6][6], r[6], u[6];
+    system_matrix(sys, A, r);
+    if (!sml::cholesky6(A, r, u)) {
+        double A2[6][6], r2[6]; // rank-deficient: pseudo-inverse on its own copy
+        system_matrix(sys, A2, r2);
+        sml::pinv6(A2, r2, u);
+    }
+    return step_pose(u, Pm, Qm);
+}
+
+#if defined(__CUDACC__)
+// solve_step by one warp (every lane calls it and gets the pose): the Cholesky factorisation
+// runs one row per lane (sml::cholesky6_warp); identical results.
+__device__ __forceinline__ Pose34 solve_step_warp(const float sys[kNumSystem], const float Pm[3],
+                                                  const float Qm[3]) {
+    double A[6][6], r[6], u[6];
+    system_matrix(sys, A, r);
+    if (!sml::cholesky6_warp(A, r, u)) {
+        double A2[6][6], r2[6];
+        system_matrix(sys, A2, r2);
+        sml::pinv6(A2, r2, u);
+    }
+    return step_pose(u, Pm, Qm);
+}
+#endif
+
+SM_HD Pose34 step_pose(const double u[6], const float Pm[3], const float Qm[3]) {
     const double an = sml::dsqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
     const double h  = sml::dsqrt(1.0 + an * an);
-    const double sn = an / h, cs = 1.0 / h;
+    const double cs = 1.0 / h, sn = an * cs;
     double       a[3] = {0.0, 0.0, 0.0};
     if (an > 0.0) {
-        a[0] = u[0] / an;
-        a[1] = u[1] / an;
-        a[2] = u[2] / an;
+        const double ia = 1.0 / an;
+        a[0]            = u[0] * ia;
+        a[1]            = u[1] * ia;
+        a[2]            = u[2] * ia;
     }
     const double W[3][3] = {{0.0, -a[2], a[1]}, {a[2], 0.0, -a[0]}, {-a[1], a[0], 0.0}};
     double       Ri[3][3], R[3][3];
+    SML_UNROLL
     for (int i = 0; i < 3; i++)
+        SML_UNROLL
         for (int j = 0; j < 3; j++) {
             double w2 = 0.0;
+            SML_UNROLL
             for (int m = 0; m < 3; m++)
                 w2 += W[i][m] * W[m][j];
             Ri[i][j] = (i == j ? 1.0 : 0.0) + sn * W[i][j] + (1.0 - cs) * w2;
         }
+    SML_UNROLL
     for (int i = 0; i < 3; i++)
+        SML_UNROLL
         for (int j = 0; j < 3; j++) {
             double s = 0.0;
+            SML_UNROLL
             for (int m = 0; m < 3; m++)
                 s += Ri[i][m] * Ri[m][j];
             R[i][j] = s;
         }
     const double tt[3] = {cs * u[3], cs * u[4], cs * u[5]};
     Pose34       o;
+    SML_UNROLL
     for (int i = 0; i < 3; i++) {
         double t = 0.0;
+        SML_UNROLL
         for (int m = 0; m < 3; m++)
             t += R[i][m] * (-(double)Pm[m]) + Ri[i][m] * tt[m];
         t += (double)Qm[i];
+        SML_UNROLL
         for (int j = 0; j < 3; j++)
             o.m[i * 4 + j] = (float)R[i][j];
         o.m[i * 4 + 3] = (float)t;

@@ -17,6 +17,13 @@
 #else
 #define SML_HD inline
 #endif
+// Full unrolling of fixed-size loops on the device, so small matrices stay in registers
+// (the operations and their order are unchanged).
+#if defined(__CUDA_ARCH__)
+#define SML_UNROLL _Pragma("unroll")
+#else
+#define SML_UNROLL
+#endif
 
 namespace sml {
 
@@ -56,9 +63,12 @@ template <int N> SML_HD void jacobi_eig(double A[N][N], double V[N][N], double d
                 const double apq = A[p][q];
                 if (apq == 0.0)
                     continue;
-                const double theta = (A[q][q] - A[p][p]) / (2.0 * apq);
-                double       t     = 1.0 / (dabs(theta) + dsqrt(theta * theta + 1.0));
-                if (theta < 0.0)
+                // t = sgn(theta) / (|theta| + sqrt(theta^2 + 1)) with theta = dq / (2 apq),
+                // multiplied through by 2 |apq| (one division fewer)
+                const double dq = A[q][q] - A[p][p];
+                const double t2 = 2.0 * apq;
+                double       t  = t2 / (dabs(dq) + dsqrt(dq * dq + t2 * t2));
+                if (dq < 0.0)
                     t = -t;
                 const double c = 1.0 / dsqrt(t * t + 1.0);
                 const double s = t * c;
@@ -207,42 +217,119 @@ SML_HD float quat_angle(const double q[4]) {
 // pivot is not positive relative to the matrix scale; the caller then uses the
 // eigen-decomposition pseudo-inverse below.
 SML_HD bool cholesky6(const double A[6][6], const double r[6], double u[6]) {
-    double L[6][6];
+    double L[6][6], inv[6]; // inv[j] = 1 / L[j][j]: one division per pivot
     double dmax = 0.0;
+    SML_UNROLL
     for (int i = 0; i < 6; i++)
         dmax = A[i][i] > dmax ? A[i][i] : dmax;
     if (!(dmax > 0.0))
         return false;
+    SML_UNROLL
     for (int j = 0; j < 6; j++) {
         double s = A[j][j];
+        SML_UNROLL
         for (int k = 0; k < j; k++)
             s -= L[j][k] * L[j][k];
         if (!(s > dmax * 1e-13))
             return false;
         const double ljj = dsqrt(s);
         L[j][j]          = ljj;
+        inv[j]           = 1.0 / ljj;
+        SML_UNROLL
         for (int i = j + 1; i < 6; i++) {
             double t = A[i][j];
+            SML_UNROLL
             for (int k = 0; k < j; k++)
                 t -= L[i][k] * L[j][k];
-            L[i][j] = t / ljj;
+            L[i][j] = t * inv[j];
         }
     }
     double y[6];
+    SML_UNROLL
     for (int i = 0; i < 6; i++) {
         double t = r[i];
+        SML_UNROLL
         for (int k = 0; k < i; k++)
             t -= L[i][k] * y[k];
-        y[i] = t / L[i][i];
+        y[i] = t * inv[i];
     }
+    SML_UNROLL
     for (int i = 5; i >= 0; i--) {
         double t = y[i];
-        for (int k = i + 1; k < 6; k++)
+        SML_UNROLL
+        for (int k = 5; k > i; k--) // descending k: the order of the warp version's column sweep
             t -= L[k][i] * u[k];
-        u[i] = t / L[i][i];
+        u[i] = t * inv[i];
     }
     return true;
 }
+
+#if defined(__CUDACC__)
+// cholesky6 by one warp, one row per lane (lanes 0-5; every lane calls it): per column the
+// pivot's square root, then all rows' updates and divisions at once; the triangular solves
+// column by column. Each element sees the same operations in the same order as cholesky6,
+// so the results are identical; every lane gets u. Returns false where cholesky6 does.
+__device__ __forceinline__ bool cholesky6_warp(const double A[6][6], const double r[6], double u[6]) {
+    const int lane = threadIdx.x & 31;
+    const int row  = lane < 6 ? lane : 5;
+    double    Lr[6]; // row `row` of L
+    double    inv  = 0.0; // 1 / L[row][row]
+    double    dmax = 0.0;
+    SML_UNROLL
+    for (int i = 0; i < 6; i++)
+        dmax = A[i][i] > dmax ? A[i][i] : dmax;
+    if (!(dmax > 0.0))
+        return false;
+    SML_UNROLL
+    for (int j = 0; j < 6; j++) {
+        // the pivot row j: s = A[j][j] - sum_k L[j][k]^2 (lane j), broadcast
+        double s = A[j][j];
+        SML_UNROLL
+        for (int k = 0; k < j; k++) {
+            const double ljk = __shfl_sync(0xffffffffu, Lr[k], j);
+            s -= ljk * ljk;
+        }
+        if (!(s > dmax * 1e-13))
+            return false;
+        const double ljj  = dsqrt(s);
+        const double invj = 1.0 / ljj;
+        if (row == j)
+            inv = invj;
+        // rows i > j: t = A[i][j] - sum_k L[i][k] L[j][k], L[i][j] = t * (1 / L[j][j])
+        double t = A[row][j];
+        SML_UNROLL
+        for (int k = 0; k < j; k++)
+            t -= Lr[k] * __shfl_sync(0xffffffffu, Lr[k], j);
+        Lr[j] = row == j ? ljj : (row > j ? t * invj : 0.0);
+    }
+    // forward: y_i = (r_i - sum_{k<i} L[i][k] y_k) * (1 / L[i][i]), column by column
+    double ti = r[row], y[6];
+    SML_UNROLL
+    for (int k = 0; k < 6; k++) {
+        const double yk = __shfl_sync(0xffffffffu, ti * inv, k);
+        y[k]            = yk;
+        if (row > k)
+            ti -= Lr[k] * yk;
+    }
+    // back: u_i = (y_i - sum_{k>i, descending} L[k][i] u_k) * (1 / L[i][i]); L[k][i] is row k's
+    double tb = y[row];
+    SML_UNROLL
+    for (int k = 5; k >= 0; k--) {
+        const double uk  = __shfl_sync(0xffffffffu, tb * inv, k);
+        u[k]             = uk;
+        double lki = 0.0; // L[k][row] held by lane k
+        SML_UNROLL
+        for (int i = 0; i < 6; i++) {
+            const double v = __shfl_sync(0xffffffffu, Lr[i], k);
+            if (i == row)
+                lki = v;
+        }
+        if (row < k)
+            tb -= lki * uk;
+    }
+    return true;
+}
+#endif
 
 // Least-squares / minimum-norm solve of a symmetric PSD 6x6 system through its
 // eigen-decomposition, discarding eigenvalues below 1e-6 of the largest (rank-deficient
