@@ -257,7 +257,7 @@ void train(Ctx &c, Model &m, const float *xyzIn, const float *nrmIn, int64_t n64
     if (nvalid == 0)
         throw Error(SM_ERR_RUNTIME, "Invalid Input: empty model in trainModel");
     int *valid = c.arena.get<int>("t.vids", n);
-    compact(c, val, n, valid, "t.cv");
+    compact_known(c, val, n, valid, "t.cv");
     const float diam         = box.diameter();
     const float sampleStep   = diam * sdRel;
     const float reSampleStep = diam * tp.poseRefRelSamplingDistance;
@@ -370,7 +370,7 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
     Box          box;
     const int    nvalid = prep_points(c, xyz, nin, n, pos, nrm, val, box);
     int         *valid  = c.arena.get<int>("m.vids", n);
-    compact(c, val, n, valid, "m.cv");
+    compact_known(c, val, n, valid, "m.cv"); // nvalid points
     record(c, 1);
     float ext[3] = {box.ext(0), box.ext(1), box.ext(2)};
 

@@ -225,34 +225,46 @@ __global__ void k_cell_sort(const int *__restrict__ start, long long nc, int *__
 }
 
 // ---------------------------------------------------------------------------------------
-__global__ void k_occ_flags(const int *__restrict__ start, long long nc, int *__restrict__ flag) {
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < nc)
-        flag[c] = start[c + 1] > start[c] ? 1 : 0;
+// Occupied cells per phase, counted (pass 1) and listed (pass 2) on the device: `ph` holds
+// 8 counts, then 8 list offsets, then 8 fill pointers. rank[cell] = the cell's list slot
+// (index of its kept-point record); cells within a phase in any order (they do not
+// interact).
+__global__ void k_phase_count(const int *__restrict__ start, long long nc, int dim0, int dim1,
+                              int *__restrict__ ph) {
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
+         c += (long long)gridDim.x * blockDim.x) {
+        if (start[c + 1] <= start[c])
+            continue;
+        const int cx = (int)(c % dim0), cy = (int)((c / dim0) % dim1), cz = (int)(c / ((long long)dim0 * dim1));
+        atomicAdd(&ph[smg::phase_of(cx, cy, cz)], 1);
+    }
 }
 
-__global__ void k_occ_rank(const int *__restrict__ occ, int nocc, int *__restrict__ rank, int dim0,
-                           int dim1, int *__restrict__ phaseCnt, int *__restrict__ phaseOf) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nocc)
+__global__ void k_phase_offsets(int *__restrict__ ph) {
+    if (threadIdx.x != 0)
         return;
-    const int c  = occ[i];
-    rank[c]      = i;
-    const int cx = c % dim0, cy = (c / dim0) % dim1, cz = c / (dim0 * dim1);
-    const int ph = smg::phase_of(cx, cy, cz);
-    phaseOf[i]   = ph;
-    atomicAdd(&phaseCnt[ph], 1);
+    int o = 0;
+    for (int p = 0; p < 8; p++) {
+        ph[8 + p]  = o;
+        ph[16 + p] = o;
+        o += ph[p];
+    }
 }
 
-__global__ void k_phase_scatter(const int *__restrict__ occ, const int *__restrict__ phaseOf,
-                                int nocc, int *__restrict__ phaseFill, int *__restrict__ lists) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nocc)
-        return;
-    const int slot = atomicAdd(&phaseFill[phaseOf[i]], 1);
-    lists[slot]    = occ[i];
+__global__ void k_phase_list(const int *__restrict__ start, long long nc, int dim0, int dim1,
+                             int *__restrict__ ph, int *__restrict__ lists, int *__restrict__ rank) {
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
+         c += (long long)gridDim.x * blockDim.x) {
+        if (start[c + 1] <= start[c])
+            continue;
+        const int cx = (int)(c % dim0), cy = (int)((c / dim0) % dim1), cz = (int)(c / ((long long)dim0 * dim1));
+        const int slot = atomicAdd(&ph[16 + smg::phase_of(cx, cy, cz)], 1);
+        lists[slot]    = (int)c;
+        rank[c]        = slot;
+    }
 }
 
+// ---------------------------------------------------------------------------------------
 constexpr int kSpWarps = 4;   // warps (cells) per CTA of the phase kernel
 constexpr int kSpIds   = 384; // cell sizes held in shared memory
 constexpr int kSpStage = 384; // neighbours' kept points staged in shared memory
@@ -267,128 +279,131 @@ constexpr int kSpStage = 384; // neighbours' kept points staged in shared memory
 // points and the cell's points are staged in shared memory; cells too large for the
 // staging buffers take the same steps in global memory (`alive` flags in aliveTmp).
 __global__ void __launch_bounds__(kSpWarps * 32)
-    k_sample_phase(const float4 *__restrict__ pos, GridView G, const int *__restrict__ cells,
-                   int ncells, const int *__restrict__ rank, int *__restrict__ keptCnt,
-                   float4 *__restrict__ keptPos, int cap, float r2, int *__restrict__ keptFlag,
-                   int *__restrict__ overflow, int *__restrict__ aliveTmp) {
+    k_sample_phase(const float4 *__restrict__ pos, GridView G, const int *__restrict__ lists,
+                   const int *__restrict__ ph, int phase, const int *__restrict__ rank,
+                   int *__restrict__ keptCnt, float4 *__restrict__ keptPos, int cap, float r2,
+                   int *__restrict__ keptFlag, int *__restrict__ overflow,
+                   int *__restrict__ aliveTmp) {
     __shared__ float4 stage[kSpWarps][kSpStage];
     __shared__ float4 cpos[kSpWarps][kSpIds];
     __shared__ int    cid[kSpWarps][kSpIds];
     __shared__ int    calive[kSpWarps][kSpIds];
     __shared__ int    snr[kSpWarps][26], scnt[kSpWarps][26];
-    const int wl   = threadIdx.x >> 5;
-    const int w    = blockIdx.x * kSpWarps + wl;
-    const int lane = threadIdx.x & 31;
-    if (w >= ncells)
-        return;
-    const int cell = cells[w];
-    const int rk   = rank[cell];
-    const int cx = cell % G.dim[0], cy = (cell / G.dim[0]) % G.dim[1],
-              cz = cell / (G.dim[0] * G.dim[1]);
-    const int s = G.start[cell], e = G.start[cell + 1], n = e - s;
-    // neighbour l (lane < 26) of the 3x3x3 block without its centre
-    int nr = -1, cnt = 0;
-    if (lane < 26) {
-        const int o = lane < 13 ? lane : lane + 1;
-        const int x = cx + o % 3 - 1, y = cy + (o / 3) % 3 - 1, z = cz + o / 9 - 1;
-        if (x >= 0 && y >= 0 && z >= 0 && x < G.dim[0] && y < G.dim[1] && z < G.dim[2]) {
-            nr  = rank[grid_cell(G, x, y, z)];
-            cnt = nr >= 0 ? keptCnt[nr] : 0;
-        }
-        snr[wl][lane]  = nr;
-        scnt[wl][lane] = cnt;
-    }
-    __syncwarp();
-    const int  incl    = warp_incl_scan(cnt);
-    const int  excl    = incl - cnt;
-    const int  NK      = __shfl_sync(0xffffffffu, incl, 31);
-    const bool stageNb = NK <= kSpStage;
-    const bool stageC  = n <= kSpIds;
-    float4    *st      = stage[wl];
-    if (stageNb) {
-        for (int base = 0; base < NK; base += 32) {
-            const int t  = base + lane;
-            int       lo = 0;
-#pragma unroll
-            for (int step = 16; step >= 1; step >>= 1) {
-                const int mid = lo + step;
-                const int ev  = __shfl_sync(0xffffffffu, excl, mid & 31);
-                if (mid < 26 && ev <= t)
-                    lo = mid;
+    const int  wl     = threadIdx.x >> 5;
+    const int  lane   = threadIdx.x & 31;
+    const int  ncells = ph[phase];
+    const int *cells  = lists + ph[8 + phase];
+    for (int w = blockIdx.x * kSpWarps + wl; w < ncells; w += gridDim.x * kSpWarps) {
+        const int cell = cells[w];
+        const int rk   = rank[cell];
+        const int cx = cell % G.dim[0], cy = (cell / G.dim[0]) % G.dim[1],
+                  cz = cell / (G.dim[0] * G.dim[1]);
+        const int s = G.start[cell], e = G.start[cell + 1], n = e - s;
+        // neighbour l (lane < 26) of the 3x3x3 block without its centre
+        int nr = -1, cnt = 0;
+        if (lane < 26) {
+            const int o = lane < 13 ? lane : lane + 1;
+            const int x = cx + o % 3 - 1, y = cy + (o / 3) % 3 - 1, z = cz + o / 9 - 1;
+            if (x >= 0 && y >= 0 && z >= 0 && x < G.dim[0] && y < G.dim[1] && z < G.dim[2]) {
+                nr  = rank[grid_cell(G, x, y, z)];
+                cnt = nr >= 0 ? keptCnt[nr] : 0;
             }
-            const int nj = __shfl_sync(0xffffffffu, nr, lo);
-            const int ej = __shfl_sync(0xffffffffu, excl, lo);
-            if (t < NK)
-                st[t] = keptPos[(size_t)nj * cap + (t - ej)];
+            snr[wl][lane]  = nr;
+            scnt[wl][lane] = cnt;
         }
-    }
-    int *alive = stageC ? calive[wl] : aliveTmp + s;
-    // survivors of the neighbours' kept points
-    for (int i = lane; i < n; i += 32) {
-        const int    id = G.ids[s + i];
-        const float4 q  = pos[id];
-        bool         ok = true;
+        __syncwarp();
+        const int  incl    = warp_incl_scan(cnt);
+        const int  excl    = incl - cnt;
+        const int  NK      = __shfl_sync(0xffffffffu, incl, 31);
+        const bool stageNb = NK <= kSpStage;
+        const bool stageC  = n <= kSpIds;
+        float4    *st      = stage[wl];
         if (stageNb) {
-            for (int k = 0; k < NK && ok; k++) {
-                const float4 o = st[k];
-                if (smm::dist2(o.x, o.y, o.z, q.x, q.y, q.z) < r2)
-                    ok = false;
+            for (int base = 0; base < NK; base += 32) {
+                const int t  = base + lane;
+                int       lo = 0;
+    #pragma unroll
+                for (int step = 16; step >= 1; step >>= 1) {
+                    const int mid = lo + step;
+                    const int ev  = __shfl_sync(0xffffffffu, excl, mid & 31);
+                    if (mid < 26 && ev <= t)
+                        lo = mid;
+                }
+                const int nj = __shfl_sync(0xffffffffu, nr, lo);
+                const int ej = __shfl_sync(0xffffffffu, excl, lo);
+                if (t < NK)
+                    st[t] = keptPos[(size_t)nj * cap + (t - ej)];
             }
-        } else {
-            for (int j = 0; j < 26 && ok; j++) {
-                const int nj = snr[wl][j], cj = scnt[wl][j];
-                for (int k = 0; k < cj && ok; k++) {
-                    const float4 o = keptPos[(size_t)nj * cap + k];
+        }
+        int *alive = stageC ? calive[wl] : aliveTmp + s;
+        // survivors of the neighbours' kept points
+        for (int i = lane; i < n; i += 32) {
+            const int    id = G.ids[s + i];
+            const float4 q  = pos[id];
+            bool         ok = true;
+            if (stageNb) {
+                for (int k = 0; k < NK && ok; k++) {
+                    const float4 o = st[k];
                     if (smm::dist2(o.x, o.y, o.z, q.x, q.y, q.z) < r2)
                         ok = false;
                 }
+            } else {
+                for (int j = 0; j < 26 && ok; j++) {
+                    const int nj = snr[wl][j], cj = scnt[wl][j];
+                    for (int k = 0; k < cj && ok; k++) {
+                        const float4 o = keptPos[(size_t)nj * cap + k];
+                        if (smm::dist2(o.x, o.y, o.z, q.x, q.y, q.z) < r2)
+                            ok = false;
+                    }
+                }
             }
-        }
-        alive[i] = ok ? 1 : 0;
-        if (stageC) {
-            cid[wl][i]  = id;
-            cpos[wl][i] = q;
-        }
-    }
-    __syncwarp();
-    // keep the smallest surviving index, drop the survivors within the step, repeat
-    float4 *mine = keptPos + (size_t)rk * cap;
-    int     nk   = 0;
-    for (;;) {
-        int myMin = INT_MAX;
-        for (int i = lane; i < n; i += 32)
-            if (alive[i]) {
-                const int id = stageC ? cid[wl][i] : G.ids[s + i];
-                myMin        = min(myMin, id);
+            alive[i] = ok ? 1 : 0;
+            if (stageC) {
+                cid[wl][i]  = id;
+                cpos[wl][i] = q;
             }
-        int m = myMin;
-#pragma unroll
-        for (int o = 16; o >= 1; o >>= 1)
-            m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (m == INT_MAX)
-            break;
-        const float4 kp4 = pos[m];
-        const float4 kp  = make_float4(kp4.x, kp4.y, kp4.z, 0.0f);
-        if (lane == 0) {
-            keptFlag[m] = 1;
-            if (nk < cap)
-                mine[nk] = kp;
-            else
-                atomicExch(overflow, 1);
-        }
-        nk = min(nk + 1, cap);
-        for (int i = lane; i < n; i += 32) {
-            if (!alive[i])
-                continue;
-            const int    id = stageC ? cid[wl][i] : G.ids[s + i];
-            const float4 q  = stageC ? cpos[wl][i] : pos[id];
-            if (id == m || smm::dist2(kp.x, kp.y, kp.z, q.x, q.y, q.z) < r2)
-                alive[i] = 0;
         }
         __syncwarp();
+        // keep the smallest surviving index, drop the survivors within the step, repeat
+        float4 *mine = keptPos + (size_t)rk * cap;
+        int     nk   = 0;
+        for (;;) {
+            int myMin = INT_MAX;
+            for (int i = lane; i < n; i += 32)
+                if (alive[i]) {
+                    const int id = stageC ? cid[wl][i] : G.ids[s + i];
+                    myMin        = min(myMin, id);
+                }
+            int m = myMin;
+    #pragma unroll
+            for (int o = 16; o >= 1; o >>= 1)
+                m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+            if (m == INT_MAX)
+                break;
+            const float4 kp4 = pos[m];
+            const float4 kp  = make_float4(kp4.x, kp4.y, kp4.z, 0.0f);
+            if (lane == 0) {
+                keptFlag[m] = 1;
+                if (nk < cap)
+                    mine[nk] = kp;
+                else
+                    atomicExch(overflow, 1);
+            }
+            nk = min(nk + 1, cap);
+            for (int i = lane; i < n; i += 32) {
+                if (!alive[i])
+                    continue;
+                const int    id = stageC ? cid[wl][i] : G.ids[s + i];
+                const float4 q  = stageC ? cpos[wl][i] : pos[id];
+                if (id == m || smm::dist2(kp.x, kp.y, kp.z, q.x, q.y, q.z) < r2)
+                    alive[i] = 0;
+            }
+            __syncwarp();
+        }
+        if (lane == 0)
+            keptCnt[rk] = nk;
+        __syncwarp(); // the next cell reuses the warp's staging buffers
     }
-    if (lane == 0)
-        keptCnt[rk] = nk;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -404,9 +419,10 @@ __global__ void k_mark_todo(const int *__restrict__ ids, int m, const float4 *__
 
 // One warp per query (exact k nearest neighbours, sm_device.cuh warp_knn_sorted); lane j
 // writes the j-th neighbour, and with smoothing marks it when it still needs a normal.
-__global__ void k_knn(const int *__restrict__ list, int nl, HGridView G, const float4 *__restrict__ pos,
+__global__ void k_knn(const int *__restrict__ list, const int *__restrict__ nlp, HGridView G, const float4 *__restrict__ pos,
                       int k, int *__restrict__ nbr, int *__restrict__ nbrCnt, int markNeighbours,
                       const float4 *__restrict__ nrm, int *__restrict__ need) {
+    const int nl = *nlp; // device-side count of the list
     const int lane = threadIdx.x & 31;
     const int t    = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     if (t >= nl)
@@ -423,12 +439,14 @@ __global__ void k_knn(const int *__restrict__ list, int nl, HGridView G, const f
         need[id] = 1;
 }
 
-void launch_knn(cudaStream_t st, const int *list, int nl, const HGridView &G, const float4 *pos,
-                int k, int *nbr, int *cnt, int mark, const float4 *nrm, int *need) {
-    if (nl <= 0)
+// list[0 .. *nlp) on the device; nlMax bounds it for the launch.
+void launch_knn(cudaStream_t st, const int *list, const int *nlp, int nlMax, const HGridView &G,
+                const float4 *pos, int k, int *nbr, int *cnt, int mark, const float4 *nrm,
+                int *need) {
+    if (nlMax <= 0)
         return;
-    k_knn<<<nblocks((long long)nl * 32, 256), 256, 0, st>>>(list, nl, G, pos, k, nbr, cnt, mark,
-                                                            nrm, need);
+    k_knn<<<nblocks((long long)nlMax * 32, 256), 256, 0, st>>>(list, nlp, G, pos, k, nbr, cnt,
+                                                               mark, nrm, need);
     SM_LAUNCH_CHECK();
 }
 
@@ -495,17 +513,18 @@ __global__ void k_flags_grid_order(const int *__restrict__ gids, int m, const in
         flags[i] = need[gids[i]] == eq ? 1 : 0;
 }
 
-__global__ void k_map_ids(const int *__restrict__ idx, int n, const int *__restrict__ gids,
-                          int *__restrict__ out) {
+__global__ void k_scatter_ids(const int *__restrict__ flags, const int *__restrict__ pre, int n,
+                              const int *__restrict__ gids, int *__restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n)
-        out[i] = gids[idx[i]];
+    if (i < n && flags[i])
+        out[pre[i]] = gids[i];
 }
 
 // Phase A: centroid and FP32-Kahan covariance of the neighbourhood, FP64 eigensolve.
-__global__ void k_pca(const int *__restrict__ list, int nl, const int *__restrict__ nbr,
+__global__ void k_pca(const int *__restrict__ list, const int *__restrict__ nlp, const int *__restrict__ nbr,
                       const int *__restrict__ nbrCnt, int k, const float4 *__restrict__ pos,
                       float4 *__restrict__ cen, float4 *__restrict__ nout) {
+    const int nl = *nlp; // device-side count of the list
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nl)
         return;
@@ -550,9 +569,10 @@ __global__ void k_pca(const int *__restrict__ list, int nl, const int *__restric
     nout[t] = make_float4(n3[0], n3[1], n3[2], 1.0f);
 }
 
-__global__ void k_pca_write(const int *__restrict__ list, int nl, const float4 *__restrict__ cen,
+__global__ void k_pca_write(const int *__restrict__ list, const int *__restrict__ nlp, const float4 *__restrict__ cen,
                             const float4 *__restrict__ nin, float4 *__restrict__ pos,
                             float4 *__restrict__ nrm) {
+    const int nl = *nlp; // device-side count of the list
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nl || cen[t].w < 0.0f)
         return;
@@ -562,9 +582,10 @@ __global__ void k_pca_write(const int *__restrict__ list, int nl, const float4 *
 }
 
 // Phase B: sign-aligned sum of the raw neighbourhood normals (util.cpp:292-306).
-__global__ void k_smooth(const int *__restrict__ list, int nl, const int *__restrict__ nbr,
+__global__ void k_smooth(const int *__restrict__ list, const int *__restrict__ nlp, const int *__restrict__ nbr,
                          const int *__restrict__ nbrCnt, int k, const float4 *__restrict__ nrm,
                          float4 *__restrict__ out) {
+    const int nl = *nlp; // device-side count of the list
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nl)
         return;
@@ -598,8 +619,9 @@ __global__ void k_smooth(const int *__restrict__ list, int nl, const int *__rest
     out[t] = make_float4(sx, sy, sz, 1.0f);
 }
 
-__global__ void k_smooth_write(const int *__restrict__ list, int nl, const float4 *__restrict__ sm,
+__global__ void k_smooth_write(const int *__restrict__ list, const int *__restrict__ nlp, const float4 *__restrict__ sm,
                                float4 *__restrict__ nrm) {
+    const int nl = *nlp; // device-side count of the list
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nl || sm[t].w < 0.0f)
         return;
@@ -685,6 +707,14 @@ static int scan_impl(Ctx &c, const int *in, int *out, long long n, int eq, const
     return c.hostCounts[0];
 }
 
+// Exclusive scan of 0/1 flags without a host round trip; returns the device address of the
+// total.
+static int *scan_flags_total(Ctx &c, const int *flags, int *pre, int n, const std::string &tag) {
+    scan_impl(c, flags, pre, n, kNoEq, tag, false);
+    const int nparts = (int)((n + kScanTile - 1) / kScanTile);
+    return c.arena.get<int>(tag + ".scanpart", nparts + 1) + nparts;
+}
+
 int scan_excl(Ctx &c, const int *in, int *out, long long n, const std::string &tag, bool wantTotal) {
     return scan_impl(c, in, out, n, kNoEq, tag, wantTotal);
 }
@@ -703,21 +733,32 @@ int compact(Ctx &c, const int *flags, int n, int *outIds, const std::string &tag
     return compact_eq(c, flags, n, kNoEq, outIds, tag);
 }
 
-// The points p of grid H with need[p] == eq, in H's cell order.
-static int compact_grid_order(Ctx &c, const HGrid &H, const int *need, int eq, int *out,
-                              const std::string &tag) {
-    if (H.m <= 0)
-        return 0;
-    int *flags = c.arena.get<int>(tag + ".gf", H.m);
-    int *idx   = c.arena.get<int>(tag + ".gi", H.m);
+void compact_known(Ctx &c, const int *flags, int n, int *outIds, const std::string &tag) {
+    if (n <= 0)
+        return;
+    int *pre = c.arena.get<int>(tag + ".pre", n);
+    scan_impl(c, flags, pre, n, kNoEq, tag, false);
+    k_scatter_flags<<<nblocks(n, 256), 256, 0, c.stream>>>(flags, pre, n, kNoEq, outIds);
+    SM_LAUNCH_CHECK();
+}
+
+// The points p of grid H with need[p] == eq, in H's cell order, into out; returns the device
+// address of their count (no host round trip).
+static int *compact_grid_order(Ctx &c, const HGrid &H, const int *need, int eq, int *out,
+                               const std::string &tag) {
+    int *flags = c.arena.get<int>(tag + ".gf", std::max(H.m, 1));
+    int *pre   = c.arena.get<int>(tag + ".gp", std::max(H.m, 1));
+    if (H.m <= 0) {
+        int *z = c.arena.get<int>(tag + ".gz", 1);
+        SM_CUDA(cudaMemsetAsync(z, 0, sizeof(int), c.stream));
+        return z;
+    }
     k_flags_grid_order<<<nblocks(H.m, 256), 256, 0, c.stream>>>(H.ids, H.m, need, eq, flags);
     SM_LAUNCH_CHECK();
-    const int n = compact(c, flags, H.m, idx, tag + ".gc");
-    if (n > 0) {
-        k_map_ids<<<nblocks(n, 256), 256, 0, c.stream>>>(idx, n, H.ids, out);
-        SM_LAUNCH_CHECK();
-    }
-    return n;
+    int *total = scan_flags_total(c, flags, pre, H.m, tag + ".gc");
+    k_scatter_ids<<<nblocks(H.m, 256), 256, 0, c.stream>>>(flags, pre, H.m, H.ids, out);
+    SM_LAUNCH_CHECK();
+    return total;
 }
 
 void build_grid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &box, float g,
@@ -811,57 +852,51 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
     const float g = smg::sample_cell(step, ext);
     Grid        G;
     build_grid(c, pos, ids, m, box, g, false, G, tag + ".g");
-    int *occFlag = c.arena.get<int>(tag + ".occf", G.nc);
-    k_occ_flags<<<nblocks(G.nc, 256), 256, 0, c.stream>>>(G.start, G.nc, occFlag);
-    SM_LAUNCH_CHECK();
-    int *occ  = c.arena.get<int>(tag + ".occ", std::max<long long>(G.nc, 1));
-    int  nocc = compact(c, occFlag, (int)G.nc, occ, tag + ".occc");
-    int *rank = c.arena.get<int>(tag + ".rank", G.nc);
+    // occupied cells per phase, listed on the device (no host round trip); at most
+    // min(cells, points) of them
+    const long long maxOcc = std::max<long long>(1, std::min<long long>(G.nc, m));
+    int *ph    = c.arena.get<int>(tag + ".ph", 24);
+    int *rank  = c.arena.get<int>(tag + ".rank", G.nc);
+    int *lists = c.arena.get<int>(tag + ".phl", maxOcc);
+    SM_CUDA(cudaMemsetAsync(ph, 0, 24 * sizeof(int), c.stream));
     SM_CUDA(cudaMemsetAsync(rank, 0xff, G.nc * sizeof(int), c.stream));
-    int *phaseCnt = c.arena.get<int>(tag + ".phc", 16);
-    SM_CUDA(cudaMemsetAsync(phaseCnt, 0, 16 * sizeof(int), c.stream));
-    int *phaseOf = c.arena.get<int>(tag + ".pho", std::max(nocc, 1));
-    k_occ_rank<<<nblocks(nocc, 256), 256, 0, c.stream>>>(occ, nocc, rank, G.dim[0], G.dim[1],
-                                                         phaseCnt, phaseOf);
+    const int gc = (int)std::min<long long>(nblocks(G.nc, 256), 152LL * 16);
+    k_phase_count<<<gc, 256, 0, c.stream>>>(G.start, G.nc, G.dim[0], G.dim[1], ph);
     SM_LAUNCH_CHECK();
-    SM_CUDA(cudaMemcpyAsync(c.hostCounts, phaseCnt, 8 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-    c.sync();
-    int off[9];
-    off[0] = 0;
-    for (int p = 0; p < 8; p++)
-        off[p + 1] = off[p] + c.hostCounts[p];
-    int *phaseFill = phaseCnt + 8;
-    SM_CUDA(cudaMemcpyAsync(phaseFill, off, 8 * sizeof(int), cudaMemcpyHostToDevice, c.stream));
-    int *lists = c.arena.get<int>(tag + ".phl", std::max(nocc, 1));
-    k_phase_scatter<<<nblocks(nocc, 256), 256, 0, c.stream>>>(occ, phaseOf, nocc, phaseFill, lists);
+    k_phase_offsets<<<1, 32, 0, c.stream>>>(ph);
+    SM_LAUNCH_CHECK();
+    k_phase_list<<<gc, 256, 0, c.stream>>>(G.start, G.nc, G.dim[0], G.dim[1], ph, lists, rank);
     SM_LAUNCH_CHECK();
     // kept-list capacity: points at pairwise distance >= step inside a cube of side g fit
     // disjoint balls of radius step/2 inside the cube grown by step/2.
     const double s   = (double)g / (double)step;
     const int    cap = (int)std::floor((s + 1.0) * (s + 1.0) * (s + 1.0) / (3.14159265358979 / 6.0)) + 1;
-    int *keptCnt  = c.arena.get<int>(tag + ".kc", std::max(nocc, 1));
-    float4 *keptPos = c.arena.get<float4>(tag + ".kp", (size_t)std::max(nocc, 1) * cap);
+    int    *keptCnt  = c.arena.get<int>(tag + ".kc", maxOcc);
+    float4 *keptPos  = c.arena.get<float4>(tag + ".kp", (size_t)maxOcc * cap);
     int    *aliveTmp = c.arena.get<int>(tag + ".al", std::max(m, 1));
-    int *keptFlag = c.arena.get<int>(tag + ".kf", std::max(npoints, 1) + 1);
-    int *overflow = keptFlag + npoints;
-    SM_CUDA(cudaMemsetAsync(keptCnt, 0, std::max(nocc, 1) * sizeof(int), c.stream));
+    int    *keptFlag = c.arena.get<int>(tag + ".kf", std::max(npoints, 1) + 1);
+    int    *overflow = keptFlag + npoints;
+    SM_CUDA(cudaMemsetAsync(keptCnt, 0, maxOcc * sizeof(int), c.stream));
     SM_CUDA(cudaMemsetAsync(keptFlag, 0, (npoints + 1) * sizeof(int), c.stream));
     const float r2 = step * step;
+    const int   gp = (int)std::min<long long>((maxOcc + kSpWarps - 1) / kSpWarps, 152LL * 16);
     for (int p = 0; p < 8; p++) {
-        const int nc = off[p + 1] - off[p];
-        if (nc == 0)
-            continue;
-        k_sample_phase<<<nblocks(nc, kSpWarps), kSpWarps * 32, 0, c.stream>>>(
-            pos, G.view(), lists + off[p], nc, rank, keptCnt, keptPos, cap, r2, keptFlag, overflow,
-            aliveTmp);
+        k_sample_phase<<<gp, kSpWarps * 32, 0, c.stream>>>(pos, G.view(), lists, ph, p, rank,
+                                                           keptCnt, keptPos, cap, r2, keptFlag,
+                                                           overflow, aliveTmp);
         SM_LAUNCH_CHECK();
     }
-    const int kept = compact(c, keptFlag, npoints, outIds, tag + ".out");
-    SM_CUDA(cudaMemcpyAsync(c.hostCounts, overflow, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    // the kept points in index order, and the overflow flag, in one round trip
+    int *pre   = c.arena.get<int>(tag + ".out.pre", std::max(npoints, 1));
+    int *total = scan_flags_total(c, keptFlag, pre, npoints, tag + ".out");
+    k_scatter_flags<<<nblocks(npoints, 256), 256, 0, c.stream>>>(keptFlag, pre, npoints, kNoEq, outIds);
+    SM_LAUNCH_CHECK();
+    SM_CUDA(cudaMemcpyAsync(c.hostCounts, total, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    SM_CUDA(cudaMemcpyAsync(c.hostCounts + 1, overflow, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     c.sync();
-    if (c.hostCounts[0])
+    if (c.hostCounts[1])
         throw Error(SM_ERR_CAPACITY, "sampler: kept-point capacity per cell exceeded");
-    return kept;
+    return c.hostCounts[0];
 }
 
 void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *ids, int m,
@@ -877,45 +912,43 @@ void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *
     SM_CUDA(cudaMemsetAsync(need, 0, npoints * sizeof(int), c.stream));
     k_mark_todo<<<nblocks(m, 256), 256, 0, c.stream>>>(ids, m, nrm, need);
     SM_LAUNCH_CHECK();
-    int *todo  = c.arena.get<int>(tag + ".todo", m);
-    int  ntodo = compact_grid_order(c, query, need, 2, todo, tag + ".ct");
-    int *nbrT  = c.arena.get<int>(tag + ".nbrT", (size_t)std::max(ntodo, 1) * k);
-    int *cntT  = c.arena.get<int>(tag + ".cntT", std::max(ntodo, 1));
-    launch_knn(c.stream, todo, ntodo, query.view(), pos, k, nbrT, cntT, smooth ? 1 : 0, nrm, need);
-    int  nextra = 0;
-    int *extra = nullptr, *nbrE = nullptr, *cntE = nullptr;
-    if (smooth && ntodo > 0) {
-        extra  = c.arena.get<int>(tag + ".extra", npoints);
+    // the query lists and their counts stay on the device; launches are sized by bounds
+    int       *todo   = c.arena.get<int>(tag + ".todo", m);
+    const int *ntodo  = compact_grid_order(c, query, need, 2, todo, tag + ".ct");
+    int       *nbrT   = c.arena.get<int>(tag + ".nbrT", (size_t)m * k);
+    int       *cntT   = c.arena.get<int>(tag + ".cntT", m);
+    launch_knn(c.stream, todo, ntodo, m, query.view(), pos, k, nbrT, cntT, smooth ? 1 : 0, nrm, need);
+    const int  extraMax = smooth ? (int)std::min<long long>(npoints, (long long)m * k) : 0;
+    int       *extra = nullptr, *nbrE = nullptr, *cntE = nullptr;
+    const int *nextra = nullptr;
+    if (extraMax > 0) {
+        extra  = c.arena.get<int>(tag + ".extra", extraMax);
         nextra = compact_grid_order(c, query, need, 1, extra, tag + ".ce");
-        nbrE   = c.arena.get<int>(tag + ".nbrE", (size_t)std::max(nextra, 1) * k);
-        cntE   = c.arena.get<int>(tag + ".cntE", std::max(nextra, 1));
-        launch_knn(c.stream, extra, nextra, query.view(), pos, k, nbrE, cntE, 0, nrm, need);
+        nbrE   = c.arena.get<int>(tag + ".nbrE", (size_t)extraMax * k);
+        cntE   = c.arena.get<int>(tag + ".cntE", extraMax);
+        launch_knn(c.stream, extra, nextra, extraMax, query.view(), pos, k, nbrE, cntE, 0, nrm, need);
     }
-    const int nmax = std::max(ntodo, nextra);
-    float4   *cen  = c.arena.get<float4>(tag + ".cen", 2 * (size_t)std::max(nmax, 1));
-    float4   *nn   = c.arena.get<float4>(tag + ".nn", 2 * (size_t)std::max(nmax, 1));
-    if (ntodo > 0) {
-        k_pca<<<nblocks(ntodo, 128), 128, 0, c.stream>>>(todo, ntodo, nbrT, cntT, k, pos, cen, nn);
+    const int nmax = std::max(m, extraMax);
+    float4   *cen  = c.arena.get<float4>(tag + ".cen", 2 * (size_t)nmax);
+    float4   *nn   = c.arena.get<float4>(tag + ".nn", 2 * (size_t)nmax);
+    k_pca<<<nblocks(m, 128), 128, 0, c.stream>>>(todo, ntodo, nbrT, cntT, k, pos, cen, nn);
+    SM_LAUNCH_CHECK();
+    if (extraMax > 0) {
+        k_pca<<<nblocks(extraMax, 128), 128, 0, c.stream>>>(extra, nextra, nbrE, cntE, k, pos,
+                                                             cen + nmax, nn + nmax);
         SM_LAUNCH_CHECK();
     }
-    if (nextra > 0) {
-        k_pca<<<nblocks(nextra, 128), 128, 0, c.stream>>>(extra, nextra, nbrE, cntE, k, pos,
-                                                           cen + nmax, nn + nmax);
+    k_pca_write<<<nblocks(m, 256), 256, 0, c.stream>>>(todo, ntodo, cen, nn, pos, nrm);
+    SM_LAUNCH_CHECK();
+    if (extraMax > 0) {
+        k_pca_write<<<nblocks(extraMax, 256), 256, 0, c.stream>>>(extra, nextra, cen + nmax,
+                                                                   nn + nmax, pos, nrm);
         SM_LAUNCH_CHECK();
     }
-    if (ntodo > 0) {
-        k_pca_write<<<nblocks(ntodo, 256), 256, 0, c.stream>>>(todo, ntodo, cen, nn, pos, nrm);
+    if (smooth) {
+        k_smooth<<<nblocks(m, 256), 256, 0, c.stream>>>(todo, ntodo, nbrT, cntT, k, nrm, cen);
         SM_LAUNCH_CHECK();
-    }
-    if (nextra > 0) {
-        k_pca_write<<<nblocks(nextra, 256), 256, 0, c.stream>>>(extra, nextra, cen + nmax, nn + nmax,
-                                                                 pos, nrm);
-        SM_LAUNCH_CHECK();
-    }
-    if (smooth && ntodo > 0) {
-        k_smooth<<<nblocks(ntodo, 256), 256, 0, c.stream>>>(todo, ntodo, nbrT, cntT, k, nrm, cen);
-        SM_LAUNCH_CHECK();
-        k_smooth_write<<<nblocks(ntodo, 256), 256, 0, c.stream>>>(todo, ntodo, cen, nrm);
+        k_smooth_write<<<nblocks(m, 256), 256, 0, c.stream>>>(todo, ntodo, cen, nrm);
         SM_LAUNCH_CHECK();
     }
     const bool hasVp = vp && std::isfinite(vp[0]) && std::isfinite(vp[1]) && std::isfinite(vp[2]);

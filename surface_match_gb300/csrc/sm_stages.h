@@ -39,6 +39,8 @@ int scan_excl(Ctx &c, const int *in, int *out, long long n, const std::string &t
               bool wantTotal = true);
 // Ascending indices i with flags[i] != 0; returns the count (synchronises).
 int compact(Ctx &c, const int *flags, int n, int *outIds, const std::string &tag);
+// The same when the count is known already (no host round trip).
+void compact_known(Ctx &c, const int *flags, int n, int *outIds, const std::string &tag);
 // Grid over points ids[0..m) with cell side g over `box`; sortCells orders each cell's
 // ids ascending (needed by the sampler).
 void build_grid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &box, float g,
