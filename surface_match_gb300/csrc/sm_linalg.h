@@ -97,37 +97,84 @@ template <int N> SML_HD void jacobi_eig(double A[N][N], double V[N][N], double d
         d[i] = A[i][i];
 }
 
-// Normal of a 3x3 covariance: the unit eigenvector of the eigenvalue of least magnitude
-// (first such in ascending-eigenvalue order, as util.cpp:264-267 picks it).
+// Normal of a 3x3 covariance: the unit eigenvector of its smallest eigenvalue, in closed
+// form (the reference solves this 3x3 problem directly too, util.cpp:262-267
+// SelfAdjointEigenSolver::computeDirect). The smallest root of the characteristic cubic
+// p(l) = l^3 - c2 l^2 + c1 l - c0 is found by Newton's method from a Gershgorin lower bound:
+// p is negative, increasing and concave left of its smallest root, so the iterates rise
+// monotonically to it; iteration stops when they no longer increase. The eigenvector is the
+// longest cross product of two rows of A - l I. Where the smallest eigenvalue is repeated
+// (rows of A - l I parallel or zero) a unit vector orthogonal to the longest row is taken,
+// and e_x for A = qI. FP64 throughout, basic operations only, so GPU and CPU agree bit for bit.
 SML_HD void normal_from_cov(const double C[6] /*xx xy xz yy yz zz*/, float out[3]) {
-    double A[3][3] = {{C[0], C[1], C[2]}, {C[1], C[3], C[4]}, {C[2], C[4], C[5]}};
-    double V[3][3], d[3];
-    jacobi_eig<3>(A, V, d);
-    int order[3] = {0, 1, 2};
-    for (int i = 0; i < 3; i++) // ascending eigenvalues, stable
-        for (int j = 0; j < 2 - i; j++)
-            if (d[order[j]] > d[order[j + 1]]) {
-                int t        = order[j];
-                order[j]     = order[j + 1];
-                order[j + 1] = t;
-            }
-    int    best = order[0];
-    double bv   = dabs(d[order[0]]);
-    for (int k = 1; k < 3; k++)
-        if (dabs(d[order[k]]) < bv) {
-            bv   = dabs(d[order[k]]);
-            best = order[k];
-        }
-    double x = V[0][best], y = V[1][best], z = V[2][best];
-    double n = dsqrt(x * x + y * y + z * z);
-    if (n > 0.0) {
-        x /= n;
-        y /= n;
-        z /= n;
+    const double a00 = C[0], a01 = C[1], a02 = C[2], a11 = C[3], a12 = C[4], a22 = C[5];
+    const double c2 = a00 + a11 + a22;
+    const double c1 = (a00 * a11 - a01 * a01) + (a00 * a22 - a02 * a02) + (a11 * a22 - a12 * a12);
+    const double c0 = a00 * (a11 * a22 - a12 * a12) - a01 * (a01 * a22 - a12 * a02) +
+                      a02 * (a01 * a12 - a11 * a02);
+    // Gershgorin lower bound of the spectrum (and not above 0: covariances are PSD)
+    double l = a00 - (dabs(a01) + dabs(a02));
+    const double g1 = a11 - (dabs(a01) + dabs(a12)), g2 = a22 - (dabs(a02) + dabs(a12));
+    l = g1 < l ? g1 : l;
+    l = g2 < l ? g2 : l;
+    l = l < 0.0 ? l : 0.0;
+    for (int it = 0; it < 100; it++) {
+        const double pv = ((l - c2) * l + c1) * l - c0;
+        const double dv = (3.0 * l - 2.0 * c2) * l + c1;
+        if (!(dv > 0.0) || !(pv < 0.0))
+            break;
+        const double nl = l - pv / dv;
+        if (!(nl > l))
+            break;
+        l = nl;
     }
-    out[0] = (float)x;
-    out[1] = (float)y;
-    out[2] = (float)z;
+    // rows of M = A - l I and their cross products
+    const double r0[3] = {a00 - l, a01, a02}, r1[3] = {a01, a11 - l, a12}, r2[3] = {a02, a12, a22 - l};
+    const double x01[3] = {r0[1] * r1[2] - r0[2] * r1[1], r0[2] * r1[0] - r0[0] * r1[2],
+                           r0[0] * r1[1] - r0[1] * r1[0]};
+    const double x02[3] = {r0[1] * r2[2] - r0[2] * r2[1], r0[2] * r2[0] - r0[0] * r2[2],
+                           r0[0] * r2[1] - r0[1] * r2[0]};
+    const double x12[3] = {r1[1] * r2[2] - r1[2] * r2[1], r1[2] * r2[0] - r1[0] * r2[2],
+                           r1[0] * r2[1] - r1[1] * r2[0]};
+    const double n01 = x01[0] * x01[0] + x01[1] * x01[1] + x01[2] * x01[2];
+    const double n02 = x02[0] * x02[0] + x02[1] * x02[1] + x02[2] * x02[2];
+    const double n12 = x12[0] * x12[0] + x12[1] * x12[1] + x12[2] * x12[2];
+    const double m0  = r0[0] * r0[0] + r0[1] * r0[1] + r0[2] * r0[2];
+    const double m1  = r1[0] * r1[0] + r1[1] * r1[1] + r1[2] * r1[2];
+    const double m2  = r2[0] * r2[0] + r2[1] * r2[1] + r2[2] * r2[2];
+    const double mmax = m0 > m1 ? (m0 > m2 ? m0 : m2) : (m1 > m2 ? m1 : m2);
+    double v[3], nv;
+    if (n01 >= n02 && n01 >= n12) {
+        v[0] = x01[0], v[1] = x01[1], v[2] = x01[2], nv = n01;
+    } else if (n02 >= n12) {
+        v[0] = x02[0], v[1] = x02[1], v[2] = x02[2], nv = n02;
+    } else {
+        v[0] = x12[0], v[1] = x12[1], v[2] = x12[2], nv = n12;
+    }
+    if (!(nv > mmax * mmax * 1e-20)) {
+        // repeated smallest eigenvalue: any unit vector orthogonal to the longest row
+        const double *r = m0 >= m1 && m0 >= m2 ? r0 : (m1 >= m2 ? r1 : r2);
+        if (!(mmax > 0.0)) {
+            out[0] = 1.0f;
+            out[1] = 0.0f;
+            out[2] = 0.0f;
+            return;
+        }
+        // cross with the axis least aligned with r
+        const double ax = dabs(r[0]), ay = dabs(r[1]), az = dabs(r[2]);
+        if (ax <= ay && ax <= az) { // r x e_x
+            v[0] = 0.0, v[1] = r[2], v[2] = -r[1];
+        } else if (ay <= az) { // r x e_y
+            v[0] = -r[2], v[1] = 0.0, v[2] = r[0];
+        } else { // r x e_z
+            v[0] = r[1], v[1] = -r[0], v[2] = 0.0;
+        }
+        nv = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    }
+    const double inv = 1.0 / dsqrt(nv);
+    out[0]           = (float)(v[0] * inv);
+    out[1]           = (float)(v[1] * inv);
+    out[2]           = (float)(v[2] * inv);
 }
 
 // Markley quaternion average (util.cpp:553-577): eigenvector of the largest eigenvalue of
