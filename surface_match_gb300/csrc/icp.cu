@@ -3,16 +3,18 @@
 // step (icp.cpp:39-121) and inliner (util.cpp:628-641).
 //
 // All candidates are refined at once and each candidate's source points are spread over
-// ceil(n / 256) CTAs, so the whole GPU works even for a handful of candidates. One ICP
-// iteration is seven launches: correspondences (grid nearest neighbour, per scene point
-// the closest model point wins a 64-bit atomicMin of (distance bits, model index), which
-// is the reference's "first minimum in model order" without its O(n*m) grouping scan),
-// pair selection, centroids, normal-equation terms, their reduction + FP64 solve,
-// residual distances, their reduction + the convergence logic. Every reduction has the
-// same fixed layout: 256 slots (slot = source index mod 256), each a Kahan sum over its
-// source points in ascending order, merged by a fixed binary tree - the layout the CPU
-// oracle emulates, so poses are bit-identical. The selection walk over the candidates
-// (numMatches) runs on the host afterwards and only reads the per-candidate results.
+// several CTAs, so the whole GPU works even for a handful of candidates. One ICP iteration
+// is six launches: correspondences (one warp per source point on the grid cell walker; per
+// scene point the closest source point wins a 64-bit atomicMin of (distance bits, source
+// index), which is the reference's "first minimum in model order" without its O(n*m)
+// grouping scan), pair selection, pair count + centroids, normal-equation terms with their
+// reduction and the FP64 solve, residual distances, and their reduction + the convergence
+// logic. Every reduction has the same fixed layout: kIcpSlots slots (slot = source index mod
+// kIcpSlots, kIcpBlocks CTAs of 256 per candidate), each a Kahan sum over its source points
+// in ascending order, merged by a fixed tree (warp, CTA, then the last CTA over the CTA
+// partials) - the layout the CPU oracle emulates, so poses are bit-identical. The selection
+// walk over the candidates (numMatches) runs on the host afterwards and only reads the
+// per-candidate results.
 #include <cfloat>
 
 #include "sm_icp.h"
