@@ -73,7 +73,7 @@ __device__ __forceinline__ bool cand_live(const Cand &c, const Stage &s) {
 }
 
 // K1: correspondences, one warp per source point (warp-cooperative grid search)
-__global__ void __launch_bounds__(kT) k_corr(Work w, Stage s) {
+__global__ void __launch_bounds__(kT, 4) k_corr(Work w, Stage s) {
     const int   ci = blockIdx.y;
     const Cand &C  = w.cand[ci];
     if (!cand_live(C, s))
@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(kT) k_solve(Work w, Stage s) {
 }
 
 // K6: residual distance of each pair after the step, one warp per pair
-__global__ void __launch_bounds__(kT) k_resid(Work w, Stage s) {
+__global__ void __launch_bounds__(kT, 4) k_resid(Work w, Stage s) {
     const int   ci = blockIdx.y;
     const Cand &C  = w.cand[ci];
     if (!cand_live(C, s) || C.cnt < 6)
@@ -408,7 +408,7 @@ __global__ void k_stage_end(Work w, int ncand, int failStatus) {
 
 // Inliers of each candidate: source points with a scene point closer than the scoring
 // distance, one warp per point (warp_any_within).
-__global__ void __launch_bounds__(kT) k_inliers(Work w, const float4 *__restrict__ src, int n,
+__global__ void __launch_bounds__(kT, 4) k_inliers(Work w, const float4 *__restrict__ src, int n,
                                                 HGridView F, float r2) {
     __shared__ int sc[kW];
     const int      ci = blockIdx.y;
@@ -473,7 +473,7 @@ __global__ void k_rank(const int *__restrict__ ids, int m, int *__restrict__ ran
 void run_stage(Ctx &c, Work &w, const Stage &s, int ncand) {
     const dim3 g2(s.nb, ncand);
     const dim3 gr(smi::kIcpBlocks, ncand);                    // reductions
-    const dim3 gw(std::max(1, nblocks(s.n, kW * 4)), ncand); // warp kernels: 4 points per warp
+    const dim3 gw(std::max(1, nblocks(s.n, kW)), ncand); // warp kernels: a warp per point
     k_stage_begin<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand);
     SM_LAUNCH_CHECK();
     for (int it = 0; it < s.iters; it++) {
@@ -525,7 +525,7 @@ void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, con
         run_stage(c, w, s, ncand);
         k_stage_end<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, 2);
         SM_LAUNCH_CHECK();
-        k_inliers<<<dim3(std::max(1, nblocks(m.ns, kW * 4)), ncand), kT, 0, c.stream>>>(
+        k_inliers<<<dim3(std::max(1, nblocks(m.ns, kW)), ncand), kT, 0, c.stream>>>(
             w, m.sp, m.ns, sc.full.view(), sc2);
         SM_LAUNCH_CHECK();
         k_score<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, m.ns, p.minScore, 3, 0);
@@ -536,7 +536,7 @@ void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, con
             run_stage(c, w, d, ncand);
             k_stage_end<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, 4);
             SM_LAUNCH_CHECK();
-            k_inliers<<<dim3(std::max(1, nblocks(m.nr, kW * 4)), ncand), kT, 0, c.stream>>>(
+            k_inliers<<<dim3(std::max(1, nblocks(m.nr, kW)), ncand), kT, 0, c.stream>>>(
                 w, m.rp, m.nr, sc.full.view(), sc2);
             SM_LAUNCH_CHECK();
             k_score<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, m.nr, p.minScore, 5, 1);

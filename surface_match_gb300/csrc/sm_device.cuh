@@ -43,13 +43,12 @@ struct HGridView {
     const int    *ids;
     const float4 *pts;
     const uint32_t *occ; // one bit per cell of the dim box (nullptr: not built)
-    __device__ __forceinline__ void range(int x, int y, int z, int &s, int &e) const {
-        const unsigned long long key =
-            ((unsigned long long)z * (unsigned)dim[1] + (unsigned)y) * (unsigned)dim[0] + (unsigned)x;
-        if (occ && !((occ[key >> 5] >> (key & 31)) & 1u)) {
-            s = e = 0; // empty cell: no table probe
-            return;
-        }
+    __device__ __forceinline__ unsigned long long key_of(int x, int y, int z) const {
+        return ((unsigned long long)z * (unsigned)dim[1] + (unsigned)y) * (unsigned)dim[0] +
+               (unsigned)x;
+    }
+    // the table entry of an occupied cell (s = e = 0 when the cell holds no point)
+    __device__ __forceinline__ void lookup(unsigned long long key, int &s, int &e) const {
         uint32_t h = (uint32_t)smm::mix64(key) & mask;
         for (uint32_t p = 0; p <= mask; p++) {
             const uint4 v = slot[h];
@@ -63,6 +62,14 @@ struct HGridView {
             h = (h + 1) & mask;
         }
         s = e = 0;
+    }
+    __device__ __forceinline__ void range(int x, int y, int z, int &s, int &e) const {
+        const unsigned long long key = key_of(x, y, z);
+        if (occ && !((occ[key >> 5] >> (key & 31)) & 1u)) {
+            s = e = 0; // empty cell: no table probe
+            return;
+        }
+        lookup(key, s, e);
     }
 };
 
@@ -134,14 +141,42 @@ __device__ __forceinline__ unsigned long long warp_merge_low(unsigned long long 
     return m;
 }
 
+// The points of the cells the lanes hold (lane: cell points [b, e) of g.pts), flattened
+// over the warp by a prefix sum: visit(p, valid) is called by all lanes for each round of 32
+// points (p = position with the point index in w; valid false on idle lanes) and returns a
+// warp-uniform "done" that ends the rounds early.
+template <class G, class V>
+__device__ __forceinline__ bool warp_visit_cells(const G &g, int b, int e, V &&visit) {
+    const int lane = threadIdx.x & 31;
+    const int cnt  = e - b;
+    const int incl = warp_incl_scan(cnt);
+    const int excl = incl - cnt;
+    const int T    = __shfl_sync(0xffffffffu, incl, 31);
+    for (int base = 0; base < T; base += 32) {
+        const int r   = base + lane;
+        int       own = 0; // the lane whose cell holds point r: last lane with excl <= r
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const int mid = own + step;
+            if (__shfl_sync(0xffffffffu, excl, mid) <= r)
+                own = mid;
+        }
+        const int    bj    = __shfl_sync(0xffffffffu, b, own);
+        const int    ej    = __shfl_sync(0xffffffffu, excl, own);
+        const bool   valid = r < T;
+        const float4 p     = valid ? g.pts[bj + (r - ej)] : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (visit(p, valid))
+            return true;
+    }
+    return false;
+}
+
 // Warp-cooperative walk over the points around q, shell by shell (shells 0 and 1 together:
 // the 3x3x3 block; no search can stop after shell 0, whose ring bound is 0). The lanes probe
-// 32 cells at a time (occupancy bit, table), a prefix sum flattens the probed cells' points,
-// and visit(p, valid) is called by all lanes for each round of 32 points (p = position with
-// the point index in w; valid false on idle lanes). After each shell, stop(s) - evaluated by
-// all lanes, warp-uniform - ends the walk. Every point of shells 1..s is visited exactly once
-// before stop(s), so a search written on it sees the same points as one that walks the
-// cells one by one.
+// 32 cells at a time (occupancy bit, table) and warp_visit_cells visits their points. After
+// each shell, stop(s) - evaluated by all lanes, warp-uniform - ends the walk. Every point of
+// shells 1..s is visited exactly once before stop(s), so a search written on it sees the
+// same points as one that walks the cells one by one.
 template <class G, class V, class S>
 __device__ __forceinline__ void warp_walk(const G &g, float qx, float qy, float qz, V &&visit,
                                           S &&stop) {
@@ -162,29 +197,134 @@ __device__ __forceinline__ void warp_walk(const G &g, float qx, float qy, float 
                     z < g.dim[2])
                     g.range(x, y, z, b, e);
             }
-            const int cnt  = e - b;
-            const int incl = warp_incl_scan(cnt);
-            const int excl = incl - cnt;
-            const int T    = __shfl_sync(0xffffffffu, incl, 31);
-            for (int base = 0; base < T; base += 32) {
-                const int r   = base + lane;
-                int       own = 0; // the lane whose cell holds point r: last lane with excl <= r
-#pragma unroll
-                for (int step = 16; step >= 1; step >>= 1) {
-                    const int mid = own + step;
-                    if (__shfl_sync(0xffffffffu, excl, mid) <= r)
-                        own = mid;
-                }
-                const int bj = __shfl_sync(0xffffffffu, b, own);
-                const int ej = __shfl_sync(0xffffffffu, excl, own);
-                const bool   valid = r < T;
-                const float4 p     = valid ? g.pts[bj + (r - ej)] : make_float4(0.f, 0.f, 0.f, 0.f);
+            warp_visit_cells(g, b, e, [&](const float4 &p, bool valid) {
                 visit(p, valid);
-            }
+                return false;
+            });
         }
         if (stop(s))
             return;
     }
+}
+
+// Lower bound of the squared distance from q to any point filed under cell (x, y, z): the
+// distance to the cell's box grown by the 1% cell margin that covers the rounding of cell
+// coordinates (as in ring_bound).
+__device__ __forceinline__ float cell_lb2(const HGridView &g, float qx, float qy, float qz, int x,
+                                          int y, int z) {
+    const float q[3] = {qx, qy, qz};
+    const int   k[3] = {x, y, z};
+    float       s    = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float lo  = g.org[a] + ((float)k[a] - 0.01f) * g.g;
+        const float hi  = g.org[a] + ((float)k[a] + 1.01f) * g.g;
+        const float gap = fmaxf(0.0f, fmaxf(lo - q[a], q[a] - hi));
+        s += gap * gap;
+    }
+    return s;
+}
+
+// Shells 0 and 1 (the 3x3x3 block around c) in one round of cell probes, cells whose lower
+// bound exceeds b2 skipped. Returns visit's "done".
+template <class V>
+__device__ __forceinline__ bool warp_block27(const HGridView &g, float qx, float qy, float qz,
+                                             const int c[3], float b2, V &&visit) {
+    const int lane = threadIdx.x & 31;
+    int       b = 0, e = 0;
+    if (lane < 27) {
+        const int x = c[0] + lane % 3 - 1, y = c[1] + (lane / 3) % 3 - 1, z = c[2] + lane / 9 - 1;
+        if (x >= 0 && y >= 0 && z >= 0 && x < g.dim[0] && y < g.dim[1] && z < g.dim[2] &&
+            cell_lb2(g, qx, qy, qz, x, y, z) <= b2)
+            g.range(x, y, z, b, e);
+    }
+    return warp_visit_cells(g, b, e, visit);
+}
+
+// The cells of Chebyshev rings lo..hi around c whose lower bound does not exceed bound()
+// (warp-uniform, re-read every 256 cells), visited through warp_visit_cells. The ring cube is
+// screened 256 cells at a time - each lane computes 8 cells' bounds and issues their 8
+// occupancy-bit loads together - and only the occupied survivors, compacted over the warp,
+// are looked up in the table: a deep search costs a few rounds of independent loads instead
+// of one dependent probe round per 32 cells. Returns visit's "done".
+template <class B, class V>
+__device__ __forceinline__ bool warp_band(const HGridView &g, float qx, float qy, float qz,
+                                          const int c[3], int lo, int hi, B &&bound, V &&visit) {
+    const int lane = threadIdx.x & 31;
+    const int w = 2 * hi + 1, w2 = w * w, N = w2 * w;
+    for (int base = 0; base < N; base += 256) {
+        const float b2 = bound();
+        // candidates of this lane (bit j: cell base + 32 j + lane), then their occupancy
+        // bits, 8 loads in flight (the bitmap exists only for grids of <= 2^28 cells, so
+        // its keys fit 32 bits)
+        uint32_t m = 0, key[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int t = base + j * 32 + lane;
+            key[j]      = 0u;
+            if (t < N) {
+                const int tz = t / w2, ty = (t - tz * w2) / w, tx = t - tz * w2 - ty * w;
+                const int dx = tx - hi, dy = ty - hi, dz = tz - hi;
+                const int r  = max(abs(dx), max(abs(dy), abs(dz)));
+                const int x = c[0] + dx, y = c[1] + dy, z = c[2] + dz;
+                if (r >= lo && x >= 0 && y >= 0 && z >= 0 && x < g.dim[0] && y < g.dim[1] &&
+                    z < g.dim[2] && cell_lb2(g, qx, qy, qz, x, y, z) <= b2) {
+                    m |= 1u << j;
+                    key[j] = (uint32_t)g.key_of(x, y, z);
+                }
+            }
+        }
+        if (g.occ) {
+            uint32_t word[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+                word[j] = (m >> j) & 1u ? __ldg(&g.occ[key[j] >> 5]) : 0u;
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+                m &= ~((((word[j] >> (key[j] & 31u)) & 1u) ^ 1u) << j);
+        }
+        const int cnt  = __popc(m);
+        const int incl = warp_incl_scan(cnt);
+        const int excl = incl - cnt;
+        const int T    = __shfl_sync(0xffffffffu, incl, 31);
+        for (int r0 = 0; r0 < T; r0 += 32) {
+            const int r   = r0 + lane;
+            int       own = 0; // the lane holding occupied cell r: last lane with excl <= r
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+                const int mid = own + step;
+                if (__shfl_sync(0xffffffffu, excl, mid) <= r)
+                    own = mid;
+            }
+            uint32_t  om = __shfl_sync(0xffffffffu, m, own);
+            const int oe = __shfl_sync(0xffffffffu, excl, own);
+            int       b = 0, e = 0;
+            if (r < T) {
+                for (int k = r - oe; k > 0; k--)
+                    om &= om - 1u;
+                const int j  = __ffs(om) - 1;
+                const int t  = base + j * 32 + own;
+                const int tz = t / w2, ty = (t - tz * w2) / w, tx = t - tz * w2 - ty * w;
+                g.lookup(g.key_of(c[0] + tx - hi, c[1] + ty - hi, c[2] + tz - hi), b, e);
+            }
+            if (warp_visit_cells(g, b, e, visit))
+                return true;
+        }
+    }
+    return false;
+}
+
+// The last ring of the next band after ring `done`: the first ring whose bound passes b2
+// (rings beyond it cannot hold a point within b2), at most 3 rings on and never past ms.
+__device__ __forceinline__ int band_end(int done, int ms, float b2, float g) {
+    int hi = done + 1;
+    while (hi < ms && hi < done + 3) {
+        const float rb = smg::ring_bound(hi, g);
+        if (rb * rb > b2)
+            break;
+        hi++;
+    }
+    return hi;
 }
 
 // Exact k nearest neighbours (k <= 32) of q by (squared distance, index), one warp per
@@ -225,29 +365,41 @@ __device__ __forceinline__ int warp_knn_sorted(const G &g, float qx, float qy, f
     return n;
 }
 
-// Nearest point by (squared distance, index) on warp_walk, searched until the nearest is
-// below the ring bound or the ring bound passes limit2; -1 when none was found. All lanes
+// Nearest point by (squared distance, index), one warp per query: the 3x3x3 block first,
+// then bands of rings (warp_band) with cells screened against min(best, limit2), until the
+// nearest is below the ring bound or the ring bound passes limit2. A point farther than
+// limit2 may be returned (callers test the distance); -1 when none was found. All lanes
 // return the result.
-template <class G>
-__device__ __forceinline__ int warp_nn_walk(const G &g, float qx, float qy, float qz,
+__device__ __forceinline__ int warp_nn_walk(const HGridView &g, float qx, float qy, float qz,
                                             float limit2, float &outd) {
-    unsigned long long best = ~0ull;
-    warp_walk(
-        g, qx, qy, qz,
-        [&](const float4 &p, bool valid) {
-            if (valid) {
-                const float dd = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
-                const unsigned long long key =
-                    ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)__float_as_int(p.w);
-                best = key < best ? key : best;
-            }
-        },
-        [&](int s) {
-            best          = warp_min_u64(best);
-            const float b = smg::ring_bound(s, g.g);
-            return (best != ~0ull && __uint_as_float((unsigned)(best >> 32)) < b * b) ||
-                   b * b > limit2;
-        });
+    unsigned long long best  = ~0ull;
+    auto               visit = [&](const float4 &p, bool valid) {
+        if (valid) {
+            const float dd = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
+            const unsigned long long key =
+                ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)__float_as_int(p.w);
+            best = key < best ? key : best;
+        }
+        return false;
+    };
+    const float kInf = __int_as_float(0x7f800000);
+    auto        bd   = [&]() {
+        best = warp_min_u64(best);
+        return best == ~0ull ? kInf : __uint_as_float((unsigned)(best >> 32));
+    };
+    int c[3];
+    grid_cc(g, qx, qy, qz, c);
+    const int ms = max(grid_max_shell(g, c), 1);
+    warp_block27(g, qx, qy, qz, c, kInf, visit);
+    for (int done = 1;;) {
+        const float d  = bd();
+        const float rb = smg::ring_bound(done, g.g);
+        if (d < rb * rb || rb * rb > limit2 || done >= ms)
+            break;
+        const int hi = band_end(done, ms, fminf(d, limit2), g.g);
+        warp_band(g, qx, qy, qz, c, done + 1, hi, [&]() { return fminf(bd(), limit2); }, visit);
+        done = hi;
+    }
     best = warp_min_u64(best);
     if (best == ~0ull) {
         outd = 3.402823466e+38f;
@@ -257,21 +409,29 @@ __device__ __forceinline__ int warp_nn_walk(const G &g, float qx, float qy, floa
     return (int)(unsigned)(best & 0xffffffffu);
 }
 
-// Whether any point lies closer than sqrt(r2) to q, by a warp: stops at a hit or after the
-// shell whose ring bound reaches sqrt(r2).
-template <class G>
-__device__ __forceinline__ bool warp_any_within(const G &g, float qx, float qy, float qz, float r2) {
-    bool hit = false;
-    warp_walk(
-        g, qx, qy, qz,
-        [&](const float4 &p, bool valid) {
-            const bool h = valid && smm::dist2(qx, qy, qz, p.x, p.y, p.z) < r2;
-            hit          = hit || __any_sync(0xffffffffu, h);
-        },
-        [&](int s) {
-            const float b = smg::ring_bound(s, g.g);
-            return hit || b * b >= r2;
-        });
+// Whether any point lies closer than sqrt(r2) to q, by a warp: cells whose lower bound
+// reaches r2 are skipped, and the search ends at the first round with a hit or after the
+// ring whose bound reaches sqrt(r2).
+__device__ __forceinline__ bool warp_any_within(const HGridView &g, float qx, float qy, float qz,
+                                                float r2) {
+    bool hit   = false;
+    auto visit = [&](const float4 &p, bool valid) {
+        const bool h = valid && smm::dist2(qx, qy, qz, p.x, p.y, p.z) < r2;
+        hit          = hit || __any_sync(0xffffffffu, h);
+        return hit;
+    };
+    int c[3];
+    grid_cc(g, qx, qy, qz, c);
+    const int ms = max(grid_max_shell(g, c), 1);
+    warp_block27(g, qx, qy, qz, c, r2, visit);
+    for (int done = 1;;) {
+        const float rb = smg::ring_bound(done, g.g);
+        if (hit || rb * rb >= r2 || done >= ms)
+            break;
+        const int hi = band_end(done, ms, r2, g.g);
+        warp_band(g, qx, qy, qz, c, done + 1, hi, [&]() { return r2; }, visit);
+        done = hi;
+    }
     return hit;
 }
 
