@@ -306,7 +306,7 @@ void train(Ctx &c, Model &m, const float *xyzIn, const float *nrmIn, int64_t n64
     }
     std::vector<float> hsp = download4(sp, n1), hsn = download4(sn, n1);
     std::vector<float> hrp = download4(rp, n2), hrn = download4(rn, n2);
-    c.sync();
+    c.sync_checked();
     // group by key, stable in pair order
     std::vector<uint32_t> order;
     order.reserve(npair);
@@ -482,7 +482,7 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
         SM_CUDA(cudaMemcpyAsync(hp.data(), cpose, (size_t)ncand * 48, cudaMemcpyDeviceToHost, c.stream));
     }
     record(c, 7);
-    c.sync();
+    c.sync_checked();
     // selection walk (ppf.cpp:439-495) and ordering by score (ppf.cpp:498-507)
     std::vector<int> acc;
     for (int i = 0; i < ncand; i++) {
@@ -1013,7 +1013,7 @@ SM_API int sm_vote_stage(sm_model m, const float *points, const float *normals, 
         if (vo.acc)
             SM_CUDA(cudaMemcpyAsync(outAcc, vo.acc, (size_t)dk * m->m.ns * m->m.tp.featAngleResolution * 4,
                                     cudaMemcpyDeviceToHost, c.stream));
-        c.sync();
+        c.sync_checked();
     });
 }
 

@@ -16,8 +16,8 @@ using namespace smd;
 
 namespace {
 
-constexpr int kScanBs   = 1024;
-constexpr int kScanIpt  = 4;
+constexpr int kScanBs   = 512;
+constexpr int kScanIpt  = 8;
 constexpr int kScanTile = kScanBs * kScanIpt;
 constexpr int kNoEq     = INT_MIN; // scan raw values instead of (value == eq)
 
@@ -125,51 +125,101 @@ __device__ __forceinline__ int scan_val(const int *in, long long i, long long n,
     return eq == kNoEq ? v : (v == eq ? 1 : 0);
 }
 
-__global__ void k_scan_reduce(const int *__restrict__ in, long long n, int eq, int *part) {
-    __shared__ int sh[33];
-    const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanIpt;
-    int             s    = 0;
-#pragma unroll
-    for (int k = 0; k < kScanIpt; k++)
-        s += scan_val(in, base + k, n, eq);
-    int tot;
-    block_excl_scan(s, sh, &tot);
-    if (threadIdx.x == 0)
-        part[blockIdx.x] = tot;
+// Single-pass exclusive scan with decoupled look-back (Merrill & Garland, "Single-pass
+// Parallel Prefix Scan with Decoupled Look-back", 2016). Tiles of kScanTile values take a
+// ticket in launch order; a tile publishes its aggregate, then warp 0 walks back over the
+// tiles before it, 32 at a time, summing aggregates until it meets a tile whose inclusive
+// prefix is published, and publishes its own inclusive prefix. A tile waits only on tiles
+// that took earlier tickets (already running or done), so every wait ends; each is bounded
+// all the same and sets *err when its limit passes. Status words: epoch (30 bits, new per
+// scan, so the array needs no reset) | flag (2 bits: 1 aggregate, 2 inclusive) | value.
+constexpr unsigned long long kLbAgg = 1ull << 32, kLbIncl = 2ull << 32;
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-__global__ void k_scan_parts(int *part, int nparts, int *total) {
+__global__ void __launch_bounds__(kScanBs)
+    k_scan_lookback(const int *__restrict__ in, int *__restrict__ out, long long n, int eq,
+                    unsigned long long *__restrict__ status, int *__restrict__ ticket,
+                    int nparts, unsigned epoch, int *__restrict__ total) {
     __shared__ int sh[33];
-    int            carry = 0;
-    for (int b = 0; b < nparts; b += blockDim.x) {
-        const int i = b + threadIdx.x;
-        const int v = i < nparts ? part[i] : 0;
-        int       tot;
-        const int ex = block_excl_scan(v, sh, &tot);
-        if (i < nparts)
-            part[i] = carry + ex;
-        carry += tot;
+    __shared__ int sTile, sExcl;
+    if (threadIdx.x == 0) {
+        const int t = atomicAdd(ticket, 1);
+        if (t == nparts - 1)
+            ticket[0] = 0; // every ticket of this launch is taken: ready for the next scan
+        sTile = t;
     }
-    if (threadIdx.x == 0 && total)
-        *total = carry;
-}
-
-__global__ void k_scan_apply(const int *__restrict__ in, int *__restrict__ out, long long n, int eq,
-                             const int *__restrict__ part) {
-    __shared__ int  sh[33];
-    const long long base = (long long)blockIdx.x * kScanTile + (long long)threadIdx.x * kScanIpt;
+    __syncthreads();
+    const int       tile = sTile;
+    const long long base = (long long)tile * kScanTile + (long long)threadIdx.x * kScanIpt;
     int             v[kScanIpt], s = 0;
 #pragma unroll
     for (int k = 0; k < kScanIpt; k++) {
         v[k] = scan_val(in, base + k, n, eq);
         s += v[k];
     }
-    int ex = block_excl_scan(s, sh, nullptr) + part[blockIdx.x];
+    int       agg;
+    const int ex  = block_excl_scan(s, sh, &agg);
+    const unsigned long long tag = (unsigned long long)epoch << 34;
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        int       excl = 0;
+        if (tile == 0) {
+            if (lane == 0)
+                st_relaxed_u64(&status[0], tag | kLbIncl | (unsigned)agg);
+        } else {
+            if (lane == 0)
+                st_relaxed_u64(&status[tile], tag | kLbAgg | (unsigned)agg);
+            for (int top = tile - 1;; top -= 32) {
+                const int          p = top - lane; // lane 0: the nearest predecessor
+                unsigned long long w = tag | kLbIncl; // lanes before tile 0: inclusive 0
+                for (int it = 0;; it++) {
+                    if (p >= 0)
+                        w = ld_relaxed_u64(&status[p]);
+                    const bool ready = (w >> 34) == epoch && ((w >> 32) & 3ull) != 0;
+                    if (__all_sync(0xffffffffu, ready))
+                        break;
+                    if (it > (1 << 22)) {
+                        if (lane == 0)
+                            atomicExch(ticket + 1, 1);
+                        w = tag | kLbIncl;
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+                const bool     isIncl = ((w >> 32) & 3ull) == 2ull;
+                const unsigned incl   = __ballot_sync(0xffffffffu, isIncl);
+                int            val    = (int)(unsigned)(w & 0xffffffffull);
+                if (incl) {
+                    const int first = __ffs(incl) - 1;
+                    excl += __reduce_add_sync(0xffffffffu, lane <= first ? val : 0);
+                    break;
+                }
+                excl += __reduce_add_sync(0xffffffffu, val);
+            }
+            if (lane == 0)
+                st_relaxed_u64(&status[tile], tag | kLbIncl | (unsigned)(excl + agg));
+        }
+        if (lane == 0) {
+            sExcl = excl;
+            if (tile == nparts - 1 && total)
+                *total = excl + agg;
+        }
+    }
+    __syncthreads();
+    int o = ex + sExcl;
 #pragma unroll
     for (int k = 0; k < kScanIpt; k++) {
         if (base + k < n)
-            out[base + k] = ex;
-        ex += v[k];
+            out[base + k] = o;
+        o += v[k];
     }
 }
 
@@ -184,62 +234,27 @@ __global__ void k_scatter_flags(const int *__restrict__ flags, const int *__rest
 }
 
 // ---------------------------------------------------------------------------------------
+// Dense sampler grid, counting pass: the point's cell and its slot within the cell; the
+// point that opens a cell also counts the cell in its phase (ph[0..7]).
 __global__ void k_grid_count(const float4 *__restrict__ pos, const int *__restrict__ ids, int m,
-                             GridParams gp, int *__restrict__ cellOf, int *__restrict__ cnt) {
+                             GridParams gp, int *__restrict__ cellOf, int *__restrict__ sub,
+                             int *__restrict__ cnt, int *__restrict__ ph) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m)
         return;
-    const float4 p = pos[ids[i]];
+    const float4 p  = pos[ids[i]];
     const int    cx = smg::coord(p.x, gp.org[0], gp.g, gp.dim[0]);
     const int    cy = smg::coord(p.y, gp.org[1], gp.g, gp.dim[1]);
     const int    cz = smg::coord(p.z, gp.org[2], gp.g, gp.dim[2]);
     const int    c  = (cz * gp.dim[1] + cy) * gp.dim[0] + cx;
     cellOf[i]       = c;
-    atomicAdd(&cnt[c], 1);
-}
-
-__global__ void k_grid_scatter(const int *__restrict__ ids, const int *__restrict__ cellOf, int m,
-                               int *__restrict__ fill, int *__restrict__ gids) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m)
-        return;
-    const int slot = atomicAdd(&fill[cellOf[i]], 1);
-    gids[slot]     = ids[i];
-}
-
-// Sort the ids of each cell ascending (cells are small; insertion sort per thread).
-__global__ void k_cell_sort(const int *__restrict__ start, long long nc, int *__restrict__ gids) {
-    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nc)
-        return;
-    const int s = start[c], e = start[c + 1];
-    for (int i = s + 1; i < e; i++) {
-        const int v = gids[i];
-        int       j = i - 1;
-        while (j >= s && gids[j] > v) {
-            gids[j + 1] = gids[j];
-            j--;
-        }
-        gids[j + 1] = v;
-    }
-}
-
-// ---------------------------------------------------------------------------------------
-// Occupied cells per phase, counted (pass 1) and listed (pass 2) on the device: `ph` holds
-// 8 counts, then 8 list offsets, then 8 fill pointers. rank[cell] = the cell's list slot
-// (index of its kept-point record); cells within a phase in any order (they do not
-// interact).
-__global__ void k_phase_count(const int *__restrict__ start, long long nc, int dim0, int dim1,
-                              int *__restrict__ ph) {
-    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
-         c += (long long)gridDim.x * blockDim.x) {
-        if (start[c + 1] <= start[c])
-            continue;
-        const int cx = (int)(c % dim0), cy = (int)((c / dim0) % dim1), cz = (int)(c / ((long long)dim0 * dim1));
+    const int k     = atomicAdd(&cnt[c], 1);
+    sub[i]          = k;
+    if (k == 0)
         atomicAdd(&ph[smg::phase_of(cx, cy, cz)], 1);
-    }
 }
 
+// ph[8..15] = list offsets of the phases, ph[16..23] = their fill pointers.
 __global__ void k_phase_offsets(int *__restrict__ ph) {
     if (threadIdx.x != 0)
         return;
@@ -251,23 +266,34 @@ __global__ void k_phase_offsets(int *__restrict__ ph) {
     }
 }
 
-__global__ void k_phase_list(const int *__restrict__ start, long long nc, int dim0, int dim1,
-                             int *__restrict__ ph, int *__restrict__ lists, int *__restrict__ rank) {
-    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
-         c += (long long)gridDim.x * blockDim.x) {
-        if (start[c + 1] <= start[c])
-            continue;
-        const int cx = (int)(c % dim0), cy = (int)((c / dim0) % dim1), cz = (int)(c / ((long long)dim0 * dim1));
+// Placing pass: the point's position (index in w) at its cell slot; the point in slot 0
+// lists the cell in its phase (any order: cells of one phase do not interact) and records
+// rank[cell] = its list slot, the index of the cell's kept-point record.
+__global__ void k_grid_scatter(const float4 *__restrict__ pos, const int *__restrict__ ids, int m,
+                               const int *__restrict__ cellOf, const int *__restrict__ sub,
+                               const int *__restrict__ start, int dim0, int dim1,
+                               float4 *__restrict__ pts, int *__restrict__ ph,
+                               int *__restrict__ lists, int *__restrict__ rank) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m)
+        return;
+    const int    id = ids[i];
+    const int    c  = cellOf[i];
+    const float4 p  = pos[id];
+    const int    k  = sub[i];
+    pts[start[c] + k] = make_float4(p.x, p.y, p.z, __int_as_float(id));
+    if (k == 0) {
+        const int cx = c % dim0, cy = (c / dim0) % dim1, cz = c / (dim0 * dim1);
         const int slot = atomicAdd(&ph[16 + smg::phase_of(cx, cy, cz)], 1);
-        lists[slot]    = (int)c;
+        lists[slot]    = c;
         rank[c]        = slot;
     }
 }
 
 // ---------------------------------------------------------------------------------------
 constexpr int kSpWarps = 4;   // warps (cells) per CTA of the phase kernel
-constexpr int kSpIds   = 384; // cell sizes held in shared memory
-constexpr int kSpStage = 384; // neighbours' kept points staged in shared memory
+constexpr int kSpIds   = 192; // cell points held in shared memory
+constexpr int kSpStage = 256; // neighbours' kept points staged in shared memory
 
 // One warp per occupied cell of the current phase. The sequential greedy visits the cell's
 // points by ascending index and keeps a point unless a kept point lies within the step;
@@ -276,17 +302,16 @@ constexpr int kSpStage = 384; // neighbours' kept points staged in shared memory
 // smallest surviving index, drop the survivors within the step of it" - the same kept set
 // as the sequential visit, at (kept points x cell size / 32) work and without sorting.
 // Kept points are recorded as positions (keptPos, `cap` per cell). The neighbours' kept
-// points and the cell's points are staged in shared memory; cells too large for the
-// staging buffers take the same steps in global memory (`alive` flags in aliveTmp).
+// points and the cell's points (positions with the index in w, contiguous per cell) are
+// staged in shared memory; cells too large for the staging buffers take the same steps in
+// global memory (`alive` flags in aliveTmp).
 __global__ void __launch_bounds__(kSpWarps * 32)
-    k_sample_phase(const float4 *__restrict__ pos, GridView G, const int *__restrict__ lists,
-                   const int *__restrict__ ph, int phase, const int *__restrict__ rank,
-                   int *__restrict__ keptCnt, float4 *__restrict__ keptPos, int cap, float r2,
-                   int *__restrict__ keptFlag, int *__restrict__ overflow,
-                   int *__restrict__ aliveTmp) {
+    k_sample_phase(GridView G, const int *__restrict__ lists, const int *__restrict__ ph,
+                   int phase, const int *__restrict__ rank, int *__restrict__ keptCnt,
+                   float4 *__restrict__ keptPos, int cap, float r2, int *__restrict__ keptFlag,
+                   int *__restrict__ overflow, int *__restrict__ aliveTmp) {
     __shared__ float4 stage[kSpWarps][kSpStage];
     __shared__ float4 cpos[kSpWarps][kSpIds];
-    __shared__ int    cid[kSpWarps][kSpIds];
     __shared__ int    calive[kSpWarps][kSpIds];
     __shared__ int    snr[kSpWarps][26], scnt[kSpWarps][26];
     const int  wl     = threadIdx.x >> 5;
@@ -335,11 +360,11 @@ __global__ void __launch_bounds__(kSpWarps * 32)
                     st[t] = keptPos[(size_t)nj * cap + (t - ej)];
             }
         }
-        int *alive = stageC ? calive[wl] : aliveTmp + s;
+        int          *alive = stageC ? calive[wl] : aliveTmp + s;
+        const float4 *cp    = stageC ? cpos[wl] : G.pts + s;
         // survivors of the neighbours' kept points
         for (int i = lane; i < n; i += 32) {
-            const int    id = G.ids[s + i];
-            const float4 q  = pos[id];
+            const float4 q  = G.pts[s + i];
             bool         ok = true;
             if (stageNb) {
                 for (int k = 0; k < NK && ok; k++) {
@@ -358,21 +383,25 @@ __global__ void __launch_bounds__(kSpWarps * 32)
                 }
             }
             alive[i] = ok ? 1 : 0;
-            if (stageC) {
-                cid[wl][i]  = id;
+            if (stageC)
                 cpos[wl][i] = q;
-            }
         }
         __syncwarp();
-        // keep the smallest surviving index, drop the survivors within the step, repeat
+        // keep the smallest surviving index, drop the survivors within the step, repeat; the
+        // lane that holds the kept point hands its position to the warp
         float4 *mine = keptPos + (size_t)rk * cap;
         int     nk   = 0;
         for (;;) {
-            int myMin = INT_MAX;
+            int    myMin = INT_MAX;
+            float4 myP   = make_float4(0.f, 0.f, 0.f, 0.f);
             for (int i = lane; i < n; i += 32)
                 if (alive[i]) {
-                    const int id = stageC ? cid[wl][i] : G.ids[s + i];
-                    myMin        = min(myMin, id);
+                    const float4 q  = cp[i];
+                    const int    id = __float_as_int(q.w);
+                    if (id < myMin) {
+                        myMin = id;
+                        myP   = q;
+                    }
                 }
             int m = myMin;
     #pragma unroll
@@ -380,8 +409,10 @@ __global__ void __launch_bounds__(kSpWarps * 32)
                 m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
             if (m == INT_MAX)
                 break;
-            const float4 kp4 = pos[m];
-            const float4 kp  = make_float4(kp4.x, kp4.y, kp4.z, 0.0f);
+            const int    src = __ffs(__ballot_sync(0xffffffffu, myMin == m)) - 1;
+            const float4 kp  = make_float4(__shfl_sync(0xffffffffu, myP.x, src),
+                                           __shfl_sync(0xffffffffu, myP.y, src),
+                                           __shfl_sync(0xffffffffu, myP.z, src), 0.0f);
             if (lane == 0) {
                 keptFlag[m] = 1;
                 if (nk < cap)
@@ -393,9 +424,8 @@ __global__ void __launch_bounds__(kSpWarps * 32)
             for (int i = lane; i < n; i += 32) {
                 if (!alive[i])
                     continue;
-                const int    id = stageC ? cid[wl][i] : G.ids[s + i];
-                const float4 q  = stageC ? cpos[wl][i] : pos[id];
-                if (id == m || smm::dist2(kp.x, kp.y, kp.z, q.x, q.y, q.z) < r2)
+                const float4 q = cp[i];
+                if (__float_as_int(q.w) == m || smm::dist2(kp.x, kp.y, kp.z, q.x, q.y, q.z) < r2)
                     alive[i] = 0;
             }
             __syncwarp();
@@ -685,34 +715,54 @@ int prep_points(Ctx &c, const float *xyz, const float *nin, int n, float4 *pos, 
     return c.hostCounts[6];
 }
 
+// The context's look-back state, grown to at least nparts tiles (zeroed when allocated);
+// returns the next scan epoch.
+static unsigned scan_state(Ctx &c, int nparts) {
+    Ctx::ScanState &S = c.scan;
+    if (nparts > S.cap || S.epoch >= (1u << 30) - 1) {
+        const int cap = std::max(nparts, std::max(S.cap, 1024));
+        S.status      = c.arena.get<unsigned long long>("scan.status", cap);
+        S.ticket      = c.arena.get<int>("scan.ticket", 2);
+        SM_CUDA(cudaMemsetAsync(S.status, 0, (size_t)cap * 8, c.stream));
+        SM_CUDA(cudaMemsetAsync(S.ticket, 0, 2 * sizeof(int), c.stream));
+        S.cap   = cap;
+        S.epoch = 0;
+    }
+    return ++S.epoch;
+}
+
+// Exclusive scan of n values (or of value == eq flags) into out; the total goes to *total
+// (device) when given.
+static void scan_into(Ctx &c, const int *in, int *out, long long n, int eq, int *total) {
+    const int nparts = (int)((n + kScanTile - 1) / kScanTile);
+    if (nparts == 0) {
+        if (total)
+            SM_CUDA(cudaMemsetAsync(total, 0, sizeof(int), c.stream));
+        return;
+    }
+    const unsigned epoch = scan_state(c, nparts);
+    k_scan_lookback<<<nparts, kScanBs, 0, c.stream>>>(in, out, n, eq, c.scan.status, c.scan.ticket,
+                                                      nparts, epoch, total);
+    SM_LAUNCH_CHECK();
+}
+
 static int scan_impl(Ctx &c, const int *in, int *out, long long n, int eq, const std::string &tag,
                      bool wantTotal) {
-    const int nparts = (int)((n + kScanTile - 1) / kScanTile);
-    int      *part   = c.arena.get<int>(tag + ".scanpart", nparts + 1);
-    int      *total  = part + nparts;
-    if (nparts > 0) {
-        k_scan_reduce<<<nparts, kScanBs, 0, c.stream>>>(in, n, eq, part);
-        SM_LAUNCH_CHECK();
-    }
-    k_scan_parts<<<1, 1024, 0, c.stream>>>(part, nparts, total);
-    SM_LAUNCH_CHECK();
-    if (nparts > 0) {
-        k_scan_apply<<<nparts, kScanBs, 0, c.stream>>>(in, out, n, eq, part);
-        SM_LAUNCH_CHECK();
-    }
+    int *total = c.arena.get<int>(tag + ".scantot", 1);
+    scan_into(c, in, out, n, eq, total);
     if (!wantTotal)
         return -1;
     SM_CUDA(cudaMemcpyAsync(c.hostCounts, total, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-    c.sync();
+    c.sync_checked();
     return c.hostCounts[0];
 }
 
 // Exclusive scan of 0/1 flags without a host round trip; returns the device address of the
 // total.
 static int *scan_flags_total(Ctx &c, const int *flags, int *pre, int n, const std::string &tag) {
-    scan_impl(c, flags, pre, n, kNoEq, tag, false);
-    const int nparts = (int)((n + kScanTile - 1) / kScanTile);
-    return c.arena.get<int>(tag + ".scanpart", nparts + 1) + nparts;
+    int *total = c.arena.get<int>(tag + ".scantot", 1);
+    scan_into(c, flags, pre, n, kNoEq, total);
+    return total;
 }
 
 int scan_excl(Ctx &c, const int *in, int *out, long long n, const std::string &tag, bool wantTotal) {
@@ -759,39 +809,6 @@ static int *compact_grid_order(Ctx &c, const HGrid &H, const int *need, int eq, 
     k_scatter_ids<<<nblocks(H.m, 256), 256, 0, c.stream>>>(flags, pre, H.m, H.ids, out);
     SM_LAUNCH_CHECK();
     return total;
-}
-
-void build_grid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &box, float g,
-                bool sortCells, Grid &G, const std::string &tag) {
-    float ext[3] = {box.ext(0), box.ext(1), box.ext(2)};
-    G.g          = g;
-    for (int a = 0; a < 3; a++) {
-        G.org[a] = box.mn[a];
-        G.dim[a] = smg::dim_of(ext[a], g);
-    }
-    G.nc  = (long long)G.dim[0] * G.dim[1] * G.dim[2];
-    G.m   = m;
-    int *cnt    = c.arena.get<int>(tag + ".cnt", G.nc + 1);
-    G.start     = c.arena.get<int>(tag + ".start", G.nc + 1);
-    G.ids       = c.arena.get<int>(tag + ".ids", std::max(m, 1));
-    int *cellOf = c.arena.get<int>(tag + ".cellOf", std::max(m, 1));
-    SM_CUDA(cudaMemsetAsync(cnt, 0, (G.nc + 1) * sizeof(int), c.stream));
-    GridParams gp = grid_params(box, g, G.dim);
-    if (m > 0) {
-        k_grid_count<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, m, gp, cellOf, cnt);
-        SM_LAUNCH_CHECK();
-    }
-    scan_excl(c, cnt, G.start, G.nc + 1, tag, false);
-    int *fill = cnt; // reuse: fill pointers start at the cell starts
-    SM_CUDA(cudaMemcpyAsync(fill, G.start, G.nc * sizeof(int), cudaMemcpyDeviceToDevice, c.stream));
-    if (m > 0) {
-        k_grid_scatter<<<nblocks(m, 256), 256, 0, c.stream>>>(ids, cellOf, m, fill, G.ids);
-        SM_LAUNCH_CHECK();
-        if (sortCells) {
-            k_cell_sort<<<nblocks(G.nc, 256), 256, 0, c.stream>>>(G.start, G.nc, G.ids);
-            SM_LAUNCH_CHECK();
-        }
-    }
 }
 
 void build_hgrid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &box, float g,
@@ -850,22 +867,37 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
         return 0;
     float ext[3] = {box.ext(0), box.ext(1), box.ext(2)};
     const float g = smg::sample_cell(step, ext);
-    Grid        G;
-    build_grid(c, pos, ids, m, box, g, false, G, tag + ".g");
-    // occupied cells per phase, listed on the device (no host round trip); at most
-    // min(cells, points) of them
+    // dense grid over the points, its occupied cells listed per phase on the device (no host
+    // round trip; at most min(cells, points) of them)
+    Grid G;
+    G.g = g;
+    for (int a = 0; a < 3; a++) {
+        G.org[a] = box.mn[a];
+        G.dim[a] = smg::dim_of(ext[a], g);
+    }
+    G.nc                   = (long long)G.dim[0] * G.dim[1] * G.dim[2];
+    G.m                    = m;
     const long long maxOcc = std::max<long long>(1, std::min<long long>(G.nc, m));
-    int *ph    = c.arena.get<int>(tag + ".ph", 24);
-    int *rank  = c.arena.get<int>(tag + ".rank", G.nc);
-    int *lists = c.arena.get<int>(tag + ".phl", maxOcc);
+    int *cnt    = c.arena.get<int>(tag + ".g.cnt", G.nc + 1);
+    G.start     = c.arena.get<int>(tag + ".g.start", G.nc + 1);
+    G.pts       = c.arena.get<float4>(tag + ".g.pts", std::max(m, 1));
+    int *cellOf = c.arena.get<int>(tag + ".g.cellOf", std::max(m, 1));
+    int *sub    = c.arena.get<int>(tag + ".g.sub", std::max(m, 1));
+    int *ph     = c.arena.get<int>(tag + ".ph", 24);
+    int *rank   = c.arena.get<int>(tag + ".rank", G.nc);
+    int *lists  = c.arena.get<int>(tag + ".phl", maxOcc);
+    SM_CUDA(cudaMemsetAsync(cnt, 0, (G.nc + 1) * sizeof(int), c.stream));
     SM_CUDA(cudaMemsetAsync(ph, 0, 24 * sizeof(int), c.stream));
     SM_CUDA(cudaMemsetAsync(rank, 0xff, G.nc * sizeof(int), c.stream));
-    const int gc = (int)std::min<long long>(nblocks(G.nc, 256), 152LL * 16);
-    k_phase_count<<<gc, 256, 0, c.stream>>>(G.start, G.nc, G.dim[0], G.dim[1], ph);
+    const GridParams gpar = grid_params(box, g, G.dim);
+    k_grid_count<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, m, gpar, cellOf, sub, cnt, ph);
     SM_LAUNCH_CHECK();
+    scan_excl(c, cnt, G.start, G.nc + 1, tag + ".g", false);
     k_phase_offsets<<<1, 32, 0, c.stream>>>(ph);
     SM_LAUNCH_CHECK();
-    k_phase_list<<<gc, 256, 0, c.stream>>>(G.start, G.nc, G.dim[0], G.dim[1], ph, lists, rank);
+    k_grid_scatter<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, m, cellOf, sub, G.start,
+                                                          G.dim[0], G.dim[1], G.pts, ph, lists,
+                                                          rank);
     SM_LAUNCH_CHECK();
     // kept-list capacity: points at pairwise distance >= step inside a cube of side g fit
     // disjoint balls of radius step/2 inside the cube grown by step/2.
@@ -881,9 +913,9 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
     const float r2 = step * step;
     const int   gp = (int)std::min<long long>((maxOcc + kSpWarps - 1) / kSpWarps, 152LL * 16);
     for (int p = 0; p < 8; p++) {
-        k_sample_phase<<<gp, kSpWarps * 32, 0, c.stream>>>(pos, G.view(), lists, ph, p, rank,
-                                                           keptCnt, keptPos, cap, r2, keptFlag,
-                                                           overflow, aliveTmp);
+        k_sample_phase<<<gp, kSpWarps * 32, 0, c.stream>>>(G.view(), lists, ph, p, rank, keptCnt,
+                                                           keptPos, cap, r2, keptFlag, overflow,
+                                                           aliveTmp);
         SM_LAUNCH_CHECK();
     }
     // the kept points in index order, and the overflow flag, in one round trip

@@ -13,19 +13,14 @@ namespace smd {
 constexpr int kMaxKnn = 32; // largest supported knnNormal
 
 // Device view of a dense uniform grid over a subset of points: cells are stored cell-major
-// as a CSR (start[cell] .. start[cell+1] into ids). Used where per-cell state is needed
-// (the sampler).
+// as a CSR (start[cell] .. start[cell+1] into pts, the positions in cell order with the
+// point index in w). Used where per-cell state is needed (the sampler).
 struct GridView {
-    float      org[3];
-    float      g;
-    int        dim[3];
-    const int *start;
-    const int *ids;
-    __device__ __forceinline__ void range(int x, int y, int z, int &s, int &e) const {
-        const int c = (z * dim[1] + y) * dim[0] + x;
-        s           = start[c];
-        e           = start[c + 1];
-    }
+    float         org[3];
+    float         g;
+    int           dim[3];
+    const int    *start;
+    const float4 *pts;
 };
 
 // Device view of a hashed uniform grid: only occupied cells are stored, in an

@@ -88,7 +88,7 @@ struct Grid {
     int       dim[3] = {1, 1, 1};
     long long nc     = 1;
     int      *start  = nullptr; // nc + 1
-    int      *ids    = nullptr; // m
+    float4   *pts    = nullptr; // m: positions in cell order, point index in w
     int       m      = 0;
     smd::GridView view() const {
         smd::GridView v;
@@ -98,7 +98,7 @@ struct Grid {
         }
         v.g     = g;
         v.start = start;
-        v.ids   = ids;
+        v.pts   = pts;
         return v;
     }
 };

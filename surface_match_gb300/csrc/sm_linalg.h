@@ -177,8 +177,37 @@ SML_HD void normal_from_cov(const double C[6] /*xx xy xz yy yz zz*/, float out[3
     out[2]           = (float)(v[2] * inv);
 }
 
-// Markley quaternion average (util.cpp:553-577): eigenvector of the largest eigenvalue of
-// (1/M) sum q q^T, returned as a unit quaternion (w,x,y,z).
+SML_HD double det3(double a, double b, double c, double d, double e, double f, double g, double h,
+                   double i) {
+    return a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
+}
+
+// Determinant of B without row r and column c (both in 0..3).
+SML_HD double minor4(const double B[4][4], int r, int c) {
+    int rr[3], cc[3], nr = 0, nc = 0;
+    for (int k = 0; k < 4; k++) {
+        if (k != r)
+            rr[nr++] = k;
+        if (k != c)
+            cc[nc++] = k;
+    }
+    return det3(B[rr[0]][cc[0]], B[rr[0]][cc[1]], B[rr[0]][cc[2]], B[rr[1]][cc[0]],
+                B[rr[1]][cc[1]], B[rr[1]][cc[2]], B[rr[2]][cc[0]], B[rr[2]][cc[1]],
+                B[rr[2]][cc[2]]);
+}
+
+// Average of M unit quaternions from the upper triangle S of sum q q^T: the unit
+// eigenvector of the largest eigenvalue of A = S / M (Markley, Cheng, Crassidis & Oshman,
+// "Averaging Quaternions", 2007; the reference takes it from EigenSolver<Matrix4f>,
+// util.cpp:563-576), in closed form. The largest root of the characteristic quartic
+// p(l) = det(l I - A) = l^4 - c3 l^3 + c2 l^2 - c1 l + c0 is found by Newton's method from
+// a Gershgorin upper bound: right of its largest root p is positive, increasing and convex,
+// so the iterates fall monotonically to it; iteration stops when they no longer decrease.
+// For a simple root, adj(A - l I) is a multiple of v v^T: its column with the largest
+// diagonal entry is the eigenvector. Where that entry vanishes against the matrix scale
+// (a repeated largest eigenvalue) the cyclic Jacobi decomposition decides. The sign is
+// fixed by w >= 0 (q and -q are the same rotation). FP64, basic operations only, so GPU
+// and CPU agree bit for bit.
 SML_HD void quat_average_from_sum(const double S[10] /*upper triangle of sum q q^T*/, int M,
                                   double q[4]) {
     double A[4][4];
@@ -189,18 +218,73 @@ SML_HD void quat_average_from_sum(const double S[10] /*upper triangle of sum q q
             A[j][i] = A[i][j];
             k++;
         }
-    double V[4][4], d[4];
-    jacobi_eig<4>(A, V, d);
-    int best = 0;
-    for (int i = 1; i < 4; i++)
-        if (d[i] > d[best])
-            best = i;
-    double n = 0.0;
+    const double c3 = ((A[0][0] + A[1][1]) + A[2][2]) + A[3][3];
+    double       c2 = 0.0, c1 = 0.0;
+    for (int i = 0; i < 3; i++)
+        for (int j = i + 1; j < 4; j++)
+            c2 += A[i][i] * A[j][j] - A[i][j] * A[i][j];
     for (int i = 0; i < 4; i++)
-        n += V[i][best] * V[i][best];
-    n = dsqrt(n);
+        c1 += minor4(A, i, i);
+    const double c0 = (A[0][0] * minor4(A, 0, 0) - A[0][1] * minor4(A, 0, 1)) +
+                      (A[0][2] * minor4(A, 0, 2) - A[0][3] * minor4(A, 0, 3));
+    double l = 0.0;
+    for (int i = 0; i < 4; i++) {
+        double r = A[i][i];
+        for (int j = 0; j < 4; j++)
+            if (j != i)
+                r += dabs(A[i][j]);
+        l = (i == 0 || r > l) ? r : l;
+    }
+    for (int it = 0; it < 100; it++) {
+        const double pv = (((l - c3) * l + c2) * l - c1) * l + c0;
+        const double dv = ((4.0 * l - 3.0 * c3) * l + 2.0 * c2) * l - c1;
+        if (!(dv > 0.0) || !(pv > 0.0))
+            break;
+        const double nl = l - pv / dv;
+        if (!(nl < l))
+            break;
+        l = nl;
+    }
+    double B[4][4];
     for (int i = 0; i < 4; i++)
-        q[i] = (n > 0.0) ? V[i][best] / n : (i == 0 ? 1.0 : 0.0);
+        for (int j = 0; j < 4; j++)
+            B[i][j] = i == j ? A[i][j] - l : A[i][j];
+    int    jc = 0;
+    double dj = 0.0;
+    for (int j = 0; j < 4; j++) {
+        const double d = dabs(minor4(B, j, j));
+        if (j == 0 || d > dj) {
+            dj = d;
+            jc = j;
+        }
+    }
+    double v[4], n = 0.0;
+    if (c3 > 0.0 && dj > 1e-9 * (c3 * c3 * c3)) {
+        for (int i = 0; i < 4; i++) {
+            const double m = minor4(B, i, jc);
+            v[i]           = ((i + jc) & 1) ? -m : m;
+            n += v[i] * v[i];
+        }
+    } else {
+        double V[4][4], d[4];
+        jacobi_eig<4>(A, V, d);
+        int best = 0;
+        for (int i = 1; i < 4; i++)
+            if (d[i] > d[best])
+                best = i;
+        for (int i = 0; i < 4; i++) {
+            v[i] = V[i][best];
+            n += v[i] * v[i];
+        }
+    }
+    if (!(n > 0.0)) {
+        q[0] = 1.0;
+        q[1] = q[2] = q[3] = 0.0;
+        return;
+    }
+    const double inv = (v[0] < 0.0 ? -1.0 : 1.0) / dsqrt(n);
+    for (int i = 0; i < 4; i++)
+        q[i] = v[i] * inv;
 }
 
 // Unit quaternion (w,x,y,z) -> row-major rotation matrix.

@@ -25,7 +25,23 @@ struct Ctx {
         int  n = 0, ns = 0, nk = 0, nr = 0, np = 0, nc = 0, ncand = 0;
         bool valid = false;
     } last;
+    // single-pass scan state (prep.cu): per-tile status words, {ticket, wait-expired flag}
+    struct ScanState {
+        unsigned long long *status = nullptr;
+        int                *ticket = nullptr;
+        int                 cap    = 0;
+        unsigned            epoch  = 0;
+    } scan;
     void sync() { SM_CUDA(cudaStreamSynchronize(stream)); }
+    // sync, then fail loudly if a bounded device wait of the scans expired
+    void sync_checked() {
+        if (scan.ticket)
+            SM_CUDA(cudaMemcpyAsync(hostCounts + 63, scan.ticket + 1, sizeof(int),
+                                    cudaMemcpyDeviceToHost, stream));
+        sync();
+        if (scan.ticket && hostCounts[63])
+            throw Error(SM_ERR_RUNTIME, "device scan: a bounded look-back wait expired");
+    }
 };
 
 // ---- prep.cu ------------------------------------------------------------------------
@@ -41,10 +57,6 @@ int scan_excl(Ctx &c, const int *in, int *out, long long n, const std::string &t
 int compact(Ctx &c, const int *flags, int n, int *outIds, const std::string &tag);
 // The same when the count is known already (no host round trip).
 void compact_known(Ctx &c, const int *flags, int n, int *outIds, const std::string &tag);
-// Grid over points ids[0..m) with cell side g over `box`; sortCells orders each cell's
-// ids ascending (needed by the sampler).
-void build_grid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &box, float g,
-                bool sortCells, Grid &G, const std::string &tag);
 // Hashed grid over points ids[0..m) with cell side g (fine cells at any scene extent).
 void build_hgrid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &box, float g,
                  HGrid &H, const std::string &tag);
