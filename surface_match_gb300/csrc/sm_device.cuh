@@ -170,16 +170,16 @@ __device__ __forceinline__ bool warp_visit_cells(const G &g, int b, int e, V &&v
 // the 3x3x3 block; no search can stop after shell 0, whose ring bound is 0). The lanes probe
 // 32 cells at a time (occupancy bit, table) and warp_visit_cells visits their points. After
 // each shell, stop(s) - evaluated by all lanes, warp-uniform - ends the walk. Every point of
-// shells 1..s is visited exactly once before stop(s), so a search written on it sees the
+// shells s0..s is visited exactly once before stop(s), so a search written on it sees the
 // same points as one that walks the cells one by one.
 template <class G, class V, class S>
 __device__ __forceinline__ void warp_walk(const G &g, float qx, float qy, float qz, V &&visit,
-                                          S &&stop) {
+                                          S &&stop, int s0 = 1) {
     const int lane = threadIdx.x & 31;
     int       c[3];
     grid_cc(g, qx, qy, qz, c);
     const int ms = max(grid_max_shell(g, c), 1);
-    for (int s = 1; s <= ms; s++) {
+    for (int s = s0; s <= ms; s++) {
         const int lo = s == 1 ? 0 : s, w = 2 * s + 1, cube = w * w * w;
         for (int t0 = 0; t0 < cube; t0 += 32) {
             const int t = t0 + lane;
@@ -354,6 +354,90 @@ __device__ __forceinline__ int warp_knn_sorted(const G &g, float qx, float qy, f
             const float              bnd = smg::ring_bound(s, g.g);
             return __uint_as_float((unsigned)(kth >> 32)) < bnd * bnd;
         });
+    const int n = min(seen, k);
+    *id         = (int)(unsigned)(best & 0xffffffffu);
+    *d          = __uint_as_float((unsigned)(best >> 32));
+    return n;
+}
+
+// Exact k nearest neighbours (k <= 32) of q by (squared distance, index), one warp per
+// query. Each round of 32 points is sorted across the lanes and merged into the running 32
+// best (lane j holds the j-th smallest key: distance bits, index); rounds with no point
+// below the current k-th best are skipped. The 3x3x3 block is visited in ascending cell
+// lower bound, and its rounds end once the next cell's bound exceeds the k-th distance
+// (no point there can enter the list, not even by the index tie-break). The search ends
+// after shell s once k points were seen and the k-th distance is below the ring bound of s
+// (every unvisited point is farther); further shells are walked one by one. Returns the
+// number found (<= k); lane j < that count gets the j-th neighbour's index in *id and
+// squared distance in *d.
+__device__ __forceinline__ int warp_knn_sorted(const HGridView &g, float qx, float qy, float qz,
+                                               int k, int *id, float *d) {
+    const int          lane = threadIdx.x & 31;
+    unsigned long long best = ~0ull; // lane j: j-th smallest so far
+    int                seen = 0;
+    auto               kth  = [&]() { return __shfl_sync(0xffffffffu, best, k - 1); };
+    auto visit = [&](const float4 &p, bool valid) {
+        seen += __popc(__ballot_sync(0xffffffffu, valid));
+        unsigned long long key = ~0ull;
+        if (valid) {
+            const float dd = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
+            key = ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)__float_as_int(p.w);
+        }
+        if (__any_sync(0xffffffffu, key < kth()))
+            best = warp_merge_low(best, warp_bitonic_sort(key));
+    };
+    int c[3];
+    grid_cc(g, qx, qy, qz, c);
+    const int ms = max(grid_max_shell(g, c), 1);
+    {
+        // the block's occupied cells, sorted by lower bound (ties by lane)
+        int   b = 0, e = 0;
+        float lb = __int_as_float(0x7f800000);
+        if (lane < 27) {
+            const int x = c[0] + lane % 3 - 1, y = c[1] + (lane / 3) % 3 - 1, z = c[2] + lane / 9 - 1;
+            if (x >= 0 && y >= 0 && z >= 0 && x < g.dim[0] && y < g.dim[1] && z < g.dim[2]) {
+                g.range(x, y, z, b, e);
+                if (e > b)
+                    lb = cell_lb2(g, qx, qy, qz, x, y, z);
+            }
+        }
+        const unsigned long long sk =
+            warp_bitonic_sort(((unsigned long long)__float_as_uint(lb) << 32) | (unsigned)lane);
+        const int src = (int)(sk & 31u);
+        b             = __shfl_sync(0xffffffffu, b, src);
+        e             = __shfl_sync(0xffffffffu, e, src);
+        lb            = __uint_as_float((unsigned)(sk >> 32));
+        const int cnt  = e - b;
+        const int incl = warp_incl_scan(cnt);
+        const int excl = incl - cnt;
+        const int T    = __shfl_sync(0xffffffffu, incl, 31);
+        for (int base = 0; base < T; base += 32) {
+            const int r   = base + lane;
+            int       own = 0; // the lane whose cell holds point r: last lane with excl <= r
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+                const int mid = own + step;
+                if (__shfl_sync(0xffffffffu, excl, mid) <= r)
+                    own = mid;
+            }
+            const float lbr = __shfl_sync(0xffffffffu, lb, __shfl_sync(0xffffffffu, own, 0));
+            if (seen >= k && lbr > __uint_as_float((unsigned)(kth() >> 32)))
+                break;
+            const int    bj    = __shfl_sync(0xffffffffu, b, own);
+            const int    ej    = __shfl_sync(0xffffffffu, excl, own);
+            const bool   valid = r < T;
+            const float4 p     = valid ? g.pts[bj + (r - ej)] : make_float4(0.f, 0.f, 0.f, 0.f);
+            visit(p, valid);
+        }
+    }
+    auto done = [&](int s) {
+        if (seen < k)
+            return false;
+        const float bnd = smg::ring_bound(s, g.g);
+        return __uint_as_float((unsigned)(kth() >> 32)) < bnd * bnd;
+    };
+    if (!done(1) && ms >= 2)
+        warp_walk(g, qx, qy, qz, visit, done, 2);
     const int n = min(seen, k);
     *id         = (int)(unsigned)(best & 0xffffffffu);
     *d          = __uint_as_float((unsigned)(best >> 32));
