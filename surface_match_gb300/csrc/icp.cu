@@ -74,16 +74,24 @@ __device__ __forceinline__ bool cand_live(const Cand &c, const Stage &s) {
 
 // K1: correspondences, one warp per source point (warp-cooperative grid search)
 __global__ void __launch_bounds__(kT, 4) k_corr(Work w, Stage s) {
-    const int   ci = blockIdx.y;
-    const Cand &C  = w.cand[ci];
+    const int ci   = blockIdx.y;
+    const int lane = threadIdx.x & 31;
+    int       i    = blockIdx.x * kW + (threadIdx.x >> 5);
+    // the first source point is read together with the candidate's state
+    float4 sp = i < s.n ? s.src[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 sn = i < s.n ? s.srcN[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const Cand &C = w.cand[ci];
     if (!cand_live(C, s))
         return;
-    const int lane = threadIdx.x & 31;
-    for (int i = blockIdx.x * kW + (threadIdx.x >> 5); i < s.n; i += gridDim.x * kW) {
+    for (; i < s.n; i += gridDim.x * kW) {
         const size_t o = (size_t)ci * w.maxSrc + i;
         float4       x, y;
-        smi::pose_apply(C.M, s.src[i].x, s.src[i].y, s.src[i].z, x.x, x.y, x.z);
-        smi::pose_rotate(C.M, s.srcN[i].x, s.srcN[i].y, s.srcN[i].z, y.x, y.y, y.z);
+        if (i != blockIdx.x * kW + (threadIdx.x >> 5)) {
+            sp = s.src[i];
+            sn = s.srcN[i];
+        }
+        smi::pose_apply(C.M, sp.x, sp.y, sp.z, x.x, x.y, x.z);
+        smi::pose_rotate(C.M, sn.x, sn.y, sn.z, y.x, y.y, y.z);
         float      d;
         const int  j  = warp_nn_walk(s.G, x.x, x.y, x.z, s.rej2, d);
         const bool ok = j >= 0 && d <= s.rej2;

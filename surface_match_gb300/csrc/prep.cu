@@ -523,7 +523,8 @@ __global__ void k_hg_scatter(const float4 *__restrict__ pos, const int *__restri
 
 __global__ void k_hg_pack_from_start(const unsigned long long *__restrict__ keys,
                                      const int *__restrict__ start, uint32_t T,
-                                     uint4 *__restrict__ slot, uint32_t *__restrict__ occ) {
+                                     uint4 *__restrict__ slot, uint32_t *__restrict__ occ,
+                                     int2 *__restrict__ dense) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= T)
         return;
@@ -532,6 +533,8 @@ __global__ void k_hg_pack_from_start(const unsigned long long *__restrict__ keys
     slot[t] = make_uint4((uint32_t)k, (uint32_t)(k >> 32), (uint32_t)start[t], cnt);
     if (occ && cnt)
         atomicOr(&occ[k >> 5], 1u << (k & 31));
+    if (dense && cnt)
+        dense[k] = make_int2(start[t], (int)cnt);
 }
 
 // Query lists in the query grid's cell order: a warp then searches 32 neighbouring queries
@@ -856,8 +859,15 @@ void build_hgrid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &bo
         H.occ              = c.arena.get<uint32_t>(tag + ".occ", words);
         SM_CUDA(cudaMemsetAsync(H.occ, 0, words * 4, c.stream));
     }
+    // a direct {first, count} table too when the cell box has at most 2^22 cells (32 MB)
+    H.dense = nullptr;
+    if (ncell <= (1ull << 22)) {
+        H.dense = c.arena.get<int2>(tag + ".dense", (size_t)ncell);
+        SM_CUDA(cudaMemsetAsync(H.dense, 0, (size_t)ncell * sizeof(int2), c.stream));
+    }
     // counts again for the packed table: start[t+1] - start[t]
-    k_hg_pack_from_start<<<nblocks(T, 256), 256, 0, c.stream>>>(keys, start, T, H.slot, H.occ);
+    k_hg_pack_from_start<<<nblocks(T, 256), 256, 0, c.stream>>>(keys, start, T, H.slot, H.occ,
+                                                                H.dense);
     SM_LAUNCH_CHECK();
 }
 

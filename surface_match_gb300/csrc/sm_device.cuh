@@ -29,6 +29,7 @@ struct GridView {
 // and the table stays small enough to live in L2. The points of a cell are contiguous in
 // `pts` (position, point index in w), so a search reads them without an indirection, and
 // an occupancy bitmap over the cell box lets searches skip empty cells without a probe.
+// Small cell boxes also get a direct table of {first, count} per cell, read in one load.
 struct HGridView {
     float         org[3];
     float         g;
@@ -37,7 +38,8 @@ struct HGridView {
     uint32_t      mask;
     const int    *ids;
     const float4 *pts;
-    const uint32_t *occ; // one bit per cell of the dim box (nullptr: not built)
+    const uint32_t *occ;   // one bit per cell of the dim box (nullptr: not built)
+    const int2     *dense; // {first, count} per cell of the dim box (nullptr: not built)
     __device__ __forceinline__ unsigned long long key_of(int x, int y, int z) const {
         return ((unsigned long long)z * (unsigned)dim[1] + (unsigned)y) * (unsigned)dim[0] +
                (unsigned)x;
@@ -60,6 +62,12 @@ struct HGridView {
     }
     __device__ __forceinline__ void range(int x, int y, int z, int &s, int &e) const {
         const unsigned long long key = key_of(x, y, z);
+        if (dense) {
+            const int2 v = __ldg(&dense[key]);
+            s            = v.x;
+            e            = v.x + v.y;
+            return;
+        }
         if (occ && !((occ[key >> 5] >> (key & 31)) & 1u)) {
             s = e = 0; // empty cell: no table probe
             return;
@@ -250,8 +258,8 @@ __device__ __forceinline__ bool warp_band(const HGridView &g, float qx, float qy
     for (int base = 0; base < N; base += 256) {
         const float b2 = bound();
         // candidates of this lane (bit j: cell base + 32 j + lane), then their occupancy
-        // bits, 8 loads in flight (the bitmap exists only for grids of <= 2^28 cells, so
-        // its keys fit 32 bits)
+        // (direct-table counts or bitmap bits), 8 loads in flight (both exist only for grids
+        // of <= 2^28 cells, so their keys fit 32 bits)
         uint32_t m = 0, key[8];
 #pragma unroll
         for (int j = 0; j < 8; j++) {
@@ -269,7 +277,15 @@ __device__ __forceinline__ bool warp_band(const HGridView &g, float qx, float qy
                 }
             }
         }
-        if (g.occ) {
+        if (g.dense) {
+            int cnt8[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+                cnt8[j] = (m >> j) & 1u ? __ldg(&g.dense[key[j]]).y : 0;
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+                m &= ~((cnt8[j] > 0 ? 0u : 1u) << j);
+        } else if (g.occ) {
             uint32_t word[8];
 #pragma unroll
             for (int j = 0; j < 8; j++)
@@ -300,7 +316,14 @@ __device__ __forceinline__ bool warp_band(const HGridView &g, float qx, float qy
                 const int j  = __ffs(om) - 1;
                 const int t  = base + j * 32 + own;
                 const int tz = t / w2, ty = (t - tz * w2) / w, tx = t - tz * w2 - ty * w;
-                g.lookup(g.key_of(c[0] + tx - hi, c[1] + ty - hi, c[2] + tz - hi), b, e);
+                const unsigned long long k = g.key_of(c[0] + tx - hi, c[1] + ty - hi, c[2] + tz - hi);
+                if (g.dense) {
+                    const int2 v = __ldg(&g.dense[k]);
+                    b            = v.x;
+                    e            = v.x + v.y;
+                } else {
+                    g.lookup(k, b, e);
+                }
             }
             if (warp_visit_cells(g, b, e, visit))
                 return true;

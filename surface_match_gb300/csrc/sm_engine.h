@@ -113,6 +113,7 @@ struct HGrid {
     int      *ids    = nullptr;
     float4   *pts    = nullptr; // positions in cell order, point index in w (bit pattern)
     uint32_t *occ    = nullptr; // occupancy bit per cell (nullptr when the cell box is too large)
+    int2     *dense  = nullptr; // {first, count} per cell (nullptr unless the cell box is small)
     int       m      = 0;
     smd::HGridView view() const {
         smd::HGridView v;
@@ -125,7 +126,8 @@ struct HGrid {
         v.mask = mask;
         v.ids  = ids;
         v.pts  = pts;
-        v.occ  = occ;
+        v.occ   = occ;
+        v.dense = dense;
         return v;
     }
 };
