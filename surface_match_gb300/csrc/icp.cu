@@ -4,12 +4,12 @@
 //
 // All candidates are refined at once and each candidate's source points are spread over
 // several CTAs, so the whole GPU works even for a handful of candidates. One ICP iteration
-// is six launches: correspondences (one warp per source point on the grid cell walker; per
+// is five launches: correspondences (one warp per source point on the grid cell walker; per
 // scene point the closest source point wins a 64-bit atomicMin of (distance bits, source
 // index), which is the reference's "first minimum in model order" without its O(n*m)
-// grouping scan), pair selection, pair count + centroids, normal-equation terms with their
-// reduction and the FP64 solve, residual distances, and their reduction + the convergence
-// logic. Every reduction has the same fixed layout: kIcpSlots slots (slot = source index mod
+// grouping scan), pair selection with the pair count and centroids, normal-equation terms
+// with their reduction and the FP64 solve, residual distances, and their reduction + the
+// convergence logic. Every reduction has the same fixed layout: kIcpSlots slots (slot = source index mod
 // kIcpSlots, kIcpBlocks CTAs of 256 per candidate), each a Kahan sum over its source points
 // in ascending order, merged by a fixed tree (warp, CTA, then the last CTA over the CTA
 // partials) - the layout the CPU oracle emulates, so poses are bit-identical. The selection
@@ -73,7 +73,7 @@ __device__ __forceinline__ bool cand_live(const Cand &c, const Stage &s) {
 }
 
 // K1: correspondences, one warp per source point (warp-cooperative grid search)
-__global__ void __launch_bounds__(kT, 4) k_corr(Work w, Stage s) {
+__global__ void __launch_bounds__(kT, 6) k_corr(Work w, Stage s) {
     const int ci   = blockIdx.y;
     const int lane = threadIdx.x & 31;
     int       i    = blockIdx.x * kW + (threadIdx.x >> 5);
@@ -107,23 +107,6 @@ __global__ void __launch_bounds__(kT, 4) k_corr(Work w, Stage s) {
                 atomicMin(&w.win[(size_t)ci * w.maxDst + r], win_key(d, i));
         }
     }
-}
-
-// K2: keep only the closest source point per scene point
-__global__ void __launch_bounds__(kT) k_pairs(Work w, Stage s) {
-    const int   ci = blockIdx.y;
-    const Cand &C  = w.cand[ci];
-    if (!cand_live(C, s))
-        return;
-    const int i = blockIdx.x * kT + threadIdx.x;
-    if (i >= s.n)
-        return;
-    const size_t o = (size_t)ci * w.maxSrc + i;
-    const int    r = w.nnR[o];
-    if (r < 0)
-        return;
-    if (w.win[(size_t)ci * w.maxDst + r] != win_key(w.x4[o].w, i))
-        w.nnId[o] = -1;
 }
 
 // Fixed-layout reduction of W quantities (sm_icp.h): block b of candidate ci holds slots
@@ -211,7 +194,7 @@ __device__ bool slot_reduce(const Work &w, const Stage &s, int ci, F &&term, smi
     return true;
 }
 
-// K3: pair count and centroids
+// K2: pair selection, pair count and centroids
 __global__ void __launch_bounds__(kT) k_centroids(Work w, Stage s) {
     __shared__ float red[kW][6][2];
     __shared__ int   icnt[kW];
@@ -220,15 +203,25 @@ __global__ void __launch_bounds__(kT) k_centroids(Work w, Stage s) {
     Cand            &C  = w.cand[ci];
     if (!cand_live(C, s))
         return;
-    const int *nnId = w.nnId + (size_t)ci * w.maxSrc;
-    int        cnt  = 0;
-    for (int i = blockIdx.x * kT + threadIdx.x; i < s.n; i += smi::kIcpSlots)
-        cnt += nnId[i] >= 0 ? 1 : 0;
+    // keep only the closest source point per scene point (the atomicMin winner); the thread
+    // that drops a pair is the one that reduces it below
+    int          *nnId = w.nnId + (size_t)ci * w.maxSrc;
+    const int    *nnR  = w.nnR + (size_t)ci * w.maxSrc;
+    const float4 *x4   = w.x4 + (size_t)ci * w.maxSrc;
+    int           cnt  = 0;
+    for (int i = blockIdx.x * kT + threadIdx.x; i < s.n; i += smi::kIcpSlots) {
+        const int r = nnR[i];
+        if (r < 0)
+            continue;
+        if (w.win[(size_t)ci * w.maxDst + r] == win_key(x4[i].w, i))
+            cnt++;
+        else
+            nnId[i] = -1;
+    }
     cnt = __reduce_add_sync(0xffffffffu, cnt);
     if ((threadIdx.x & 31) == 0)
         icnt[threadIdx.x >> 5] = cnt;
-    const float4 *x4 = w.x4 + (size_t)ci * w.maxSrc;
-    smi::KahanF   v[6];
+    smi::KahanF v[6];
     __syncthreads();
     if (threadIdx.x == 0) { // the block's pair count rides in the spare partial slot 26
         int t = 0;
@@ -262,7 +255,7 @@ __global__ void __launch_bounds__(kT) k_centroids(Work w, Stage s) {
     }
 }
 
-// K5: the normal-equation terms of the pairs (computed in place), reduced; FP64 solve
+// K3: the normal-equation terms of the pairs (computed in place), reduced; FP64 solve
 __global__ void __launch_bounds__(kT) k_solve(Work w, Stage s) {
     __shared__ float red[kW][smi::kNumSystem][2];
     __shared__ int   flag;
@@ -295,8 +288,8 @@ __global__ void __launch_bounds__(kT) k_solve(Work w, Stage s) {
     }
 }
 
-// K6: residual distance of each pair after the step, one warp per pair
-__global__ void __launch_bounds__(kT, 4) k_resid(Work w, Stage s) {
+// K4: residual distance of each pair after the step, one warp per pair
+__global__ void __launch_bounds__(kT, 6) k_resid(Work w, Stage s) {
     const int   ci = blockIdx.y;
     const Cand &C  = w.cand[ci];
     if (!cand_live(C, s) || C.cnt < 6)
@@ -314,7 +307,7 @@ __global__ void __launch_bounds__(kT, 4) k_resid(Work w, Stage s) {
     }
 }
 
-// K7: mean residual, the regist loop logic (icp.cpp:233-272), winner reset
+// K5: mean residual, the regist loop logic (icp.cpp:233-272), winner reset
 __global__ void __launch_bounds__(kT) k_update(Work w, Stage s) {
     __shared__ float red[kW][1][2];
     __shared__ int   flag;
@@ -416,7 +409,7 @@ __global__ void k_stage_end(Work w, int ncand, int failStatus) {
 
 // Inliers of each candidate: source points with a scene point closer than the scoring
 // distance, one warp per point (warp_any_within).
-__global__ void __launch_bounds__(kT, 4) k_inliers(Work w, const float4 *__restrict__ src, int n,
+__global__ void __launch_bounds__(kT, 6) k_inliers(Work w, const float4 *__restrict__ src, int n,
                                                 HGridView F, float r2) {
     __shared__ int sc[kW];
     const int      ci = blockIdx.y;
@@ -479,15 +472,12 @@ __global__ void k_rank(const int *__restrict__ ids, int m, int *__restrict__ ran
 }
 
 void run_stage(Ctx &c, Work &w, const Stage &s, int ncand) {
-    const dim3 g2(s.nb, ncand);
     const dim3 gr(smi::kIcpBlocks, ncand);                    // reductions
     const dim3 gw(std::max(1, nblocks(s.n, kW)), ncand); // warp kernels: a warp per point
     k_stage_begin<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand);
     SM_LAUNCH_CHECK();
     for (int it = 0; it < s.iters; it++) {
         k_corr<<<gw, kT, 0, c.stream>>>(w, s);
-        SM_LAUNCH_CHECK();
-        k_pairs<<<g2, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
         k_centroids<<<gr, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();

@@ -268,12 +268,12 @@ __global__ void k_phase_offsets(int *__restrict__ ph) {
 
 // Placing pass: the point's position (index in w) at its cell slot; the point in slot 0
 // lists the cell in its phase (any order: cells of one phase do not interact) and records
-// rank[cell] = its list slot, the index of the cell's kept-point record.
+// rankCnt[cell] = {its list slot (the index of the cell's kept-point record), 0 kept}.
 __global__ void k_grid_scatter(const float4 *__restrict__ pos, const int *__restrict__ ids, int m,
                                const int *__restrict__ cellOf, const int *__restrict__ sub,
                                const int *__restrict__ start, int dim0, int dim1,
                                float4 *__restrict__ pts, int *__restrict__ ph,
-                               int *__restrict__ lists, int *__restrict__ rank) {
+                               int *__restrict__ lists, int2 *__restrict__ rankCnt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m)
         return;
@@ -286,7 +286,7 @@ __global__ void k_grid_scatter(const float4 *__restrict__ pos, const int *__rest
         const int cx = c % dim0, cy = (c / dim0) % dim1, cz = c / (dim0 * dim1);
         const int slot = atomicAdd(&ph[16 + smg::phase_of(cx, cy, cz)], 1);
         lists[slot]    = c;
-        rank[c]        = slot;
+        rankCnt[c]     = make_int2(slot, 0);
     }
 }
 
@@ -301,15 +301,16 @@ constexpr int kSpStage = 256; // neighbours' kept points staged in shared memory
 // drops every point within the step of one of them (order-free), then repeats "keep the
 // smallest surviving index, drop the survivors within the step of it" - the same kept set
 // as the sequential visit, at (kept points x cell size / 32) work and without sorting.
-// Kept points are recorded as positions (keptPos, `cap` per cell). The neighbours' kept
-// points and the cell's points (positions with the index in w, contiguous per cell) are
-// staged in shared memory; cells too large for the staging buffers take the same steps in
-// global memory (`alive` flags in aliveTmp).
+// Kept points are recorded as positions (keptPos, `cap` per cell) and their number in
+// rankCnt[cell].y, next to the cell's record index (one load per neighbour). The
+// neighbours' kept points and the cell's points (positions with the index in w, contiguous
+// per cell) are staged in shared memory; cells too large for the staging buffers take the
+// same steps in global memory (`alive` flags in aliveTmp).
 __global__ void __launch_bounds__(kSpWarps * 32)
     k_sample_phase(GridView G, const int *__restrict__ lists, const int *__restrict__ ph,
-                   int phase, const int *__restrict__ rank, int *__restrict__ keptCnt,
-                   float4 *__restrict__ keptPos, int cap, float r2, int *__restrict__ keptFlag,
-                   int *__restrict__ overflow, int *__restrict__ aliveTmp) {
+                   int phase, int2 *__restrict__ rankCnt, float4 *__restrict__ keptPos, int cap,
+                   float r2, int *__restrict__ keptFlag, int *__restrict__ overflow,
+                   int *__restrict__ aliveTmp) {
     __shared__ float4 stage[kSpWarps][kSpStage];
     __shared__ float4 cpos[kSpWarps][kSpIds];
     __shared__ int    calive[kSpWarps][kSpIds];
@@ -320,18 +321,22 @@ __global__ void __launch_bounds__(kSpWarps * 32)
     const int *cells  = lists + ph[8 + phase];
     for (int w = blockIdx.x * kSpWarps + wl; w < ncells; w += gridDim.x * kSpWarps) {
         const int cell = cells[w];
-        const int rk   = rank[cell];
+        const int rk   = rankCnt[cell].x;
         const int cx = cell % G.dim[0], cy = (cell / G.dim[0]) % G.dim[1],
                   cz = cell / (G.dim[0] * G.dim[1]);
         const int s = G.start[cell], e = G.start[cell + 1], n = e - s;
-        // neighbour l (lane < 26) of the 3x3x3 block without its centre
+        // the cell's first 32 points, read while the neighbours are looked up
+        const float4 q0 = lane < n ? G.pts[s + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+        // neighbour l (lane < 26) of the 3x3x3 block without its centre; cells of later
+        // phases have no kept points yet (count 0), empty cells have no record (-1)
         int nr = -1, cnt = 0;
         if (lane < 26) {
             const int o = lane < 13 ? lane : lane + 1;
             const int x = cx + o % 3 - 1, y = cy + (o / 3) % 3 - 1, z = cz + o / 9 - 1;
             if (x >= 0 && y >= 0 && z >= 0 && x < G.dim[0] && y < G.dim[1] && z < G.dim[2]) {
-                nr  = rank[grid_cell(G, x, y, z)];
-                cnt = nr >= 0 ? keptCnt[nr] : 0;
+                const int2 v = rankCnt[grid_cell(G, x, y, z)];
+                nr           = v.x;
+                cnt          = nr >= 0 ? v.y : 0;
             }
             snr[wl][lane]  = nr;
             scnt[wl][lane] = cnt;
@@ -364,7 +369,7 @@ __global__ void __launch_bounds__(kSpWarps * 32)
         const float4 *cp    = stageC ? cpos[wl] : G.pts + s;
         // survivors of the neighbours' kept points
         for (int i = lane; i < n; i += 32) {
-            const float4 q  = G.pts[s + i];
+            const float4 q  = i < 32 ? q0 : G.pts[s + i];
             bool         ok = true;
             if (stageNb) {
                 for (int k = 0; k < NK && ok; k++) {
@@ -431,7 +436,7 @@ __global__ void __launch_bounds__(kSpWarps * 32)
             __syncwarp();
         }
         if (lane == 0)
-            keptCnt[rk] = nk;
+            rankCnt[cell].y = nk;
         __syncwarp(); // the next cell reuses the warp's staging buffers
     }
 }
@@ -893,12 +898,12 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
     G.pts       = c.arena.get<float4>(tag + ".g.pts", std::max(m, 1));
     int *cellOf = c.arena.get<int>(tag + ".g.cellOf", std::max(m, 1));
     int *sub    = c.arena.get<int>(tag + ".g.sub", std::max(m, 1));
-    int *ph     = c.arena.get<int>(tag + ".ph", 24);
-    int *rank   = c.arena.get<int>(tag + ".rank", G.nc);
-    int *lists  = c.arena.get<int>(tag + ".phl", maxOcc);
+    int  *ph      = c.arena.get<int>(tag + ".ph", 24);
+    int2 *rankCnt = c.arena.get<int2>(tag + ".rank", G.nc);
+    int  *lists   = c.arena.get<int>(tag + ".phl", maxOcc);
     SM_CUDA(cudaMemsetAsync(cnt, 0, (G.nc + 1) * sizeof(int), c.stream));
     SM_CUDA(cudaMemsetAsync(ph, 0, 24 * sizeof(int), c.stream));
-    SM_CUDA(cudaMemsetAsync(rank, 0xff, G.nc * sizeof(int), c.stream));
+    SM_CUDA(cudaMemsetAsync(rankCnt, 0xff, G.nc * sizeof(int2), c.stream));
     const GridParams gpar = grid_params(box, g, G.dim);
     k_grid_count<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, m, gpar, cellOf, sub, cnt, ph);
     SM_LAUNCH_CHECK();
@@ -907,23 +912,21 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
     SM_LAUNCH_CHECK();
     k_grid_scatter<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, m, cellOf, sub, G.start,
                                                           G.dim[0], G.dim[1], G.pts, ph, lists,
-                                                          rank);
+                                                          rankCnt);
     SM_LAUNCH_CHECK();
     // kept-list capacity: points at pairwise distance >= step inside a cube of side g fit
     // disjoint balls of radius step/2 inside the cube grown by step/2.
     const double s   = (double)g / (double)step;
     const int    cap = (int)std::floor((s + 1.0) * (s + 1.0) * (s + 1.0) / (3.14159265358979 / 6.0)) + 1;
-    int    *keptCnt  = c.arena.get<int>(tag + ".kc", maxOcc);
     float4 *keptPos  = c.arena.get<float4>(tag + ".kp", (size_t)maxOcc * cap);
     int    *aliveTmp = c.arena.get<int>(tag + ".al", std::max(m, 1));
     int    *keptFlag = c.arena.get<int>(tag + ".kf", std::max(npoints, 1) + 1);
     int    *overflow = keptFlag + npoints;
-    SM_CUDA(cudaMemsetAsync(keptCnt, 0, maxOcc * sizeof(int), c.stream));
     SM_CUDA(cudaMemsetAsync(keptFlag, 0, (npoints + 1) * sizeof(int), c.stream));
     const float r2 = step * step;
     const int   gp = (int)std::min<long long>((maxOcc + kSpWarps - 1) / kSpWarps, 152LL * 16);
     for (int p = 0; p < 8; p++) {
-        k_sample_phase<<<gp, kSpWarps * 32, 0, c.stream>>>(G.view(), lists, ph, p, rank, keptCnt,
+        k_sample_phase<<<gp, kSpWarps * 32, 0, c.stream>>>(G.view(), lists, ph, p, rankCnt,
                                                            keptPos, cap, r2, keptFlag, overflow,
                                                            aliveTmp);
         SM_LAUNCH_CHECK();
