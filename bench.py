@@ -526,6 +526,10 @@ def main():
     traffic = vote_traffic()
     sm_mhz = clocks.get("sm_mhz") or 2070.0
     vote_rate = votes / (vk / 1000.0)
+    # the vote kernel's bounding operation, measured on this GPU after the timed steps
+    from surface_match_gb300 import probe_vote_atomics
+    atomic_peak = probe_vote_atomics(torch.cuda.current_device())
+    n_sm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
     line = {"metric": METRIC, "value": value, "unit": "scenes/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -551,8 +555,15 @@ def main():
                          "note": "bucket entries and hit records are L2-resident (traffic is "
                                  "DRAM bytes per launch); the kernel's own limit is the "
                                  "shared-memory vote atomics, see shared_atomics",
-                         "shared_atomics": {"votes_per_s": vote_rate,
-                                            "per_sm_per_clk": vote_rate / 152 / (sm_mhz * 1e6)}},
+                         "shared_atomics": {
+                             "votes_per_s": vote_rate,
+                             "per_sm_per_clk": vote_rate / n_sm / (sm_mhz * 1e6),
+                             "probe_peak_per_s": atomic_peak,
+                             "probe_peak_per_sm_per_clk": atomic_peak / n_sm / (sm_mhz * 1e6),
+                             "frac_of_probe_peak": vote_rate / atomic_peak,
+                             "probe": "sm_probe_vote_atomics: 16-bit shared counters at "
+                                      "pseudo-random cells of a 48 KB accumulator, 512-thread "
+                                      "CTAs, 2 per SM (one vote = one increment)"}},
             "vote_stage_ms": {"pairs_probe_k_ppf": statistics.median(ppf_ms),
                               "accumulate_k_vote_acc": vk,
                               "stage": stats["ms"][3]},

@@ -238,6 +238,12 @@ SM_API const char *sm_version(void);
 /* Number of CUDA kernels the library has launched so far in this process. */
 SM_API int64_t sm_launch_count(void);
 
+/* Measured rate of the vote stage's bounding operation on `device`: shared-memory atomic
+ * increments of 16-bit counters at pseudo-random cells of a 48 KB accumulator, 512-thread
+ * CTAs, two per SM (the vote kernel's shape). Writes increments per second (whole GPU).
+ * Used as the denominator of the vote kernel's roofline; no counterpart in the reference. */
+SM_API int sm_probe_vote_atomics(int device, double *atomics_per_second);
+
 #ifdef __cplusplus
 }
 #endif

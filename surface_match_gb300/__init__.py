@@ -5,7 +5,7 @@ include/surface_match.h (libsurface_match.so, CUDA kernels in csrc/), ``include/
 the C++ Detector over it, and this package is the Python mirror of the same API.
 """
 from .detector import (Context, Detector, MatchParam, MatchResult, PointCloud,  # noqa: F401
-                       RangeError, Server, TrainParam, match_batch)
+                       RangeError, Server, TrainParam, match_batch, probe_vote_atomics)
 
 __all__ = ["Context", "Detector", "MatchParam", "MatchResult", "PointCloud", "RangeError",
-           "Server", "TrainParam", "match_batch"]
+           "Server", "TrainParam", "match_batch", "probe_vote_atomics"]

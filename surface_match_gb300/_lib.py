@@ -87,6 +87,7 @@ _SIGNATURES = {
     "sm_last_error": (C.c_char_p, []),
     "sm_version": (C.c_char_p, []),
     "sm_launch_count": (C.c_int64, []),
+    "sm_probe_vote_atomics": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
 }
 
 

@@ -102,7 +102,8 @@ template <int N> SML_HD void jacobi_eig(double A[N][N], double V[N][N], double d
 // SelfAdjointEigenSolver::computeDirect). The smallest root of the characteristic cubic
 // p(l) = l^3 - c2 l^2 + c1 l - c0 is found by Newton's method from a Gershgorin lower bound:
 // p is negative, increasing and concave left of its smallest root, so the iterates rise
-// monotonically to it; iteration stops when they no longer increase. The eigenvector is the
+// monotonically to it; iteration stops when they no longer increase. An FP32 pass of the
+// same iteration supplies a start just below the root, so that few FP64 steps remain. The eigenvector is the
 // longest cross product of two rows of A - l I. Where the smallest eigenvalue is repeated
 // (rows of A - l I parallel or zero) a unit vector orthogonal to the longest row is taken,
 // and e_x for A = qI. FP64 throughout, basic operations only, so GPU and CPU agree bit for bit.
@@ -118,6 +119,26 @@ SML_HD void normal_from_cov(const double C[6] /*xx xy xz yy yz zz*/, float out[3
     l = g1 < l ? g1 : l;
     l = g2 < l ? g2 : l;
     l = l < 0.0 ? l : 0.0;
+    {
+        // the same iteration in FP32 first (a fraction of the FP64 cost); its root, moved
+        // down by 1e-4 of the trace (far above the FP32 error), starts the FP64 iterations
+        // when p is still negative there, i.e. when it lies below the root
+        const float f2 = (float)c2, f1 = (float)c1, f0 = (float)c0;
+        float       lf = (float)l;
+        for (int it = 0; it < 100; it++) {
+            const float pv = ((lf - f2) * lf + f1) * lf - f0;
+            const float dv = (3.0f * lf - 2.0f * f2) * lf + f1;
+            if (!(dv > 0.0f) || !(pv < 0.0f))
+                break;
+            const float nl = lf - pv / dv;
+            if (!(nl > lf))
+                break;
+            lf = nl;
+        }
+        const double l1 = (double)lf - 1e-4 * (c2 > 0.0 ? c2 : 0.0);
+        if (l1 > l && ((l1 - c2) * l1 + c1) * l1 - c0 < 0.0)
+            l = l1;
+    }
     for (int it = 0; it < 100; it++) {
         const double pv = ((l - c2) * l + c1) * l - c0;
         const double dv = (3.0 * l - 2.0 * c2) * l + c1;

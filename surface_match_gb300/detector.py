@@ -30,6 +30,14 @@ def _check(status):
     raise RuntimeError(msg)
 
 
+def probe_vote_atomics(device: int = 0) -> float:
+    """Measured shared-memory atomic increments per second of the vote kernel's access
+    pattern on `device` (include/surface_match.h sm_probe_vote_atomics)."""
+    out = C.c_double(0.0)
+    _check(_lib.load().sm_probe_vote_atomics(int(device), C.byref(out)))
+    return float(out.value)
+
+
 @dataclass
 class TrainParam:
     """ppf::TrainParam (type.h:39-74); validated on construction (type.cpp:71-88)."""

@@ -196,3 +196,15 @@ def test_poses_within_tolerance_of_reference_order(gpu, oracle_ref, data):
                     for i, Q in enumerate(r.poses) if i not in used), key=lambda t: t[2])
         used.add(best[0])
         assert best[1] < 0.1 and best[2] < 1e-3 * diam, best
+
+
+def test_vote_atomic_probe_rate_is_plausible():
+    """The measured shared-atomic rate that the vote kernel's roofline is quoted against:
+    positive, and between 0.05 and 64 increments per SM per clock at any clock the GPU runs
+    (a 32-lane warp instruction per clock is the hard ceiling)."""
+    import torch
+    from surface_match_gb300 import probe_vote_atomics
+    rate = probe_vote_atomics(0)
+    props = torch.cuda.get_device_properties(0)
+    per_sm = rate / props.multi_processor_count
+    assert 0.05 * 0.5e9 < per_sm < 64 * 3.0e9
