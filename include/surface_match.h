@@ -190,7 +190,9 @@ SM_API int sm_server_status(sm_server server, int64_t *out6);
  * order (nbr_off: K + 1 offsets into nbr_ids; each list contains the keypoint itself, as
  * the reference's radius search returns it). Outputs per keypoint: out_stats[K x 8] =
  * {neighbours, skipped (0 voted, 1 NaN normal, 2 below threshold), hits, votes,
- * accumulator fingerprint, n candidates, n poses, 0}; out_cands[K x 9] = up to 3
+ * accumulator fingerprint, n candidates, n poses, counter bound (sum over the hits of the
+ * bucket's largest entry count of one reference point: a bound on every accumulator cell,
+ * which picks 16- or 32-bit counters)}; out_cands[K x 9] = up to 3
  * (vote, ref, angle bin) triples (-1 padded); out_poses[K x 3 x 18] (nullable) = pose
  * 3x4, quaternion wxyz, rotation angle, votes. out_acc (nullable) receives the full
  * refNum x featAngleResolution accumulators of the first dump_k keypoints. */

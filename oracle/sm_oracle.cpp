@@ -338,7 +338,15 @@ struct Model {
     std::vector<uint32_t> refs;          // entries, per bucket in insertion order
     std::vector<float>    alphas;
     std::unordered_map<uint32_t, uint32_t> slot; // key -> bucket
+    std::vector<uint32_t> maxMult; // per bucket: most entries of one reference point
 };
+
+// Per-bucket multiplicities of the finished table (the GPU keeps them in its table slots).
+void finish_table(Model &m) {
+    m.maxMult.resize(m.keys.size());
+    for (size_t b = 0; b < m.keys.size(); b++)
+        m.maxMult[b] = smm::bucket_max_ref_multiplicity(m.refs.data(), m.offs[b], m.offs[b + 1]);
+}
 
 // Normal estimation (estimateNormal / computeNormal, util.cpp:234-334) in the two-phase
 // form. `knn(q, k, idx, d2)` returns the k nearest points of q in the full cloud, sorted.
@@ -499,6 +507,7 @@ void build_table(Model &m) {
         m.offs.push_back((uint32_t)m.refs.size());
         m.slot[order[b]] = (uint32_t)b;
     }
+    finish_table(m);
 }
 
 Model *train(const float *xyz, const float *nrm, int64_t n, float sdRel, const TrainParam &tp,
@@ -582,7 +591,7 @@ void pose_update(PoseRec &p) { // Pose::updatePose (type.cpp:53-59)
 
 struct KpOut {
     int      searched = 0, skipped = 1; // skipped: 1 = NaN normal, 2 = below vote threshold
-    int64_t  hits = 0, votes = 0;
+    int64_t  hits = 0, votes = 0, bound = 0; // bound: sum of the hits' bucket multiplicities
     uint64_t accHash = 0;
     int      nc = 0;
     float    cv[3];
@@ -636,6 +645,7 @@ void vote_keypoint(const Model &m, const std::vector<V3> &P, const std::vector<V
         float asT = smm::alpha_tail_shift(as);
         o.hits++;
         o.votes += B;
+        o.bound += m.maxMult[it->second];
         for (uint32_t e = 0; e < B; e++) {
             uint32_t bin = smm::vote_bin(e < bvec, m.alphas[b0 + e], as, asT, smax);
             if (bin > (uint32_t)(A - 1)) bin = A - 1; // unreachable; keeps the index in range
@@ -1267,6 +1277,7 @@ void *orc_model_import(int64_t ns, const float *sp, const float *sn, int64_t nr,
     m->refs.assign(refs, refs + offs[nk]);
     m->alphas.assign(alphas, alphas + offs[nk]);
     for (int64_t b = 0; b < nk; b++) m->slot[keys[b]] = (uint32_t)b;
+    finish_table(*m);
     return m;
 }
 
@@ -1289,7 +1300,7 @@ void orc_match_free(void *r) { delete (MatchOut *)r; }
 //  0 sampled ids (int32)     1 keypoint ids (int32)     2 resampled ids (int32)
 //  3 positions (f32 x3)      4 normals (f32 x3)         5 nbr offsets (int32, K+1)
 //  6 nbr ids (int32)         7 per-keypoint stats (int64 x8: searched, skipped, hits,
-//    votes, accHash, ncand, npose, 0)                   8 candidates (f32 x9: v0 r0 a0 ..)
+//    votes, accHash, ncand, npose, counter bound)                   8 candidates (f32 x9: v0 r0 a0 ..)
 //  9 pose list (f32 x18: 12 pose, 4 q, angle, votes)   10 clustered (f32 x18)
 // 11 cluster sizes (int32)  12 candidate status (int32) 13 candidate score (f32)
 // 14 candidate pose (f32 x12)  15 results (f32 x13: 12 pose + score)
@@ -1339,7 +1350,7 @@ void orc_res_get(void *rp, int field, void *dst) {
             int64_t *d = (int64_t *)dst;
             for (size_t c = 0; c < r->kp.size(); c++) {
                 auto &k = r->kp[c];
-                int64_t v[8] = {k.searched, k.skipped, k.hits, k.votes, (int64_t)k.accHash, k.nc, k.npose, 0};
+                int64_t v[8] = {k.searched, k.skipped, k.hits, k.votes, (int64_t)k.accHash, k.nc, k.npose, k.bound};
                 memcpy(d + 8 * c, v, 64);
             }
             break;
@@ -1403,7 +1414,7 @@ void orc_vote_stage(void *model, const float *pts, const float *nrms, int64_t n,
     }
     for (int64_t c = 0; c < K; c++) {
         auto &k = out[c];
-        int64_t v[8] = {k.searched, k.skipped, k.hits, k.votes, (int64_t)k.accHash, k.nc, k.npose, 0};
+        int64_t v[8] = {k.searched, k.skipped, k.hits, k.votes, (int64_t)k.accHash, k.nc, k.npose, k.bound};
         memcpy(stats + 8 * c, v, 64);
         for (int t = 0; t < 3; t++) {
             cands[9 * c + 3 * t]     = t < k.nc ? k.cv[t] : -1.f;

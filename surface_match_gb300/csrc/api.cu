@@ -183,7 +183,8 @@ void upload_model(Model &m, const std::vector<float> &sp, const std::vector<floa
         uint32_t i = keys[b] & (size - 1);
         while (tab[i].z != 0)
             i = (i + 1) & (size - 1);
-        tab[i] = make_uint4(keys[b], offs[b], offs[b + 1] - offs[b], 0);
+        tab[i] = make_uint4(keys[b], offs[b], offs[b + 1] - offs[b],
+                            smm::bucket_max_ref_multiplicity(refs.data(), offs[b], offs[b + 1]));
     }
     m.hmask = size - 1;
     SM_CUDA(cudaMalloc((void **)&m.hkeys, size * sizeof(uint4)));

@@ -251,6 +251,24 @@ SM_HD uint32_t murmur4(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3) {
     return h;
 }
 
+} // namespace smm
+#include <algorithm>
+#include <vector>
+namespace smm {
+// (host) Largest number of entries one reference point has in a bucket (refs[b0..b1)): a hit on
+// the bucket adds at most this many votes to any accumulator cell, so the sum over a
+// keypoint's hits bounds its largest cell (it picks the accumulator's counter width).
+inline uint32_t bucket_max_ref_multiplicity(const uint32_t *refs, uint32_t b0, uint32_t b1) {
+    std::vector<uint32_t> t(refs + b0, refs + b1);
+    std::sort(t.begin(), t.end());
+    uint32_t best = t.empty() ? 0u : 1u, run = 1;
+    for (size_t i = 1; i < t.size(); i++) {
+        run  = t[i] == t[i - 1] ? run + 1 : 1;
+        best = run > best ? run : best;
+    }
+    return best;
+}
+
 // splitmix64 finaliser (S. Vigna): fingerprint mixing of accumulator cells.
 SM_HD uint64_t mix64(uint64_t z) {
     z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;

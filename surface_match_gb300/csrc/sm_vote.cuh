@@ -44,6 +44,7 @@ struct VoteArgs {
     int       *poseOk;
     int       *acc;
     int        dumpK;
+    int        forceWide; // 32-bit counters for every keypoint (a test switch)
 };
 
 struct Cand {
@@ -73,14 +74,15 @@ __device__ __forceinline__ void top3_insert(Cand t[3], const Cand &c) {
 
 // Open-addressed model table of uint4 {key, first entry, entry count, 0}; count 0 = empty.
 __device__ __forceinline__ uint32_t probe(const uint4 *__restrict__ tab, uint32_t mask, uint32_t key,
-                                          uint32_t &off) {
+                                          uint32_t &off, uint32_t &mult) {
     uint32_t i = key & mask;
     for (uint32_t n = 0; n <= mask; n++) {
         const uint4 s = tab[i];
         if (s.z == 0)
             return 0;
         if (s.x == key) {
-            off = s.y;
+            off  = s.y;
+            mult = s.w;
             return s.z;
         }
         i = (i + 1) & mask;
@@ -192,12 +194,12 @@ __device__ __forceinline__ void dump_chunk(const VoteArgs &a, int c, const uint3
 
 // The keypoint's result: the block's top-3 candidates by (votes desc, reference asc), the
 // poses of those within 95% of the best (ppf.cpp:391-409) and its statistics row
-// {searched, 0, hits, votes, fingerprint, candidates, poses, 0}. wc needs blockDim/32 x 3
-// Cand, shash one zeroed word; both in shared memory.
+// {searched, 0, hits, votes, fingerprint, candidates, poses, counter bound}. wc needs
+// blockDim/32 x 3 Cand, shash one zeroed word; both in shared memory.
 __device__ __forceinline__ void finish_keypoint(const VoteArgs &a, int c, const smm::RT &rt,
                                                 Cand top[3], unsigned long long myHash,
                                                 long long searched, long long nHits,
-                                                long long V, Cand (*wc)[3],
+                                                long long V, long long bound, Cand (*wc)[3],
                                                 unsigned long long *shash) {
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
 #pragma unroll
@@ -260,7 +262,7 @@ __device__ __forceinline__ void finish_keypoint(const VoteArgs &a, int c, const 
     st[4]         = (long long)*shash;
     st[5]         = nc;
     st[6]         = npose;
-    st[7]         = 0;
+    st[7]         = bound;
 }
 
 // A keypoint that casts no votes: its normal is not finite (flag 1) or fewer neighbours

@@ -28,9 +28,9 @@ __global__ void __launch_bounds__(kVoteBs, 2) k_vote_fused(VoteArgs a) {
     __shared__ int       sh[33];
     __shared__ smm::RT   rt;
     __shared__ Cand      wc[kVoteBs / 32][3];
-    __shared__ long long sHitsTot, sVotesTot;
+    __shared__ long long sHitsTot, sVotesTot, sBoundTot;
     __shared__ unsigned long long shash;
-    __shared__ int       sRows, sHits, sVotes, sTail;
+    __shared__ int       sRows, sHits, sVotes, sBound, sTail;
 
     const int    c       = blockIdx.x;
     const int    tid     = threadIdx.x;
@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(kVoteBs, 2) k_vote_fused(VoteArgs a) {
     int R;
     block_excl_scan(myR, sh, &R);
     if (tid == 0) {
-        sHitsTot = sVotesTot = 0;
+        sHitsTot = sVotesTot = sBoundTot = 0;
         shash                = 0;
         rt                   = smm::transform_rt(p1.x, p1.y, p1.z, n1.x, n1.y, n1.z);
     }
@@ -99,6 +99,7 @@ __global__ void __launch_bounds__(kVoteBs, 2) k_vote_fused(VoteArgs a) {
                 sRows  = 0;
                 sHits  = 0;
                 sVotes = 0;
+                sBound = 0;
             }
             __syncthreads();
             // the window's rows, compacted (any order: votes are counts); bit 0 = block lane
@@ -128,11 +129,12 @@ __global__ void __launch_bounds__(kVoteBs, 2) k_vote_fused(VoteArgs a) {
                 const float as = smm::alpha_of(blk, rt, q.x, q.y, q.z);
                 if (smm::fisnan(as))
                     continue;
-                uint32_t  off = 0;
-                const int cnt = (int)probe(a.htab, a.hmask, key, off);
+                uint32_t  off = 0, mult = 0;
+                const int cnt = (int)probe(a.htab, a.hmask, key, off, mult);
                 if (cnt > 0) {
                     const int hp = atomicAdd(&sHits, 1);
                     atomicAdd(&sVotes, cnt);
+                    atomicAdd(&sBound, (int)mult);
                     hOff[hp] = (int)off;
                     hCnt[hp] = cnt;
                     hAs[hp]  = as;
@@ -155,6 +157,7 @@ __global__ void __launch_bounds__(kVoteBs, 2) k_vote_fused(VoteArgs a) {
                 if (!statsDone) {
                     sHitsTot += nHits;
                     sVotesTot += sVotes;
+                    sBoundTot += sBound;
                 }
             }
             __syncthreads();
@@ -163,7 +166,7 @@ __global__ void __launch_bounds__(kVoteBs, 2) k_vote_fused(VoteArgs a) {
             __syncthreads();
         }
         statsDone = true;
-        if (narrow && sVotesTot > kNarrowMax) {
+        if (narrow && sBoundTot > kNarrowMax) {
             // a counter may have overflowed 16 bits: vote again with 32-bit counters
             narrow = false;
             chunk  = a.refChunkWide;
@@ -175,7 +178,7 @@ __global__ void __launch_bounds__(kVoteBs, 2) k_vote_fused(VoteArgs a) {
         __syncthreads();
         r0 = r1;
     }
-    finish_keypoint(a, c, rt, top, myHash, listLen, sHitsTot, sVotesTot, wc, &shash);
+    finish_keypoint(a, c, rt, top, myHash, listLen, sHitsTot, sVotesTot, sBoundTot, wc, &shash);
 }
 
 // trainModel pair rows: for reference point i and column j, key and alpha with the

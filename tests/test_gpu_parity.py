@@ -124,14 +124,18 @@ def test_vote_kernel_reference_order_bit_exact(oracle_ref):
     np.testing.assert_array_equal(emitted.view(np.uint32), r.pose_list.view(np.uint32))
 
 
-@pytest.mark.parametrize("dist_rel,angles", [(0.25, 12), (0.04, 360)])
-def test_vote_kernel_counter_widths_and_passes(data, dist_rel, angles):
+@pytest.mark.parametrize("dist_rel,angles,wide", [(0.25, 12, False), (0.04, 360, False),
+                                                   (0.25, 12, True), (0.04, 360, True)])
+def test_vote_kernel_counter_widths_and_passes(data, dist_rel, angles, wide, monkeypatch):
     """The accumulator's other regimes, bit-exact against the oracle: coarse distance
-    steps make buckets so large that keypoints cast more than 65535 votes (16-bit counters
-    give way to 32-bit ones), and 360 angle bins make the accumulator larger than one CTA's
-    shared memory (several reference-point passes)."""
+    steps make buckets so large that keypoints cast more than 65535 votes (the per-cell
+    bound still keeps them on 16-bit counters), 360 angle bins make the accumulator larger
+    than one CTA's shared memory (several reference-point passes), and the 32-bit counters
+    that the bound reserves for extreme inputs are forced on (one and several passes)."""
     from oracle import MODE_REF, MatchParam, Oracle, TrainParam as OTP
     from surface_match_gb300 import Detector, TrainParam
+    if wide:
+        monkeypatch.setenv("SM_VOTE_FORCE_WIDE", "1")
     mc, sc = data
     o = Oracle(mode=MODE_REF, threads=8)
     m = o.train(mc.xyz, mc.normal, SD, OTP(featDistanceStepRel=dist_rel,
@@ -140,6 +144,7 @@ def test_vote_kernel_counter_widths_and_passes(data, dist_rel, angles):
                 dump_k=4)
     if dist_rel > 0.2:
         assert r.kp_stats[:, 3].max() > 65535
+    assert r.kp_stats[:, 7].max() <= 65535  # the bound: 16-bit unless forced
     if angles == 360:
         assert len(m.sampled) * angles * 2 > 200 * 1024
     det = Detector()
