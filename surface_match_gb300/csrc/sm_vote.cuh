@@ -112,7 +112,8 @@ __device__ __forceinline__ void cast_votes(const VoteArgs &a, uint32_t *acc, con
         else
             hi = mid - 1;
     }
-    int h = lo;
+    int        h       = lo;
+    const bool allRefs = r0 == 0 && r1 == a.ns; // one pass holds every reference point
     for (int item = i0; item < i1; item++) {
         while (cPre[h + 1] <= item)
             h++;
@@ -133,11 +134,15 @@ __device__ __forceinline__ void cast_votes(const VoteArgs &a, uint32_t *acc, con
         for (int u = 0; u < kVoteU; u++) {
             const int e   = e0 + u * 32 + lane;
             const int ref = (int)ent[u].x;
-            if (e >= eEnd || ref < r0 || ref >= r1)
+            if (e >= eEnd || (!allRefs && (ref < r0 || ref >= r1)))
                 continue;
-            uint32_t bin = smm::vote_bin(e < vecB, __uint_as_float(ent[u].y), as, asT, a.smax);
-            if (bin > (uint32_t)(a.A - 1))
-                bin = a.A - 1; // unreachable; keeps the index in range
+            const float am = __uint_as_float(ent[u].y);
+            uint32_t    bin;
+            if (e0 + u * 32 + 32 <= vecB) // warp-uniform: the round lies in the 8-lane blocks
+                bin = smm::vote_bin(true, am, as, asT, a.smax);
+            else
+                bin = smm::vote_bin(e < vecB, am, as, asT, a.smax);
+            bin         = min(bin, (uint32_t)(a.A - 1)); // unreachable; keeps the index in range
             const int c = (ref - r0) * a.A + (int)bin;
             if (narrow)
                 atomicAdd(&acc[c >> 1], 1u << ((c & 1) * 16));
