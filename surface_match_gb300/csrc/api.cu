@@ -449,16 +449,23 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
     // Nearest-neighbour grids of the refinement: cells of about a third of the rejection
     // distance (never finer than the subset's spacing), so three cell shells always cover
     // it. The inlier grid's cell just exceeds the scoring distance, so two shells decide.
-    build_hgrid(c, pos, sampled, ns, box, std::max(sampleStep, refDist / 2.98f), s.sampled, "m.gS");
+    // The subset grids name points by subset rank (the subsets are ascending, so rank order
+    // is index order), and the refinement reads rank-ordered copies of the subsets.
+    build_hgrid(c, pos, sampled, ns, box, std::max(sampleStep, refDist / 2.98f), s.sampled, "m.gS",
+                true);
     build_hgrid(c, pos, resampled, nres, box, std::max(2.0f * reSampleStep, refDist / 2.98f),
-                s.resampled, "m.gR");
+                s.resampled, "m.gR", true);
     build_hgrid(c, pos, valid, nvalid, box, std::max(scoreDist * 1.02f, gq), s.full, "m.gF");
-    int *rankS = c.arena.get<int>("m.rankS", n);
-    int *rankR = c.arena.get<int>("m.rankR", n);
-    subset_rank(c, sampled, ns, rankS);
-    subset_rank(c, resampled, nres, rankR);
-    s.rankS = rankS;
-    s.rankR = rankR;
+    float4 *posS = c.arena.get<float4>("m.posS", std::max(ns, 1));
+    float4 *nrmS = c.arena.get<float4>("m.nrmS", std::max(ns, 1));
+    float4 *posR = c.arena.get<float4>("m.posR", std::max(nres, 1));
+    float4 *nrmR = c.arena.get<float4>("m.nrmR", std::max(nres, 1));
+    gather_subset(c, pos, nrm, sampled, ns, posS, nrmS);
+    gather_subset(c, pos, nrm, resampled, nres, posR, nrmR);
+    s.posS = posS;
+    s.nrmS = nrmS;
+    s.posR = posR;
+    s.nrmR = nrmR;
     record(c, 6);
     IcpParams ip;
     ip.sparse        = mp.sparsePoseRefinement;

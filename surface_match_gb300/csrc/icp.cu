@@ -41,8 +41,8 @@ struct Cand {
 struct Stage {
     const float4 *src, *srcN; // model points / normals
     int           n, nb;      // points, CTAs per candidate
-    HGridView     G;          // scene subset grid
-    const int    *rank;       // point id -> subset index
+    HGridView     G;          // scene subset grid (pts.w = subset rank)
+    const float4 *dPos, *dNrm; // the subset's positions / normals by rank
     int           nDst;
     int           iters;
     float         mseMin, mseMax, rej2;
@@ -52,8 +52,9 @@ struct Stage {
 struct Work {
     Cand               *cand;
     const float4       *pos, *nrm;
-    int                *nnId;   // ncand x maxSrc: scene point of the pair (-1 none)
-    int                *nnR;    // ncand x maxSrc: its subset index (-1 none)
+    int                *nnId;   // ncand x maxSrc: subset rank of the pair's scene point (-1 none)
+    int                *nnR;    // ncand x maxSrc: the same, kept through pair selection
+    int                *nnPrev; // ncand x maxSrc: nearest subset point of the last iteration
     float4             *x4;     // ncand x maxSrc: moved source point, w = squared distance
     float4             *n4;     // ncand x maxSrc: rotated source normal
     float              *resid;  // ncand x maxSrc: residual distance of each pair
@@ -73,13 +74,16 @@ __device__ __forceinline__ bool cand_live(const Cand &c, const Stage &s) {
 }
 
 // K1: correspondences, one warp per source point (warp-cooperative grid search)
-__global__ void __launch_bounds__(kT, 6) k_corr(Work w, Stage s) {
+__global__ void __launch_bounds__(kT, 4) k_corr(Work w, Stage s, int usePrev) {
     const int ci   = blockIdx.y;
     const int lane = threadIdx.x & 31;
     int       i    = blockIdx.x * kW + (threadIdx.x >> 5);
-    // the first source point is read together with the candidate's state
+    // the first source point and the last iteration's nearest point are read together with
+    // the candidate's state
     float4 sp = i < s.n ? s.src[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     float4 sn = i < s.n ? s.srcN[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    int    jp = usePrev && i < s.n ? w.nnPrev[(size_t)ci * w.maxSrc + i] : -1;
+    float4 qp = jp >= 0 ? s.dPos[jp] : make_float4(0.f, 0.f, 0.f, 0.f);
     const Cand &C = w.cand[ci];
     if (!cand_live(C, s))
         return;
@@ -89,22 +93,29 @@ __global__ void __launch_bounds__(kT, 6) k_corr(Work w, Stage s) {
         if (i != blockIdx.x * kW + (threadIdx.x >> 5)) {
             sp = s.src[i];
             sn = s.srcN[i];
+            jp = usePrev ? w.nnPrev[o] : -1;
+            if (jp >= 0)
+                qp = s.dPos[jp];
         }
         smi::pose_apply(C.M, sp.x, sp.y, sp.z, x.x, x.y, x.z);
         smi::pose_rotate(C.M, sn.x, sn.y, sn.z, y.x, y.y, y.z);
+        // the last iteration's nearest point of this stage bounds the search exactly
+        float lim = s.rej2;
+        if (jp >= 0)
+            lim = fminf(lim, smm::dist2(x.x, x.y, x.z, qp.x, qp.y, qp.z));
         float      d;
-        const int  j  = warp_nn_walk(s.G, x.x, x.y, x.z, s.rej2, d);
+        const int  j  = warp_nn_walk(s.G, x.x, x.y, x.z, lim, d); // subset rank
         const bool ok = j >= 0 && d <= s.rej2;
         if (lane == 0) {
-            x.w       = d;
-            y.w       = 0.0f;
-            w.x4[o]   = x;
-            w.n4[o]   = y;
-            w.nnId[o] = ok ? j : -1;
-            const int r = ok ? s.rank[j] : -1;
-            w.nnR[o]    = r;
+            w.nnPrev[o] = j;
+            x.w         = d;
+            y.w         = 0.0f;
+            w.x4[o]     = x;
+            w.n4[o]     = y;
+            w.nnId[o]   = ok ? j : -1;
+            w.nnR[o]    = ok ? j : -1;
             if (ok)
-                atomicMin(&w.win[(size_t)ci * w.maxDst + r], win_key(d, i));
+                atomicMin(&w.win[(size_t)ci * w.maxDst + j], win_key(d, i));
         }
     }
 }
@@ -232,7 +243,7 @@ __global__ void __launch_bounds__(kT) k_centroids(Work w, Stage s) {
     }
     const bool last = slot_reduce<6>(w, s, ci,
                                      [&](int i, float *t) {
-                                         const float4 q = w.pos[nnId[i]];
+                                         const float4 q = s.dPos[nnId[i]];
                                          t[0]           = x4[i].x;
                                          t[1]           = x4[i].y;
                                          t[2]           = x4[i].z;
@@ -271,7 +282,7 @@ __global__ void __launch_bounds__(kT) k_solve(Work w, Stage s) {
         w, s, ci,
         [&](int i, float *t) {
             const int    id = w.nnId[o0 + i];
-            const float4 x = w.x4[o0 + i], xn = w.n4[o0 + i], q = w.pos[id], qn = w.nrm[id];
+            const float4 x = w.x4[o0 + i], xn = w.n4[o0 + i], q = s.dPos[id], qn = s.dNrm[id];
             smi::system_terms(x.x - Pm0, x.y - Pm1, x.z - Pm2, q.x - Qm0, q.y - Qm1, q.z - Qm2,
                               xn.x + qn.x, xn.y + qn.y, xn.z + qn.z, t);
         },
@@ -289,7 +300,7 @@ __global__ void __launch_bounds__(kT) k_solve(Work w, Stage s) {
 }
 
 // K4: residual distance of each pair after the step, one warp per pair
-__global__ void __launch_bounds__(kT, 6) k_resid(Work w, Stage s) {
+__global__ void __launch_bounds__(kT, 5) k_resid(Work w, Stage s) {
     const int   ci = blockIdx.y;
     const Cand &C  = w.cand[ci];
     if (!cand_live(C, s) || C.cnt < 6)
@@ -299,9 +310,11 @@ __global__ void __launch_bounds__(kT, 6) k_resid(Work w, Stage s) {
         if (w.nnId[o] < 0)
             continue;
         const float4 x = w.x4[o];
+        const float4 q = s.dPos[w.nnId[o]];
         float        y0, y1, y2, d;
         smi::pose_apply(C.step, x.x, x.y, x.z, y0, y1, y2);
-        warp_nn_walk(s.G, y0, y1, y2, FLT_MAX, d);
+        // the pair's scene point bounds the search exactly
+        warp_nn_walk(s.G, y0, y1, y2, smm::dist2(y0, y1, y2, q.x, q.y, q.z), d);
         if ((threadIdx.x & 31) == 0)
             w.resid[(size_t)ci * w.maxSrc + i] = smm::fsqrt(d);
     }
@@ -465,11 +478,6 @@ __global__ void k_finish(Work w, int ncand, int refine, float minScore, int *sta
         pose[(size_t)ci * 12 + e] = C.keep.m[e];
 }
 
-__global__ void k_rank(const int *__restrict__ ids, int m, int *__restrict__ rank) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < m)
-        rank[ids[i]] = i;
-}
 
 void run_stage(Ctx &c, Work &w, const Stage &s, int ncand) {
     const dim3 gr(smi::kIcpBlocks, ncand);                    // reductions
@@ -477,7 +485,7 @@ void run_stage(Ctx &c, Work &w, const Stage &s, int ncand) {
     k_stage_begin<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand);
     SM_LAUNCH_CHECK();
     for (int it = 0; it < s.iters; it++) {
-        k_corr<<<gw, kT, 0, c.stream>>>(w, s);
+        k_corr<<<gw, kT, 0, c.stream>>>(w, s, it > 0 ? 1 : 0);
         SM_LAUNCH_CHECK();
         k_centroids<<<gr, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
@@ -504,6 +512,7 @@ void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, con
     w.cand   = c.arena.get<Cand>("icp.cand", ncand);
     w.nnId   = c.arena.get<int>("icp.nnId", (size_t)ncand * w.maxSrc);
     w.nnR    = c.arena.get<int>("icp.nnR", (size_t)ncand * w.maxSrc);
+    w.nnPrev = c.arena.get<int>("icp.nnPrev", (size_t)ncand * w.maxSrc);
     w.x4     = c.arena.get<float4>("icp.x4", (size_t)ncand * w.maxSrc);
     w.n4     = c.arena.get<float4>("icp.n4", (size_t)ncand * w.maxSrc);
     w.resid  = c.arena.get<float>("icp.resid", (size_t)ncand * w.maxSrc);
@@ -518,7 +527,7 @@ void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, con
     const float rej2 = p.rejectDist * p.rejectDist;
     const float sc2  = p.scoreDist * p.scoreDist;
     if (p.sparse) {
-        Stage s{m.sp, m.sn, m.ns, nblocks(m.ns, kT), sc.sampled.view(), sc.rankS, sc.sampled.m, 5,
+        Stage s{m.sp, m.sn, m.ns, nblocks(m.ns, kT), sc.sampled.view(), sc.posS, sc.nrmS, sc.sampled.m, 5,
                 p.sampleStep * 0.5f, p.sampleStep, rej2, 0};
         run_stage(c, w, s, ncand);
         k_stage_end<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, 2);
@@ -529,7 +538,7 @@ void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, con
         k_score<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, m.ns, p.minScore, 3, 0);
         SM_LAUNCH_CHECK();
         if (p.dense) {
-            Stage d{m.rp, m.rn, m.nr, nblocks(m.nr, kT), sc.resampled.view(), sc.rankR,
+            Stage d{m.rp, m.rn, m.nr, nblocks(m.nr, kT), sc.resampled.view(), sc.posR, sc.nrmR,
                     sc.resampled.m, p.denseSteps, p.reSampleStep * 0.5f, p.sampleStep, rej2, 1};
             run_stage(c, w, d, ncand);
             k_stage_end<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, 4);
@@ -543,13 +552,6 @@ void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, con
     }
     k_finish<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, (p.sparse || p.dense) ? 1 : 0,
                                                          p.minScore, status, score, pose);
-    SM_LAUNCH_CHECK();
-}
-
-void subset_rank(Ctx &c, const int *ids, int m, int *rank) {
-    if (m <= 0)
-        return;
-    k_rank<<<nblocks(m, 256), 256, 0, c.stream>>>(ids, m, rank);
     SM_LAUNCH_CHECK();
 }
 

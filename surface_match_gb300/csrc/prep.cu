@@ -515,7 +515,7 @@ __global__ void k_hg_insert(const float4 *__restrict__ pos, const int *__restric
 
 __global__ void k_hg_scatter(const float4 *__restrict__ pos, const int *__restrict__ ids,
                              const int *__restrict__ slotOf, int m, int *__restrict__ fill,
-                             int *__restrict__ gids, float4 *__restrict__ pts) {
+                             int *__restrict__ gids, float4 *__restrict__ pts, int wIsRank) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m)
         return;
@@ -523,7 +523,19 @@ __global__ void k_hg_scatter(const float4 *__restrict__ pos, const int *__restri
     const float4 p  = pos[id];
     const int    k  = atomicAdd(&fill[slotOf[i]], 1);
     gids[k]         = id;
-    pts[k]          = make_float4(p.x, p.y, p.z, __int_as_float(id));
+    pts[k]          = make_float4(p.x, p.y, p.z, __int_as_float(wIsRank ? i : id));
+}
+
+// Rank-ordered copies of a subset's positions and normals: out[r] = in[ids[r]].
+__global__ void k_gather_subset(const float4 *__restrict__ pos, const float4 *__restrict__ nrm,
+                                const int *__restrict__ ids, int m, float4 *__restrict__ subPos,
+                                float4 *__restrict__ subNrm) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= m)
+        return;
+    const int id = ids[r];
+    subPos[r]    = pos[id];
+    subNrm[r]    = nrm[id];
 }
 
 __global__ void k_hg_pack_from_start(const unsigned long long *__restrict__ keys,
@@ -820,7 +832,7 @@ static int *compact_grid_order(Ctx &c, const HGrid &H, const int *need, int eq, 
 }
 
 void build_hgrid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &box, float g,
-                 HGrid &H, const std::string &tag) {
+                 HGrid &H, const std::string &tag, bool wIsRank) {
     // cells per axis stay below 2^20 so that cell keys fit 60 bits (coarser cells if needed)
     while (smg::dim_of(box.ext(0), g) >= (1 << 20) || smg::dim_of(box.ext(1), g) >= (1 << 20) ||
            smg::dim_of(box.ext(2), g) >= (1 << 20))
@@ -853,7 +865,8 @@ void build_hgrid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &bo
     int *fill = cnt;
     SM_CUDA(cudaMemcpyAsync(fill, start, (size_t)T * 4, cudaMemcpyDeviceToDevice, c.stream));
     if (m > 0) {
-        k_hg_scatter<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, slotOf, m, fill, H.ids, H.pts);
+        k_hg_scatter<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, slotOf, m, fill, H.ids, H.pts,
+                                                             wIsRank ? 1 : 0);
         SM_LAUNCH_CHECK();
     }
     // occupancy bits over the cell box, when it has at most 2^28 cells (32 MB)
@@ -873,6 +886,14 @@ void build_hgrid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &bo
     // counts again for the packed table: start[t+1] - start[t]
     k_hg_pack_from_start<<<nblocks(T, 256), 256, 0, c.stream>>>(keys, start, T, H.slot, H.occ,
                                                                 H.dense);
+    SM_LAUNCH_CHECK();
+}
+
+void gather_subset(Ctx &c, const float4 *pos, const float4 *nrm, const int *ids, int m,
+                   float4 *subPos, float4 *subNrm) {
+    if (m <= 0)
+        return;
+    k_gather_subset<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, nrm, ids, m, subPos, subNrm);
     SM_LAUNCH_CHECK();
 }
 

@@ -106,13 +106,13 @@ __device__ __forceinline__ int warp_incl_scan(int v) {
     return v;
 }
 
+// Warp minimum of a 64-bit key: the high words' minimum, then the low words' minimum among
+// the lanes that hold it (two single-instruction warp reductions).
 __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
-#pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) {
-        const unsigned long long t = __shfl_xor_sync(0xffffffffu, v, o);
-        v                          = t < v ? t : v;
-    }
-    return v;
+    const unsigned hi = (unsigned)(v >> 32), lo = (unsigned)v;
+    const unsigned mh = __reduce_min_sync(0xffffffffu, hi);
+    const unsigned ml = __reduce_min_sync(0xffffffffu, hi == mh ? lo : 0xffffffffu);
+    return ((unsigned long long)mh << 32) | ml;
 }
 
 // Ascending bitonic sort of one 64-bit key per lane across the warp.
@@ -468,10 +468,11 @@ __device__ __forceinline__ int warp_knn_sorted(const HGridView &g, float qx, flo
 }
 
 // Nearest point by (squared distance, index), one warp per query: the 3x3x3 block first,
-// then bands of rings (warp_band) with cells screened against min(best, limit2), until the
-// nearest is below the ring bound or the ring bound passes limit2. A point farther than
-// limit2 may be returned (callers test the distance); -1 when none was found. All lanes
-// return the result.
+// then bands of rings (warp_band), cells screened against min(best, limit2) throughout,
+// until the nearest is below the ring bound or the ring bound passes limit2. A point
+// farther than limit2 may be returned (callers test the distance); -1 when none was found.
+// A caller that knows a point of the grid at squared distance u from q may pass limit2 <= u:
+// the nearest is then found exactly with fewer cells visited. All lanes return the result.
 __device__ __forceinline__ int warp_nn_walk(const HGridView &g, float qx, float qy, float qz,
                                             float limit2, float &outd) {
     unsigned long long best  = ~0ull;
@@ -492,7 +493,7 @@ __device__ __forceinline__ int warp_nn_walk(const HGridView &g, float qx, float 
     int c[3];
     grid_cc(g, qx, qy, qz, c);
     const int ms = max(grid_max_shell(g, c), 1);
-    warp_block27(g, qx, qy, qz, c, kInf, visit);
+    warp_block27(g, qx, qy, qz, c, limit2, visit);
     for (int done = 1;;) {
         const float d  = bd();
         const float rb = smg::ring_bound(done, g.g);

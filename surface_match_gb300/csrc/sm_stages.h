@@ -59,7 +59,10 @@ int compact(Ctx &c, const int *flags, int n, int *outIds, const std::string &tag
 void compact_known(Ctx &c, const int *flags, int n, int *outIds, const std::string &tag);
 // Hashed grid over points ids[0..m) with cell side g (fine cells at any scene extent).
 void build_hgrid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &box, float g,
-                 HGrid &H, const std::string &tag);
+                 HGrid &H, const std::string &tag, bool wIsRank = false);
+// subPos[r] = pos[ids[r]], subNrm[r] = nrm[ids[r]] for r < m.
+void gather_subset(Ctx &c, const float4 *pos, const float4 *nrm, const int *ids, int m,
+                   float4 *subPos, float4 *subNrm);
 // Greedy thinning at `step` in (phase, cell, index) order; writes kept ids ascending,
 // returns their count.
 int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m, const Box &box,
@@ -103,8 +106,8 @@ int cluster(Ctx &c, const float *poses, int np, float distThr, float angThr,
 // ---- icp.cu ---------------------------------------------------------------------------
 struct IcpScene {
     const float4 *pos, *nrm;
-    HGrid         sampled, resampled, full;
-    const int    *rankS, *rankR; // point id -> index in the sampled / resampled subsets
+    HGrid         sampled, resampled, full; // the subset grids carry subset ranks in pts.w
+    const float4 *posS, *nrmS, *posR, *nrmR; // the sampled / resampled subsets, rank order
 };
 struct IcpParams {
     int   sparse, dense, denseSteps;
@@ -112,8 +115,6 @@ struct IcpParams {
 };
 // ICP refinement + scoring of every candidate in parallel. Outputs per candidate: status,
 // score, refined pose (12 floats).
-// rank[ids[i]] = i
-void subset_rank(Ctx &c, const int *ids, int m, int *rank);
 void icp_all(Ctx &c, const Model &m, const IcpScene &s, const IcpParams &p, const float *cands,
              int ncand, int *status, float *score, float *pose, float *trace = nullptr);
 constexpr int kIcpTraceFloats = 2 * 32 * 4 + 2; // per candidate, see icp.cu
