@@ -78,30 +78,30 @@ __global__ void __launch_bounds__(kT, 4) k_corr(Work w, Stage s, int usePrev) {
     const int ci   = blockIdx.y;
     const int lane = threadIdx.x & 31;
     int       i    = blockIdx.x * kW + (threadIdx.x >> 5);
-    // the first source point and the last iteration's nearest point are read together with
-    // the candidate's state
+    // the first source point is read together with the candidate's state
     float4 sp = i < s.n ? s.src[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     float4 sn = i < s.n ? s.srcN[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    int    jp = usePrev && i < s.n ? w.nnPrev[(size_t)ci * w.maxSrc + i] : -1;
-    float4 qp = jp >= 0 ? s.dPos[jp] : make_float4(0.f, 0.f, 0.f, 0.f);
     const Cand &C = w.cand[ci];
     if (!cand_live(C, s))
-        return;
+        return; // (a candidate that is not live has no nearest points of this stage)
     for (; i < s.n; i += gridDim.x * kW) {
         const size_t o = (size_t)ci * w.maxSrc + i;
         float4       x, y;
         if (i != blockIdx.x * kW + (threadIdx.x >> 5)) {
             sp = s.src[i];
             sn = s.srcN[i];
-            jp = usePrev ? w.nnPrev[o] : -1;
-            if (jp >= 0)
-                qp = s.dPos[jp];
         }
+        // written by this candidate's previous iteration of this stage (usePrev: not the
+        // first iteration), a rank of this stage's subset or -1
+        const int jp = usePrev ? w.nnPrev[o] : -1;
+        float4    qp = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (jp >= 0 && jp < s.nDst)
+            qp = s.dPos[jp];
         smi::pose_apply(C.M, sp.x, sp.y, sp.z, x.x, x.y, x.z);
         smi::pose_rotate(C.M, sn.x, sn.y, sn.z, y.x, y.y, y.z);
         // the last iteration's nearest point of this stage bounds the search exactly
         float lim = s.rej2;
-        if (jp >= 0)
+        if (jp >= 0 && jp < s.nDst)
             lim = fminf(lim, smm::dist2(x.x, x.y, x.z, qp.x, qp.y, qp.z));
         float      d;
         const int  j  = warp_nn_walk(s.G, x.x, x.y, x.z, lim, d); // subset rank
