@@ -677,6 +677,7 @@ SM_API int sm_context_create(int device, void *stream, sm_context *out) {
         SM_CUDA(cudaMallocHost((void **)&c->ctx.hostCounts, 64 * sizeof(int)));
         for (auto &e : c->ctx.ev)
             SM_CUDA(cudaEventCreate(&e));
+        c->ctx.arena.set_stream(c->ctx.stream, device);
         *out = c.release();
     });
 }

@@ -46,6 +46,7 @@ std::unique_ptr<Ctx> acquire_worker(int device) {
     SM_CUDA(cudaMallocHost((void **)&c->hostCounts, 64 * sizeof(int)));
     for (auto &e : c->ev)
         SM_CUDA(cudaEventCreate(&e));
+    c->arena.set_stream(c->stream, device);
     return c;
 }
 

@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <map>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -37,10 +38,17 @@ extern long long g_launches;
 
 inline int nblocks(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 
-// Device buffers by name, grown on demand and reused across calls.
+// Device buffers by name, grown on demand and reused across calls. With a stream set, a
+// buffer grows by stream-ordered free + allocation on that stream (the device's default
+// memory pool, which keeps freed memory for reuse), so that growing one context's
+// workspace never waits for the work of other contexts on the device.
 class Arena {
 public:
     ~Arena() { release(); }
+    void set_stream(cudaStream_t s, int device) {
+        stream_ = s;
+        keep_pool_memory(device);
+    }
     void *get(const std::string &name, size_t bytes) {
         if (bytes == 0)
             bytes = 16;
@@ -48,12 +56,15 @@ public:
         if (it != slots_.end() && it->second.second >= bytes)
             return it->second.first;
         if (it != slots_.end()) {
-            cudaFree(it->second.first);
+            if (stream_)
+                cudaFreeAsync(it->second.first, stream_);
+            else
+                cudaFree(it->second.first);
             slots_.erase(it);
         }
-        size_t cap = bytes + bytes / 4;
-        void  *p   = nullptr;
-        cudaError_t e = cudaMalloc(&p, cap);
+        size_t      cap = bytes + bytes / 4;
+        void       *p   = nullptr;
+        cudaError_t e   = stream_ ? cudaMallocAsync(&p, cap, stream_) : cudaMalloc(&p, cap);
         if (e != cudaSuccess) {
             cudaGetLastError();
             throw Error(SM_ERR_NOMEM, "device allocation of " + std::to_string(cap) +
@@ -71,6 +82,7 @@ public:
             s += kv.second.second;
         return s;
     }
+    // frees everything (synchronising: the stream may be gone by then)
     void release() {
         for (auto &kv : slots_)
             cudaFree(kv.second.first);
@@ -78,6 +90,22 @@ public:
     }
 
 private:
+    static void keep_pool_memory(int device) {
+        static std::mutex mu;
+        static std::vector<int> done;
+        std::lock_guard<std::mutex> lk(mu);
+        for (int d : done)
+            if (d == device)
+                return;
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t keep = ~0ull;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        cudaGetLastError();
+        done.push_back(device);
+    }
+    cudaStream_t                                     stream_ = nullptr;
     std::map<std::string, std::pair<void *, size_t>> slots_;
 };
 
