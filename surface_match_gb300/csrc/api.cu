@@ -373,6 +373,21 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
     int         *valid  = c.arena.get<int>("m.vids", n);
     compact_known(c, val, n, valid, "m.cv"); // nvalid points
     record(c, 1);
+    if (nvalid == 0) {
+        // no finite point: the reference's search structures are empty and it returns no
+        // pose; nothing is sampled (there is no bounding box to build grids on)
+        c.sync_checked();
+        res.pose.clear();
+        res.score.clear();
+        c.last       = Ctx::Last{};
+        c.last.n     = n;
+        c.last.valid = true;
+        if (stats) {
+            memset(stats, 0, sizeof(*stats));
+            stats->n_points = n;
+        }
+        return;
+    }
     float ext[3] = {box.ext(0), box.ext(1), box.ext(2)};
 
     const float diam         = m.box.diameter();

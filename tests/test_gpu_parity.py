@@ -213,3 +213,68 @@ def test_vote_atomic_probe_rate_is_plausible():
     props = torch.cuda.get_device_properties(0)
     per_sm = rate / props.multi_processor_count
     assert 0.05 * 0.5e9 < per_sm < 64 * 3.0e9
+
+
+def test_errors_mirror_reference(data):
+    """matchScene's argument checks, in the reference's order and with its exception types
+    and messages (ppf.cpp:153-168): untrained model, fractions out of range, empty scene."""
+    from surface_match_gb300 import Detector, PointCloud, RangeError
+    mc, sc = data
+    with pytest.raises(RuntimeError, match="No trained model in matchScene"):
+        Detector().matchScene(PointCloud(sc.cloud.xyz), SD, KP, MS)
+    det = Detector()
+    det.trainModel(PointCloud(mc.xyz, mc.normal), SD)
+    for args, what in (((1.5, KP, MS), "samplingDistanceRel"), ((SD, -0.1, MS), "keyPointFraction"),
+                       ((SD, KP, 2.0), "minScore")):
+        with pytest.raises(RangeError, match=what):
+            det.matchScene(PointCloud(sc.cloud.xyz), *args)
+    with pytest.raises(RuntimeError, match="empty scene in matchScene"):
+        det.matchScene(PointCloud(np.zeros((0, 3), np.float32)), SD, KP, MS)
+
+
+def test_nan_points_like_the_oracle(data):
+    """Scenes with non-finite coordinates (removeNan, util.cpp:86-105): with 5% of the points
+    broken, every stage and the final poses are bit-exact against the oracle on the same
+    input; a scene with no finite point returns no pose."""
+    from oracle import MODE_GRID, MatchParam as OMP, Oracle
+    from surface_match_gb300 import Detector, MatchParam, PointCloud
+    mc, sc = data
+    xyz = sc.cloud.xyz.copy()
+    rng = np.random.default_rng(11)
+    bad = rng.choice(len(xyz), len(xyz) // 20, replace=False)
+    xyz[bad, rng.integers(0, 3, len(bad))] = np.nan
+    det = Detector()
+    det.trainModel(PointCloud(mc.xyz, mc.normal), SD)
+    poses, scores = det.matchScene(PointCloud(xyz, None, sc.viewpoint), SD, KP, MS,
+                                   MatchParam(numMatches=8))
+    o = Oracle(mode=MODE_GRID, threads=8)
+    m = o.train(mc.xyz, mc.normal, SD)
+    r = o.match(m, xyz, None, sc.viewpoint, SD, KP, MS, OMP(numMatches=8))
+    np.testing.assert_array_equal(det.debug(0), r.sampled)
+    np.testing.assert_array_equal(det.debug(1), r.keypoints)
+    np.testing.assert_array_equal(det.debug(7), r.kp_stats)
+    assert len(scores) == len(r.scores) > 0
+    np.testing.assert_array_equal(scores, r.scores)
+    np.testing.assert_array_equal(poses[:, :3, :].reshape(len(scores), -1), r.results[:, :12])
+    none, _ = det.matchScene(PointCloud(np.full((1000, 3), np.nan, np.float32)), SD, KP, MS)
+    assert len(none) == 0
+
+
+def test_workspace_reuse_across_scene_sizes():
+    """One detector matching scenes of alternating sizes (its workspace grows and is
+    reused, entries of earlier calls stay behind): every result equals a fresh detector's."""
+    from surface_match_gb300 import Detector, MatchParam, PointCloud, synth
+    mc, _, _ = synth.gear_model(8000, seed=5)
+    scenes = [synth.scene_small(seed=1), synth.scene_tiny(seed=3), synth.scene_small(seed=4),
+              synth.scene_tiny(seed=5, n_inst=3, pts=4000)]
+    param = MatchParam(numMatches=8)
+    det = Detector()
+    det.trainModel(PointCloud(mc.xyz, mc.normal), SD)
+    for sc in scenes + scenes[::-1]:
+        pc = PointCloud(sc.cloud.xyz, None, sc.viewpoint)
+        p1, s1 = det.matchScene(pc, SD, KP, MS, param)
+        fresh = Detector()
+        fresh.trainModel(PointCloud(mc.xyz, mc.normal), SD)
+        p2, s2 = fresh.matchScene(pc, SD, KP, MS, param)
+        np.testing.assert_array_equal(s1, s2)
+        np.testing.assert_array_equal(p1, p2)
