@@ -1,17 +1,17 @@
 // cluster.cu - pose clustering of matchScene (ppf.cpp:414-418): sortPoses, clusterPose,
 // avgClusters, sortPoses, clusterPose2 (util.cpp:486-601).
 //
-// Three kernels. k_cluster_a (one CTA): stable rank-by-counting sort on (votes desc, list
-// position), then clusterPose, a greedy first-fit clustering (a pose joins the first
-// earlier head it is compatible with). Its compatibility of every pose with every earlier
-// pose is evaluated in parallel into a bit matrix in shared memory; heads are then
-// resolved in parallel rounds (a pose compatible with a head is a member, one whose
-// compatible earlier poses are all members is a head), which reproduces the sequential
-// decisions, and a member's cluster is its lowest compatible head - the first in creation
-// order. Larger pose lists walk the poses with one warp instead. k_cluster_avg: one block
-// per cluster sums its members in pose order (FP32 translation, FP64 quaternion moments)
-// and averages them, so the clusters' FP64 work spreads over the SMs. k_cluster_b (one
-// CTA): the second sort and clusterPose2. Results are identical to the oracle's
+// Five kernels. k_cluster_rank (all CTAs): stable rank-by-counting sort on (votes desc,
+// list position). k_cluster_bits (all CTAs): the compatibility of every pose with every
+// earlier pose, as a bit matrix. k_cluster_a (one CTA): clusterPose, a greedy first-fit
+// clustering (a pose joins the first earlier head it is compatible with), resolved from the
+// bits (in shared memory) in parallel rounds (a pose compatible with a head is a member,
+// one whose compatible earlier poses are all members is a head), which reproduces the
+// sequential decisions; a member's cluster is its lowest compatible head - the first in
+// creation order. Larger pose lists walk the poses with one warp instead. k_cluster_avg:
+// one block per cluster sums its members in pose order (FP32 translation, FP64 quaternion
+// moments) and averages them, so the clusters' FP64 work spreads over the SMs. k_cluster_b
+// (one CTA): the second sort and clusterPose2. Results are identical to the oracle's
 // sequential restatement.
 #include <cmath>
 #include <cstring>
@@ -48,6 +48,7 @@ struct ClArgs {
     int         *nhOut;     // cluster count
     int          smemState; // per-pose state in shared memory
     int          useBits;   // compatibility bits in shared memory
+    uint32_t    *bitsG;     // W x np compatibility words (word-major), filled by k_cluster_bits
 };
 
 // out[rank(i)] = in[i] for the stable sort by votes (float 17) descending; `votes` holds
@@ -80,6 +81,49 @@ __device__ __forceinline__ bool compat(const float4 &a, const float4 &b, float s
     return x * x + (y * y + z * z) < sqThr && smm::fabs_(a.w - b.w) < angThr;
 }
 
+// sortPoses (util.cpp:486-491) as a stable rank by votes (float 17) descending, one thread
+// per pose over all CTAs: out[rank(i)] = in[i], with the sorted {tx, ty, tz, angle} keys
+// (gbuf4), {tx, ty, tz, votes} and quaternions. The lanes of a warp read the same vote at a
+// time (one cached transaction).
+__global__ void k_cluster_rank(ClArgs a) {
+    const int np = a.np;
+    const int i  = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np)
+        return;
+    const float v    = __ldg(&a.poses[(size_t)i * PF + 17]);
+    int         rank = 0;
+    for (int j = 0; j < np; j++) {
+        const float u = __ldg(&a.poses[(size_t)j * PF + 17]);
+        rank += (u > v || (u == v && j < i)) ? 1 : 0;
+    }
+    const float *P = a.poses + (size_t)i * PF;
+    for (int e = 0; e < PF; e++)
+        a.sorted[(size_t)rank * PF + e] = P[e];
+    a.gbuf4[rank] = make_float4(P[3], P[7], P[11], P[16]);
+    a.tv[rank]    = make_float4(P[3], P[7], P[11], P[17]);
+    a.qv[rank]    = make_float4(P[12], P[13], P[14], P[15]);
+}
+
+// Compatibility bits over all CTAs: word w of row i (bitsG[w * np + i]), bit b set when
+// sorted pose i is compatible with the earlier sorted pose 32 w + b.
+__global__ void k_cluster_bits(ClArgs a) {
+    const int  np = a.np, W = (np + 31) >> 5;
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)np * W)
+        return;
+    const int    w = (int)(idx / np), i = (int)(idx % np);
+    const float4 P = a.gbuf4[i];
+    uint32_t     m = 0;
+    if (w * 32 < i) {
+        for (int b = 0; b < 32; b++) {
+            const int j = w * 32 + b;
+            if (j < i && compat(P, a.gbuf4[j], a.sqThr, a.angThr))
+                m |= 1u << b;
+        }
+    }
+    a.bitsG[idx] = m;
+}
+
 __global__ void __launch_bounds__(kClBs) k_cluster_a(ClArgs a) {
     extern __shared__ float4 dsm4[];
     __shared__ int sNh;
@@ -96,27 +140,17 @@ __global__ void __launch_bounds__(kClBs) k_cluster_a(ClArgs a) {
     uint32_t      *newH  = unkB + W;                  // W
     uint32_t      *newM  = newH + W;                  // W
     int           *hpre  = (int *)(newM + W);         // W + 1
-    for (int i = tid; i < np; i += kClBs)
-        votes[i] = a.poses[(size_t)i * PF + 17];
-    __syncthreads();
-    stable_sort_votes(a.poses, votes, np, a.sorted, key, a.tv, a.qv);
+    (void)votes;
+    // the sorted keys (k_cluster_rank, in gbuf4) into shared memory
+    if (a.smemState)
+        for (int i = tid; i < np; i += kClBs)
+            key[i] = a.gbuf4[i];
     __syncthreads();
     if (a.useBits) {
-        // word w of row i (stored at bits[w * np + i]), bit b: pose i is compatible with the
-        // earlier pose 32 w + b
-        for (int idx = tid; idx < np * W; idx += kClBs) {
-            const int    w = idx / np, i = idx % np;
-            const float4 P = key[i];
-            uint32_t     m = 0;
-            if (w * 32 < i) {
-                for (int b = 0; b < 32; b++) {
-                    const int j = w * 32 + b;
-                    if (j < i && compat(P, key[j], a.sqThr, a.angThr))
-                        m |= 1u << b;
-                }
-            }
-            bits[idx] = m;
-        }
+        // the compatibility words of k_cluster_bits (bits[w * np + i], bit b: pose i is
+        // compatible with the earlier pose 32 w + b)
+        for (int idx = tid; idx < np * W; idx += kClBs)
+            bits[idx] = a.bitsG[idx];
         for (int w = tid; w < W; w += kClBs) {
             headB[w] = 0u;
             const int rem = np - w * 32;
@@ -274,36 +308,48 @@ __global__ void k_cluster_avg(ClArgs a) {
 }
 
 // sortPoses of the averaged clusters and clusterPose2 (overlap of the transformed model-box
-// centres); one block.
+// centres, util.cpp:522-551); one block. The greedy walk runs on one warp with the centres,
+// the leader list and the leaders' vote sums in shared memory (global memory beyond
+// kClMaxC clusters); the vote sums keep the sequential order of the walk, and the output
+// records are written by all threads afterwards.
 __global__ void __launch_bounds__(kClBs) k_cluster_b(ClArgs a) {
-    __shared__ int sNout;
-    const int      tid = threadIdx.x, lane = tid & 31;
-    const int      nh  = *a.nhOut;
-    float         *votes = (float *)a.gbuf;
+    __shared__ int    sNout;
+    __shared__ float4 sTr[kClMaxC];
+    __shared__ float  sVote[kClMaxC], sSum[kClMaxC];
+    __shared__ int    sLead[kClMaxC];
+    const int         tid = threadIdx.x, lane = tid & 31;
+    const int         nh  = *a.nhOut;
+    float            *votes = (float *)a.gbuf;
     for (int h = tid; h < nh; h += kClBs)
         votes[h] = a.avg[(size_t)h * PF + 17];
     __syncthreads();
     stable_sort_votes(a.avg, votes, nh, a.avgSorted, nullptr, nullptr, nullptr);
     __syncthreads();
+    const bool inSm = nh <= kClMaxC;
+    float4    *tr   = inSm ? sTr : a.tr;
+    float     *vote = inSm ? sVote : votes; // votes of the sorted clusters
+    float     *sum  = inSm ? sSum : votes + nh;
+    int       *lead = inSm ? sLead : a.heads;
     for (int h = tid; h < nh; h += kClBs) {
         smi::Pose34 T;
         for (int e = 0; e < 12; e++)
             T.m[e] = a.avgSorted[(size_t)h * PF + e];
         float x, y, z;
         smi::pose_apply(T, a.cx, a.cy, a.cz, x, y, z);
-        a.tr[h] = make_float4(x, y, z, 0.f);
+        tr[h]   = make_float4(x, y, z, 0.f);
+        vote[h] = a.avgSorted[(size_t)h * PF + 17];
     }
     __syncthreads();
     if (tid < 32) {
         int nl = 0;
         for (int i = 0; i < nh; i++) {
-            const float4 ti    = a.tr[i];
+            const float4 ti    = tr[i];
             int          found = -1;
             for (int h0 = 0; h0 < nl && found < 0; h0 += 32) {
                 const int h  = h0 + lane;
                 bool      ok = false;
                 if (h < nl) {
-                    const float4 th = a.tr[a.heads[h]];
+                    const float4 th = tr[lead[h]];
                     const float  dx = th.x - ti.x, dy = th.y - ti.y, dz = th.z - ti.z;
                     ok              = dx * dx + (dy * dy + dz * dz) < a.thr2;
                 }
@@ -313,13 +359,10 @@ __global__ void __launch_bounds__(kClBs) k_cluster_b(ClArgs a) {
             }
             if (lane == 0) {
                 if (found < 0) {
-                    a.heads[nl] = i; // heads[] reused: leaders of clusterPose2
-                    float *O    = a.out + (size_t)nl * PF;
-                    for (int e = 0; e < PF; e++)
-                        O[e] = a.avgSorted[(size_t)i * PF + e];
+                    lead[nl] = i;
+                    sum[nl]  = vote[i];
                 } else {
-                    float *O = a.out + (size_t)found * PF;
-                    O[17]    = O[17] + a.avgSorted[(size_t)i * PF + 17];
+                    sum[found] = sum[found] + vote[i];
                 }
             }
             if (found < 0)
@@ -330,8 +373,13 @@ __global__ void __launch_bounds__(kClBs) k_cluster_b(ClArgs a) {
             sNout = nl;
     }
     __syncthreads();
+    const int nl = sNout;
+    for (int idx = tid; idx < nl * PF; idx += kClBs) {
+        const int l = idx / PF, e = idx - l * PF;
+        a.out[idx]  = e == 17 ? sum[l] : a.avgSorted[(size_t)lead[l] * PF + e];
+    }
     if (tid == 0)
-        *a.outCount = sNout;
+        *a.outCount = nl;
 }
 
 // Smallest float v >= 0 with sqrtf(v) >= t (IEEE square root is correctly rounded and
@@ -393,6 +441,14 @@ int cluster(Ctx &c, const float *poses, int np, float distThr, float angThr, con
     const size_t smem  = a.smemState ? state + (a.useBits ? bitsB : 0) : 0;
     if (smem > allow_dynamic_smem((const void *)k_cluster_a, c.device))
         throw Error(SM_ERR_CAPACITY, "shared-memory request above the device limit");
+    k_cluster_rank<<<nblocks(np, 128), 128, 0, c.stream>>>(a);
+    SM_LAUNCH_CHECK();
+    a.bitsG = nullptr;
+    if (a.useBits) {
+        a.bitsG = c.arena.get<uint32_t>(tag + ".bits", (size_t)np * W);
+        k_cluster_bits<<<nblocks((long long)np * W, 256), 256, 0, c.stream>>>(a);
+        SM_LAUNCH_CHECK();
+    }
     k_cluster_a<<<1, kClBs, smem, c.stream>>>(a);
     SM_LAUNCH_CHECK();
     k_cluster_avg<<<std::min(np, 152 * 8), 32, 0, c.stream>>>(a);
