@@ -254,39 +254,69 @@ __global__ void __launch_bounds__(kClBs) k_cluster_a(ClArgs a) {
 }
 
 // avgClusters: one block per cluster (grid-stride); the warp finds the members in pose
-// order 32 at a time, lane 0 sums them in that order (mean translation, summed votes,
-// Markley quaternion average in FP64).
+// order (cluster numbers read 256 poses ahead) and sums them in that order, one sum per lane:
+// lane e < 10 the FP64 quaternion moment e, lanes 10..13 the FP32 translation and votes (the
+// same additions in the same order as one thread summing all of them); then the Markley
+// quaternion average in FP64.
 __global__ void k_cluster_avg(ClArgs a) {
     const int lane = threadIdx.x & 31;
     const int nh   = *a.nhOut;
+    // moment e of lane e: q[r] * q[s] over the upper triangle in row order
+    int er = 0, es = 0;
+    for (int r = 0, e = 0; r < 4; r++)
+        for (int s2 = r; s2 < 4; s2++, e++)
+            if (e == lane) {
+                er = r;
+                es = s2;
+            }
     for (int h = blockIdx.x; h < nh; h += gridDim.x) {
         const int head = a.heads[h];
-        float     px = 0.f, py = 0.f, pz = 0.f, vs = 0.f;
-        double    S[10];
-        for (int e = 0; e < 10; e++)
-            S[e] = 0.0;
-        int cnt = 0;
-        for (int base = head; base < a.np; base += 32) {
-            const int      i   = base + lane;
-            const bool     mem = i < a.np && a.clu[i] == h;
-            const uint32_t m   = __ballot_sync(0xffffffffu, mem);
-            if (lane == 0) {
+        double    Sd   = 0.0; // lane e < 10: moment e
+        float     Pf   = 0.0f; // lanes 10..13: tx, ty, tz, votes
+        int       cnt  = 0;
+        for (int base = head; base < a.np; base += 32 * 8) {
+            int cl[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int i = base + u * 32 + lane;
+                cl[u]       = i < a.np ? a.clu[i] : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int      i   = base + u * 32 + lane;
+                const bool     mem = cl[u] == h;
+                const uint32_t m   = __ballot_sync(0xffffffffu, mem);
+                if (!m)
+                    continue;
+                float4 t = make_float4(0.f, 0.f, 0.f, 0.f), q4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (mem) {
+                    t  = a.tv[i];
+                    q4 = a.qv[i];
+                }
                 for (uint32_t r = m; r; r &= r - 1) {
-                    const int    k  = base + __ffs(r) - 1;
-                    const float4 t = a.tv[k], q4 = a.qv[k];
-                    px             = px + t.x;
-                    py             = py + t.y;
-                    pz             = pz + t.z;
-                    vs             = vs + t.w;
-                    const double v[4] = {q4.x, q4.y, q4.z, q4.w};
-                    int          e    = 0;
-                    for (int rr = 0; rr < 4; rr++)
-                        for (int ss = rr; ss < 4; ss++)
-                            S[e++] += v[rr] * v[ss];
+                    const int   src = __ffs(r) - 1;
+                    const float tv[4] = {__shfl_sync(0xffffffffu, t.x, src),
+                                         __shfl_sync(0xffffffffu, t.y, src),
+                                         __shfl_sync(0xffffffffu, t.z, src),
+                                         __shfl_sync(0xffffffffu, t.w, src)};
+                    const float qv[4] = {__shfl_sync(0xffffffffu, q4.x, src),
+                                         __shfl_sync(0xffffffffu, q4.y, src),
+                                         __shfl_sync(0xffffffffu, q4.z, src),
+                                         __shfl_sync(0xffffffffu, q4.w, src)};
+                    if (lane < 10)
+                        Sd += (double)qv[er] * (double)qv[es];
+                    else if (lane < 14)
+                        Pf = Pf + tv[lane - 10];
                     cnt++;
                 }
             }
         }
+        double S[10];
+#pragma unroll
+        for (int e = 0; e < 10; e++)
+            S[e] = __shfl_sync(0xffffffffu, Sd, e);
+        const float px = __shfl_sync(0xffffffffu, Pf, 10), py = __shfl_sync(0xffffffffu, Pf, 11),
+                    pz = __shfl_sync(0xffffffffu, Pf, 12), vs = __shfl_sync(0xffffffffu, Pf, 13);
         if (lane != 0)
             continue;
         double q[4], R[9];

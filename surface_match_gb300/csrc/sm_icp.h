@@ -165,27 +165,21 @@ SM_HD Pose34 step_pose(const double u[6], const float Pm[3], const float Qm[3]) 
         a[1]            = u[1] * ia;
         a[2]            = u[2] * ia;
     }
+    // W = [a]x and W^2 = a a^T - (a.a) I; R_i = I + sin(t) W + (1 - cos(t)) W^2 with
+    // sin(t) = sn, cos(t) = cs, and R = R_i^2 = I + sin(2t) W + (1 - cos(2t)) W^2 with
+    // sin(2t) = 2 sn cs, 1 - cos(2t) = 2 sn^2 (the same rotation, by the double angle)
     const double W[3][3] = {{0.0, -a[2], a[1]}, {a[2], 0.0, -a[0]}, {-a[1], a[0], 0.0}};
+    const double aa      = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+    const double s1 = sn, c1 = 1.0 - cs, s2 = 2.0 * sn * cs, c2 = 2.0 * sn * sn;
     double       Ri[3][3], R[3][3];
     SML_UNROLL
     for (int i = 0; i < 3; i++)
         SML_UNROLL
         for (int j = 0; j < 3; j++) {
-            double w2 = 0.0;
-            SML_UNROLL
-            for (int m = 0; m < 3; m++)
-                w2 += W[i][m] * W[m][j];
-            Ri[i][j] = (i == j ? 1.0 : 0.0) + sn * W[i][j] + (1.0 - cs) * w2;
-        }
-    SML_UNROLL
-    for (int i = 0; i < 3; i++)
-        SML_UNROLL
-        for (int j = 0; j < 3; j++) {
-            double s = 0.0;
-            SML_UNROLL
-            for (int m = 0; m < 3; m++)
-                s += Ri[i][m] * Ri[m][j];
-            R[i][j] = s;
+            const double w2 = a[i] * a[j] - (i == j ? aa : 0.0);
+            const double id = i == j ? 1.0 : 0.0;
+            Ri[i][j]        = id + s1 * W[i][j] + c1 * w2;
+            R[i][j]         = id + s2 * W[i][j] + c2 * w2;
         }
     const double tt[3] = {cs * u[3], cs * u[4], cs * u[5]};
     Pose34       o;
