@@ -120,6 +120,22 @@ def cpu_match(model_xyz, model_nrm, scene, threads):
     return time.perf_counter() - t, r
 
 
+def job_totals(totals_ms, dist=None, device="cpu"):
+    """The job's timed totals (ms): each the maximum over ranks (the job ends with its
+    slowest rank); `dist` is torch.distributed when several ranks run, else None."""
+    if dist is None:
+        return [float(t) for t in totals_ms]
+    import torch
+    t = torch.tensor([float(x) for x in totals_ms], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
+def job_rate(world, steps, total_ms):
+    """Whole-job scenes/s: every rank matched `steps` scenes (replicas, weak scaling)."""
+    return world * steps / (total_ms / 1000.0)
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -502,14 +518,9 @@ def main():
         sampler.wait()
         sf.close()
     clocks = read_clocks(clk_path, local) if clk_path else {"sm_mhz": None}
-    tot = sum(dev_ms)
-    tot_e2e = sum(e2e_ms)
-    if dist:
-        t = torch.tensor([tot, tot_e2e], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot, tot_e2e = float(t[0]), float(t[1])
-    value = world * args.steps / (tot / 1000.0)
-    e2e = world * args.steps / (tot_e2e / 1000.0)
+    tot, tot_e2e = job_totals([sum(dev_ms), sum(e2e_ms)], dist, "cuda")
+    value = job_rate(world, args.steps, tot)
+    e2e = job_rate(world, args.steps, tot_e2e)
     votes = stats["n_votes"]
     pairs = stats["n_pairs"]
     vk = statistics.median(vote_ms)  # k_vote_acc, CUDA events on the matching stream
