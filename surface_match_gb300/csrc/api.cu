@@ -388,8 +388,6 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
         }
         return;
     }
-    float ext[3] = {box.ext(0), box.ext(1), box.ext(2)};
-
     const float diam         = m.box.diameter();
     const int   A            = m.tp.featAngleResolution;
     const float angleStep    = smm::k2PiF / (float)A;
