@@ -83,17 +83,22 @@ __device__ __forceinline__ bool compat(const float4 &a, const float4 &b, float s
 
 // sortPoses (util.cpp:486-491) as a stable rank by votes (float 17) descending, one thread
 // per pose over all CTAs: out[rank(i)] = in[i], with the sorted {tx, ty, tz, angle} keys
-// (gbuf4), {tx, ty, tz, votes} and quaternions. The lanes of a warp read the same vote at a
-// time (one cached transaction).
+// (gbuf4), {tx, ty, tz, votes} and quaternions. The votes are staged per CTA in shared
+// memory (all lanes read the same one at a time: a broadcast).
 __global__ void k_cluster_rank(ClArgs a) {
-    const int np = a.np;
-    const int i  = blockIdx.x * blockDim.x + threadIdx.x;
+    constexpr int kStage = 8192; // votes staged in shared memory (the rest read from L1/L2)
+    __shared__ float sv[kStage];
+    const int        np = a.np, ns = min(np, kStage);
+    for (int j = threadIdx.x; j < ns; j += blockDim.x)
+        sv[j] = a.poses[(size_t)j * PF + 17];
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np)
         return;
-    const float v    = __ldg(&a.poses[(size_t)i * PF + 17]);
+    const float v    = i < ns ? sv[i] : __ldg(&a.poses[(size_t)i * PF + 17]);
     int         rank = 0;
     for (int j = 0; j < np; j++) {
-        const float u = __ldg(&a.poses[(size_t)j * PF + 17]);
+        const float u = j < ns ? sv[j] : __ldg(&a.poses[(size_t)j * PF + 17]);
         rank += (u > v || (u == v && j < i)) ? 1 : 0;
     }
     const float *P = a.poses + (size_t)i * PF;

@@ -266,7 +266,8 @@ __global__ void k_phase_offsets(int *__restrict__ ph) {
     }
 }
 
-// Placing pass: the point's position (index in w) at its cell slot; the point in slot 0
+// Placing pass: the point's position (its place i in the ascending id list in w: list order
+// is index order) at its cell slot; the point in slot 0
 // lists the cell in its phase (any order: cells of one phase do not interact) and records
 // rankCnt[cell] = {its list slot (the index of the cell's kept-point record), 0 kept}.
 __global__ void k_grid_scatter(const float4 *__restrict__ pos, const int *__restrict__ ids, int m,
@@ -281,7 +282,7 @@ __global__ void k_grid_scatter(const float4 *__restrict__ pos, const int *__rest
     const int    c  = cellOf[i];
     const float4 p  = pos[id];
     const int    k  = sub[i];
-    pts[start[c] + k] = make_float4(p.x, p.y, p.z, __int_as_float(id));
+    pts[start[c] + k] = make_float4(p.x, p.y, p.z, __int_as_float(i));
     if (k == 0) {
         const int cx = c % dim0, cy = (c / dim0) % dim1, cz = c / (dim0 * dim1);
         const int slot = atomicAdd(&ph[16 + smg::phase_of(cx, cy, cz)], 1);
@@ -302,10 +303,11 @@ constexpr int kSpStage = 256; // neighbours' kept points staged in shared memory
 // smallest surviving index, drop the survivors within the step of it" - the same kept set
 // as the sequential visit, at (kept points x cell size / 32) work and without sorting.
 // Kept points are recorded as positions (keptPos, `cap` per cell) and their number in
-// rankCnt[cell].y, next to the cell's record index (one load per neighbour). The
-// neighbours' kept points and the cell's points (positions with the index in w, contiguous
-// per cell) are staged in shared memory; cells too large for the staging buffers take the
-// same steps in global memory (`alive` flags in aliveTmp).
+// rankCnt[cell].y, next to the cell's record index (one load per neighbour). Points are
+// named by their place in the ascending id list (same order as the index), and keptFlag is
+// over those places. The neighbours' kept points and the cell's points (positions with the
+// place in w, contiguous per cell) are staged in shared memory; cells too large for the
+// staging buffers take the same steps in global memory (`alive` flags in aliveTmp).
 __global__ void __launch_bounds__(kSpWarps * 32)
     k_sample_phase(GridView G, const int *__restrict__ lists, const int *__restrict__ ph,
                    int phase, int2 *__restrict__ rankCnt, float4 *__restrict__ keptPos, int cap,
@@ -941,9 +943,9 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
     const int    cap = (int)std::floor((s + 1.0) * (s + 1.0) * (s + 1.0) / (3.14159265358979 / 6.0)) + 1;
     float4 *keptPos  = c.arena.get<float4>(tag + ".kp", (size_t)maxOcc * cap);
     int    *aliveTmp = c.arena.get<int>(tag + ".al", std::max(m, 1));
-    int    *keptFlag = c.arena.get<int>(tag + ".kf", std::max(npoints, 1) + 1);
-    int    *overflow = keptFlag + npoints;
-    SM_CUDA(cudaMemsetAsync(keptFlag, 0, (npoints + 1) * sizeof(int), c.stream));
+    int    *keptFlag = c.arena.get<int>(tag + ".kf", (size_t)m + 1); // over the list places
+    int    *overflow = keptFlag + m;
+    SM_CUDA(cudaMemsetAsync(keptFlag, 0, ((size_t)m + 1) * sizeof(int), c.stream));
     const float r2 = step * step;
     const int   gp = (int)std::min<long long>((maxOcc + kSpWarps - 1) / kSpWarps, 152LL * 16);
     for (int p = 0; p < 8; p++) {
@@ -952,10 +954,10 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
                                                            aliveTmp);
         SM_LAUNCH_CHECK();
     }
-    // the kept points in index order, and the overflow flag, in one round trip
-    int *pre   = c.arena.get<int>(tag + ".out.pre", std::max(npoints, 1));
-    int *total = scan_flags_total(c, keptFlag, pre, npoints, tag + ".out");
-    k_scatter_flags<<<nblocks(npoints, 256), 256, 0, c.stream>>>(keptFlag, pre, npoints, kNoEq, outIds);
+    // the kept points in index order (list order), and the overflow flag, in one round trip
+    int *pre   = c.arena.get<int>(tag + ".out.pre", std::max(m, 1));
+    int *total = scan_flags_total(c, keptFlag, pre, m, tag + ".out");
+    k_scatter_ids<<<nblocks(m, 256), 256, 0, c.stream>>>(keptFlag, pre, m, ids, outIds);
     SM_LAUNCH_CHECK();
     SM_CUDA(cudaMemcpyAsync(c.hostCounts, total, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     SM_CUDA(cudaMemcpyAsync(c.hostCounts + 1, overflow, sizeof(int), cudaMemcpyDeviceToHost, c.stream));

@@ -63,8 +63,8 @@ void build_hgrid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &bo
 // subPos[r] = pos[ids[r]], subNrm[r] = nrm[ids[r]] for r < m.
 void gather_subset(Ctx &c, const float4 *pos, const float4 *nrm, const int *ids, int m,
                    float4 *subPos, float4 *subNrm);
-// Greedy thinning at `step` in (phase, cell, index) order; writes kept ids ascending,
-// returns their count.
+// Greedy thinning of ids[0..m) (ascending) at `step` in (phase, cell, index) order; writes
+// kept ids ascending, returns their count.
 int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m, const Box &box,
                   float step, int *outIds, const std::string &tag);
 // Two-phase normal estimation of ids[0..m) (see sm_oracle.cpp estimate_normals).
