@@ -363,6 +363,10 @@ void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const in
           const VoteOut &out, int dumpK) {
     if (K <= 0)
         return;
+    // rows (keypoint, neighbour) are counted and offset in 32-bit ints: at most K x ncand in
+    // radius mode (every candidate a neighbour of every keypoint)
+    if (!nbrOff && (long long)K * (long long)ncand > 0x7fffffffll)
+        throw Error(SM_ERR_CAPACITY, "too many keypoint x sampled point pairs for one call");
     VoteArgs a{};
     fill_vote_model(m, minScore, a);
     a.pos    = pos;
