@@ -523,7 +523,7 @@ def main():
     e2e = job_rate(world, args.steps, tot_e2e)
     votes = stats["n_votes"]
     pairs = stats["n_pairs"]
-    vk = statistics.median(vote_ms)  # k_vote_acc, CUDA events on the matching stream
+    vk = statistics.mean(vote_ms)  # k_vote_acc: mean launch time, CUDA events on its stream
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -575,7 +575,7 @@ def main():
                              "probe": "sm_probe_vote_atomics: 16-bit shared counters at "
                                       "pseudo-random cells of a 48 KB accumulator, 512-thread "
                                       "CTAs, 2 per SM (one vote = one increment)"}},
-            "vote_stage_ms": {"pairs_probe_k_ppf": statistics.median(ppf_ms),
+            "vote_stage_ms": {"pairs_probe_k_ppf": statistics.mean(ppf_ms),
                               "accumulate_k_vote_acc": vk,
                               "stage": stats["ms"][3]},
             "clocks": clocks}
