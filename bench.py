@@ -500,9 +500,9 @@ def main():
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    sampler, sf = start_clock_sampler(os.path.join(ROOT, "gpurun_out", f"clocks_r{rank}.csv")
-                                      if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
-                                      else f"/tmp/sm_clocks_r{rank}.csv")
+    import tempfile
+    clk_dir = os.environ.get("SM_CLOCKS_DIR") or tempfile.gettempdir()
+    sampler, sf = start_clock_sampler(os.path.join(clk_dir, f"sm_clocks_r{rank}.csv"))
     clk_path = sf.name if sf else None
     torch.cuda.synchronize()
     vote_ms = []
