@@ -45,7 +45,10 @@ struct Vec3f {
 };
 struct Vec3i {
     int v[3] = {0, 0, 0};
-    int &operator[](int i) { return v[i]; }
+    Vec3i() = default;
+    Vec3i(int a, int b, int c) : v{a, b, c} {}
+    int       &operator[](int i) { return v[i]; }
+    const int &operator[](int i) const { return v[i]; }
 };
 struct Mat4f { // row-major storage, (r, c) access like Eigen
     float  m[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};

@@ -87,10 +87,12 @@ class MatchParam:
 
 @dataclass
 class PointCloud:
-    """ppf::PointCloud (type.h:22-33): points, optional normals, optional viewpoint."""
+    """ppf::PointCloud (type.h:22-33): points, optional normals, optional viewpoint,
+    optional triangles (mesh models read from PLY files)."""
     point: object
     normal: object = None
     viewPoint: object = None
+    face: object = None
 
 
 @dataclass
