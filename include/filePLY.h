@@ -1,5 +1,5 @@
 /*
- * ply.h - PLY point-cloud / mesh files for ppf::PointCloud (the reference's filePLY.h:6-9:
+ * filePLY.h - PLY point-cloud / mesh files for ppf::PointCloud (the reference's filePLY.h:6-9:
  * readPLY, writePLY), header-only, written from the PLY format description (Turk, "The PLY
  * Polygon File Format"): ASCII and binary (either byte order) files, any scalar property
  * type, list properties. readPLY takes the vertex element's x, y, z (and nx, ny, nz when all

@@ -1,5 +1,5 @@
 """PLY point-cloud / mesh files (the reference's filePLY.h:6-9 readPLY / writePLY), the
-Python counterpart of include/ply.h with the same rules: ASCII and binary files of either
+Python counterpart of include/filePLY.h with the same rules: ASCII and binary files of either
 byte order, any scalar type, list properties; the vertex element's x, y, z (and nx, ny, nz
 when all three are present) and the face element's vertex_indices / vertex_index lists,
 polygons with more than three corners cut into triangles by ear clipping (convex about

@@ -1,4 +1,4 @@
-"""PLY files (the reference's filePLY.h readPLY / writePLY): the C++ header include/ply.h and
+"""PLY files (the reference's filePLY.h readPLY / writePLY): the C++ header include/filePLY.h and
 the Python module read the same files to the same clouds - ASCII and binary of both byte
 orders, foreign properties and elements skipped, polygons cut into triangles - and each
 writer's files read back unchanged. CPU only."""
@@ -13,7 +13,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 CPP = r'''
 #include <ppf.h>
-#include <ply.h>
+#include <filePLY.h>
 #include <cstdio>
 // usage: t read <in.ply> <out.txt> | t write <in.txt> <out.ply> <ascii 0/1>
 int main(int argc, char **argv) {
