@@ -587,6 +587,18 @@ def main():
                                           "in reference (k-d tree) order, OpenMP 8 threads "
                                           "(the reference's cap, ppf.cpp:23)",
                                 "votes_per_s": float(r.kp_stats[:, 3].sum()) / dt}
+        # end-to-end agreement at full size with that run (reference search order): same
+        # instances, poses within the tolerance modulo the gear's symmetries
+        from surface_match_gb300 import synth
+        gpu_poses, _ = step(xyz_host)
+        ref = [np.vstack([Q, [0, 0, 0, 1]]) for Q in r.poses]
+        err = synth.match_poses(gpu_poses, ref, synth.gear_symmetries())
+        diam = float(np.linalg.norm(model.xyz.max(0) - model.xyz.min(0)))
+        line["reference_order_parity"] = {
+            "instances_gpu": int(len(gpu_poses)), "instances_reference_order": int(len(ref)),
+            "max_rotation_deg": max((e[0] for e in err), default=0.0),
+            "max_translation_mm": max((e[1] for e in err), default=0.0),
+            "tolerance": {"rotation_deg": 0.1, "translation_mm": 1e-3 * diam}}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

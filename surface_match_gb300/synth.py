@@ -483,3 +483,43 @@ def serving_models(seed=31):
     for k, (name, s) in enumerate(surfs.items()):
         out[name] = model_cloud(name, 20000, seed + k, surface=s)
     return out
+
+
+def gear_symmetries(teeth=24):
+    """Rotations mapping the procedural spur gear onto itself (model frame): turns about z
+    by a tooth pitch, and half-turns about the in-plane axes through tooth and gap
+    centres."""
+    out = []
+    pitch = 2 * np.pi / teeth
+    for k in range(teeth):
+        a = k * pitch
+        out.append(np.array([[np.cos(a), -np.sin(a), 0], [np.sin(a), np.cos(a), 0], [0, 0, 1]]))
+    for k in range(teeth):
+        phi = 0.25 * pitch + k * 0.5 * pitch
+        u = np.array([np.cos(phi), np.sin(phi), 0.0])
+        out.append(2 * np.outer(u, u) - np.eye(3))
+    return out
+
+
+def pose_error_sym(A, B, syms):
+    """Rotation (deg) and translation error between 4x4 poses A and B of a symmetric model:
+    B = A * S for the symmetry S closest to A^-1 B."""
+    Ra, Rb = A[:3, :3].astype(np.float64), B[:3, :3].astype(np.float64)
+    Rs = Ra.T @ Rb
+    ang = min(np.degrees(np.arccos(np.clip((np.trace(S.T @ Rs) - 1) / 2, -1, 1))) for S in syms)
+    return ang, float(np.linalg.norm(A[:3, 3].astype(np.float64) - B[:3, 3]))
+
+
+def match_poses(poses, ref_poses, syms):
+    """Each pose paired with the unused reference pose nearest to it (rotation error modulo
+    the symmetries, then translation); returns [(rotation deg, translation)]."""
+    used, out = set(), []
+    for P in poses:
+        cands = [(i,) + pose_error_sym(P, Q, syms) for i, Q in enumerate(ref_poses) if i not in used]
+        if not cands:
+            break
+        best = min(cands, key=lambda t: t[2])
+        used.add(best[0])
+        out.append(best[1:])
+    return out
+

@@ -160,47 +160,18 @@ def test_vote_kernel_counter_widths_and_passes(data, dist_rel, angles, wide, mon
     np.testing.assert_array_equal(emitted.view(np.uint32), r.pose_list.view(np.uint32))
 
 
-def gear_symmetries(teeth=24):
-    """Rotations mapping the procedural spur gear onto itself (model frame): turns about z
-    by a tooth pitch, and half-turns about the in-plane axes through tooth and gap
-    centres."""
-    out = []
-    pitch = 2 * np.pi / teeth
-    for k in range(teeth):
-        a = k * pitch
-        out.append(np.array([[np.cos(a), -np.sin(a), 0], [np.sin(a), np.cos(a), 0], [0, 0, 1]]))
-    for k in range(teeth):
-        phi = 0.25 * pitch + k * 0.5 * pitch
-        u = np.array([np.cos(phi), np.sin(phi), 0.0])
-        out.append(2 * np.outer(u, u) - np.eye(3))
-    return out
-
-
-def pose_err_sym(A, B, syms):
-    """Rotation (deg) and translation error between poses A and B of a symmetric model:
-    B = A * S for the symmetry S closest to A^-1 B."""
-    Ra, Rb = A[:3, :3].astype(np.float64), B[:3, :3].astype(np.float64)
-    Rs = Ra.T @ Rb
-    ang = min(np.degrees(np.arccos(np.clip((np.trace(S.T @ Rs) - 1) / 2, -1, 1)))
-              for S in syms)
-    return ang, float(np.linalg.norm(A[:3, 3].astype(np.float64) - B[:3, 3]))
-
-
 def test_poses_within_tolerance_of_reference_order(gpu, oracle_ref, data):
     """End to end against the reference-order pipeline (k-d tree sampling and neighbour
     order): same instance count; each GPU pose within 0.1 deg / 1e-3 * diameter of the
     reference-order pose it matches, modulo the gear's symmetry group."""
+    from surface_match_gb300 import synth
     det, poses, scores = gpu
     m, r = oracle_ref
     diam = float(np.linalg.norm(m.box[3:] - m.box[:3]))
-    syms = gear_symmetries()
     assert len(scores) == len(r.scores)
-    used = set()
-    for P in poses:
-        best = min(((i,) + pose_err_sym(P, np.vstack([Q, [0, 0, 0, 1]]), syms)
-                    for i, Q in enumerate(r.poses) if i not in used), key=lambda t: t[2])
-        used.add(best[0])
-        assert best[1] < 0.1 and best[2] < 1e-3 * diam, best
+    ref = [np.vstack([Q, [0, 0, 0, 1]]) for Q in r.poses]
+    for rot, tr in synth.match_poses(poses, ref, synth.gear_symmetries()):
+        assert rot < 0.1 and tr < 1e-3 * diam, (rot, tr)
 
 
 def test_vote_atomic_probe_rate_is_plausible():
