@@ -283,4 +283,36 @@ private:
     bool       trained_ = false;
 };
 
+// estimateNormalMLS (privateUtil.h:13, util.cpp:336-457) on the device: moving-least-squares
+// normals and projected points of the listed points (all when `indices` is empty), in
+// place, oriented toward pc.viewPoint (or +z) and reversed when `invert`; normals are
+// created as NaN when the cloud has none. The reference passes the k-d tree to search; the
+// device builds its own search structure over the cloud's finite points. `order` is 1..4.
+inline void estimateNormalMLS(PointCloud &pc, const std::vector<std::size_t> &indices, float radius,
+                              int order, bool invert = false) {
+    if (pc.point.empty())
+        return;
+    const std::size_t        n   = pc.point.size();
+    const std::vector<float> xyz = detail::flat(pc.point);
+    std::vector<float>       nrm;
+    if (pc.hasNormal())
+        nrm = detail::flat(pc.normal);
+    std::vector<int64_t> idx(indices.begin(), indices.end());
+    std::vector<float>   outP(n * 3), outN(n * 3);
+    const float vp[3] = {pc.viewPoint[0], pc.viewPoint[1], pc.viewPoint[2]};
+    sm_context  ctx   = nullptr;
+    detail::check(sm_context_create(0, nullptr, &ctx));
+    const int st = sm_estimate_normals_mls(ctx, xyz.data(), nrm.empty() ? nullptr : nrm.data(),
+                                           (int64_t)n, idx.empty() ? nullptr : idx.data(),
+                                           (int64_t)idx.size(), radius, order, invert ? 1 : 0, vp,
+                                           outP.data(), outN.data());
+    sm_context_destroy(ctx);
+    detail::check(st);
+    pc.normal.resize(n);
+    for (std::size_t i = 0; i < n; i++) {
+        pc.point[i]  = Vec3f(outP[3 * i], outP[3 * i + 1], outP[3 * i + 2]);
+        pc.normal[i] = Vec3f(outN[3 * i], outN[3 * i + 1], outN[3 * i + 2]);
+    }
+}
+
 } // namespace ppf

@@ -246,6 +246,27 @@ SM_API int64_t sm_launch_count(void);
  * Used as the denominator of the vote kernel's roofline; no counterpart in the reference. */
 SM_API int sm_probe_vote_atomics(int device, double *atomics_per_second);
 
+/* Moving-least-squares normals and surface projection (estimateNormalMLS,
+ * privateUtil.h:13, util.cpp:336-457; the reference declares it privately and builds the
+ * k-d tree it takes from the cloud). For each point that `indices` lists (n_indices of
+ * them, host int64 in [0, n); NULL: every point) and that has at least 3 finite points
+ * closer than |radius|: the PCA plane of those neighbours, a weighted least-squares fit of
+ * the polynomial of total degree `order` (1..4) over the plane, and the point moved onto
+ * the fit with its normal, oriented toward view_point (3 floats; NULL or non-finite: +z)
+ * and reversed when `invert`. out_xyz and out_normal (n x 3, host or device) receive the
+ * input points and normals (NaN where `normal` is NULL) with the listed points' results in
+ * place; points that stop after the PCA step (order <= 1 with fewer neighbours than
+ * coefficients, or a fit that is not positive definite) get the PCA normal and keep their
+ * position. Neighbourhoods are read from the input positions (the reference moves points
+ * in place while other threads read them). SM_ERR_ARG: order outside 1..4 (the
+ * reference's order 0 reads past its coefficient vector), a non-finite radius or an index
+ * out of range. */
+SM_API int sm_estimate_normals_mls(sm_context ctx, const float *xyz, const float *normal,
+                                   int64_t n, const int64_t *indices, int64_t n_indices,
+                                   float radius, int order, int invert,
+                                   const float *view_point, float *out_xyz,
+                                   float *out_normal);
+
 #ifdef __cplusplus
 }
 #endif

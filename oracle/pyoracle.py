@@ -76,6 +76,8 @@ def lib():
                 getattr(L, nm).argtypes = [C.c_float]
             L.orc_murmur4.restype = C.c_uint32
             L.orc_murmur4.argtypes = [u32p]
+            L.orc_mls.argtypes = [f32p, C.c_int64, i64p, C.c_int64, C.c_float, C.c_int, C.c_int,
+                                  f32p, f32p, f32p, i32p]
             L.orc_kd_probe.restype = C.c_int64
             L.orc_kd_probe.argtypes = [f32p, C.c_int64, f32p, f32p, C.c_float, i32p, i32p,
                                        C.c_int64]
@@ -275,3 +277,20 @@ class Oracle:
                              _p(stats, C.c_int64), _p(cands), _p(poses), dump_k,
                              _p(acc, C.c_int32))
         return stats, cands, poses, acc
+
+
+def mls(xyz, normal=None, indices=None, radius=1.0, order=2, invert=False, viewpoint=None):
+    """estimateNormalMLS (util.cpp:336-457) by the FP64 restatement: returns the points,
+    the normals (inputs, NaN where absent, with the listed points' results in place) and the
+    status of each listed point (0 unchanged, 1 PCA normal only, 2 moved onto the fit)."""
+    pts = np.ascontiguousarray(xyz, np.float32).reshape(-1, 3)
+    n = len(pts)
+    idx = np.arange(n, dtype=np.int64) if indices is None else np.ascontiguousarray(indices, np.int64)
+    out_p = pts.copy()
+    out_n = (np.full((n, 3), np.nan, np.float32) if normal is None
+             else np.ascontiguousarray(normal, np.float32).reshape(-1, 3).copy())
+    vp = None if viewpoint is None else np.ascontiguousarray(viewpoint, np.float32)
+    status = np.zeros(len(idx), np.int32)
+    lib().orc_mls(_p(pts), n, _p(idx, C.c_int64), len(idx), float(radius), int(order),
+                  1 if invert else 0, _p(vp), _p(out_p), _p(out_n), _p(status, C.c_int32))
+    return out_p, out_n, status

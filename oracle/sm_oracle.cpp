@@ -1496,3 +1496,144 @@ extern "C" void orc_grid_probe(const float *xyz, int64_t n, const float *qs, int
         within[j] = G.any_within(q, r2) ? 1 : 0;
     }
 }
+
+// estimateNormalMLS (util.cpp:336-457) restated in FP64 and unscaled coordinates, the
+// reference's steps in its order: neighbours closer than the radius (the k-d tree's float
+// metric, nanoflann.hpp:545-579, over the finite points, found here by a scan in index
+// order); fewer than 3 leave the point unchanged (util.cpp:363-364); PCA normal of the
+// neighbourhood (util.cpp:368-381); the query projected on its plane and the frame
+// v = unitOrthogonal(n), u = n x v (util.cpp:383-390); order <= 1 with fewer neighbours
+// than coefficients stops there (util.cpp:393-394); the weighted polynomial fit solved by
+// Cholesky (util.cpp:395-436); the point and normal from the fit and the orientation
+// (util.cpp:439-455). Neighbourhoods read the input positions (two-phase, like the GPU).
+// status[i] of listed point i: 0 unchanged, 1 PCA normal only, 2 moved onto the fit.
+namespace {
+
+// Eigen's unitOrthogonal for 3-vectors: (-y, x, 0) normalised unless x and y are both
+// much smaller than z (|.| <= 1e-5 |z|, the float dummy precision), else (0, -z, y)
+// normalised.
+void unit_orthogonal(const double n[3], double v[3]) {
+    const double eps = 1e-5;
+    if (!(std::fabs(n[0]) <= std::fabs(n[2]) * eps) || !(std::fabs(n[1]) <= std::fabs(n[2]) * eps)) {
+        const double h = 1.0 / std::sqrt(n[0] * n[0] + n[1] * n[1]);
+        v[0] = -n[1] * h, v[1] = n[0] * h, v[2] = 0.0;
+    } else {
+        const double h = 1.0 / std::sqrt(n[1] * n[1] + n[2] * n[2]);
+        v[0] = 0.0, v[1] = -n[2] * h, v[2] = n[1] * h;
+    }
+}
+
+// G c = b for symmetric positive definite G (row-major n x n), by the LLT factorisation;
+// false when a pivot is not positive or the solution is not finite.
+bool llt_solve(std::vector<double> G, std::vector<double> &b, int n) {
+    for (int j = 0; j < n; j++) {
+        double d = G[j * n + j];
+        for (int k = 0; k < j; k++) d -= G[j * n + k] * G[j * n + k];
+        if (!(d > 0.0)) return false;
+        G[j * n + j] = std::sqrt(d);
+        for (int i = j + 1; i < n; i++) {
+            double v = G[i * n + j];
+            for (int k = 0; k < j; k++) v -= G[i * n + k] * G[j * n + k];
+            G[i * n + j] = v / G[j * n + j];
+        }
+    }
+    for (int i = 0; i < n; i++) {
+        for (int k = 0; k < i; k++) b[i] -= G[i * n + k] * b[k];
+        b[i] /= G[i * n + i];
+    }
+    for (int i = n - 1; i >= 0; i--) {
+        for (int k = i + 1; k < n; k++) b[i] -= G[k * n + i] * b[k];
+        b[i] /= G[i * n + i];
+        if (!std::isfinite(b[i])) return false;
+    }
+    return true;
+}
+
+} // namespace
+
+extern "C" void orc_mls(const float *xyz, int64_t n, const int64_t *idx, int64_t m, float radius,
+                        int order, int invert, const float *vp, float *outXyz, float *outNrm,
+                        int *status) {
+    const float r2 = radius * radius;
+    const int   nc = (order + 1) * (order + 2) / 2;
+    const bool  hasVp = vp && std::isfinite(vp[0]) && std::isfinite(vp[1]) && std::isfinite(vp[2]);
+    std::vector<int> fin;
+    for (int64_t j = 0; j < n; j++)
+        if (std::isfinite(xyz[3 * j]) && std::isfinite(xyz[3 * j + 1]) && std::isfinite(xyz[3 * j + 2]))
+            fin.push_back((int)j);
+    for (int64_t t = 0; t < m; t++) {
+        const int64_t id = idx[t];
+        status[t]        = 0;
+        const float  qx = xyz[3 * id], qy = xyz[3 * id + 1], qz = xyz[3 * id + 2];
+        std::vector<int> nb;
+        if (std::isfinite(qx) && std::isfinite(qy) && std::isfinite(qz))
+            for (int j : fin)
+                if (smm::dist2(qx, qy, qz, xyz[3 * j], xyz[3 * j + 1], xyz[3 * j + 2]) < r2)
+                    nb.push_back(j);
+        if (nb.size() < 3) continue;
+        // PCA
+        double c[3] = {0, 0, 0};
+        for (int j : nb)
+            for (int a = 0; a < 3; a++) c[a] += xyz[3 * j + a];
+        for (int a = 0; a < 3; a++) c[a] /= (double)nb.size();
+        double C[6] = {0, 0, 0, 0, 0, 0};
+        for (int j : nb) {
+            const double d[3] = {xyz[3 * j] - c[0], xyz[3 * j + 1] - c[1], xyz[3 * j + 2] - c[2]};
+            C[0] += d[0] * d[0], C[1] += d[0] * d[1], C[2] += d[0] * d[2];
+            C[3] += d[1] * d[1], C[4] += d[1] * d[2], C[5] += d[2] * d[2];
+        }
+        float nf[3];
+        sml::normal_from_cov(C, nf);
+        const double nv[3] = {nf[0], nf[1], nf[2]};
+        for (int a = 0; a < 3; a++) outNrm[3 * id + a] = nf[a];
+        status[t] = 1;
+        // plane projection and frame
+        const double dpl  = -(nv[0] * c[0] + nv[1] * c[1] + nv[2] * c[2]);
+        const double dist = qx * nv[0] + qy * nv[1] + qz * nv[2] + dpl;
+        const double mean[3] = {qx - dist * nv[0], qy - dist * nv[1], qz - dist * nv[2]};
+        double       v[3], u[3];
+        unit_orthogonal(nv, v);
+        u[0] = nv[1] * v[2] - nv[2] * v[1];
+        u[1] = nv[2] * v[0] - nv[0] * v[2];
+        u[2] = nv[0] * v[1] - nv[1] * v[0];
+        if (order <= 1 && nc > (int)nb.size()) continue;
+        // weighted polynomial fit of the heights
+        std::vector<double> G((size_t)nc * nc, 0.0), b(nc, 0.0), P(nc);
+        for (int j : nb) {
+            const double d[3] = {xyz[3 * j] - mean[0], xyz[3 * j + 1] - mean[1], xyz[3 * j + 2] - mean[2]};
+            const double w  = std::exp(-(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) / (double)r2);
+            const double uc = d[0] * u[0] + d[1] * u[1] + d[2] * u[2];
+            const double vc = d[0] * v[0] + d[1] * v[1] + d[2] * v[2];
+            const double f  = d[0] * nv[0] + d[1] * nv[1] + d[2] * nv[2];
+            int    k    = 0;
+            double uPow = 1;
+            for (int ui = 0; ui <= order; ui++) {
+                double vPow = 1;
+                for (int vi = 0; vi <= order - ui; vi++) {
+                    P[k++] = uPow * vPow;
+                    vPow *= vc;
+                }
+                uPow *= uc;
+            }
+            for (int a = 0; a < nc; a++) {
+                b[a] += w * P[a] * f;
+                for (int e = 0; e < nc; e++) G[(size_t)a * nc + e] += w * P[a] * P[e];
+            }
+        }
+        if (!llt_solve(G, b, nc)) continue;
+        const double p[3] = {mean[0] + b[0] * nv[0], mean[1] + b[0] * nv[1], mean[2] + b[0] * nv[2]};
+        double       nn[3];
+        for (int a = 0; a < 3; a++) nn[a] = nv[a] - b[order + 1] * u[a] - b[1] * v[a];
+        const double len = std::sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+        if (len > 0)
+            for (int a = 0; a < 3; a++) nn[a] /= len;
+        const double o = hasVp ? nn[0] * (vp[0] - p[0]) + nn[1] * (vp[1] - p[1]) + nn[2] * (vp[2] - p[2])
+                               : nn[2];
+        const bool flip = invert ? o > 0.0 : o < 0.0;
+        for (int a = 0; a < 3; a++) {
+            outXyz[3 * id + a] = (float)p[a];
+            outNrm[3 * id + a] = (float)(flip ? -nn[a] : nn[a]);
+        }
+        status[t] = 2;
+    }
+}

@@ -5,8 +5,10 @@ include/surface_match.h (libsurface_match.so, CUDA kernels in csrc/), ``include/
 the C++ Detector over it, and this package is the Python mirror of the same API.
 """
 from .detector import (Context, Detector, MatchParam, MatchResult, PointCloud,  # noqa: F401
-                       RangeError, Server, TrainParam, match_batch, probe_vote_atomics)
+                       RangeError, Server, TrainParam, estimateNormalMLS, match_batch,
+                       probe_vote_atomics)
 from .ply import read_ply, write_ply  # noqa: F401
 
 __all__ = ["Context", "Detector", "MatchParam", "MatchResult", "PointCloud", "RangeError",
-           "Server", "TrainParam", "match_batch", "probe_vote_atomics", "read_ply", "write_ply"]
+           "Server", "TrainParam", "estimateNormalMLS", "match_batch", "probe_vote_atomics",
+           "read_ply", "write_ply"]

@@ -20,7 +20,7 @@ INCLUDE = os.path.abspath(os.path.join(HERE, "..", "include"))
 LIB = os.path.join(HERE, "libsurface_match.so")
 
 CU_SOURCES = ["prep.cu", "vote.cu", "vote_pipe.cu", "cluster.cu", "icp.cu", "api.cu", "noalloc.cu", "batch.cu", "server.cu",
-              "probe.cu"]
+              "probe.cu", "mls.cu"]
 CPP_SOURCES: list = []
 HEADERS = ["sm_math.h", "sm_linalg.h", "sm_icp.h", "sm_grid.h", "sm_device.cuh", "sm_vote.cuh",
            "sm_engine.h", "sm_stages.h"]

@@ -723,6 +723,71 @@ SM_API int sm_context_synchronize(sm_context c) {
 
 SM_API void *sm_context_stream(sm_context c) { return c ? (void *)c->ctx.stream : nullptr; }
 
+// estimateNormalMLS (util.cpp:336-457): the finite points are the search set (the
+// reference's k-d tree over the cloud), the listed points are estimated (mls.cu).
+SM_API int sm_estimate_normals_mls(sm_context ctx, const float *xyzIn, const float *nrmIn,
+                                   int64_t n64, const int64_t *indices, int64_t nIdx,
+                                   float radius, int order, int invert, const float *vp,
+                                   float *outXyz, float *outNrm) {
+    return guarded([&] {
+        if (!ctx || !xyzIn || !outXyz || !outNrm)
+            throw Error(SM_ERR_ARG, "NULL argument");
+        if (order < 1 || order > kMlsMaxOrder)
+            throw Error(SM_ERR_ARG, "MLS order must be in 1.." + std::to_string(kMlsMaxOrder));
+        if (!std::isfinite(radius))
+            throw Error(SM_ERR_ARG, "MLS radius must be finite");
+        if (n64 < 0 || n64 > (1ll << 30))
+            throw Error(SM_ERR_ARG, "bad point count");
+        if (n64 == 0)
+            return;
+        const int        n = (int)n64;
+        std::vector<int> ids;
+        if (indices) {
+            if (nIdx < 0)
+                throw Error(SM_ERR_ARG, "bad index count");
+            ids.resize((size_t)nIdx);
+            for (int64_t i = 0; i < nIdx; i++) {
+                if (indices[i] < 0 || indices[i] >= n64)
+                    throw Error(SM_ERR_ARG, "point index out of range");
+                ids[(size_t)i] = (int)indices[i];
+            }
+        } else {
+            ids.resize((size_t)n);
+            for (int i = 0; i < n; i++)
+                ids[(size_t)i] = i;
+        }
+        Ctx &c = ctx->ctx;
+        SM_CUDA(cudaSetDevice(c.device));
+        const float *xyz  = to_device(c, xyzIn, n, "l.xyz");
+        const float *nin  = to_device(c, nrmIn, n, "l.nrm");
+        float4      *pos  = c.arena.get<float4>("l.pos", n);
+        float4      *nrm  = c.arena.get<float4>("l.n4", n);
+        int         *val  = c.arena.get<int>("l.valid", n);
+        float       *oXyz = c.arena.get<float>("l.oxyz", (size_t)n * 3);
+        float       *oNrm = c.arena.get<float>("l.onrm", (size_t)n * 3);
+        SM_CUDA(cudaMemcpyAsync(oXyz, xyz, (size_t)n * 12, cudaMemcpyDeviceToDevice, c.stream));
+        if (nin)
+            SM_CUDA(cudaMemcpyAsync(oNrm, nin, (size_t)n * 12, cudaMemcpyDeviceToDevice, c.stream));
+        else
+            fill_nan(c, oNrm, (long long)n * 3);
+        // validity of the search set by position only: the tree indexes every point
+        Box       box;
+        const int nvalid = prep_points(c, xyz, nullptr, n, pos, nrm, val, box);
+        if (nvalid > 0 && !ids.empty()) {
+            int *valid = c.arena.get<int>("l.vids", n);
+            compact_known(c, val, n, valid, "l.cv");
+            int *dids = c.arena.get<int>("l.ids", ids.size());
+            SM_CUDA(cudaMemcpyAsync(dids, ids.data(), ids.size() * 4, cudaMemcpyHostToDevice,
+                                    c.stream));
+            estimate_normals_mls(c, pos, valid, nvalid, box, dids, (int)ids.size(), radius, order,
+                                 invert != 0, vp, oXyz, oNrm);
+        }
+        SM_CUDA(cudaMemcpyAsync(outXyz, oXyz, (size_t)n * 12, cudaMemcpyDefault, c.stream));
+        SM_CUDA(cudaMemcpyAsync(outNrm, oNrm, (size_t)n * 12, cudaMemcpyDefault, c.stream));
+        c.sync_checked();
+    });
+}
+
 SM_API int sm_model_create(sm_context ctx, sm_model *out) {
     return guarded([&] {
         if (!ctx || !out)

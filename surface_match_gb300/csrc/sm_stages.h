@@ -74,6 +74,17 @@ void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *
 // Normalise all normals (normalizeNormal, util.cpp:163-176).
 void normalize_normals(Ctx &c, float4 *nrm, int n);
 
+// ---- mls.cu ---------------------------------------------------------------------------
+constexpr int kMlsMaxOrder = 4; // largest polynomial order of the MLS fit
+// Moving-least-squares normals and projected points of ids[0..m) (estimateNormalMLS,
+// util.cpp:336-457) with neighbours among valid[0..nvalid) within |radius|; writes the
+// listed points' results into outXyz / outNrm (n x 3 floats, pre-filled by the caller).
+void estimate_normals_mls(Ctx &c, const float4 *pos, const int *valid, int nvalid, const Box &box,
+                          const int *ids, int m, float radius, int order, bool invert,
+                          const float *vp, float *outXyz, float *outNrm);
+// x[0..n) = NaN
+void fill_nan(Ctx &c, float *x, long long n);
+
 // ---- vote.cu --------------------------------------------------------------------------
 struct VoteOut {
     long long *stats;   // K x 8

@@ -38,6 +38,41 @@ def probe_vote_atomics(device: int = 0) -> float:
     return float(out.value)
 
 
+def estimateNormalMLS(pc: "PointCloud", indices=None, radius: float = 1.0, order: int = 2,
+                      invert: bool = False, context: "Context | None" = None) -> "PointCloud":
+    """estimateNormalMLS (util.cpp:336-457) on the GPU (sm_estimate_normals_mls): for the
+    listed points (None: all) with at least 3 finite neighbours closer than |radius|, a PCA
+    plane, a weighted polynomial fit of total degree `order` (1..4) over it, the point moved
+    onto the fit and its normal oriented toward ``pc.viewPoint`` (or +z; reversed when
+    `invert`). Like the reference it updates ``pc.point`` and ``pc.normal`` in place (normals
+    are created as NaN when the cloud has none) and returns `pc`. The reference takes the
+    k-d tree to search as an argument; here the search structure is built on the device."""
+    L = _lib.load()
+    own = context is None
+    ctx = Context() if own else context
+    try:
+        pts = np.ascontiguousarray(pc.point, dtype=np.float32).reshape(-1, 3)
+        n = len(pts)
+        nrm = None if pc.normal is None else np.ascontiguousarray(pc.normal, dtype=np.float32)
+        idx = None if indices is None else np.ascontiguousarray(indices, dtype=np.int64)
+        vp = None if pc.viewPoint is None else np.ascontiguousarray(pc.viewPoint, np.float32)
+        out_p = np.empty((n, 3), np.float32)
+        out_n = np.empty((n, 3), np.float32)
+        f32 = C.POINTER(C.c_float)
+        _check(L.sm_estimate_normals_mls(
+            ctx.handle, pts.ctypes.data_as(f32), None if nrm is None else nrm.ctypes.data_as(f32),
+            n, None if idx is None else idx.ctypes.data_as(C.POINTER(C.c_int64)),
+            0 if idx is None else len(idx), float(radius), int(order), 1 if invert else 0,
+            None if vp is None else vp.ctypes.data_as(f32), out_p.ctypes.data_as(f32),
+            out_n.ctypes.data_as(f32)))
+    finally:
+        if own:
+            ctx.close()
+    pc.point = out_p
+    pc.normal = out_n
+    return pc
+
+
 @dataclass
 class TrainParam:
     """ppf::TrainParam (type.h:39-74); validated on construction (type.cpp:71-88)."""
