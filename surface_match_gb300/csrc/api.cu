@@ -11,8 +11,10 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <exception>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/surface_match.h"
@@ -342,10 +344,47 @@ struct MatchOutputs {
 
 void record(Ctx &c, int i) { SM_CUDA(cudaEventRecord(c.ev[i], c.stream)); }
 
+// The context's second stream and workspace (created on first use).
+Ctx &aux_ctx(Ctx &c) {
+    if (!c.aux) {
+        std::unique_ptr<Ctx> a(new Ctx());
+        a->device = c.device;
+        SM_CUDA(cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking));
+        a->ownStream = true;
+        SM_CUDA(cudaMallocHost((void **)&a->hostCounts, 64 * sizeof(int)));
+        for (auto &e : a->ev)
+            SM_CUDA(cudaEventCreate(&e));
+        a->arena.set_stream(a->stream, c.device);
+        SM_CUDA(cudaEventCreateWithFlags(&c.fork, cudaEventDisableTiming));
+        c.aux = std::move(a);
+    }
+    return *c.aux;
+}
+
+// Release a context's stream, events, pinned scratch and workspace (and its second
+// context's).
+void release_ctx(Ctx &c) {
+    if (c.aux) {
+        release_ctx(*c.aux);
+        c.aux.reset();
+    }
+    cudaStreamSynchronize(c.stream);
+    c.arena.release();
+    for (auto &e : c.ev)
+        if (e)
+            cudaEventDestroy(e);
+    if (c.fork)
+        cudaEventDestroy(c.fork);
+    if (c.hostCounts)
+        cudaFreeHost(c.hostCounts);
+    if (c.ownStream)
+        cudaStreamDestroy(c.stream);
+}
+
 // matchScene (ppf.cpp:149-510) on the device.
 void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64_t n64,
            const float *vp, float sdRel, float kpFrac, float minScore, const sm_match_param &mp,
-           MatchOutputs &res, sm_match_stats *stats) {
+           MatchOutputs &res, sm_match_stats *stats, bool overlap) {
     if (!m.trained)
         throw Error(SM_ERR_RUNTIME, "No trained model in matchScene");
     if (sdRel > 1 || sdRel < 0)
@@ -381,6 +420,7 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
         res.score.clear();
         c.last       = Ctx::Last{};
         c.last.n     = n;
+        c.last.dense = &c;
         c.last.valid = true;
         if (stats) {
             memset(stats, 0, sizeof(*stats));
@@ -403,6 +443,96 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
                          mp.invertNormal != 0, vp, "m.n1");
     }
     record(c, 2);
+    float maxOverlap = 0;
+    if (mp.maxOverlapDistRel > 0)
+        maxOverlap = diam * mp.maxOverlapDistRel;
+    if (mp.maxOverlapDistAbs > 0)
+        maxOverlap = mp.maxOverlapDistAbs;
+    float refDist = 0;
+    if (mp.poseRefDistThresholdRel > 0)
+        refDist = diam * mp.poseRefDistThresholdRel;
+    if (mp.poseRefDistThresholdAbs > 0)
+        refDist = mp.poseRefDistThresholdAbs;
+    float scoreDist = 0;
+    if (mp.poseRefScoringDistRel > 0)
+        scoreDist = diam * mp.poseRefScoringDistRel;
+    if (mp.poseRefScoringDistAbs > 0)
+        scoreDist = mp.poseRefScoringDistAbs;
+    // The dense refinement scene (ppf.cpp:428-434) and the refinement's search grids depend
+    // only on the positions and normals as they are now: keypoint sampling, voting and
+    // clustering write neither. With `overlap` a second context builds them from a snapshot
+    // on its own stream and host thread while this one votes and clusters, and the
+    // refinement reads that context's buffers; otherwise the same steps run here, in place,
+    // after clustering. Both give the same values.
+    int      nres = 0;
+    IcpScene s;
+    auto     prepare_dense = [&](Ctx &d) {
+        float4 *P = pos, *N = nrm;
+        if (&d != &c) {
+            SM_CUDA(cudaStreamWaitEvent(d.stream, c.fork, 0));
+            P = d.arena.get<float4>("m.pos", n);
+            N = d.arena.get<float4>("m.n4", n);
+            SM_CUDA(cudaMemcpyAsync(P, pos, (size_t)n * 16, cudaMemcpyDeviceToDevice, d.stream));
+            SM_CUDA(cudaMemcpyAsync(N, nrm, (size_t)n * 16, cudaMemcpyDeviceToDevice, d.stream));
+        }
+        int *resampled = d.arena.get<int>("m.resampled", std::max(n, 1));
+        if (mp.densePoseRefinement) {
+            nres = sample_points(d, P, n, valid, nvalid, box, reSampleStep, resampled, "m.s3");
+            if (!hasN) {
+                HGrid q2;
+                build_hgrid(d, P, valid, nvalid, box, gq, q2, "m.q");
+                estimate_normals(d, P, N, n, resampled, nres, q2, mp.knnNormal, false,
+                                 mp.invertNormal != 0, vp, "m.n2");
+            }
+        }
+        s.pos = P;
+        s.nrm = N;
+        // Nearest-neighbour grids of the refinement: cells of about a third of the rejection
+        // distance (never finer than the subset's spacing), so three cell shells always
+        // cover it. The inlier grid's cell just exceeds the scoring distance, so two shells
+        // decide. The subset grids name points by subset rank (the subsets are ascending, so
+        // rank order is index order), and the refinement reads rank-ordered copies of the
+        // subsets.
+        build_hgrid(d, P, sampled, ns, box, std::max(sampleStep, refDist / 2.98f), s.sampled,
+                    "m.gS", true);
+        build_hgrid(d, P, resampled, nres, box, std::max(2.0f * reSampleStep, refDist / 2.98f),
+                    s.resampled, "m.gR", true);
+        build_hgrid(d, P, valid, nvalid, box, std::max(scoreDist * 1.02f, gq), s.full, "m.gF");
+        float4 *posS = d.arena.get<float4>("m.posS", std::max(ns, 1));
+        float4 *nrmS = d.arena.get<float4>("m.nrmS", std::max(ns, 1));
+        float4 *posR = d.arena.get<float4>("m.posR", std::max(nres, 1));
+        float4 *nrmR = d.arena.get<float4>("m.nrmR", std::max(nres, 1));
+        gather_subset(d, P, N, sampled, ns, posS, nrmS);
+        gather_subset(d, P, N, resampled, nres, posR, nrmR);
+        s.posS = posS;
+        s.nrmS = nrmS;
+        s.posR = posR;
+        s.nrmR = nrmR;
+        if (&d != &c)
+            d.sync_checked();
+    };
+    Ctx               *dctx = &c;
+    std::thread        helper;
+    std::exception_ptr helperErr;
+    struct Joiner {
+        std::thread &t;
+        ~Joiner() {
+            if (t.joinable())
+                t.join(); // the helper reads this call's buffers: never leave it running
+        }
+    } joiner{helper};
+    if (overlap) {
+        dctx = &aux_ctx(c);
+        SM_CUDA(cudaEventRecord(c.fork, c.stream));
+        helper = std::thread([&] {
+            try {
+                SM_CUDA(cudaSetDevice(c.device));
+                prepare_dense(*dctx);
+            } catch (...) {
+                helperErr = std::current_exception();
+            }
+        });
+    }
     const float keyStep = smm::fsqrt(1.f / kpFrac) * sampleStep;
     int        *kp      = c.arena.get<int>("m.kp", std::max(ns, 1));
     const int   K       = sample_points(c, pos, n, sampled, ns, box, keyStep, kp, "m.s2");
@@ -425,60 +555,18 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
         SM_LAUNCH_CHECK();
     }
     record(c, 4);
-    float maxOverlap = 0;
-    if (mp.maxOverlapDistRel > 0)
-        maxOverlap = diam * mp.maxOverlapDistRel;
-    if (mp.maxOverlapDistAbs > 0)
-        maxOverlap = mp.maxOverlapDistAbs;
-    float refDist = 0;
-    if (mp.poseRefDistThresholdRel > 0)
-        refDist = diam * mp.poseRefDistThresholdRel;
-    if (mp.poseRefDistThresholdAbs > 0)
-        refDist = mp.poseRefDistThresholdAbs;
-    float scoreDist = 0;
-    if (mp.poseRefScoringDistRel > 0)
-        scoreDist = diam * mp.poseRefScoringDistRel;
-    if (mp.poseRefScoringDistAbs > 0)
-        scoreDist = mp.poseRefScoringDistAbs;
     const float center[3] = {(m.box.mn[0] + m.box.mx[0]) / 2.f, (m.box.mn[1] + m.box.mx[1]) / 2.f,
                              (m.box.mn[2] + m.box.mx[2]) / 2.f};
     float    *cands = c.arena.get<float>("m.cands", (size_t)std::max(np, 1) * smi::kPoseFloats);
     const int ncand = cluster(c, plist, np, 0.1f * diam, angleStep, center, maxOverlap, cands, "m.cl");
     record(c, 5);
-    // dense refinement scene
-    int *resampled = c.arena.get<int>("m.resampled", std::max(n, 1));
-    int  nres      = 0;
-    if (mp.densePoseRefinement) {
-        nres = sample_points(c, pos, n, valid, nvalid, box, reSampleStep, resampled, "m.s3");
-        if (!hasN) {
-            build_hgrid(c, pos, valid, nvalid, box, gq, q, "m.q");
-            estimate_normals(c, pos, nrm, n, resampled, nres, q, mp.knnNormal, false,
-                             mp.invertNormal != 0, vp, "m.n2");
-        }
+    if (overlap) {
+        helper.join();
+        if (helperErr)
+            std::rethrow_exception(helperErr);
+    } else {
+        prepare_dense(c);
     }
-    IcpScene s;
-    s.pos          = pos;
-    s.nrm          = nrm;
-    // Nearest-neighbour grids of the refinement: cells of about a third of the rejection
-    // distance (never finer than the subset's spacing), so three cell shells always cover
-    // it. The inlier grid's cell just exceeds the scoring distance, so two shells decide.
-    // The subset grids name points by subset rank (the subsets are ascending, so rank order
-    // is index order), and the refinement reads rank-ordered copies of the subsets.
-    build_hgrid(c, pos, sampled, ns, box, std::max(sampleStep, refDist / 2.98f), s.sampled, "m.gS",
-                true);
-    build_hgrid(c, pos, resampled, nres, box, std::max(2.0f * reSampleStep, refDist / 2.98f),
-                s.resampled, "m.gR", true);
-    build_hgrid(c, pos, valid, nvalid, box, std::max(scoreDist * 1.02f, gq), s.full, "m.gF");
-    float4 *posS = c.arena.get<float4>("m.posS", std::max(ns, 1));
-    float4 *nrmS = c.arena.get<float4>("m.nrmS", std::max(ns, 1));
-    float4 *posR = c.arena.get<float4>("m.posR", std::max(nres, 1));
-    float4 *nrmR = c.arena.get<float4>("m.nrmR", std::max(nres, 1));
-    gather_subset(c, pos, nrm, sampled, ns, posS, nrmS);
-    gather_subset(c, pos, nrm, resampled, nres, posR, nrmR);
-    s.posS = posS;
-    s.nrmS = nrmS;
-    s.posR = posR;
-    s.nrmR = nrmR;
     record(c, 6);
     IcpParams ip;
     ip.sparse        = mp.sparsePoseRefinement;
@@ -526,6 +614,7 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
     c.last.nr    = nres;
     c.last.np    = np;
     c.last.ncand = ncand;
+    c.last.dense = dctx;
     c.last.valid = true;
     if (stats) {
         memset(stats, 0, sizeof(*stats));
@@ -609,7 +698,7 @@ void match_into(Ctx &c, const Model &m, const float *xyz, const float *nrm, int6
                 const sm_match_param &mp, std::vector<float> &pose, std::vector<float> &score,
                 sm_match_stats *stats) {
     MatchOutputs res;
-    match(c, m, xyz, nrm, n, vp, sdRel, kpFrac, minScore, mp, res, stats);
+    match(c, m, xyz, nrm, n, vp, sdRel, kpFrac, minScore, mp, res, stats, false);
     pose  = std::move(res.pose);
     score = std::move(res.score);
 }
@@ -700,15 +789,7 @@ SM_API int sm_context_destroy(sm_context c) {
         if (!c)
             return;
         cudaSetDevice(c->ctx.device);
-        cudaStreamSynchronize(c->ctx.stream);
-        c->ctx.arena.release();
-        for (auto &e : c->ctx.ev)
-            if (e)
-                cudaEventDestroy(e);
-        if (c->ctx.hostCounts)
-            cudaFreeHost(c->ctx.hostCounts);
-        if (c->ctx.ownStream)
-            cudaStreamDestroy(c->ctx.stream);
+        release_ctx(c->ctx);
         delete c;
     });
 }
@@ -1020,7 +1101,8 @@ SM_API int sm_match(sm_model m, const float *xyz, const float *normal, int64_t n
             mp = *param;
         SM_CUDA(cudaSetDevice(m->m.device));
         MatchOutputs res;
-        match(m->ctx->ctx, m->m, xyz, normal, n, viewpoint, sdRel, kpFrac, minScore, mp, res, stats);
+        match(m->ctx->ctx, m->m, xyz, normal, n, viewpoint, sdRel, kpFrac, minScore, mp, res, stats,
+              true);
         const int nres = (int)res.score.size();
         const int cap  = *inoutCount;
         *inoutCount    = nres;
@@ -1109,13 +1191,16 @@ static bool debug_field(sm_model m, int field, const void *&src, int64_t &count,
     Ctx &c = m->ctx->ctx;
     if (!c.last.valid)
         return false;
-    auto get = [&](const char *name) { return c.arena.get(name, 1); };
+    auto get   = [&](const char *name) { return c.arena.get(name, 1); };
+    Ctx &dc    = c.last.dense ? *c.last.dense : c;
+    auto dense = [&](const char *name) { return dc.arena.get(name, 1); };
     switch (field) {
         case 0: src = get("m.sampled"); count = c.last.ns; elem = 4; return true;
         case 1: src = get("m.kp"); count = c.last.nk; elem = 4; return true;
-        case 2: src = get("m.resampled"); count = c.last.nr; elem = 4; return true;
-        case 3: src = get("m.pos"); count = c.last.n; elem = 16; return true;
-        case 4: src = get("m.n4"); count = c.last.n; elem = 16; return true;
+        // the refinement scene and the final positions and normals
+        case 2: src = dense("m.resampled"); count = c.last.nr; elem = 4; return true;
+        case 3: src = dense("m.pos"); count = c.last.n; elem = 16; return true;
+        case 4: src = dense("m.n4"); count = c.last.n; elem = 16; return true;
         case 7: src = get("m.kstats"); count = (int64_t)c.last.nk * 8; elem = 8; return true;
         case 8: src = get("m.kcands"); count = (int64_t)c.last.nk * 9; elem = 4; return true;
         case 9: src = get("m.plist"); count = (int64_t)c.last.np * smi::kPoseFloats; elem = 4; return true;

@@ -20,11 +20,19 @@ struct Ctx {
     Arena        arena;
     int         *hostCounts = nullptr; // pinned scratch for small device->host reads
     cudaEvent_t  ev[14]{}; // stage timing (api.cu), vote-kernel timing 10..13 (vote_pipe.cu)
-    // intermediate state of the last match (device pointers into the arena + sizes)
+    // intermediate state of the last match (device pointers into the arena + sizes);
+    // `dense` is the context whose workspace holds the refinement scene and the final
+    // positions and normals (this one, or `aux`)
     struct Last {
         int  n = 0, ns = 0, nk = 0, nr = 0, np = 0, nc = 0, ncand = 0;
         bool valid = false;
+        Ctx *dense = nullptr;
     } last;
+    // second stream and workspace of this context (api.cu): matchScene prepares the dense
+    // refinement scene there while it votes and clusters here; `fork` orders it after this
+    // stream's work. Created on first use, released with the context.
+    std::unique_ptr<Ctx> aux;
+    cudaEvent_t          fork = nullptr;
     // single-pass scan state (prep.cu): per-tile status words, {ticket, wait-expired flag}
     struct ScanState {
         unsigned long long *status = nullptr;
