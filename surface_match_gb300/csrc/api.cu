@@ -344,12 +344,16 @@ struct MatchOutputs {
 
 void record(Ctx &c, int i) { SM_CUDA(cudaEventRecord(c.ev[i], c.stream)); }
 
-// The context's second stream and workspace (created on first use).
+// The context's second stream and workspace (created on first use). The dense preparation
+// it runs is the longer of the two concurrent chains, so its stream takes the device's
+// highest priority: its kernels are scheduled first when both chains have work queued.
 Ctx &aux_ctx(Ctx &c) {
     if (!c.aux) {
         std::unique_ptr<Ctx> a(new Ctx());
         a->device = c.device;
-        SM_CUDA(cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking));
+        int least = 0, greatest = 0;
+        SM_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        SM_CUDA(cudaStreamCreateWithPriority(&a->stream, cudaStreamNonBlocking, greatest));
         a->ownStream = true;
         SM_CUDA(cudaMallocHost((void **)&a->hostCounts, 64 * sizeof(int)));
         for (auto &e : a->ev)
