@@ -27,8 +27,8 @@ constexpr int kClBs   = 1024;
 constexpr int PF      = smi::kPoseFloats;
 constexpr int kClMaxC = 1024; // poses for which the compatibility bits are precomputed
 
-// Shared-memory bytes per pose of k_cluster_a: sort key (float4), votes and one int list.
-constexpr int kClPerPose = 16 + 2 * 4;
+// Shared-memory bytes per pose of k_cluster_a: its sort key (float4).
+constexpr int kClPerPose = 16;
 
 struct ClArgs {
     const float *poses;
@@ -135,17 +135,13 @@ __global__ void __launch_bounds__(kClBs) k_cluster_a(ClArgs a) {
     const int      tid = threadIdx.x, lane = tid & 31;
     const int      np  = a.np;
     float4        *key   = a.smemState ? dsm4 : a.gbuf4;
-    int           *ib    = a.smemState ? (int *)(dsm4 + np) : a.gbuf;
-    float         *votes = (float *)ib;
-    int           *tail  = ib + np;
     const int      W     = (np + 31) >> 5;
-    uint32_t      *bits  = (uint32_t *)(ib + 2 * np); // W x np (word-major), when useBits
+    uint32_t      *bits  = (uint32_t *)(dsm4 + np); // W x np (word-major), when useBits
     uint32_t      *headB = bits + (size_t)W * np;     // W
     uint32_t      *unkB  = headB + W;                 // W
     uint32_t      *newH  = unkB + W;                  // W
     uint32_t      *newM  = newH + W;                  // W
     int           *hpre  = (int *)(newM + W);         // W + 1
-    (void)votes;
     // the sorted keys (k_cluster_rank, in gbuf4) into shared memory
     if (a.smemState)
         for (int i = tid; i < np; i += kClBs)
@@ -255,7 +251,6 @@ __global__ void __launch_bounds__(kClBs) k_cluster_a(ClArgs a) {
     __syncthreads();
     if (tid == 0)
         *a.nhOut = sNh;
-    (void)tail;
 }
 
 // avgClusters: one block per cluster (grid-stride); the warp finds the members in pose
