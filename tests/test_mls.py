@@ -71,6 +71,14 @@ def test_oracle_plane_is_exact():
         assert np.abs(p[ids] - P[ids]).max() < 1e-4
         p, n, s = po.mls(P, None, ids, radius=4.0, order=order, invert=True)
         assert np.all(n[ids, 2] < 0)
+    # a horizontal plane: the normal along z takes the frame's other branch (x and y both
+    # negligible against z)
+    H = np.c_[st, np.full(len(st), 5.0)].astype(np.float32)
+    for order in (1, 2, 4):
+        p, n, s = po.mls(H, None, ids, radius=4.0, order=order)
+        assert np.all(s == 2)
+        np.testing.assert_allclose(n[ids], np.broadcast_to([0, 0, 1], (len(ids), 3)), atol=1e-6)
+        np.testing.assert_allclose(p[ids], H[ids], atol=1e-5)
 
 
 def test_oracle_sphere_normals_and_projection():
