@@ -96,8 +96,10 @@ SM_API int  sm_train_param_check(const sm_train_param *p);
 SM_API int  sm_match_param_check(const sm_match_param *p);
 
 /* Context: device ordinal, optional external cudaStream_t (NULL = the library creates
- * its own non-blocking stream). Replaces nothing in the reference (its runtime is OpenMP,
- * ppf.cpp:26-31). */
+ * its own non-blocking stream). sm_match also uses a second stream and workspace of the
+ * context (created on its first call, at the device's highest stream priority, released
+ * with the context), ordered after the context's stream. A context serves one host thread
+ * at a time. Replaces nothing in the reference (its runtime is OpenMP, ppf.cpp:26-31). */
 SM_API int sm_context_create(int device, void *cuda_stream, sm_context *out);
 SM_API int sm_context_destroy(sm_context ctx);
 SM_API int sm_context_synchronize(sm_context ctx);
@@ -140,7 +142,9 @@ SM_API int sm_model_load(sm_model model, const char *path);
  * xyz/normal: scene points (normal may be NULL: estimated). viewpoint: 3 floats or NULL
  * (PointCloud::viewPoint, type.h:28; NULL = not set). Results are written sorted by
  * score: out_pose[i*16..] a row-major 4x4 pose, out_score[i]; *inout_count holds the
- * capacity on entry and the number of results on return. stats may be NULL. */
+ * capacity on entry and the number of results on return. stats may be NULL. The call
+ * orders after the work already on the context's stream and returns when all of its own
+ * work, on both of the context's streams, has finished. */
 SM_API int sm_match(sm_model model, const float *xyz, const float *normal, int64_t n,
                     const float *viewpoint, float samplingDistanceRel, float keyPointFraction,
                     float minScore, const sm_match_param *param, float *out_pose,
