@@ -83,8 +83,11 @@ typedef struct {
     int64_t n_pairs;      /* point pairs evaluated (keypoint x neighbour) */
     int64_t n_hits;       /* pairs whose key is in the model table */
     int64_t n_votes;      /* votes cast: matched table entries (ppf.cpp:342-346) */
-    float   ms[8];        /* stage device times (ms): prep, sampling + normals, keypoints,
-                             voting, clustering, refinement prep, refinement, total */
+    float   ms[8];        /* stage device times (ms) on the context's stream: prep, sampling +
+                             normals, keypoints, voting, clustering, refinement prep,
+                             refinement, total. sm_match prepares the refinement on its
+                             second stream beside keypoints, voting and clustering, so its
+                             refinement-prep entry is the wait for that work */
     float   vote_ms[2];   /* device times (ms) of the voting stage's two main kernels: pair
                              features + table probes, shared-memory accumulation + peaks */
 } sm_match_stats;
