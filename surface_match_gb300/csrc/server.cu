@@ -196,14 +196,16 @@ SM_API int sm_server_submit(sm_server s, sm_model model, const float *xyz, const
         Req r;
         r.model = model;
         r.n     = n;
-        if (device_pointer(xyz)) {
+        // each input on its own: device arrays are read in place when the request runs (the
+        // caller keeps them alive until it is polled), host arrays are copied now
+        if (device_pointer(xyz))
             r.devXyz = xyz;
-            r.devNrm = normal;
-        } else {
+        else
             r.xyz.assign(xyz, xyz + n * 3);
-            if (normal)
-                r.nrm.assign(normal, normal + n * 3);
-        }
+        if (normal && device_pointer(normal))
+            r.devNrm = normal;
+        else if (normal)
+            r.nrm.assign(normal, normal + n * 3);
         r.hasNrm = normal != nullptr;
         r.hasVp  = viewpoint != nullptr;
         if (viewpoint)
