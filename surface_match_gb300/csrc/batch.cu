@@ -94,8 +94,9 @@ extern "C" SM_API int sm_match_batch(int njobs, const sm_model *models, const fl
             try {
                 SM_CUDA(cudaSetDevice(device));
                 c = acquire_worker(device);
-            } catch (const Error &e) {
-                // no context: the remaining jobs are failed by the threads that have one
+            } catch (const std::exception &) {
+                // no context: the remaining jobs go to the threads that have one (or are
+                // reported as never taken below); nothing may escape the thread
                 return;
             }
             for (int j = next++; j < njobs; j = next++) {
