@@ -923,7 +923,10 @@ SM_API int sm_model_upload(sm_model m, int64_t ns, const float *sxyz, const floa
             tp = *param;
         check_train_param(tp);
         SM_CUDA(cudaSetDevice(m->m.device));
-        const int64_t      ne = nk > 0 ? offs[nk] : 0;
+        const int64_t ne = nk > 0 ? offs[nk] : 0;
+        if ((ns > 0 && (!sxyz || !snrm)) || (nr > 0 && (!rxyz || !rnrm)) ||
+            (ne > 0 && (!refs || !alphas)) || (nk > 0 && offs[0] != 0))
+            throw Error(SM_ERR_ARG, "invalid model arrays");
         std::vector<float> sp(sxyz, sxyz + ns * 3), sn(snrm, snrm + ns * 3);
         std::vector<float> rp(rxyz, rxyz + nr * 3), rn(rnrm, rnrm + nr * 3);
         std::vector<uint32_t> K(keys, keys + nk), O(offs, offs + nk + 1), R(refs, refs + ne);
@@ -1052,6 +1055,8 @@ SM_API int sm_model_load(sm_model m, const char *path) {
         if (sn.size() != sp.size() || rn.size() != rp.size())
             throw Error(SM_ERR_RUNTIME, std::string("corrupt model file:") + path);
         const uint32_t nb = r.get<uint32_t>();
+        if ((size_t)nb * 12 > s.size() - r.p) // key and two counts per bucket at least
+            throw Error(SM_ERR_RUNTIME, "truncated model file");
         struct B {
             uint32_t              key;
             std::vector<uint32_t> refs;
