@@ -1142,6 +1142,14 @@ SM_API int sm_vote_stage(sm_model m, const float *points, const float *normals, 
             throw Error(SM_ERR_ARG, "NULL argument");
         if (!m->m.trained)
             throw Error(SM_ERR_RUNTIME, "No trained model in matchScene");
+        if (n <= 0 || n > (1ll << 30) || K < 0 || K > (1ll << 30))
+            throw Error(SM_ERR_ARG, "bad point or keypoint count");
+        // the CSR lists the kernels walk: offsets from 0, never decreasing
+        if (nbrOff[0] != 0)
+            throw Error(SM_ERR_ARG, "neighbour offsets must start at 0");
+        for (int64_t k = 0; k < K; k++)
+            if (nbrOff[k + 1] < nbrOff[k])
+                throw Error(SM_ERR_ARG, "neighbour offsets must not decrease");
         Ctx &c = m->ctx->ctx;
         SM_CUDA(cudaSetDevice(m->m.device));
         const int    ni = (int)n, Ki = (int)K;
