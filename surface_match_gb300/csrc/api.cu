@@ -828,7 +828,7 @@ SM_API int sm_estimate_normals_mls(sm_context ctx, const float *xyzIn, const flo
         const int        n = (int)n64;
         std::vector<int> ids;
         if (indices) {
-            if (nIdx < 0)
+            if (nIdx < 0 || nIdx > (1ll << 31) - 1)
                 throw Error(SM_ERR_ARG, "bad index count");
             ids.resize((size_t)nIdx);
             for (int64_t i = 0; i < nIdx; i++) {
