@@ -107,6 +107,9 @@ SM_API int sm_context_create(int device, void *cuda_stream, sm_context *out);
 SM_API int sm_context_destroy(sm_context ctx);
 SM_API int sm_context_synchronize(sm_context ctx);
 SM_API void *sm_context_stream(sm_context ctx);
+/* Device bytes the context's workspace holds (both of its streams' workspaces). It grows on
+ * demand and is reused across calls; no counterpart in the reference. */
+SM_API int sm_context_workspace_bytes(sm_context ctx, int64_t *bytes);
 
 /* Model handle (ppf::Detector::IMPL, privateType.h:56-66). */
 SM_API int sm_model_create(sm_context ctx, sm_model *out);
@@ -214,12 +217,19 @@ SM_API int sm_vote_stage(sm_model model, const float *points, const float *norma
  * counterpart in the reference (its voting loop, ppf.cpp:247-409, allocates per call).
  * Same arguments, meaning and results as sm_vote_stage, except that every pointer is a
  * DEVICE pointer owned by the caller (nbr_ids holding nbr_off[K] entries), and out_poses
- * is required. The call allocates nothing: its staging lives in a fixed array in the
- * library's device image (about 4.8 MiB, held on every GPU that loads the library until
- * the process exits), which limits a call to n <= 131072 points and K <= 65536 keypoints;
- * larger sizes return SM_ERR_CAPACITY. The first call on a device resolves that array's
- * address, so make it before any stream capture. All calls share the array: calls whose
- * GPU work overlaps race on it. Returns after the results are written. */
+ * is required. The call runs on the model context's stream and does not wait for other
+ * streams: the caller's device inputs must be complete (e.g. synchronised) before the
+ * call. Offsets are validated before any list is read: off[0] must be 0, offsets must not
+ * decrease and no list may be longer than n; nbr_off[K] entries must fit in the device
+ * allocation that holds nbr_ids (checked with the driver's address range of that pointer);
+ * then every id is checked. Violations return SM_ERR_ARG. The call allocates nothing: its
+ * staging lives in a fixed array in the library's device image (about 4.8 MiB, held on
+ * every GPU that loads the library until the process exits), which limits a call to
+ * n <= 131072 points and K <= 65536 keypoints; larger sizes return SM_ERR_CAPACITY. The
+ * first call on a device (and the first after the device's context is created anew)
+ * resolves that array's address, so make it before any stream capture. All calls share
+ * the array: calls whose GPU work overlaps race on it. Returns after the results are
+ * written. */
 SM_API int sm_vote_stage_noalloc(sm_model model, const float *points, const float *normals,
                                  int64_t n, const int32_t *keypoints, int64_t K,
                                  const int32_t *nbr_off, const int32_t *nbr_ids, float minScore,

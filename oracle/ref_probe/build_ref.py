@@ -11,7 +11,9 @@ import tempfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "..", "_ref")
-REF = os.environ.get("SM_REFERENCE_DIR", "/root/reference")
+# The reference's source tree: SM_REFERENCE_DIR, else the build container's copy (this
+# recipe is the one place that names it; nothing on the GPU machine reads it).
+REF = os.environ.get("SM_REFERENCE_DIR") or "/root/reference"
 
 
 def available() -> bool:

@@ -360,7 +360,8 @@ Ctx &aux_ctx(Ctx &c) {
             SM_CUDA(cudaEventCreate(&e));
         a->arena.set_stream(a->stream, c.device);
         SM_CUDA(cudaEventCreateWithFlags(&c.fork, cudaEventDisableTiming));
-        c.aux = std::move(a);
+        c.aux    = std::move(a);
+        c.helper.reset(new Helper());
     }
     return *c.aux;
 }
@@ -368,6 +369,7 @@ Ctx &aux_ctx(Ctx &c) {
 // Release a context's stream, events, pinned scratch and workspace (and its second
 // context's).
 void release_ctx(Ctx &c) {
+    c.helper.reset(); // joins the helper thread (idle: every call waits for its task)
     if (c.aux) {
         release_ctx(*c.aux);
         c.aux.reset();
@@ -515,27 +517,28 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
         if (&d != &c)
             d.sync_checked();
     };
-    Ctx               *dctx = &c;
-    std::thread        helper;
-    std::exception_ptr helperErr;
-    struct Joiner {
-        std::thread &t;
-        ~Joiner() {
-            if (t.joinable())
-                t.join(); // the helper reads this call's buffers: never leave it running
+    Ctx *dctx = &c;
+    // the helper reads this call's buffers: never leave the call while its task runs
+    struct Waiter {
+        Helper *h = nullptr;
+        ~Waiter() {
+            if (h) {
+                try {
+                    h->wait();
+                } catch (...) {
+                }
+            }
         }
-    } joiner{helper};
+    } waiter;
     if (overlap) {
         dctx = &aux_ctx(c);
         SM_CUDA(cudaEventRecord(c.fork, c.stream));
-        helper = std::thread([&] {
-            try {
-                SM_CUDA(cudaSetDevice(c.device));
-                prepare_dense(*dctx);
-            } catch (...) {
-                helperErr = std::current_exception();
-            }
+        Ctx *d = dctx;
+        c.helper->post([&, d] {
+            SM_CUDA(cudaSetDevice(c.device));
+            prepare_dense(*d);
         });
+        waiter.h = c.helper.get();
     }
     const float keyStep = smm::fsqrt(1.f / kpFrac) * sampleStep;
     int        *kp      = c.arena.get<int>("m.kp", std::max(ns, 1));
@@ -565,9 +568,8 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
     const int ncand = cluster(c, plist, np, 0.1f * diam, angleStep, center, maxOverlap, cands, "m.cl");
     record(c, 5);
     if (overlap) {
-        helper.join();
-        if (helperErr)
-            std::rethrow_exception(helperErr);
+        waiter.h = nullptr;
+        c.helper->wait(); // rethrows the preparation's error
     } else {
         prepare_dense(c);
     }
@@ -807,6 +809,17 @@ SM_API int sm_context_synchronize(sm_context c) {
 }
 
 SM_API void *sm_context_stream(sm_context c) { return c ? (void *)c->ctx.stream : nullptr; }
+
+SM_API int sm_context_workspace_bytes(sm_context c, int64_t *bytes) {
+    return guarded([&] {
+        if (!c || !bytes)
+            throw Error(SM_ERR_ARG, "NULL argument");
+        int64_t b = (int64_t)c->ctx.arena.bytes();
+        if (c->ctx.aux)
+            b += (int64_t)c->ctx.aux->arena.bytes();
+        *bytes = b;
+    });
+}
 
 // estimateNormalMLS (util.cpp:336-457): the finite points are the search set (the
 // reference's k-d tree over the cloud), the listed points are estimated (mls.cu).

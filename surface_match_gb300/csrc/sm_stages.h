@@ -4,14 +4,84 @@
 
 #include <cuda_runtime.h>
 
+#include <condition_variable>
+#include <exception>
 #include <functional>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "sm_engine.h"
 
 namespace sm {
+
+// A host thread kept for the life of a context that runs one task at a time: matchScene
+// hands it the dense-refinement preparation (which drives the context's second stream)
+// instead of starting a thread per call.
+class Helper {
+public:
+    Helper() : th_([this] { loop(); }) {}
+    ~Helper() {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        th_.join();
+    }
+    void post(std::function<void()> f) {
+        std::lock_guard<std::mutex> lk(mu_);
+        task_ = std::move(f);
+        busy_ = true;
+        err_  = nullptr;
+        cv_.notify_all();
+    }
+    // waits for the posted task; rethrows its exception
+    void wait() {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [this] { return !busy_; });
+        if (err_) {
+            std::exception_ptr e = err_;
+            err_                 = nullptr;
+            std::rethrow_exception(e);
+        }
+    }
+    bool busy() {
+        std::lock_guard<std::mutex> lk(mu_);
+        return busy_;
+    }
+
+private:
+    void loop() {
+        std::unique_lock<std::mutex> lk(mu_);
+        for (;;) {
+            cv_.wait(lk, [this] { return stop_ || (busy_ && task_); });
+            if (stop_ && !busy_)
+                return;
+            std::function<void()> f = std::move(task_);
+            task_                   = nullptr;
+            lk.unlock();
+            std::exception_ptr e;
+            try {
+                f();
+            } catch (...) {
+                e = std::current_exception();
+            }
+            lk.lock();
+            err_  = e;
+            busy_ = false;
+            cv_.notify_all();
+        }
+    }
+    std::mutex              mu_;
+    std::condition_variable cv_;
+    std::function<void()>   task_;
+    bool                    busy_ = false, stop_ = false;
+    std::exception_ptr      err_;
+    std::thread             th_;
+};
 
 struct Ctx {
     int          device    = 0;
@@ -31,8 +101,9 @@ struct Ctx {
     // second stream and workspace of this context (api.cu): matchScene prepares the dense
     // refinement scene there while it votes and clusters here; `fork` orders it after this
     // stream's work. Created on first use, released with the context.
-    std::unique_ptr<Ctx> aux;
-    cudaEvent_t          fork = nullptr;
+    std::unique_ptr<Ctx>    aux;
+    cudaEvent_t             fork = nullptr;
+    std::unique_ptr<Helper> helper; // host thread that drives `aux` (created with it)
     // single-pass scan state (prep.cu): per-tile status words, {ticket, wait-expired flag}
     struct ScanState {
         unsigned long long *status = nullptr;

@@ -8,6 +8,7 @@
 // point x angle bin) accumulator with shared atomics. Peaks, the top three candidates and
 // their poses come out of the same kernel. The multi-kernel pipeline in vote_pipe.cu
 // produces the same results with more parallelism when a workspace is available.
+#include <cstdlib>
 #include "sm_stages.h"
 #include "sm_vote.cuh"
 
@@ -84,8 +85,8 @@ __global__ void __launch_bounds__(kVoteBs, 2) k_vote_fused(VoteArgs a) {
         top[t] = Cand{-1.0f, INT_MAX, 0};
     unsigned long long myHash = 0;
 
-    bool narrow    = true;
-    int  chunk     = a.refChunk;
+    bool narrow    = !a.forceWide;
+    int  chunk     = narrow ? a.refChunk : a.refChunkWide;
     bool statsDone = false;
     for (int r0 = 0; r0 < a.ns;) {
         const int r1     = min(r0 + chunk, a.ns);
@@ -243,6 +244,9 @@ void vote_fused(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, co
     a.poseOk = out.poseOk;
     a.acc    = out.acc;
     a.dumpK  = out.acc ? dumpK : 0;
+    // the same test switch as the pipelined stage: 32-bit counters for every keypoint
+    const char *fw = std::getenv("SM_VOTE_FORCE_WIDE");
+    a.forceWide    = (fw && fw[0] == '1') ? 1 : 0;
     int optin = 0, perSM = 0;
     SM_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));
     SM_CUDA(cudaDeviceGetAttribute(&perSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c.device));

@@ -13,9 +13,14 @@ def pytest_configure(config):
 
 
 def reference_dir():
-    """The reference source tree, present only in the build container."""
-    d = os.environ.get("SM_REFERENCE_DIR", "/root/reference")
-    return d if os.path.exists(os.path.join(d, "kdtree", "nanoflann.hpp")) else None
+    """The reference source tree (present only where the reference's sources are), as the
+    oracle's build recipe for the reference probes locates it; None when absent."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle", "ref_probe"))
+    try:
+        import build_ref
+    finally:
+        sys.path.pop(0)
+    return build_ref.REF if build_ref.available() else None
 
 
 @pytest.fixture(scope="session")

@@ -20,6 +20,13 @@ def _dev_ptr(t):
     return C.c_void_p(t.data_ptr())
 
 
+def _workspace_bytes(det):
+    from surface_match_gb300 import _lib
+    b = C.c_int64(-1)
+    assert _lib.load().sm_context_workspace_bytes(det.ctx.handle, C.byref(b)) == 0
+    return b.value
+
+
 def _inputs():
     from surface_match_gb300 import Detector, MatchParam, PointCloud, synth
     mc, _, _ = synth.gear_model(6000, seed=5)
@@ -40,36 +47,91 @@ def _inputs():
     return det, pos.astype(np.float32), nrm, kp.astype(np.int32), off, ids
 
 
-def test_noalloc_vote_stage_matches_allocating_entry_twice():
+def _run_noalloc(det, L, pos, nrm, kp, off, ids, n_acc, dump):
     import torch
-    from surface_match_gb300 import _lib
-    det, pos, nrm, kp, off, ids = _inputs()
-    L = _lib.load()
-    dump = 3
-    ref_stats, ref_cands, ref_poses, ref_acc = det.vote_stage(pos, nrm, kp, off, ids, 0.2,
-                                                              dump_k=dump)
     K = len(kp)
     dpos = torch.from_numpy(pos).cuda()
     dnrm = torch.from_numpy(nrm).cuda()
     dkp = torch.from_numpy(kp).cuda()
     doff = torch.from_numpy(off).cuda()
     dids = torch.from_numpy(ids).cuda()
+    stats = torch.full((K, 8), -7, dtype=torch.int64, device="cuda")
+    cands = torch.full((K, 9), -7.0, dtype=torch.float32, device="cuda")
+    poses = torch.full((K, 3, 18), -7.0, dtype=torch.float32, device="cuda")
+    acc = torch.full((max(n_acc, 1),), -7, dtype=torch.int32, device="cuda")
+    # the library works on its context's own stream: the inputs and the -7 fills, written on
+    # torch's stream, must be complete before the call
+    torch.cuda.synchronize()
+    rc = L.sm_vote_stage_noalloc(det.model, _dev_ptr(dpos), _dev_ptr(dnrm), len(pos),
+                                 _dev_ptr(dkp), K, _dev_ptr(doff), _dev_ptr(dids), 0.2,
+                                 _dev_ptr(stats), _dev_ptr(cands), _dev_ptr(poses), dump,
+                                 _dev_ptr(acc))
+    return rc, stats.cpu().numpy(), cands.cpu().numpy(), poses.cpu().numpy(), \
+        acc.cpu().numpy()[:n_acc]
+
+
+def _check_equal(got, ref, what):
+    stats, cands, poses, acc = got
+    ref_stats, ref_cands, ref_poses, ref_acc = ref
+    np.testing.assert_array_equal(stats, ref_stats, err_msg=what)
+    np.testing.assert_array_equal(cands, ref_cands, err_msg=what)
+    np.testing.assert_array_equal(poses.view(np.uint32), ref_poses.view(np.uint32), err_msg=what)
+    np.testing.assert_array_equal(acc, ref_acc, err_msg=what)
+
+
+def test_noalloc_vote_stage_matches_allocating_entry_twice():
+    from surface_match_gb300 import _lib
+    det, pos, nrm, kp, off, ids = _inputs()
+    L = _lib.load()
+    dump = 3
+    ref = det.vote_stage(pos, nrm, kp, off, ids, 0.2, dump_k=dump)
+    ws = _workspace_bytes(det)
     for call in range(2):
-        stats = torch.full((K, 8), -7, dtype=torch.int64, device="cuda")
-        cands = torch.full((K, 9), -7.0, dtype=torch.float32, device="cuda")
-        poses = torch.full((K, 3, 18), -7.0, dtype=torch.float32, device="cuda")
-        acc = torch.full((len(ref_acc),), -7, dtype=torch.int32, device="cuda")
-        rc = L.sm_vote_stage_noalloc(det.model, _dev_ptr(dpos), _dev_ptr(dnrm), len(pos),
-                                     _dev_ptr(dkp), K, _dev_ptr(doff), _dev_ptr(dids), 0.2,
-                                     _dev_ptr(stats), _dev_ptr(cands), _dev_ptr(poses), dump,
-                                     _dev_ptr(acc))
+        rc, *got = _run_noalloc(det, L, pos, nrm, kp, off, ids, len(ref[3]), dump)
         assert rc == 0, _lib.last_error()
-        np.testing.assert_array_equal(stats.cpu().numpy(), ref_stats, err_msg=f"call {call}")
-        np.testing.assert_array_equal(cands.cpu().numpy(), ref_cands, err_msg=f"call {call}")
-        np.testing.assert_array_equal(poses.cpu().numpy().view(np.uint32),
-                                      ref_poses.view(np.uint32), err_msg=f"call {call}")
-        np.testing.assert_array_equal(acc.cpu().numpy(), ref_acc, err_msg=f"call {call}")
-    assert (ref_stats[:, 3] > 0).any(), "the case must cast votes"
+        _check_equal(got, ref, f"call {call}")
+    # the entry's contract: nothing is allocated, the context's workspace did not grow
+    assert _workspace_bytes(det) == ws
+    assert (ref[0][:, 3] > 0).any(), "the case must cast votes"
+
+
+def test_noalloc_vote_stage_matches_on_32bit_counters(monkeypatch):
+    """The switch that forces 32-bit accumulator counters reaches both entries; their
+    results still agree bit for bit."""
+    from surface_match_gb300 import _lib
+    det, pos, nrm, kp, off, ids = _inputs()
+    L = _lib.load()
+    monkeypatch.setenv("SM_VOTE_FORCE_WIDE", "1")
+    ref = det.vote_stage(pos, nrm, kp, off, ids, 0.2, dump_k=2)
+    rc, *got = _run_noalloc(det, L, pos, nrm, kp, off, ids, len(ref[3]), 2)
+    assert rc == 0, _lib.last_error()
+    _check_equal(got, ref, "32-bit counters")
+
+
+def test_noalloc_vote_stage_rejects_bad_offsets_before_reading_lists():
+    """Decreasing offsets whose last entry lies far beyond the ids buffer, and monotone
+    offsets whose total runs past the ids allocation, are argument errors; the lists are
+    never read with them."""
+    from surface_match_gb300 import _lib
+    det, pos, nrm, kp, off, ids = _inputs()
+    L = _lib.load()
+    bad = off.copy()
+    bad[1] = bad[2] + 5  # decreasing at 1 -> 2
+    bad[-1] = 1 << 30
+    rc, *_ = _run_noalloc(det, L, pos, nrm, kp, bad, ids, 0, 0)
+    assert rc == _lib.SM_ERR_ARG, _lib.last_error()
+    # monotone lists of at most n entries each, whose total (2000 x n ids, tens of MB) runs
+    # far past the small allocation that holds the ids
+    kp2 = np.resize(kp, 2000).astype(np.int32)
+    huge = (np.arange(2001, dtype=np.int64) * len(pos)).astype(np.int32)
+    rc, *_ = _run_noalloc(det, L, pos, nrm, kp2, huge, ids, 0, 0)
+    assert rc == _lib.SM_ERR_ARG, _lib.last_error()
+    assert "nbr_ids" in _lib.last_error()
+    # the context is still usable after the rejections
+    ref = det.vote_stage(pos, nrm, kp, off, ids, 0.2)
+    rc, *got = _run_noalloc(det, L, pos, nrm, kp, off, ids, 0, 0)
+    assert rc == 0, _lib.last_error()
+    _check_equal(got, (ref[0], ref[1], ref[2], np.zeros(0, np.int32)), "after rejections")
 
 
 def test_noalloc_vote_stage_rejects_sizes_beyond_its_scratch():
