@@ -248,6 +248,21 @@ SM_API int sm_vote_stage_noalloc(sm_model model, const float *points, const floa
 SM_API int64_t sm_debug_size(sm_model model, int field);
 SM_API int     sm_debug_get(sm_model model, int field, void *dst);
 
+/* Reference-order k-d tree probe, for parity checks of the search order the reference
+ * uses (KDTreeVectorOfVectorsAdaptor, kdtree/kdtree.h:65-79, over the vendored nanoflann:
+ * middle-split build with leaves of 10, depth-first searches). Builds the tree over the
+ * finite points of xyz (n x 3, host or device) with their tight box as root box and writes
+ * out_vacc[n]: the point ids in tree order (-1 after the finite ones; nullable). With
+ * step > 0, out_sampled receives samplePointCloud's result (util.cpp:107-139: greedy
+ * thinning at `step` in tree order, the kept ids in that order; capacity n) and
+ * *out_n_sampled its count. With nq > 0, out_knn[nq x k] receives the k nearest ids of each
+ * query (nq x 3 floats) in the reference's order (distance, then first found) and
+ * out_knn_dist (nullable) their squared distances. k <= 32. */
+SM_API int sm_kdtree_probe(sm_context ctx, const float *xyz, int64_t n, float step,
+                           int32_t *out_vacc, int32_t *out_sampled, int64_t *out_n_sampled,
+                           const float *queries, int64_t nq, int k, int32_t *out_knn,
+                           float *out_knn_dist);
+
 /* Message of the last failing call on this thread ("" if none). */
 SM_API const char *sm_last_error(void);
 

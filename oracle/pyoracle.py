@@ -81,6 +81,9 @@ def lib():
             L.orc_kd_probe.restype = C.c_int64
             L.orc_kd_probe.argtypes = [f32p, C.c_int64, f32p, f32p, C.c_float, i32p, i32p,
                                        C.c_int64]
+            L.orc_kd_sample.restype = C.c_int64
+            L.orc_kd_sample.argtypes = [f32p, C.c_int64, f32p, C.c_float, i32p]
+            L.orc_kd_knn.argtypes = [f32p, C.c_int64, f32p, f32p, C.c_int64, C.c_int, i32p, f32p]
             _lib = L
         return _lib
 
@@ -294,3 +297,29 @@ def mls(xyz, normal=None, indices=None, radius=1.0, order=2, invert=False, viewp
     lib().orc_mls(_p(pts), n, _p(idx, C.c_int64), len(idx), float(radius), int(order),
                   1 if invert else 0, _p(vp), _p(out_p), _p(out_n), _p(status, C.c_int32))
     return out_p, out_n, status
+
+
+def kd_reference(xyz, step=0.0, queries=None, k=10):
+    """The oracle's k-d tree over all points of xyz (tight box): vAcc order, the greedy
+    sample at `step` in tree order (when step > 0) and the k nearest of each query."""
+    L = lib()
+    xyz = np.ascontiguousarray(xyz, np.float32)
+    n = len(xyz)
+    box = np.concatenate([xyz.min(0), xyz.max(0)]).astype(np.float32)
+    vacc = np.zeros(n, np.int32)
+    q0 = np.zeros(3, np.float32)
+    found = np.zeros(1, np.int32)
+    L.orc_kd_probe(_p(xyz), n, _p(box), _p(q0), 0.0, _p(vacc, C.c_int32), _p(found, C.c_int32), 0)
+    sampled = None
+    if step > 0:
+        out = np.zeros(n, np.int32)
+        ns = L.orc_kd_sample(_p(xyz), n, _p(box), step, _p(out, C.c_int32))
+        sampled = out[:ns].copy()
+    knn = dist = None
+    if queries is not None:
+        qs = np.ascontiguousarray(queries, np.float32)
+        knn = np.zeros((len(qs), k), np.int32)
+        dist = np.zeros((len(qs), k), np.float32)
+        L.orc_kd_knn(_p(xyz), n, _p(box), _p(qs), len(qs), k, _p(knn, C.c_int32), _p(dist))
+    return vacc, sampled, knn, dist
+

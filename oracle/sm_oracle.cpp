@@ -1453,6 +1453,19 @@ int64_t orc_kd_probe(const float *xyz, int64_t n, const float *box, const float 
     return (int64_t)f.size();
 }
 
+// samplePointCloud (util.cpp:107-139) on the full tree of all n points: kept ids in tree
+// order into out (capacity n); returns their count.
+int64_t orc_kd_sample(const float *xyz, int64_t n, const float *box, float step, int *out) {
+    std::vector<V3> P(n);
+    for (int64_t i = 0; i < n; i++) P[i] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+    std::vector<int> valid(n);
+    std::iota(valid.begin(), valid.end(), 0);
+    orc::KdTree t(P, valid, V3{box[0], box[1], box[2]}, V3{box[3], box[4], box[5]});
+    std::vector<int> r = kd_sample(t, step, nullptr);
+    memcpy(out, r.data(), r.size() * 4);
+    return (int64_t)r.size();
+}
+
 } // extern "C"
 
 extern "C" void orc_kd_knn(const float *xyz, int64_t n, const float *box, const float *qs,

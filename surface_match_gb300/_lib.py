@@ -83,6 +83,8 @@ _SIGNATURES = {
     "sm_server_status": (C.c_int, [_vp, _i64p]),
     "sm_vote_stage_noalloc": (C.c_int, [_vp, _vp, _vp, C.c_int64, _vp, C.c_int64, _vp, _vp,
                                         C.c_float, _vp, _vp, _vp, C.c_int, _vp]),
+    "sm_kdtree_probe": (C.c_int, [_vp, _f32p, C.c_int64, C.c_float, _i32p, _i32p, _i64p, _f32p,
+                                  C.c_int64, C.c_int, _i32p, _f32p]),
     "sm_debug_size": (C.c_int64, [_vp, C.c_int]),
     "sm_debug_get": (C.c_int, [_vp, C.c_int, _vp]),
     "sm_last_error": (C.c_char_p, []),

@@ -19,10 +19,11 @@ BUILD = os.path.join(HERE, "_build")
 INCLUDE = os.path.abspath(os.path.join(HERE, "..", "include"))
 LIB = os.path.join(HERE, "libsurface_match.so")
 
-CU_SOURCES = ["prep.cu", "vote.cu", "vote_pipe.cu", "cluster.cu", "icp.cu", "api.cu", "noalloc.cu", "batch.cu", "server.cu",
+CU_SOURCES = ["sort.cu", "kdtree.cu", "prep.cu", "vote.cu", "vote_pipe.cu", "cluster.cu", "icp.cu", "api.cu", "noalloc.cu", "batch.cu", "server.cu",
               "probe.cu", "mls.cu"]
 CPP_SOURCES: list = []
 HEADERS = ["sm_math.h", "sm_linalg.h", "sm_icp.h", "sm_grid.h", "sm_device.cuh", "sm_vote.cuh",
+           "sm_kdtree.cuh",
            "sm_engine.h", "sm_stages.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-prec-div=true",

@@ -886,6 +886,66 @@ SM_API int sm_estimate_normals_mls(sm_context ctx, const float *xyzIn, const flo
     });
 }
 
+// Reference-order k-d tree probe (kdtree.h:65-79, util.cpp:107-139, nanoflann
+// findNeighbors): the tree over the finite points with their tight box as root box.
+SM_API int sm_kdtree_probe(sm_context ctx, const float *xyzIn, int64_t n64, float step,
+                           int32_t *outVacc, int32_t *outSampled, int64_t *outNSampled,
+                           const float *queries, int64_t nq64, int k, int32_t *outKnn,
+                           float *outKnnDist) {
+    return guarded([&] {
+        if (!ctx || !xyzIn)
+            throw Error(SM_ERR_ARG, "NULL argument");
+        if (n64 <= 0 || n64 > (1ll << 30) || nq64 < 0 || nq64 > (1ll << 30))
+            throw Error(SM_ERR_ARG, "bad point count");
+        if (nq64 > 0 && (!queries || !outKnn || k < 1))
+            throw Error(SM_ERR_ARG, "kNN queries need queries, out_knn and k >= 1");
+        const int n = (int)n64, nq = (int)nq64;
+        Ctx      &c = ctx->ctx;
+        SM_CUDA(cudaSetDevice(c.device));
+        const float *xyz = to_device(c, xyzIn, n, "kp.xyz");
+        float4      *pos = c.arena.get<float4>("kp.pos", n);
+        float4      *nrm = c.arena.get<float4>("kp.n4", n);
+        int         *val = c.arena.get<int>("kp.valid", n);
+        Box          box;
+        const int    nvalid = prep_points(c, xyz, nullptr, n, pos, nrm, val, box);
+        int         *valid  = c.arena.get<int>("kp.vids", n);
+        compact_known(c, val, n, valid, "kp.cv");
+        KdTree T;
+        build_kdtree(c, pos, n, valid, nvalid, box, T, "kp.tree");
+        if (outVacc) {
+            std::vector<int> h(n, -1);
+            if (nvalid)
+                SM_CUDA(cudaMemcpy(h.data(), T.vacc, (size_t)nvalid * 4, cudaMemcpyDeviceToHost));
+            memcpy(outVacc, h.data(), (size_t)n * 4);
+        }
+        if (step > 0 && outSampled) {
+            int      *ids = c.arena.get<int>("kp.sampled", n);
+            const int ns  = kd_sample(c, T, nullptr, pos, step, box, ids, nullptr, "kp.s");
+            if (ns)
+                SM_CUDA(cudaMemcpy(outSampled, ids, (size_t)ns * 4, cudaMemcpyDeviceToHost));
+            if (outNSampled)
+                *outNSampled = ns;
+        }
+        if (nq > 0) {
+            float4 *q4 = c.arena.get<float4>("kp.q4", nq);
+            float  *qd = c.arena.get<float>("kp.q", (size_t)nq * 3);
+            SM_CUDA(cudaMemcpyAsync(qd, queries, (size_t)nq * 12, cudaMemcpyDefault, c.stream));
+            k_f3_to_f4<<<nblocks(nq, 256), 256, 0, c.stream>>>(qd, nq, q4);
+            SM_LAUNCH_CHECK();
+            int   *cnt = c.arena.get<int>("kp.nq", 1);
+            int   *nb  = c.arena.get<int>("kp.nb", (size_t)nq * k);
+            float *nd  = c.arena.get<float>("kp.nd", (size_t)nq * k);
+            SM_CUDA(cudaMemcpyAsync(cnt, &nq, sizeof(int), cudaMemcpyHostToDevice, c.stream));
+            kd_knn(c, T, nullptr, pos, q4, nullptr, cnt, nq, k, nb, nd, nullptr);
+            c.sync_checked();
+            SM_CUDA(cudaMemcpy(outKnn, nb, (size_t)nq * k * 4, cudaMemcpyDeviceToHost));
+            if (outKnnDist)
+                SM_CUDA(cudaMemcpy(outKnnDist, nd, (size_t)nq * k * 4, cudaMemcpyDeviceToHost));
+        }
+        c.sync_checked();
+    });
+}
+
 SM_API int sm_model_create(sm_context ctx, sm_model *out) {
     return guarded([&] {
         if (!ctx || !out)

@@ -1,0 +1,960 @@
+// kdtree.cu - the reference-order k-d tree on the GPU: build, searches, and the greedy
+// sampler in tree order.
+//
+// Reference counterparts: KDTreeVectorOfVectorsAdaptor (kdtree/kdtree.h:52-161) over the
+// vendored nanoflann (kdtree/nanoflann.hpp: divideTree 1120-1176, middleSplit_ 1290-1339,
+// planeSplit 1352-1393, searchLevel 1846-1930) and samplePointCloud (util.cpp:107-139).
+//
+// Build. nanoflann splits a node's index range [left, right) recursively: the cut axis is
+// the one of largest point spread among the axes whose box side is within (1 - 1e-5) of
+// the widest, the cut value the box middle clamped to the points' range, and the range is
+// reordered by two in-place Hoare passes (values < cut to the front, then values <= cut).
+// Each pass has a closed form: with T the number of elements that go to the front, the
+// j-th element of the front part that does not belong there is swapped with the j-th
+// element from the back of the rear part that does - so a pass is a prefix sum and a
+// batch of disjoint swaps. The GPU builds all nodes of one depth at once (segments of the
+// position array, one kernel per step, prefix sums over the whole array) until every open
+// range holds at most kSmall points; those finish in one CTA each, in shared memory, with
+// the same steps. Node bounds are then tightened bottom-up (divlow/divhigh are the
+// children's tight bounds, the root box becomes the tight box of all points, as nanoflann
+// does through its by-reference bbox).
+//
+// Greedy sampling in tree order. The reference keeps a point unless an already kept point's
+// radius search found it, visiting points in tree position order. On the GPU the points
+// are bucketed into grid cells of side >= step, each cell's points in tree order; a warp
+// advances a cell's cursor point by point: the point is dropped if a kept point of its own
+// or a neighbouring cell with an earlier tree position reaches it, and kept once every
+// neighbouring cell has decided all its points before it. Cells wait only on cells whose
+// pending point comes earlier in tree order, so the cell holding the earliest undecided
+// point always advances. "Reaches" is the reference's radius search membership: squared
+// distance below step^2 and not pruned by the search above the point's leaf - decided by
+// walking the point's root-to-leaf path (smk::kd_reaches) unless the distance bound proves
+// the pruning cannot happen (points moved by normal estimation can leave their leaf's box).
+#include <climits>
+#include <cmath>
+
+#include "sm_kdtree.cuh"
+#include "sm_stages.h"
+
+namespace sm {
+using namespace smd;
+using smk::KdView;
+
+namespace {
+
+struct GridParamsK {
+    float org[3], g;
+    int   dim[3];
+};
+
+constexpr int kSmall    = 1024; // ranges of at most this many points finish in one CTA
+constexpr int kSmallSeg = 96;   // open sub-ranges per level inside that CTA (> 10 points each: <= 93)
+
+// An open range of the build (one future node) and its split.
+struct Seg {
+    int   left, right, node, cutfeat;
+    float lo[3], hi[3]; // the box nanoflann passes down (parent box cut at the split)
+    int   mn[3], mx[3]; // ordered-int min / max of the points (computeMinMax)
+    float cutval;
+    int   index;    // split offset from left
+    int   child[2]; // next-level segment of each child (-1: leaf or small range)
+    int   depth;    // depth of the node (root 0)
+};
+
+// Lanes add their point's ordered coordinates to the bounds of their range (s < 0: none);
+// a warp whose lanes share one range reduces first and adds once.
+template <class S>
+__device__ __forceinline__ void add_bounds(S *seg, int s, const float4 &p) {
+    const int  o[3] = {f2ord(p.x), f2ord(p.y), f2ord(p.z)};
+    const int  s0   = __shfl_sync(0xffffffffu, s, 0);
+    const bool same = __all_sync(0xffffffffu, s == s0);
+    if (same) {
+        if (s0 < 0)
+            return;
+        int lo[3], hi[3];
+        for (int a = 0; a < 3; a++) {
+            lo[a] = __reduce_min_sync(0xffffffffu, o[a]);
+            hi[a] = __reduce_max_sync(0xffffffffu, o[a]);
+        }
+        if ((threadIdx.x & 31) == 0)
+            for (int a = 0; a < 3; a++) {
+                atomicMin(&seg[s0].mn[a], lo[a]);
+                atomicMax(&seg[s0].mx[a], hi[a]);
+            }
+        return;
+    }
+    if (s >= 0)
+        for (int a = 0; a < 3; a++) {
+            atomicMin(&seg[s].mn[a], o[a]);
+            atomicMax(&seg[s].mx[a], o[a]);
+        }
+}
+
+__device__ __forceinline__ float coord_of(const float4 &p, int a) {
+    return a == 0 ? p.x : (a == 1 ? p.y : p.z);
+}
+
+// middleSplit_'s choice of axis and cut value (nanoflann.hpp:1290-1329).
+__device__ void choose_cut(const float lo[3], const float hi[3], const int mn[3], const int mx[3],
+                           int &cutfeat, float &cutval) {
+    const float EPS     = 0.00001f;
+    float       maxSpan = hi[0] - lo[0];
+    for (int i = 1; i < 3; ++i) {
+        const float span = hi[i] - lo[i];
+        if (span > maxSpan)
+            maxSpan = span;
+    }
+    float maxSpread = -1.0f, minElem = 0.0f, maxElem = 0.0f;
+    cutfeat = 0;
+    for (int i = 0; i < 3; ++i) {
+        const float span = hi[i] - lo[i];
+        if (span > (1.0f - EPS) * maxSpan) {
+            const float a = ord2f(mn[i]), b = ord2f(mx[i]);
+            const float spread = b - a;
+            if (spread > maxSpread) {
+                cutfeat   = i;
+                maxSpread = spread;
+                minElem   = a;
+                maxElem   = b;
+            }
+        }
+    }
+    const float splitVal = (lo[cutfeat] + hi[cutfeat]) / 2.0f;
+    if (splitVal < minElem)
+        cutval = minElem;
+    else if (splitVal > maxElem)
+        cutval = maxElem;
+    else
+        cutval = splitVal;
+}
+
+// middleSplit_'s split offset from the two partition limits (nanoflann.hpp:1333-1338).
+__device__ __forceinline__ int split_index(int count, int lim1, int lim2) {
+    if (lim1 > count / 2)
+        return lim1;
+    if (lim2 < count / 2)
+        return lim2;
+    return count / 2;
+}
+
+__device__ __forceinline__ int4 leaf_node(int l, int r) { return make_int4(l, r, -1, 0); }
+
+// ---- top levels: one kernel per step over the whole position array -------------------
+__global__ void k_kd_root(Seg *seg, Seg *small, int m, Box box, int4 *nd, int *parent, int *cnt) {
+    Seg s{};
+    s.left  = 0;
+    s.right = m;
+    s.node  = 0;
+    s.depth = 0;
+    for (int a = 0; a < 3; a++) {
+        s.lo[a] = box.mn[a];
+        s.hi[a] = box.mx[a];
+        s.mn[a] = INT_MAX;
+        s.mx[a] = INT_MIN;
+    }
+    s.child[0] = s.child[1] = -1;
+    seg[0]     = s;
+    parent[0]  = -1;
+    cnt[0]     = 1;                    // nodes
+    cnt[4]     = m > kSmall ? 1 : 0;  // open ranges of the first level
+    if (m <= smk::kLeafMax) {
+        nd[0] = leaf_node(0, m);
+    } else if (m <= kSmall) {
+        small[0] = s;                  // the whole cloud is one small range
+        cnt[2]   = 1;
+    }
+}
+
+__global__ void k_kd_init(const float4 *__restrict__ pos, const int *__restrict__ ids, int m,
+                          float4 *__restrict__ rec, int *__restrict__ segOf, Seg *__restrict__ seg) {
+    const int i  = blockIdx.x * blockDim.x + threadIdx.x;
+    float4    p  = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (i < m) {
+        const int id = ids[i];
+        p            = pos[id];
+        rec[i]       = make_float4(p.x, p.y, p.z, __int_as_float(id));
+        segOf[i]     = 0;
+    }
+    add_bounds(seg, i < m ? 0 : -1, p);
+}
+
+__global__ void k_kd_cut(Seg *__restrict__ seg, const int *__restrict__ nseg) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= *nseg)
+        return;
+    Seg &S = seg[s];
+    choose_cut(S.lo, S.hi, S.mn, S.mx, S.cutfeat, S.cutval);
+}
+
+// pass 1: value < cut over [left, right); pass 2: value <= cut over [left + lim1, right)
+__device__ __forceinline__ int pass_start(const Seg &S, int pass, const int *g1) {
+    return pass == 1 ? S.left : S.left + (g1[S.right] - g1[S.left]);
+}
+
+__global__ void k_kd_flags(const float4 *__restrict__ rec, const int *__restrict__ segOf, int m,
+                           const Seg *__restrict__ seg, int pass, const int *__restrict__ g1,
+                           int *__restrict__ flag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > m)
+        return;
+    int f = 0;
+    if (i < m) {
+        const int s = segOf[i];
+        if (s >= 0) {
+            const Seg &S = seg[s];
+            if (i >= pass_start(S, pass, g1)) {
+                const float x = coord_of(rec[i], S.cutfeat);
+                f             = pass == 1 ? (x < S.cutval) : (x <= S.cutval);
+            }
+        }
+    }
+    flag[i] = f;
+}
+
+// The back part's misplaced elements record their positions by rank from the back.
+__global__ void k_kd_rank(const int *__restrict__ segOf, int m, const Seg *__restrict__ seg,
+                          int pass, const int *__restrict__ g1, const int *__restrict__ flag,
+                          const int *__restrict__ g, int *__restrict__ badR) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m || !flag[i])
+        return;
+    const int s = segOf[i];
+    if (s < 0)
+        return;
+    const Seg &S = seg[s];
+    const int  a = pass_start(S, pass, g1);
+    if (i < a)
+        return;
+    const int T = g[S.right] - g[a], lt = g[i] - g[a];
+    if (i - a >= T)
+        badR[a + (T - lt - 1)] = i;
+}
+
+// The front part's misplaced elements swap with their partners (disjoint pairs).
+__global__ void k_kd_swap(float4 *__restrict__ rec, const int *__restrict__ segOf, int m,
+                          const Seg *__restrict__ seg, int pass, const int *__restrict__ g1,
+                          const int *__restrict__ flag, const int *__restrict__ g,
+                          const int *__restrict__ badR) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m || flag[i])
+        return;
+    const int s = segOf[i];
+    if (s < 0)
+        return;
+    const Seg &S = seg[s];
+    const int  a = pass_start(S, pass, g1);
+    if (i < a)
+        return;
+    const int T = g[S.right] - g[a], lt = g[i] - g[a];
+    if (i - a < T) {
+        const int    p = badR[a + (i - a - lt)];
+        const float4 x = rec[i];
+        rec[i]         = rec[p];
+        rec[p]         = x;
+    }
+}
+
+// Children of every open range: nodes, leaves, small ranges and next-level ranges.
+__global__ void k_kd_children(Seg *__restrict__ seg, const int *__restrict__ nseg,
+                              const int *__restrict__ g1, const int *__restrict__ g2,
+                              int4 *__restrict__ nd, int *__restrict__ parent,
+                              int *__restrict__ nodeCount, Seg *__restrict__ next,
+                              int *__restrict__ nnext, Seg *__restrict__ small,
+                              int *__restrict__ nsmall, int *__restrict__ depthErr) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= *nseg)
+        return;
+    Seg      &S     = seg[s];
+    const int count = S.right - S.left;
+    const int lim1  = g1[S.right] - g1[S.left];
+    const int lim2  = lim1 + (g2[S.right] - g2[S.left + lim1]);
+    const int index = split_index(count, lim1, lim2);
+    S.index         = index;
+    const int c1    = atomicAdd(nodeCount, 2);
+    nd[S.node]      = make_int4(0, 0, c1 | (S.cutfeat << 30), S.left + index);
+    if (S.depth + 1 >= smk::kMaxDepth)
+        atomicExch(depthErr, 1);
+    for (int k = 0; k < 2; k++) {
+        const int l = k == 0 ? S.left : S.left + index;
+        const int r = k == 0 ? S.left + index : S.right;
+        Seg       C{};
+        C.left  = l;
+        C.right = r;
+        C.node  = c1 + k;
+        for (int a = 0; a < 3; a++) {
+            C.lo[a] = S.lo[a];
+            C.hi[a] = S.hi[a];
+            C.mn[a] = INT_MAX;
+            C.mx[a] = INT_MIN;
+        }
+        if (k == 0)
+            C.hi[S.cutfeat] = S.cutval;
+        else
+            C.lo[S.cutfeat] = S.cutval;
+        C.child[0] = C.child[1] = -1;
+        C.depth    = S.depth + 1;
+        parent[c1 + k]          = S.node;
+        S.child[k]              = -1;
+        if (r - l <= smk::kLeafMax) {
+            nd[c1 + k] = leaf_node(l, r);
+        } else if (r - l <= kSmall) {
+            small[atomicAdd(nsmall, 1)] = C;
+        } else {
+            const int id = atomicAdd(nnext, 1);
+            next[id]     = C;
+            S.child[k]   = id;
+        }
+    }
+}
+
+// Next-level segment of every position, and the next level's point bounds.
+__global__ void k_kd_advance(const float4 *__restrict__ rec, int *__restrict__ segOf, int m,
+                             const Seg *__restrict__ seg, Seg *__restrict__ next) {
+    const int i  = blockIdx.x * blockDim.x + threadIdx.x;
+    int       ns = -1;
+    float4    p  = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (i < m) {
+        const int s = segOf[i];
+        if (s >= 0) {
+            const Seg &S = seg[s];
+            ns           = S.child[i < S.left + S.index ? 0 : 1];
+            segOf[i]     = ns;
+            p            = rec[i];
+        }
+    }
+    add_bounds(next, ns, p);
+}
+
+// ---- small ranges: one CTA of 1024 threads, one position per thread -------------------
+struct SubSeg {
+    int   left, right, node, cutfeat;
+    float lo[3], hi[3];
+    int   mn[3], mx[3];
+    float cutval;
+    int   index, child[2], depth;
+};
+
+__global__ void __launch_bounds__(kSmall)
+    k_kd_small(const Seg *__restrict__ small, float4 *__restrict__ rec, int4 *__restrict__ nd,
+               int *__restrict__ parent, int *__restrict__ nodeCount, int *__restrict__ err) {
+    __shared__ float4 r[kSmall];
+    __shared__ short  sid[kSmall];
+    __shared__ int    sc1[kSmall + 1], sc2[kSmall + 1], bad[kSmall];
+    __shared__ SubSeg ss[2][kSmallSeg];
+    __shared__ int    nsub[2];
+    __shared__ int    wsum[33];
+    const Seg S0  = small[blockIdx.x];
+    const int n   = S0.right - S0.left;
+    const int t   = threadIdx.x;
+    if (t < n)
+        r[t] = rec[S0.left + t];
+    sid[t] = (short)(t < n ? 0 : -1);
+    if (t == 0) {
+        SubSeg z{};
+        z.left  = 0;
+        z.right = n;
+        z.node  = S0.node;
+        z.depth = S0.depth;
+        for (int a = 0; a < 3; a++) {
+            z.lo[a] = S0.lo[a];
+            z.hi[a] = S0.hi[a];
+            z.mn[a] = INT_MAX;
+            z.mx[a] = INT_MIN;
+        }
+        ss[0][0] = z;
+        nsub[0]  = 1;
+        nsub[1]  = 0;
+    }
+    __syncthreads();
+    int cur = 0;
+    while (nsub[cur] > 0) {
+        SubSeg *L = ss[cur];
+        SubSeg *N = ss[cur ^ 1];
+        // point bounds per open range
+        add_bounds(L, sid[t], r[t]);
+        __syncthreads();
+        if (t < nsub[cur])
+            choose_cut(L[t].lo, L[t].hi, L[t].mn, L[t].mx, L[t].cutfeat, L[t].cutval);
+        __syncthreads();
+        for (int pass = 1; pass <= 2; pass++) {
+            int *sc = pass == 1 ? sc1 : sc2;
+            int  f  = 0;
+            int  a  = 0;
+            if (sid[t] >= 0) {
+                const SubSeg &Q = L[sid[t]];
+                a = pass == 1 ? Q.left : Q.left + (sc1[Q.right] - sc1[Q.left]);
+                if (t >= a) {
+                    const float x = coord_of(r[t], Q.cutfeat);
+                    f             = pass == 1 ? (x < Q.cutval) : (x <= Q.cutval);
+                }
+            }
+            int tot;
+            const int ex = block_excl_scan(f, wsum, &tot);
+            sc[t]        = ex;
+            if (t == 0)
+                sc[kSmall] = tot;
+            __syncthreads();
+            int T = 0, lt = 0;
+            if (sid[t] >= 0 && t >= a) {
+                const SubSeg &Q = L[sid[t]];
+                T               = sc[Q.right] - sc[a];
+                lt              = sc[t] - sc[a];
+                if (f && t - a >= T)
+                    bad[a + (T - lt - 1)] = t;
+            }
+            __syncthreads();
+            float4 mine = r[t], other = mine;
+            int    p    = -1;
+            if (sid[t] >= 0 && t >= a && !f && t - a < T) {
+                p     = bad[a + (t - a - lt)];
+                other = r[p];
+            }
+            __syncthreads();
+            if (p >= 0) {
+                r[t] = other;
+                r[p] = mine;
+            }
+            __syncthreads();
+        }
+        if (t == 0)
+            nsub[cur ^ 1] = 0;
+        __syncthreads();
+        if (t < nsub[cur]) {
+            SubSeg   &Q     = L[t];
+            const int count = Q.right - Q.left;
+            const int lim1  = sc1[Q.right] - sc1[Q.left];
+            const int lim2  = lim1 + (sc2[Q.right] - sc2[Q.left + lim1]);
+            const int index = split_index(count, lim1, lim2);
+            Q.index         = index;
+            const int c1    = atomicAdd(nodeCount, 2);
+            nd[Q.node]      = make_int4(0, 0, c1 | (Q.cutfeat << 30), S0.left + Q.left + index);
+            if (Q.depth + 1 >= smk::kMaxDepth)
+                atomicExch(err, 1);
+            for (int k = 0; k < 2; k++) {
+                const int l = k == 0 ? Q.left : Q.left + index;
+                const int rr = k == 0 ? Q.left + index : Q.right;
+                parent[c1 + k] = Q.node;
+                Q.child[k]     = -1;
+                if (rr - l <= smk::kLeafMax) {
+                    nd[c1 + k] = leaf_node(S0.left + l, S0.left + rr);
+                } else {
+                    const int id = atomicAdd(&nsub[cur ^ 1], 1);
+                    if (id >= kSmallSeg) {
+                        atomicExch(err, 2);
+                        continue;
+                    }
+                    SubSeg C{};
+                    C.left  = l;
+                    C.right = rr;
+                    C.node  = c1 + k;
+                    C.depth = Q.depth + 1;
+                    for (int a = 0; a < 3; a++) {
+                        C.lo[a] = Q.lo[a];
+                        C.hi[a] = Q.hi[a];
+                        C.mn[a] = INT_MAX;
+                        C.mx[a] = INT_MIN;
+                    }
+                    if (k == 0)
+                        C.hi[Q.cutfeat] = Q.cutval;
+                    else
+                        C.lo[Q.cutfeat] = Q.cutval;
+                    N[id]      = C;
+                    Q.child[k] = id;
+                }
+            }
+        }
+        __syncthreads();
+        if (t == 0 && nsub[cur ^ 1] > kSmallSeg)
+            nsub[cur ^ 1] = 0; // overflow reported through err; stop
+        if (sid[t] >= 0) {
+            const SubSeg &Q = L[sid[t]];
+            sid[t]          = (short)Q.child[t < Q.left + Q.index ? 0 : 1];
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+    if (t < n)
+        rec[S0.left + t] = r[t];
+}
+
+// ---- finish: tight boxes bottom-up, split bounds, per-position indexes ----------------
+__global__ void k_kd_finish(int4 *__restrict__ nd, const int *__restrict__ parent,
+                            const int *__restrict__ nodeCount, const float4 *__restrict__ rec,
+                            float *__restrict__ box, int *__restrict__ arrive,
+                            int *__restrict__ vacc, int *__restrict__ leafOf,
+                            int *__restrict__ treePos) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= *nodeCount)
+        return;
+    const int4 n = nd[v];
+    if (!smk::is_leaf(n))
+        return;
+    float lo[3], hi[3];
+    {
+        const float4 p = rec[n.x];
+        lo[0] = hi[0] = p.x;
+        lo[1] = hi[1] = p.y;
+        lo[2] = hi[2] = p.z;
+    }
+    for (int i = n.x; i < n.y; i++) {
+        const float4 p  = rec[i];
+        const float  c3[3] = {p.x, p.y, p.z};
+        for (int a = 0; a < 3; a++) {
+            if (lo[a] > c3[a])
+                lo[a] = c3[a];
+            if (hi[a] < c3[a])
+                hi[a] = c3[a];
+        }
+        const int id = __float_as_int(p.w);
+        vacc[i]      = id;
+        leafOf[i]    = v;
+        treePos[id]  = i;
+    }
+    for (int a = 0; a < 3; a++) {
+        box[6 * v + a]     = lo[a];
+        box[6 * v + 3 + a] = hi[a];
+    }
+    // the second child to finish tightens the parent
+    int u = v;
+    for (;;) {
+        const int p = parent[u];
+        if (p < 0)
+            return;
+        __threadfence();
+        if (atomicAdd(&arrive[p], 1) == 0)
+            return;
+        __threadfence();
+        const int4 pn = nd[p];
+        const int  c1 = smk::child1_of(pn), cf = smk::divfeat_of(pn);
+        const volatile float *b1 = box + 6 * c1;
+        const volatile float *b2 = box + 6 * (c1 + 1);
+        for (int a = 0; a < 3; a++) {
+            box[6 * p + a]     = fminf(b1[a], b2[a]);
+            box[6 * p + 3 + a] = fmaxf(b1[3 + a], b2[3 + a]);
+        }
+        nd[p].x = __float_as_int(b1[3 + cf]); // divlow: child1's upper bound on the cut axis
+        nd[p].y = __float_as_int(b2[cf]);     // divhigh: child2's lower bound
+        u       = p;
+    }
+}
+
+// ---- greedy sampling in tree order ---------------------------------------------------
+constexpr uint32_t kNoCell    = 1u << 23; // sort key of positions reduce() excluded
+constexpr int      kSpBs      = 256;
+constexpr long long kSpIdle   = 1ll << 22; // passes without progress before giving up
+
+struct SampleArgs {
+    KdView          t;
+    const float    *nodeBox;
+    const int      *leafOf;
+    float           org[3], g;
+    int             dim[3];
+    const uint32_t *sortPos;  // tree positions grouped by cell, tree order inside a cell
+    const int      *cellRank; // dense cell -> occupied rank (-1: empty)
+    const int      *cellList; // occupied rank -> dense cell
+    const int      *cellEnd;  // occupied rank -> end of its run in sortPos
+    int            *cursor;   // occupied rank -> next undecided entry of its run
+    int            *cursorPos;// occupied rank -> tree position of that entry (INT_MAX: done)
+    int            *keptCnt;  // occupied rank -> kept points
+    float4         *kept;     // occupied rank x cap: {x, y, z, tree position bits}
+    int             cap, ncells;
+    float           r2;
+    double          safe2;
+    int            *keptFlag; // per tree position
+    int            *err;      // [0] kept capacity, [1] wait limit
+};
+
+__device__ __forceinline__ int ld_vol(const int *p) { return *(const volatile int *)p; }
+
+// Distance of a (moved) point from its leaf's build-time box.
+__device__ __forceinline__ double excursion(const float *box, const float4 &p) {
+    const float c[3] = {p.x, p.y, p.z};
+    double      s    = 0.0;
+    for (int a = 0; a < 3; a++) {
+        const double lo = box[a], hi = box[3 + a], x = c[a];
+        const double o  = x < lo ? lo - x : (x > hi ? x - hi : 0.0);
+        s += o * o;
+    }
+    return sqrt(s);
+}
+
+// Whether the radius search from kept point q reaches the point p at tree position ip
+// (radiusSearch membership, nanoflann.hpp:1736-1749): distance first; the search's
+// lower bound at any node above p's leaf is at most (|q - p| + excursion)^2, so the path
+// walk is needed only near the radius or for points that left their leaf's box. The
+// margin covers the float rounding of the search's running bound.
+__device__ __forceinline__ bool reaches(const SampleArgs &a, const float4 &q, const float4 &p,
+                                        int ip, double e) {
+    const float qq[3] = {q.x, q.y, q.z};
+    const float d     = smk::eval_metric(qq, p);
+    if (!(d < a.r2))
+        return false;
+    const double b = sqrt((double)d) + e;
+    if (b * b < a.safe2)
+        return true;
+    uint64_t key;
+    return smk::kd_reaches(a.t, qq, ip, a.r2, &key);
+}
+
+__global__ void k_sp_keys(const int *__restrict__ vaccA, const float4 *__restrict__ pos, int m,
+                          GridParamsK gp, uint32_t *__restrict__ key, uint32_t *__restrict__ val) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m)
+        return;
+    const int id = vaccA[i];
+    uint32_t  k  = kNoCell;
+    if (id >= 0) {
+        const float4 p  = pos[id];
+        const int    cx = smg::coord(p.x, gp.org[0], gp.g, gp.dim[0]);
+        const int    cy = smg::coord(p.y, gp.org[1], gp.g, gp.dim[1]);
+        const int    cz = smg::coord(p.z, gp.org[2], gp.g, gp.dim[2]);
+        k               = (uint32_t)((cz * gp.dim[1] + cy) * gp.dim[0] + cx);
+    }
+    key[i] = k;
+    val[i] = (uint32_t)i;
+}
+
+__global__ void k_sp_heads(const uint32_t *__restrict__ key, int m, int *__restrict__ head) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > m)
+        return;
+    head[k] = (k < m && key[k] != kNoCell && (k == 0 || key[k - 1] != key[k])) ? 1 : 0;
+}
+
+__global__ void k_sp_cells(const uint32_t *__restrict__ key, const uint32_t *__restrict__ val,
+                           int m, const int *__restrict__ head, const int *__restrict__ rank,
+                           int *__restrict__ cellRank, int *__restrict__ cellList,
+                           int *__restrict__ cellEnd, int *__restrict__ cursor,
+                           int *__restrict__ cursorPos, int *__restrict__ keptCnt) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m || key[k] == kNoCell)
+        return;
+    const int r = rank[k] + head[k] - 1; // the run's occupied rank
+    if (head[k]) {
+        cellRank[key[k]] = r;
+        cellList[r]      = (int)key[k];
+        cursor[r]        = k;
+        cursorPos[r]     = (int)val[k];
+        keptCnt[r]       = 0;
+    }
+    if (k == m - 1 || key[k + 1] != key[k])
+        cellEnd[r] = k + 1;
+}
+
+// One warp per cell (cells dealt round-robin to the warps of a co-resident grid); a warp
+// sweeps its cells, advancing each cursor as far as its neighbours allow, until all are
+// done.
+__global__ void __launch_bounds__(kSpBs) k_sp_run(SampleArgs a) {
+    const int  lane = threadIdx.x & 31;
+    const int  gw   = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+    const int  nw   = (int)(((long long)gridDim.x * blockDim.x) >> 5);
+    long long  idle = 0;
+    for (;;) {
+        bool open = false, moved = false;
+        for (int r = gw; r < a.ncells; r += nw) {
+            int       k   = ld_vol(&a.cursor[r]);
+            const int end = a.cellEnd[r];
+            if (k >= end)
+                continue;
+            open          = true;
+            const int cid = a.cellList[r];
+            const int cx = cid % a.dim[0], cy = (cid / a.dim[0]) % a.dim[1],
+                      cz = cid / (a.dim[0] * a.dim[1]);
+            int nr = -1;
+            if (lane < 27) {
+                const int x = cx + lane % 3 - 1, y = cy + (lane / 3) % 3 - 1, z = cz + lane / 9 - 1;
+                if (x >= 0 && y >= 0 && z >= 0 && x < a.dim[0] && y < a.dim[1] && z < a.dim[2])
+                    nr = a.cellRank[(z * a.dim[1] + y) * a.dim[0] + x];
+            }
+            while (k < end) {
+                const int ip = (int)a.sortPos[k];
+                bool      ok = true;
+                if (nr >= 0 && nr != r)
+                    ok = ld_vol(&a.cursorPos[nr]) >= ip;
+                if (!__all_sync(0xffffffffu, ok))
+                    break;
+                __threadfence(); // the neighbours' kept lists are complete below ip
+                const float4 p = a.t.pos[a.t.vacc[ip]];
+                const double e = excursion(a.nodeBox + 6 * (size_t)a.leafOf[ip], p);
+                bool         cov = false;
+                if (nr >= 0) {
+                    const int kc = ld_vol(&a.keptCnt[nr]);
+                    for (int t = 0; t < kc && !cov; t++) {
+                        const volatile float4 *qp = a.kept + (size_t)nr * a.cap + t;
+                        const float4 q = make_float4(qp->x, qp->y, qp->z, qp->w);
+                        if (__float_as_int(q.w) < ip)
+                            cov = reaches(a, q, p, ip, e);
+                    }
+                }
+                cov = __any_sync(0xffffffffu, cov);
+                k++;
+                if (lane == 0) {
+                    if (!cov) {
+                        const int kc = a.keptCnt[r];
+                        if (kc < a.cap) {
+                            a.kept[(size_t)r * a.cap + kc] = make_float4(p.x, p.y, p.z, __int_as_float(ip));
+                            __threadfence();
+                            *(volatile int *)&a.keptCnt[r] = kc + 1;
+                        } else {
+                            atomicExch(&a.err[0], 1);
+                        }
+                        a.keptFlag[ip] = 1;
+                    }
+                    __threadfence();
+                    *(volatile int *)&a.cursor[r]    = k;
+                    *(volatile int *)&a.cursorPos[r] = k < end ? (int)a.sortPos[k] : INT_MAX;
+                }
+                __syncwarp();
+                moved = true;
+            }
+        }
+        if (!open)
+            return;
+        if (moved) {
+            idle = 0;
+        } else {
+            if (++idle > kSpIdle) {
+                if (lane == 0)
+                    atomicExch(&a.err[1], 1);
+                return;
+            }
+            __nanosleep(128);
+        }
+        if (ld_vol(&a.err[1]))
+            return;
+    }
+}
+
+__global__ void k_sp_out(const int *__restrict__ flag, const int *__restrict__ pre, int m,
+                         const int *__restrict__ vaccA, int *__restrict__ outIds,
+                         int *__restrict__ ioi) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m)
+        return;
+    const bool kept = flag[i] != 0;
+    if (kept)
+        outIds[pre[i]] = vaccA[i];
+    if (ioi)
+        ioi[i] = kept ? vaccA[i] : -1;
+}
+
+// ---- k-nearest searches on the tree (one query per thread) -----------------------------
+// Query t: position qpos[t], or pos[list[t]] when qpos is null; t < *nq (device count).
+// Writes its k nearest ids in the reference's order (distance, then first found) and
+// their squared distances; cnt[t] = how many were found.
+__global__ void k_kd_knn(KdView t, const float4 *__restrict__ qpos, const int *__restrict__ list,
+                         const int *__restrict__ nq, int k, int *__restrict__ nbr,
+                         float *__restrict__ dist, int *__restrict__ cnt, int *__restrict__ err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nq)
+        return;
+    const float4 p    = qpos ? qpos[i] : t.pos[list[i]];
+    const float  q[3] = {p.x, p.y, p.z};
+    smk::KnnSet<kMaxKnn> rs;
+    rs.init(k);
+    if (!smk::kd_search(t, q, rs))
+        atomicExch(err, 1);
+    for (int j = 0; j < k; j++) {
+        nbr[(size_t)i * k + j] = j < rs.count ? rs.idx[j] : -1;
+        if (dist)
+            dist[(size_t)i * k + j] = rs.dist[j];
+    }
+    if (cnt)
+        cnt[i] = rs.count;
+}
+
+} // namespace
+
+// =======================================================================================
+void build_kdtree(Ctx &c, const float4 *pos, int npoints, const int *ids, int m, const Box &box,
+                  KdTree &T, const std::string &tag) {
+    if (m >= (1 << 28))
+        throw Error(SM_ERR_CAPACITY, "k-d tree over more than 2^28 points is not supported");
+    T.m       = m;
+    T.npoints = npoints;
+    const int cap = std::max(2 * m, 1);
+    T.nd      = c.arena.get<int4>(tag + ".nd", cap);
+    T.box     = c.arena.get<float>(tag + ".box", (size_t)6 * cap);
+    T.vacc    = c.arena.get<int>(tag + ".vacc", std::max(m, 1));
+    T.leafOf  = c.arena.get<int>(tag + ".leaf", std::max(m, 1));
+    T.treePos = c.arena.get<int>(tag + ".tpos", std::max(npoints, 1));
+    T.rec     = c.arena.get<float4>(tag + ".rec", std::max(m, 1));
+    int *parent  = c.arena.get<int>(tag + ".par", cap);
+    int *arrive  = c.arena.get<int>(tag + ".arr", cap);
+    int *cnt     = c.arena.get<int>(tag + ".cnt", 8); // nodes, nnext, nsmall, err
+    int *segOf   = c.arena.get<int>(tag + ".segof", std::max(m, 1));
+    int *flag    = c.arena.get<int>(tag + ".flag", (size_t)m + 1);
+    int *g1      = c.arena.get<int>(tag + ".g1", (size_t)m + 1);
+    int *g2      = c.arena.get<int>(tag + ".g2", (size_t)m + 1);
+    int *badR    = c.arena.get<int>(tag + ".badr", std::max(m, 1));
+    const int maxSeg = std::max(m / (smk::kLeafMax + 1) + 2, 2);
+    Seg *segA  = c.arena.get<Seg>(tag + ".segA", maxSeg);
+    Seg *segB  = c.arena.get<Seg>(tag + ".segB", maxSeg);
+    Seg *small = c.arena.get<Seg>(tag + ".small", maxSeg);
+    SM_CUDA(cudaMemsetAsync(cnt, 0, 8 * sizeof(int), c.stream));
+    SM_CUDA(cudaMemsetAsync(T.treePos, 0xff, (size_t)std::max(npoints, 1) * 4, c.stream));
+    if (m == 0)
+        return;
+    int *nseg = cnt + 4; // open ranges of the current level (device)
+    k_kd_root<<<1, 1, 0, c.stream>>>(segA, small, m, box, T.nd, parent, cnt);
+    SM_LAUNCH_CHECK();
+    k_kd_init<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, m, T.rec, segOf, segA);
+    SM_LAUNCH_CHECK();
+    int hostSeg = m > kSmall ? 1 : 0;
+    Seg *cur = segA, *nxt = segB;
+    const int gm = nblocks((long long)m + 1, 256);
+    while (hostSeg > 0) {
+        k_kd_cut<<<nblocks(hostSeg, 128), 128, 0, c.stream>>>(cur, nseg);
+        SM_LAUNCH_CHECK();
+        for (int pass = 1; pass <= 2; pass++) {
+            int *g = pass == 1 ? g1 : g2;
+            k_kd_flags<<<gm, 256, 0, c.stream>>>(T.rec, segOf, m, cur, pass, g1, flag);
+            SM_LAUNCH_CHECK();
+            scan_excl(c, flag, g, (long long)m + 1, tag + ".scan", false);
+            k_kd_rank<<<gm, 256, 0, c.stream>>>(segOf, m, cur, pass, g1, flag, g, badR);
+            SM_LAUNCH_CHECK();
+            k_kd_swap<<<gm, 256, 0, c.stream>>>(T.rec, segOf, m, cur, pass, g1, flag, g, badR);
+            SM_LAUNCH_CHECK();
+        }
+        SM_CUDA(cudaMemsetAsync(cnt + 1, 0, sizeof(int), c.stream));
+        k_kd_children<<<nblocks(hostSeg, 128), 128, 0, c.stream>>>(
+            cur, nseg, g1, g2, T.nd, parent, cnt, nxt, cnt + 1, small, cnt + 2, cnt + 3);
+        SM_LAUNCH_CHECK();
+        k_kd_advance<<<nblocks(m, 256), 256, 0, c.stream>>>(T.rec, segOf, m, cur, nxt);
+        SM_LAUNCH_CHECK();
+        SM_CUDA(cudaMemcpyAsync(nseg, cnt + 1, sizeof(int), cudaMemcpyDeviceToDevice, c.stream));
+        SM_CUDA(cudaMemcpyAsync(c.hostCounts, cnt, 4 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+        c.sync_checked();
+        hostSeg = c.hostCounts[1];
+        std::swap(cur, nxt);
+        if (c.hostCounts[3])
+            throw Error(SM_ERR_CAPACITY, "k-d tree deeper than " + std::to_string(smk::kMaxDepth));
+    }
+    SM_CUDA(cudaMemcpyAsync(c.hostCounts, cnt, 4 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    c.sync_checked();
+    const int nsmall = c.hostCounts[2];
+    if (nsmall > 0) {
+        k_kd_small<<<nsmall, kSmall, 0, c.stream>>>(small, T.rec, T.nd, parent, cnt, cnt + 3);
+        SM_LAUNCH_CHECK();
+    }
+    SM_CUDA(cudaMemsetAsync(arrive, 0, (size_t)cap * 4, c.stream));
+    k_kd_finish<<<nblocks(cap, 256), 256, 0, c.stream>>>(T.nd, parent, cnt, T.rec, T.box, arrive,
+                                                         T.vacc, T.leafOf, T.treePos);
+    SM_LAUNCH_CHECK();
+    SM_CUDA(cudaMemcpyAsync(c.hostCounts, cnt, 4 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    c.sync_checked();
+    T.nnodes = c.hostCounts[0];
+    if (c.hostCounts[3] == 1)
+        throw Error(SM_ERR_CAPACITY, "k-d tree deeper than " + std::to_string(smk::kMaxDepth));
+    if (c.hostCounts[3] == 2)
+        throw Error(SM_ERR_CAPACITY, "k-d tree build: too many open ranges in a small range");
+}
+
+int kd_sample(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos, float step,
+              const Box &box, int *outIds, int *ioi, const std::string &tag) {
+    const int m = T.m;
+    if (m <= 0)
+        return 0;
+    const int *vaccA = vaccActive ? vaccActive : T.vacc;
+    float      ext[3] = {box.ext(0), box.ext(1), box.ext(2)};
+    GridParamsK gp;
+    gp.g = smg::sample_cell(step, ext);
+    for (int a = 0; a < 3; a++) {
+        gp.org[a] = box.mn[a];
+        gp.dim[a] = smg::dim_of(ext[a], gp.g);
+    }
+    const long long nc = (long long)gp.dim[0] * gp.dim[1] * gp.dim[2];
+    uint32_t *key   = c.arena.get<uint32_t>(tag + ".key", m);
+    uint32_t *val   = c.arena.get<uint32_t>(tag + ".val", m);
+    int      *head  = c.arena.get<int>(tag + ".head", (size_t)m + 1);
+    int      *rank  = c.arena.get<int>(tag + ".rank", (size_t)m + 1);
+    int      *cRank = c.arena.get<int>(tag + ".crank", nc);
+    k_sp_keys<<<nblocks(m, 256), 256, 0, c.stream>>>(vaccA, pos, m, gp, key, val);
+    SM_LAUNCH_CHECK();
+    radix_sort_pairs(c, key, val, m, 24, tag);
+    k_sp_heads<<<nblocks((long long)m + 1, 256), 256, 0, c.stream>>>(key, m, head);
+    SM_LAUNCH_CHECK();
+    const int ncells = scan_excl(c, head, rank, (long long)m + 1, tag + ".hs", true);
+    // kept capacity per cell: points pairwise at least `step` apart inside a cube of side g
+    // fit disjoint balls of radius step/2 inside the cube grown by step/2; doubled for
+    // points that a pruned search did not reach
+    const double sc  = (double)gp.g / (double)step;
+    const int    cap = 2 * ((int)std::floor((sc + 1.0) * (sc + 1.0) * (sc + 1.0) / (3.14159265358979 / 6.0)) + 1);
+    int    *cellList  = c.arena.get<int>(tag + ".clist", std::max(ncells, 1));
+    int    *cellEnd   = c.arena.get<int>(tag + ".cend", std::max(ncells, 1));
+    int    *cursor    = c.arena.get<int>(tag + ".cur", std::max(ncells, 1));
+    int    *cursorPos = c.arena.get<int>(tag + ".cpos", std::max(ncells, 1));
+    int    *keptCnt   = c.arena.get<int>(tag + ".kc", std::max(ncells, 1));
+    float4 *kept      = c.arena.get<float4>(tag + ".kept", (size_t)std::max(ncells, 1) * cap);
+    int    *flag      = c.arena.get<int>(tag + ".flag", (size_t)m + 1);
+    int    *err       = c.arena.get<int>(tag + ".err", 2);
+    SM_CUDA(cudaMemsetAsync(cRank, 0xff, (size_t)nc * 4, c.stream));
+    SM_CUDA(cudaMemsetAsync(flag, 0, ((size_t)m + 1) * 4, c.stream));
+    SM_CUDA(cudaMemsetAsync(err, 0, 2 * sizeof(int), c.stream));
+    k_sp_cells<<<nblocks(m, 256), 256, 0, c.stream>>>(key, val, m, head, rank, cRank, cellList,
+                                                     cellEnd, cursor, cursorPos, keptCnt);
+    SM_LAUNCH_CHECK();
+    SampleArgs a{};
+    a.t        = T.view(vaccA, pos);
+    a.nodeBox  = T.box;
+    a.leafOf   = T.leafOf;
+    for (int d = 0; d < 3; d++) {
+        a.org[d] = gp.org[d];
+        a.dim[d] = gp.dim[d];
+    }
+    a.g         = gp.g;
+    a.sortPos   = val;
+    a.cellRank  = cRank;
+    a.cellList  = cellList;
+    a.cellEnd   = cellEnd;
+    a.cursor    = cursor;
+    a.cursorPos = cursorPos;
+    a.keptCnt   = keptCnt;
+    a.kept      = kept;
+    a.cap       = cap;
+    a.ncells    = ncells;
+    a.r2        = step * step;
+    a.safe2     = (double)a.r2 * (1.0 - 1e-4);
+    a.keptFlag  = flag;
+    a.err       = err;
+    if (ncells > 0) {
+        // every block resident at once (a cooperative launch guarantees it): warps wait on
+        // cells that other warps own
+        int dev = c.device, nsm = 0, perSm = 0;
+        SM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        SM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_sp_run, kSpBs, 0));
+        const int want = (ncells + kSpBs / 32 - 1) / (kSpBs / 32);
+        const int grid = std::max(1, std::min(want, nsm * std::max(perSm, 1)));
+        void     *args[] = {&a};
+        SM_CUDA(cudaLaunchCooperativeKernel((const void *)k_sp_run, grid, kSpBs, args, 0, c.stream));
+        SM_LAUNCH_CHECK();
+    }
+    int *pre = c.arena.get<int>(tag + ".pre", (size_t)m + 1);
+    scan_excl(c, flag, pre, (long long)m + 1, tag + ".os", false);
+    k_sp_out<<<nblocks(m, 256), 256, 0, c.stream>>>(flag, pre, m, vaccA, outIds, ioi);
+    SM_LAUNCH_CHECK();
+    SM_CUDA(cudaMemcpyAsync(c.hostCounts, pre + m, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    SM_CUDA(cudaMemcpyAsync(c.hostCounts + 1, err, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    c.sync_checked();
+    if (c.hostCounts[2])
+        throw Error(SM_ERR_RUNTIME, "tree-order sampler: a bounded wait expired");
+    if (c.hostCounts[1])
+        throw Error(SM_ERR_CAPACITY, "tree-order sampler: kept-point capacity per cell exceeded");
+    return c.hostCounts[0];
+}
+
+void kd_knn(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos,
+            const float4 *qpos, const int *list, const int *nq, int nqMax, int k, int *nbr,
+            float *dist, int *cnt) {
+    if (nqMax <= 0 || T.m <= 0)
+        return;
+    if (k < 1 || k > kMaxKnn)
+        throw Error(SM_ERR_RANGE, "knnNormal larger than " + std::to_string(kMaxKnn) + " is not supported");
+    int *err = c.arena.get<int>("kd.knn.err", 1);
+    SM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c.stream));
+    k_kd_knn<<<nblocks(nqMax, 128), 128, 0, c.stream>>>(T.view(vaccActive, pos), qpos, list, nq, k,
+                                                        nbr, dist, cnt, err);
+    SM_LAUNCH_CHECK();
+}
+
+} // namespace sm

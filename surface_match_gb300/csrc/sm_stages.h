@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "sm_engine.h"
+#include "sm_kdtree.cuh"
 
 namespace sm {
 
@@ -152,6 +153,51 @@ void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *
                       const std::string &tag);
 // Normalise all normals (normalizeNormal, util.cpp:163-176).
 void normalize_normals(Ctx &c, float4 *nrm, int n);
+
+// ---- sort.cu --------------------------------------------------------------------------
+// Stable LSD radix sort of n (key, value) pairs by the low `bits` bits of the key, in place.
+void radix_sort_pairs(Ctx &c, uint32_t *keys, uint32_t *vals, int n, int bits,
+                      const std::string &tag);
+
+// ---- kdtree.cu ------------------------------------------------------------------------
+// The reference-order k-d tree over points ids[0..m) (device arrays in the context's
+// workspace, named by `tag`).
+struct KdTree {
+    int     m = 0, npoints = 0, nnodes = 0;
+    int4   *nd      = nullptr; // nodes (sm_kdtree.cuh layout), root 0
+    float  *box     = nullptr; // per node tight box (lo xyz, hi xyz), build-time positions
+    int    *vacc    = nullptr; // per tree position: point id
+    int    *leafOf  = nullptr; // per tree position: its leaf
+    int    *treePos = nullptr; // per point id: tree position (-1: not in the tree)
+    float4 *rec     = nullptr; // build-time positions in tree order (w = point id)
+    smk::KdView view(const int *vaccActive, const float4 *pos) const {
+        smk::KdView v;
+        v.nd   = nd;
+        v.box  = box;
+        v.vacc = vaccActive ? vaccActive : vacc;
+        v.pos  = pos;
+        return v;
+    }
+};
+// KDTree construction of the reference (kdtree.h:65-79, nanoflann divideTree): the tree
+// over ids[0..m) (the valid points in index order), root box `box`.
+void build_kdtree(Ctx &c, const float4 *pos, int npoints, const int *ids, int m, const Box &box,
+                  KdTree &T, const std::string &tag);
+// samplePointCloud (util.cpp:107-139) on the tree: greedy thinning at `step` in tree
+// position order over the positions whose vaccActive entry is >= 0 (the reduce()d tree),
+// distances on the live positions `pos`. Writes the kept ids in tree order to outIds and,
+// when ioi is given, the reduce() array (kept point id per tree position, else -1).
+// Returns the number kept. `box` bounds the grid that buckets the points (points outside
+// are clamped into its border cells).
+int kd_sample(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos, float step,
+              const Box &box, int *outIds, int *ioi, const std::string &tag);
+// KNNResultSet searches (nanoflann findNeighbors) on the tree, one per query: query t is at
+// qpos[t] (or pos[list[t]] when qpos is null) for t < *nq (a device count, nqMax bounds the
+// launch); nbr[t*k + j] / dist[t*k + j] (dist nullable) its j-th nearest, cnt[t] (nullable)
+// how many there are.
+void kd_knn(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos,
+            const float4 *qpos, const int *list, const int *nq, int nqMax, int k, int *nbr,
+            float *dist, int *cnt);
 
 // ---- mls.cu ---------------------------------------------------------------------------
 constexpr int kMlsMaxOrder = 4; // largest polynomial order of the MLS fit
