@@ -41,6 +41,11 @@ extern "C" {
 #define SM_ERR_NOMEM 5    /* device allocation failed */
 #define SM_ERR_CAPACITY 6 /* an internal capacity was exceeded (reported, never silent) */
 
+/* search orders (sm_model_set_search_order) */
+#define SM_ORDER_GRID 0      /* the GPU's grid order (fast; same rules, another visiting order) */
+#define SM_ORDER_REFERENCE 1 /* the reference's k-d tree order (bit-exact with the reference's
+                                single-threaded sampling, neighbour order and search pruning) */
+
 typedef struct sm_context_s *sm_context; /* one device + one CUDA stream + workspace */
 typedef struct sm_model_s *sm_model;     /* a trained model resident on the device */
 typedef struct sm_server_s *sm_server;   /* a matchScene serving loop on one device */
@@ -130,6 +135,18 @@ SM_API int sm_model_upload(sm_model model, int64_t n_sampled, const float *sampl
                            const float *box6, int64_t n_keys, const uint32_t *keys,
                            const uint32_t *offsets, const uint32_t *refs, const float *alphas,
                            float samplingDistanceRel, const sm_train_param *param);
+
+/* Search order of the model's subsequent sm_model_train and sm_match calls (and of the
+ * batch and serving entries on it). The reference samples clouds greedily in the leaf
+ * order of its k-d tree and evaluates each keypoint's neighbours in the tree's depth-first
+ * order, which decides which point pairs take its 8-lane SIMD quantisation and which its
+ * scalar one (util.cpp:107-139, 765-827; ppf.cpp:273-346). SM_ORDER_REFERENCE builds that
+ * tree on the GPU (nanoflann's middle-split rules) and follows its orders and its search
+ * pruning in every search of the path: sampling, normals, voting lists, refinement and
+ * scoring. SM_ORDER_GRID (default) applies the same rules in the order of uniform grids,
+ * which is faster; the results are equally valid but not the same samples. */
+SM_API int sm_model_set_search_order(sm_model model, int order);
+SM_API int sm_model_search_order(sm_model model);
 
 /* sizes[4] = {n_sampled, n_resampled, n_keys, n_entries} */
 SM_API int sm_model_sizes(sm_model model, int64_t *sizes);

@@ -10,6 +10,7 @@ LIB_PATH = os.path.join(HERE, "libsurface_match.so")
 
 SM_OK, SM_ERR_RANGE, SM_ERR_RUNTIME, SM_ERR_CUDA, SM_ERR_ARG, SM_ERR_NOMEM, SM_ERR_CAPACITY = \
     range(7)
+SM_ORDER_GRID, SM_ORDER_REFERENCE = 0, 1
 
 
 class TrainParamC(C.Structure):
@@ -61,6 +62,8 @@ _SIGNATURES = {
     "sm_model_upload": (C.c_int, [_vp, C.c_int64, _f32p, _f32p, C.c_int64, _f32p, _f32p, _f32p,
                                   C.c_int64, _u32p, _u32p, _u32p, _f32p, C.c_float,
                                   C.POINTER(TrainParamC)]),
+    "sm_model_set_search_order": (C.c_int, [_vp, C.c_int]),
+    "sm_model_search_order": (C.c_int, [_vp]),
     "sm_model_sizes": (C.c_int, [_vp, _i64p]),
     "sm_model_download": (C.c_int, [_vp, _f32p, _f32p, _f32p, _f32p, _f32p, _u32p, _u32p,
                                     _u32p, _f32p, _f32p, C.POINTER(TrainParamC)]),

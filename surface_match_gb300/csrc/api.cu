@@ -112,6 +112,20 @@ __global__ void k_gather_poses(const float *__restrict__ poses, const int *__res
         out[(size_t)i * smi::kPoseFloats + e] = poses[(size_t)s * smi::kPoseFloats + e];
 }
 
+__global__ void k_rank_of(const int *__restrict__ ids, int m, int *__restrict__ rank) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < m)
+        rank[ids[r]] = r;
+}
+
+// rank[ids[r]] = r for r < m
+void rank_of(Ctx &c, const int *ids, int m, int *rank) {
+    if (m <= 0)
+        return;
+    k_rank_of<<<nblocks(m, 256), 256, 0, c.stream>>>(ids, m, rank);
+    SM_LAUNCH_CHECK();
+}
+
 __global__ void k_f3_to_f4(const float *__restrict__ a, int n, float4 *__restrict__ o) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n)
@@ -266,17 +280,34 @@ void train(Ctx &c, Model &m, const float *xyzIn, const float *nrmIn, int64_t n64
     const float reSampleStep = diam * tp.poseRefRelSamplingDistance;
     int        *idx1         = c.arena.get<int>("t.idx1", n);
     int        *idx2         = c.arena.get<int>("t.idx2", n);
-    const int   n1 = sample_points(c, pos, n, valid, nvalid, box, sampleStep, idx1, "t.s1");
-    const int   n2 = sample_points(c, pos, n, valid, nvalid, box, reSampleStep, idx2, "t.s2");
-    if (!nrmIn) {
-        HGrid q;
-        const float gq = knn_cell(nvalid, n1, sampleStep, tp.knnNormal);
-        build_hgrid(c, pos, valid, nvalid, box, gq, q, "t.q");
-        estimate_normals(c, pos, nrm, n, idx1, n1, q, tp.knnNormal, tp.smoothNormal != 0, false,
-                         nullptr, "t.n1");
-        build_hgrid(c, pos, valid, nvalid, box, gq, q, "t.q");
-        estimate_normals(c, pos, nrm, n, idx2, n2, q, tp.knnNormal, tp.smoothNormal != 0, false,
-                         nullptr, "t.n2");
+    int         n1 = 0, n2 = 0;
+    if (m.order == SM_ORDER_REFERENCE) {
+        // the reference's tree over the model (ppf.cpp:77-83): both samplings in tree order
+        // on the positions as given, then normals from the tree's k nearest
+        KdTree T;
+        build_kdtree(c, pos, n, valid, nvalid, box, T, "t.tree");
+        n1 = kd_sample(c, T, nullptr, pos, sampleStep, box, idx1, nullptr, "t.s1");
+        n2 = kd_sample(c, T, nullptr, pos, reSampleStep, box, idx2, nullptr, "t.s2");
+        if (!nrmIn) {
+            HGrid none;
+            estimate_normals(c, pos, nrm, n, idx1, n1, none, tp.knnNormal, tp.smoothNormal != 0,
+                             false, nullptr, "t.n1", &T);
+            estimate_normals(c, pos, nrm, n, idx2, n2, none, tp.knnNormal, tp.smoothNormal != 0,
+                             false, nullptr, "t.n2", &T);
+        }
+    } else {
+        n1 = sample_points(c, pos, n, valid, nvalid, box, sampleStep, idx1, "t.s1");
+        n2 = sample_points(c, pos, n, valid, nvalid, box, reSampleStep, idx2, "t.s2");
+        if (!nrmIn) {
+            HGrid q;
+            const float gq = knn_cell(nvalid, n1, sampleStep, tp.knnNormal);
+            build_hgrid(c, pos, valid, nvalid, box, gq, q, "t.q");
+            estimate_normals(c, pos, nrm, n, idx1, n1, q, tp.knnNormal, tp.smoothNormal != 0, false,
+                             nullptr, "t.n1");
+            build_hgrid(c, pos, valid, nvalid, box, gq, q, "t.q");
+            estimate_normals(c, pos, nrm, n, idx2, n2, q, tp.knnNormal, tp.smoothNormal != 0, false,
+                             nullptr, "t.n2");
+        }
     }
     float4 *sp = c.arena.get<float4>("t.sp", std::max(n1, 1));
     float4 *sn = c.arena.get<float4>("t.sn", std::max(n1, 1));
@@ -440,13 +471,29 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
     const float reSampleStep = diam * m.tp.poseRefRelSamplingDistance;
     const float sampleStep   = diam * sdRel;
     int        *sampled      = c.arena.get<int>("m.sampled", std::max(n, 1));
-    const int   ns = sample_points(c, pos, n, valid, nvalid, box, sampleStep, sampled, "m.s1");
+    const bool  ref          = m.order == SM_ORDER_REFERENCE;
+    // reference order: the scene's k-d tree (ppf.cpp:197) over the valid points; `ioi` is
+    // its reduce() array of the sampled points (ppf.cpp:201-213)
+    KdTree      T;
+    int        *ioi = nullptr;
+    int         ns  = 0;
     HGrid       q;
-    const float gq = knn_cell(nvalid, ns, sampleStep, mp.knnNormal);
-    if (!hasN) {
-        build_hgrid(c, pos, valid, nvalid, box, gq, q, "m.q");
-        estimate_normals(c, pos, nrm, n, sampled, ns, q, mp.knnNormal, mp.smoothNormal != 0,
-                         mp.invertNormal != 0, vp, "m.n1");
+    float       gq  = 0.0f;
+    if (ref) {
+        build_kdtree(c, pos, n, valid, nvalid, box, T, "m.tree");
+        ioi = c.arena.get<int>("m.ioi", std::max(nvalid, 1));
+        ns  = kd_sample(c, T, nullptr, pos, sampleStep, box, sampled, ioi, "m.s1");
+        if (!hasN)
+            estimate_normals(c, pos, nrm, n, sampled, ns, q, mp.knnNormal, mp.smoothNormal != 0,
+                             mp.invertNormal != 0, vp, "m.n1", &T);
+    } else {
+        ns = sample_points(c, pos, n, valid, nvalid, box, sampleStep, sampled, "m.s1");
+        gq = knn_cell(nvalid, ns, sampleStep, mp.knnNormal);
+        if (!hasN) {
+            build_hgrid(c, pos, valid, nvalid, box, gq, q, "m.q");
+            estimate_normals(c, pos, nrm, n, sampled, ns, q, mp.knnNormal, mp.smoothNormal != 0,
+                             mp.invertNormal != 0, vp, "m.n1");
+        }
     }
     record(c, 2);
     float maxOverlap = 0;
@@ -482,28 +529,54 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
             SM_CUDA(cudaMemcpyAsync(N, nrm, (size_t)n * 16, cudaMemcpyDeviceToDevice, d.stream));
         }
         int *resampled = d.arena.get<int>("m.resampled", std::max(n, 1));
-        if (mp.densePoseRefinement) {
-            nres = sample_points(d, P, n, valid, nvalid, box, reSampleStep, resampled, "m.s3");
-            if (!hasN) {
-                HGrid q2;
-                build_hgrid(d, P, valid, nvalid, box, gq, q2, "m.q");
-                estimate_normals(d, P, N, n, resampled, nres, q2, mp.knnNormal, false,
-                                 mp.invertNormal != 0, vp, "m.n2");
-            }
-        }
         s.pos = P;
         s.nrm = N;
-        // Nearest-neighbour grids of the refinement: cells of about a third of the rejection
-        // distance (never finer than the subset's spacing), so three cell shells always
-        // cover it. The inlier grid's cell just exceeds the scoring distance, so two shells
-        // decide. The subset grids name points by subset rank (the subsets are ascending, so
-        // rank order is index order), and the refinement reads rank-ordered copies of the
-        // subsets.
-        build_hgrid(d, P, sampled, ns, box, std::max(sampleStep, refDist / 2.98f), s.sampled,
-                    "m.gS", true);
-        build_hgrid(d, P, resampled, nres, box, std::max(2.0f * reSampleStep, refDist / 2.98f),
-                    s.resampled, "m.gR", true);
-        build_hgrid(d, P, valid, nvalid, box, std::max(scoreDist * 1.02f, gq), s.full, "m.gF");
+        if (ref) {
+            // restore() and resample the whole tree, normals without smoothing (ppf.cpp:428-
+            // 434); the refinement searches the tree reduced to each subset, and scores on
+            // the whole tree
+            int *ioi2 = d.arena.get<int>("m.ioi2", std::max(nvalid, 1));
+            if (mp.densePoseRefinement) {
+                nres = kd_sample(d, T, nullptr, P, reSampleStep, box, resampled, ioi2, "m.s3");
+                if (!hasN) {
+                    HGrid none;
+                    estimate_normals(d, P, N, n, resampled, nres, none, mp.knnNormal, false,
+                                     mp.invertNormal != 0, vp, "m.n2", &T);
+                }
+            }
+            int *rankS = d.arena.get<int>("m.rankS", std::max(n, 1));
+            int *rankR = d.arena.get<int>("m.rankR", std::max(n, 1));
+            rank_of(d, sampled, ns, rankS);
+            rank_of(d, resampled, nres, rankR);
+            s.tree        = &T;
+            s.ioiS        = ioi;
+            s.ioiR        = ioi2;
+            s.rankS       = rankS;
+            s.rankR       = rankR;
+            s.sampled.m   = ns;
+            s.resampled.m = nres;
+        } else {
+            if (mp.densePoseRefinement) {
+                nres = sample_points(d, P, n, valid, nvalid, box, reSampleStep, resampled, "m.s3");
+                if (!hasN) {
+                    HGrid q2;
+                    build_hgrid(d, P, valid, nvalid, box, gq, q2, "m.q");
+                    estimate_normals(d, P, N, n, resampled, nres, q2, mp.knnNormal, false,
+                                     mp.invertNormal != 0, vp, "m.n2");
+                }
+            }
+            // Nearest-neighbour grids of the refinement: cells of about a third of the
+            // rejection distance (never finer than the subset's spacing), so three cell
+            // shells always cover it. The inlier grid's cell just exceeds the scoring
+            // distance, so two shells decide. The subset grids name points by subset rank
+            // (the subsets are ascending, so rank order is index order), and the refinement
+            // reads rank-ordered copies of the subsets.
+            build_hgrid(d, P, sampled, ns, box, std::max(sampleStep, refDist / 2.98f), s.sampled,
+                        "m.gS", true);
+            build_hgrid(d, P, resampled, nres, box, std::max(2.0f * reSampleStep, refDist / 2.98f),
+                        s.resampled, "m.gR", true);
+            build_hgrid(d, P, valid, nvalid, box, std::max(scoreDist * 1.02f, gq), s.full, "m.gF");
+        }
         float4 *posS = d.arena.get<float4>("m.posS", std::max(ns, 1));
         float4 *nrmS = d.arena.get<float4>("m.nrmS", std::max(ns, 1));
         float4 *posR = d.arena.get<float4>("m.posR", std::max(nres, 1));
@@ -542,7 +615,9 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
     }
     const float keyStep = smm::fsqrt(1.f / kpFrac) * sampleStep;
     int        *kp      = c.arena.get<int>("m.kp", std::max(ns, 1));
-    const int   K       = sample_points(c, pos, n, sampled, ns, box, keyStep, kp, "m.s2");
+    // keypoints: the tree reduced to the sampled points (ppf.cpp:213-215)
+    const int K = ref ? kd_sample(c, T, ioi, pos, keyStep, box, kp, nullptr, "m.s2")
+                      : sample_points(c, pos, n, sampled, ns, box, keyStep, kp, "m.s2");
     record(c, 3);
     // voting
     VoteOut vo;
@@ -552,7 +627,15 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
     vo.poseOk = c.arena.get<int>("m.kposeok", (size_t)std::max(K, 1) * 3);
     vo.acc    = nullptr;
     record(c, 8);
-    vote(c, m, pos, nrm, kp, K, nullptr, nullptr, sampled, ns, minScore, vo, 0);
+    if (ref) {
+        // the keypoints' radius searches in the reduced tree, tail rows last (ppf.cpp:273-299)
+        int        *off = nullptr, *ids = nullptr;
+        const float dm  = m.box.diameter();
+        kd_vote_lists(c, T, ioi, pos, kp, K, sampled, ns, dm * dm, &off, &ids, "m.rl");
+        vote(c, m, pos, nrm, kp, K, off, ids, nullptr, 0, minScore, vo, 0);
+    } else {
+        vote(c, m, pos, nrm, kp, K, nullptr, nullptr, sampled, ns, minScore, vo, 0);
+    }
     record(c, 9);
     int      *slots = c.arena.get<int>("m.slots", (size_t)std::max(K, 1) * 3);
     const int np    = compact(c, vo.poseOk, K * 3, slots, "m.cp");
@@ -1012,6 +1095,18 @@ SM_API int sm_model_upload(sm_model m, int64_t ns, const float *sxyz, const floa
         m->m.tp    = tp;
     });
 }
+
+SM_API int sm_model_set_search_order(sm_model m, int order) {
+    return guarded([&] {
+        if (!m)
+            throw Error(SM_ERR_ARG, "NULL model");
+        if (order != SM_ORDER_GRID && order != SM_ORDER_REFERENCE)
+            throw Error(SM_ERR_ARG, "unknown search order " + std::to_string(order));
+        m->m.order = order;
+    });
+}
+
+SM_API int sm_model_search_order(sm_model m) { return m ? m->m.order : -1; }
 
 SM_API int sm_model_sizes(sm_model m, int64_t *sizes) {
     return guarded([&] {

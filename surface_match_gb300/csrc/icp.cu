@@ -47,6 +47,10 @@ struct Stage {
     int           iters;
     float         mseMin, mseMax, rej2;
     int           traceOff; // 0 sparse, 1 dense
+    // reference search order: nearest points from the k-d tree reduced to the stage's
+    // subset (rankOf maps a point id to its subset rank); tree.nd == nullptr: the grid G
+    smk::KdView   tree;
+    const int    *rankOf;
 };
 
 struct Work {
@@ -117,6 +121,59 @@ __global__ void __launch_bounds__(kT, 4) k_corr(Work w, Stage s, int usePrev) {
             if (ok)
                 atomicMin(&w.win[(size_t)ci * w.maxDst + j], win_key(d, i));
         }
+    }
+}
+
+// K1 with the reference's search: one thread per source point, the nearest point of the
+// reduced k-d tree (findClosestPoint, util.cpp:603-626: a 1-nearest search from the root,
+// with the tree's pruning) - the same pair rules as k_corr.
+__global__ void __launch_bounds__(kT) k_corr_tree(Work w, Stage s) {
+    const int   ci = blockIdx.y;
+    const Cand &C  = w.cand[ci];
+    if (!cand_live(C, s))
+        return;
+    for (int i = blockIdx.x * kT + threadIdx.x; i < s.n; i += gridDim.x * kT) {
+        const size_t o  = (size_t)ci * w.maxSrc + i;
+        const float4 sp = s.src[i], sn = s.srcN[i];
+        float4       x, y;
+        smi::pose_apply(C.M, sp.x, sp.y, sp.z, x.x, x.y, x.z);
+        smi::pose_rotate(C.M, sn.x, sn.y, sn.z, y.x, y.y, y.z);
+        const float q[3] = {x.x, x.y, x.z};
+        smk::NnSet  rs;
+        rs.init();
+        smk::kd_search(s.tree, q, rs);
+        const int   j  = rs.count ? s.rankOf[rs.idx] : -1;
+        const float d  = rs.dist;
+        const bool  ok = j >= 0 && d <= s.rej2;
+        w.nnPrev[o] = j;
+        x.w         = d;
+        y.w         = 0.0f;
+        w.x4[o]     = x;
+        w.n4[o]     = y;
+        w.nnId[o]   = ok ? j : -1;
+        w.nnR[o]    = ok ? j : -1;
+        if (ok)
+            atomicMin(&w.win[(size_t)ci * w.maxDst + j], win_key(d, i));
+    }
+}
+
+// K4 with the reference's search: residual of each pair, one thread per pair.
+__global__ void __launch_bounds__(kT) k_resid_tree(Work w, Stage s) {
+    const int   ci = blockIdx.y;
+    const Cand &C  = w.cand[ci];
+    if (!cand_live(C, s) || C.cnt < 6)
+        return;
+    for (int i = blockIdx.x * kT + threadIdx.x; i < s.n; i += gridDim.x * kT) {
+        const size_t o = (size_t)ci * w.maxSrc + i;
+        if (w.nnId[o] < 0)
+            continue;
+        const float4 x = w.x4[o];
+        float        y[3];
+        smi::pose_apply(C.step, x.x, x.y, x.z, y[0], y[1], y[2]);
+        smk::NnSet rs;
+        rs.init();
+        smk::kd_search(s.tree, y, rs);
+        w.resid[o] = smm::fsqrt(rs.dist);
     }
 }
 
@@ -448,6 +505,37 @@ __global__ void __launch_bounds__(kT, 6) k_inliers(Work w, const float4 *__restr
     }
 }
 
+// Inliers with the reference's search: the nearest point of the full tree closer than the
+// scoring distance (inliner, util.cpp:628-641), one thread per source point.
+__global__ void __launch_bounds__(kT) k_inliers_tree(Work w, const float4 *__restrict__ src, int n,
+                                                     smk::KdView F, float r2) {
+    __shared__ int sc[kW];
+    const int      ci = blockIdx.y;
+    const Cand    &C  = w.cand[ci];
+    if (!C.active)
+        return;
+    int c = 0;
+    for (int i = blockIdx.x * kT + threadIdx.x; i < n; i += gridDim.x * kT) {
+        float q[3];
+        smi::pose_apply(C.M, src[i].x, src[i].y, src[i].z, q[0], q[1], q[2]);
+        smk::NnSet rs;
+        rs.init();
+        smk::kd_search(F, q, rs);
+        c += (rs.count && rs.dist < r2) ? 1 : 0;
+    }
+    c = __reduce_add_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31) == 0)
+        sc[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int k = 0; k < kW; k++)
+            t += sc[k];
+        if (t)
+            atomicAdd(&w.cand[ci].inl, t);
+    }
+}
+
 __global__ void k_score(Work w, int ncand, int n, float minScore, int failStatus, int slot) {
     const int ci = blockIdx.x * blockDim.x + threadIdx.x;
     if (ci >= ncand)
@@ -482,16 +570,24 @@ __global__ void k_finish(Work w, int ncand, int refine, float minScore, int *sta
 void run_stage(Ctx &c, Work &w, const Stage &s, int ncand) {
     const dim3 gr(smi::kIcpBlocks, ncand);                    // reductions
     const dim3 gw(std::max(1, nblocks(s.n, kW)), ncand); // warp kernels: a warp per point
+    const dim3 gt(std::max(1, nblocks(s.n, kT)), ncand); // tree searches: a thread per point
+    const bool tree = s.tree.nd != nullptr;
     k_stage_begin<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand);
     SM_LAUNCH_CHECK();
     for (int it = 0; it < s.iters; it++) {
-        k_corr<<<gw, kT, 0, c.stream>>>(w, s, it > 0 ? 1 : 0);
+        if (tree)
+            k_corr_tree<<<gt, kT, 0, c.stream>>>(w, s);
+        else
+            k_corr<<<gw, kT, 0, c.stream>>>(w, s, it > 0 ? 1 : 0);
         SM_LAUNCH_CHECK();
         k_centroids<<<gr, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
         k_solve<<<gr, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
-        k_resid<<<gw, kT, 0, c.stream>>>(w, s);
+        if (tree)
+            k_resid_tree<<<gt, kT, 0, c.stream>>>(w, s);
+        else
+            k_resid<<<gw, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
         k_update<<<gr, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
@@ -526,26 +622,40 @@ void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, con
     SM_LAUNCH_CHECK();
     const float rej2 = p.rejectDist * p.rejectDist;
     const float sc2  = p.scoreDist * p.scoreDist;
+    const bool tree = sc.tree != nullptr;
+    auto inliers = [&](const float4 *src, int n) {
+        if (tree)
+            k_inliers_tree<<<dim3(std::max(1, nblocks(n, kT)), ncand), kT, 0, c.stream>>>(
+                w, src, n, sc.tree->view(nullptr, sc.pos), sc2);
+        else
+            k_inliers<<<dim3(std::max(1, nblocks(n, kW)), ncand), kT, 0, c.stream>>>(
+                w, src, n, sc.full.view(), sc2);
+        SM_LAUNCH_CHECK();
+    };
     if (p.sparse) {
         Stage s{m.sp, m.sn, m.ns, nblocks(m.ns, kT), sc.sampled.view(), sc.posS, sc.nrmS, sc.sampled.m, 5,
                 p.sampleStep * 0.5f, p.sampleStep, rej2, 0};
+        if (tree) {
+            s.tree   = sc.tree->view(sc.ioiS, sc.pos);
+            s.rankOf = sc.rankS;
+        }
         run_stage(c, w, s, ncand);
         k_stage_end<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, 2);
         SM_LAUNCH_CHECK();
-        k_inliers<<<dim3(std::max(1, nblocks(m.ns, kW)), ncand), kT, 0, c.stream>>>(
-            w, m.sp, m.ns, sc.full.view(), sc2);
-        SM_LAUNCH_CHECK();
+        inliers(m.sp, m.ns);
         k_score<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, m.ns, p.minScore, 3, 0);
         SM_LAUNCH_CHECK();
         if (p.dense) {
             Stage d{m.rp, m.rn, m.nr, nblocks(m.nr, kT), sc.resampled.view(), sc.posR, sc.nrmR,
                     sc.resampled.m, p.denseSteps, p.reSampleStep * 0.5f, p.sampleStep, rej2, 1};
+            if (tree) {
+                d.tree   = sc.tree->view(sc.ioiR, sc.pos);
+                d.rankOf = sc.rankR;
+            }
             run_stage(c, w, d, ncand);
             k_stage_end<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, 4);
             SM_LAUNCH_CHECK();
-            k_inliers<<<dim3(std::max(1, nblocks(m.nr, kW)), ncand), kT, 0, c.stream>>>(
-                w, m.rp, m.nr, sc.full.view(), sc2);
-            SM_LAUNCH_CHECK();
+            inliers(m.rp, m.nr);
             k_score<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, m.nr, p.minScore, 5, 1);
             SM_LAUNCH_CHECK();
         }

@@ -744,7 +744,8 @@ __global__ void k_sp_out(const int *__restrict__ flag, const int *__restrict__ p
 // their squared distances; cnt[t] = how many were found.
 __global__ void k_kd_knn(KdView t, const float4 *__restrict__ qpos, const int *__restrict__ list,
                          const int *__restrict__ nq, int k, int *__restrict__ nbr,
-                         float *__restrict__ dist, int *__restrict__ cnt, int *__restrict__ err) {
+                         float *__restrict__ dist, int *__restrict__ cnt, int *__restrict__ err,
+                         const float4 *__restrict__ nrm, int *__restrict__ need) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *nq)
         return;
@@ -755,12 +756,154 @@ __global__ void k_kd_knn(KdView t, const float4 *__restrict__ qpos, const int *_
     if (!smk::kd_search(t, q, rs))
         atomicExch(err, 1);
     for (int j = 0; j < k; j++) {
-        nbr[(size_t)i * k + j] = j < rs.count ? rs.idx[j] : -1;
+        const int id           = j < rs.count ? rs.idx[j] : -1;
+        nbr[(size_t)i * k + j] = id;
         if (dist)
             dist[(size_t)i * k + j] = rs.dist[j];
+        // with smoothing, neighbours that still need a normal are marked for estimation
+        if (need && id >= 0 && need[id] == 0) {
+            const float4 n = nrm[id];
+            if (!(isfinite(n.x) && isfinite(n.y) && isfinite(n.z)))
+                need[id] = 1;
+        }
     }
     if (cnt)
         cnt[i] = rs.count;
+}
+
+// ---- the voting stage's radius searches (ppf.cpp:273-276) -------------------------------
+constexpr int kRlBs  = 256;
+constexpr int kTailN = 7; // rows % 8 < 8
+
+struct TailKey {
+    uint64_t key;
+    int                pos, cand; // tree position, candidate index
+};
+__device__ __forceinline__ bool tail_after(const TailKey &a, const TailKey &b) {
+    return a.key > b.key || (a.key == b.key && a.pos > b.pos);
+}
+
+// One CTA per keypoint over the candidates (the sampled points): membership of the radius
+// search of radius^2 r2 in the reduced tree (distance and the search's pruning), as a
+// bitmask over the candidate list; the member count; and the candidates of the last
+// (rows mod 8) rows other than the keypoint itself in the search's depth-first order -
+// the rows the reference evaluates one by one after its 8-lane blocks.
+__global__ void __launch_bounds__(kRlBs)
+    k_kd_radius(KdView t, const int *__restrict__ treePos, const int *__restrict__ kp, int K,
+                const int *__restrict__ cand, int ncand, float r2, uint32_t *__restrict__ mask,
+                int words, int *__restrict__ count, int *__restrict__ tail) {
+    __shared__ TailKey sk[kRlBs];
+    __shared__ int     sh[33];
+    const int c = blockIdx.x;
+    if (c >= K)
+        return;
+    const int    pid  = kp[c];
+    const float4 p    = t.pos[pid];
+    const float  q[3] = {p.x, p.y, p.z};
+    TailKey      top[kTailN];
+    for (int k = 0; k < kTailN; k++)
+        top[k] = TailKey{0ull, -1, -1};
+    int       nTop = 0, S = 0;
+    bool      self = false;
+    uint32_t *mrow = mask + (size_t)c * words;
+    for (int j0 = 0; j0 < ncand; j0 += kRlBs) {
+        const int j   = j0 + threadIdx.x;
+        bool      mem = false;
+        if (j < ncand) {
+            const int id = cand[j];
+            const float d = smk::eval_metric(q, t.pos[id]);
+            if (d < r2) {
+                const int ip = treePos[id];
+                uint64_t  key;
+                mem = smk::kd_reaches(t, q, ip, r2, &key);
+                self = self || (mem && id == pid);
+                if (mem && id != pid) {
+                    TailKey e{key, ip, j};
+                    // keep the kTailN latest in search order, sorted latest first
+                    int at = nTop < kTailN ? nTop : kTailN;
+                    while (at > 0 && tail_after(e, top[at - 1]))
+                        at--;
+                    if (at < kTailN) {
+                        for (int k = (nTop < kTailN ? nTop : kTailN - 1); k > at; k--)
+                            top[k] = top[k - 1];
+                        top[at] = e;
+                        if (nTop < kTailN)
+                            nTop++;
+                    }
+                }
+            }
+        }
+        const uint32_t b = __ballot_sync(0xffffffffu, mem);
+        if ((threadIdx.x & 31) == 0 && ((j0 + threadIdx.x) >> 5) < words)
+            mrow[(j0 + threadIdx.x) >> 5] = b;
+        S += mem ? 1 : 0;
+    }
+    int tot;
+    block_excl_scan(S, sh, &tot);
+    // rows = the members other than the keypoint (which its own search finds)
+    const int rows = tot - (__syncthreads_or(self ? 1 : 0) ? 1 : 0);
+    const int need = rows % 8;
+    // the `need` latest rows: rounds of a block-wide maximum over the threads' lists
+    int head = 0;
+    for (int r = 0; r < need; r++) {
+        sk[threadIdx.x] = head < nTop ? top[head] : TailKey{0ull, -1, -1};
+        __syncthreads();
+        for (int o = kRlBs / 2; o > 0; o >>= 1) {
+            if (threadIdx.x < o && tail_after(sk[threadIdx.x + o], sk[threadIdx.x]))
+                sk[threadIdx.x] = sk[threadIdx.x + o];
+            __syncthreads();
+        }
+        const TailKey w = sk[0];
+        if (head < nTop && top[head].pos == w.pos && top[head].cand == w.cand)
+            head++;
+        if (threadIdx.x == 0)
+            tail[(size_t)c * kTailN + r] = w.cand;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        count[c] = tot;
+        for (int r = need; r < kTailN; r++)
+            tail[(size_t)c * kTailN + r] = -1;
+    }
+}
+
+// The CSR list of keypoint blockIdx.x: its members in candidate order except the tail
+// rows, then the tail rows (the voting stage marks the last rows % 8 rows of a list as the
+// reference's one-by-one rows).
+__global__ void __launch_bounds__(kRlBs)
+    k_kd_fill(const uint32_t *__restrict__ mask, int words, const int *__restrict__ cand,
+              int ncand, const int *__restrict__ off, const int *__restrict__ tail,
+              int *__restrict__ ids) {
+    __shared__ int sh[33];
+    __shared__ int sT[kTailN];
+    const int c = blockIdx.x;
+    if (threadIdx.x < kTailN)
+        sT[threadIdx.x] = tail[(size_t)c * kTailN + threadIdx.x];
+    __syncthreads();
+    int nt = 0;
+    for (int k = 0; k < kTailN; k++)
+        nt += sT[k] >= 0 ? 1 : 0;
+    const uint32_t *mrow = mask + (size_t)c * words;
+    int            *out  = ids + off[c];
+    const int       len  = off[c + 1] - off[c];
+    int             base = 0;
+    for (int j0 = 0; j0 < ncand; j0 += kRlBs) {
+        const int j  = j0 + threadIdx.x;
+        bool      in = j < ncand && ((mrow[j >> 5] >> (j & 31)) & 1u);
+        if (in)
+            for (int k = 0; k < kTailN; k++)
+                if (sT[k] == j)
+                    in = false;
+        int       tot;
+        const int ex = block_excl_scan(in ? 1 : 0, sh, &tot);
+        if (in)
+            out[base + ex] = cand[j];
+        base += tot;
+    }
+    // the tail rows last, in search order (earliest first)
+    if (threadIdx.x == 0)
+        for (int k = nt - 1, o = len - nt; k >= 0; k--, o++)
+            out[o] = cand[sT[k]];
 }
 
 } // namespace
@@ -945,7 +1088,7 @@ int kd_sample(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos,
 
 void kd_knn(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos,
             const float4 *qpos, const int *list, const int *nq, int nqMax, int k, int *nbr,
-            float *dist, int *cnt) {
+            float *dist, int *cnt, const float4 *nrm, int *need) {
     if (nqMax <= 0 || T.m <= 0)
         return;
     if (k < 1 || k > kMaxKnn)
@@ -953,8 +1096,34 @@ void kd_knn(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos,
     int *err = c.arena.get<int>("kd.knn.err", 1);
     SM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c.stream));
     k_kd_knn<<<nblocks(nqMax, 128), 128, 0, c.stream>>>(T.view(vaccActive, pos), qpos, list, nq, k,
-                                                        nbr, dist, cnt, err);
+                                                        nbr, dist, cnt, err, nrm, need);
     SM_LAUNCH_CHECK();
+}
+
+int kd_vote_lists(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos,
+                  const int *kp, int K, const int *cand, int ncand, float r2, int **offOut,
+                  int **idsOut, const std::string &tag) {
+    int *off = c.arena.get<int>(tag + ".off", (size_t)K + 1);
+    *offOut  = off;
+    if (K <= 0) {
+        *idsOut = c.arena.get<int>(tag + ".ids", 1);
+        return 0;
+    }
+    const int words = std::max((ncand + 31) / 32, 1);
+    uint32_t *mask  = c.arena.get<uint32_t>(tag + ".mask", (size_t)K * words);
+    int      *cnt   = c.arena.get<int>(tag + ".cnt", (size_t)K + 1);
+    int      *tail  = c.arena.get<int>(tag + ".tail", (size_t)K * kTailN);
+    SM_CUDA(cudaMemsetAsync(mask, 0, (size_t)K * words * 4, c.stream));
+    SM_CUDA(cudaMemsetAsync(cnt + K, 0, sizeof(int), c.stream));
+    k_kd_radius<<<K, kRlBs, 0, c.stream>>>(T.view(vaccActive, pos), T.treePos, kp, K, cand, ncand,
+                                            r2, mask, words, cnt, tail);
+    SM_LAUNCH_CHECK();
+    const int total = scan_excl(c, cnt, off, (long long)K + 1, tag + ".scan", true);
+    int      *ids   = c.arena.get<int>(tag + ".ids", std::max(total, 1));
+    *idsOut         = ids;
+    k_kd_fill<<<K, kRlBs, 0, c.stream>>>(mask, words, cand, ncand, off, tail, ids);
+    SM_LAUNCH_CHECK();
+    return total;
 }
 
 } // namespace sm

@@ -967,9 +967,22 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
     return c.hostCounts[0];
 }
 
+// The points p < n with need[p] == eq, ascending, into out; returns the device address of
+// their count (no host round trip).
+static int *compact_need(Ctx &c, const int *need, int n, int eq, int *out, const std::string &tag) {
+    int *total = c.arena.get<int>(tag + ".scantot", 1);
+    int *pre   = c.arena.get<int>(tag + ".pre", std::max(n, 1));
+    scan_into(c, need, pre, n, eq, total);
+    if (n > 0) {
+        k_scatter_flags<<<nblocks(n, 256), 256, 0, c.stream>>>(need, pre, n, eq, out);
+        SM_LAUNCH_CHECK();
+    }
+    return total;
+}
+
 void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *ids, int m,
                       const HGrid &query, int k, bool smooth, bool invert, const float *vp,
-                      const std::string &tag) {
+                      const std::string &tag, const KdTree *tree) {
     if (m <= 0)
         return;
     if (k < 3)
@@ -981,20 +994,31 @@ void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *
     k_mark_todo<<<nblocks(m, 256), 256, 0, c.stream>>>(ids, m, nrm, need);
     SM_LAUNCH_CHECK();
     // the query lists and their counts stay on the device; launches are sized by bounds
-    int       *todo   = c.arena.get<int>(tag + ".todo", m);
-    const int *ntodo  = compact_grid_order(c, query, need, 2, todo, tag + ".ct");
+    // with the reference's k-d tree the k nearest come from its depth-first search (ties:
+    // first found); the lists are then in index order (the results do not depend on it)
+    int       *todo   = c.arena.get<int>(tag + ".todo", std::max(tree ? npoints : m, 1));
+    const int *ntodo  = tree ? compact_need(c, need, npoints, 2, todo, tag + ".ct")
+                             : compact_grid_order(c, query, need, 2, todo, tag + ".ct");
     int       *nbrT   = c.arena.get<int>(tag + ".nbrT", (size_t)m * k);
     int       *cntT   = c.arena.get<int>(tag + ".cntT", m);
-    launch_knn(c.stream, todo, ntodo, m, query.view(), pos, k, nbrT, cntT, smooth ? 1 : 0, nrm, need);
+    if (tree)
+        kd_knn(c, *tree, nullptr, pos, nullptr, todo, ntodo, m, k, nbrT, nullptr, cntT, nrm,
+               smooth ? need : nullptr);
+    else
+        launch_knn(c.stream, todo, ntodo, m, query.view(), pos, k, nbrT, cntT, smooth ? 1 : 0, nrm, need);
     const int  extraMax = smooth ? (int)std::min<long long>(npoints, (long long)m * k) : 0;
     int       *extra = nullptr, *nbrE = nullptr, *cntE = nullptr;
     const int *nextra = nullptr;
     if (extraMax > 0) {
-        extra  = c.arena.get<int>(tag + ".extra", extraMax);
-        nextra = compact_grid_order(c, query, need, 1, extra, tag + ".ce");
+        extra  = c.arena.get<int>(tag + ".extra", std::max(tree ? npoints : extraMax, 1));
+        nextra = tree ? compact_need(c, need, npoints, 1, extra, tag + ".ce")
+                      : compact_grid_order(c, query, need, 1, extra, tag + ".ce");
         nbrE   = c.arena.get<int>(tag + ".nbrE", (size_t)extraMax * k);
         cntE   = c.arena.get<int>(tag + ".cntE", extraMax);
-        launch_knn(c.stream, extra, nextra, extraMax, query.view(), pos, k, nbrE, cntE, 0, nrm, need);
+        if (tree)
+            kd_knn(c, *tree, nullptr, pos, nullptr, extra, nextra, extraMax, k, nbrE, nullptr, cntE);
+        else
+            launch_knn(c.stream, extra, nextra, extraMax, query.view(), pos, k, nbrE, cntE, 0, nrm, need);
     }
     const int nmax = std::max(m, extraMax);
     float4   *cen  = c.arena.get<float4>(tag + ".cen", 2 * (size_t)nmax);

@@ -174,6 +174,7 @@ struct Box {
 struct Model {
     int            device = 0;
     bool           trained = false;
+    int            order   = SM_ORDER_GRID; // search order of train and match
     float          sdRel   = 0.04f;
     sm_train_param tp{};
     Box            box{};

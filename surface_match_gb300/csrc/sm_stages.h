@@ -147,10 +147,14 @@ void gather_subset(Ctx &c, const float4 *pos, const float4 *nrm, const int *ids,
 // kept ids ascending, returns their count.
 int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m, const Box &box,
                   float step, int *outIds, const std::string &tag);
-// Two-phase normal estimation of ids[0..m) (see sm_oracle.cpp estimate_normals).
+struct KdTree;
+// Two-phase normal estimation of ids[0..m) (estimateNormal, util.cpp:234-334; all
+// neighbourhoods from the positions at the start of the call, then smoothing). The k
+// nearest come from the grid `query`, or, when `tree` is given, from the reference's k-d
+// tree (over all points, searched on the live positions `pos`).
 void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *ids, int m,
                       const HGrid &query, int k, bool smooth, bool invert, const float *vp,
-                      const std::string &tag);
+                      const std::string &tag, const KdTree *tree = nullptr);
 // Normalise all normals (normalizeNormal, util.cpp:163-176).
 void normalize_normals(Ctx &c, float4 *nrm, int n);
 
@@ -197,7 +201,15 @@ int kd_sample(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos,
 // how many there are.
 void kd_knn(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos,
             const float4 *qpos, const int *list, const int *nq, int nqMax, int k, int *nbr,
-            float *dist, int *cnt);
+            float *dist, int *cnt, const float4 *nrm = nullptr, int *need = nullptr);
+// The voting stage's radius searches (ppf.cpp:273-276) in the reduced tree: for each of the
+// K keypoints the candidates (cand[0..ncand), the sampled points) its search of radius^2 r2
+// returns, as CSR lists (*offOut: K + 1 offsets, *idsOut: ids) whose last (rows mod 8) rows
+// other than the keypoint are the search's last ones in depth-first order (the reference's
+// scalar-tail rows); the rest in candidate order. Returns the total list length.
+int kd_vote_lists(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos,
+                  const int *kp, int K, const int *cand, int ncand, float r2, int **offOut,
+                  int **idsOut, const std::string &tag);
 
 // ---- mls.cu ---------------------------------------------------------------------------
 constexpr int kMlsMaxOrder = 4; // largest polynomial order of the MLS fit
@@ -244,6 +256,11 @@ struct IcpScene {
     const float4 *pos, *nrm;
     HGrid         sampled, resampled, full; // the subset grids carry subset ranks in pts.w
     const float4 *posS, *nrmS, *posR, *nrmR; // the sampled / resampled subsets, rank order
+    // reference search order (tree != nullptr): searches in the k-d tree, reduced to the
+    // sampled (ioiS) or resampled (ioiR) points, whose ids map to subset ranks by rankS /
+    // rankR; the grids are then unused (only their point counts m are read)
+    const KdTree *tree = nullptr;
+    const int    *ioiS = nullptr, *ioiR = nullptr, *rankS = nullptr, *rankR = nullptr;
 };
 struct IcpParams {
     int   sparse, dense, denseSteps;

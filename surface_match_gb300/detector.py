@@ -184,7 +184,10 @@ class Context:
 class Detector:
     """GPU ppf::Detector: trainModel / matchScene / save / load."""
 
-    def __init__(self, context: Context | None = None, device: int = 0):
+    def __init__(self, context: Context | None = None, device: int = 0,
+                 search_order: str = "grid"):
+        """search_order: "grid" (the GPU's fast orders) or "reference" (the reference's k-d
+        tree orders and search pruning, see sm_model_set_search_order)."""
         self.ctx = context or Context(device)
         self._own_ctx = context is None
         h = C.c_void_p()
@@ -192,6 +195,14 @@ class Detector:
         self.model = h
         self.trained = False
         self.last_stats = None
+        self.set_search_order(search_order)
+
+    def set_search_order(self, order: str):
+        codes = {"grid": _lib.SM_ORDER_GRID, "reference": _lib.SM_ORDER_REFERENCE}
+        if order not in codes:
+            raise ValueError(f"search_order must be one of {sorted(codes)}")
+        _check(_lib.load().sm_model_set_search_order(self.model, codes[order]))
+        self.search_order = order
 
     def close(self):
         if getattr(self, "model", None):
