@@ -548,6 +548,23 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
             int *rankR = d.arena.get<int>("m.rankR", std::max(n, 1));
             rank_of(d, sampled, ns, rankS);
             rank_of(d, resampled, nres, rankR);
+            // the refinement's searches: empty subtrees of the reduced trees are skipped,
+            // leaves read tree-ordered records of the positions as they are now
+            int    *neS = d.arena.get<int>("m.neS", std::max(T.nnodes, 1));
+            int    *neR = d.arena.get<int>("m.neR", std::max(T.nnodes, 1));
+            float4 *tpS = d.arena.get<float4>("m.tpS", std::max(T.m, 1));
+            float4 *tpR = d.arena.get<float4>("m.tpR", std::max(T.m, 1));
+            float4 *tpF = d.arena.get<float4>("m.tpF", std::max(T.m, 1));
+            kd_mark_nonempty(d, T, ioi, neS);
+            kd_mark_nonempty(d, T, ioi2, neR);
+            kd_tree_positions(d, T, ioi, P, tpS);
+            kd_tree_positions(d, T, ioi2, P, tpR);
+            kd_tree_positions(d, T, nullptr, P, tpF);
+            s.neS         = neS;
+            s.neR         = neR;
+            s.tpS         = tpS;
+            s.tpR         = tpR;
+            s.tpF         = tpF;
             s.tree        = &T;
             s.ioiS        = ioi;
             s.ioiR        = ioi2;

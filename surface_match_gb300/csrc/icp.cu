@@ -626,7 +626,7 @@ void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, con
     auto inliers = [&](const float4 *src, int n) {
         if (tree)
             k_inliers_tree<<<dim3(std::max(1, nblocks(n, kT)), ncand), kT, 0, c.stream>>>(
-                w, src, n, sc.tree->view(nullptr, sc.pos), sc2);
+                w, src, n, sc.tree->view(nullptr, sc.pos, nullptr, sc.tpF), sc2);
         else
             k_inliers<<<dim3(std::max(1, nblocks(n, kW)), ncand), kT, 0, c.stream>>>(
                 w, src, n, sc.full.view(), sc2);
@@ -636,7 +636,7 @@ void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, con
         Stage s{m.sp, m.sn, m.ns, nblocks(m.ns, kT), sc.sampled.view(), sc.posS, sc.nrmS, sc.sampled.m, 5,
                 p.sampleStep * 0.5f, p.sampleStep, rej2, 0};
         if (tree) {
-            s.tree   = sc.tree->view(sc.ioiS, sc.pos);
+            s.tree   = sc.tree->view(sc.ioiS, sc.pos, sc.neS, sc.tpS);
             s.rankOf = sc.rankS;
         }
         run_stage(c, w, s, ncand);
@@ -649,7 +649,7 @@ void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, con
             Stage d{m.rp, m.rn, m.nr, nblocks(m.nr, kT), sc.resampled.view(), sc.posR, sc.nrmR,
                     sc.resampled.m, p.denseSteps, p.reSampleStep * 0.5f, p.sampleStep, rej2, 1};
             if (tree) {
-                d.tree   = sc.tree->view(sc.ioiR, sc.pos);
+                d.tree   = sc.tree->view(sc.ioiR, sc.pos, sc.neR, sc.tpR);
                 d.rankOf = sc.rankR;
             }
             run_stage(c, w, d, ncand);

@@ -20,16 +20,17 @@
 // does through its by-reference bbox).
 //
 // Greedy sampling in tree order. The reference keeps a point unless an already kept point's
-// radius search found it, visiting points in tree position order. On the GPU the points
-// are bucketed into grid cells of side >= step, each cell's points in tree order; a warp
-// advances a cell's cursor point by point: the point is dropped if a kept point of its own
-// or a neighbouring cell with an earlier tree position reaches it, and kept once every
-// neighbouring cell has decided all its points before it. Cells wait only on cells whose
-// pending point comes earlier in tree order, so the cell holding the earliest undecided
-// point always advances. "Reaches" is the reference's radius search membership: squared
-// distance below step^2 and not pruned by the search above the point's leaf - decided by
-// walking the point's root-to-leaf path (smk::kd_reaches) unless the distance bound proves
-// the pruning cannot happen (points moved by normal estimation can leave their leaf's box).
+// radius search found it, visiting points in tree position order (util.cpp:107-139). Each
+// point's fate depends only on the earlier points within the step: it is dropped once a
+// kept one reaches it, and kept once all of them are decided and none of the kept ones
+// reaches it. The GPU counts those earlier points per point (neighbourhoods from grid cells
+// of side >= step, each cell's points in tree order), then decides points as their counts
+// run out, through a device queue: every point is handled exactly once, and decisions
+// travel along the dependency chains of the greedy order. "Reaches" is the reference's
+// radius search membership: squared distance below step^2 and not pruned by the search
+// above the point's leaf - decided by walking the point's root-to-leaf path
+// (smk::kd_reaches) unless the distance bound proves the pruning cannot happen (points
+// moved by normal estimation can leave their leaf's box).
 #include <climits>
 #include <cmath>
 
@@ -539,29 +540,32 @@ __global__ void k_kd_finish(int4 *__restrict__ nd, const int *__restrict__ paren
 }
 
 // ---- greedy sampling in tree order ---------------------------------------------------
-constexpr uint32_t kNoCell    = 1u << 23; // sort key of positions reduce() excluded
-constexpr int      kSpBs      = 256;
-constexpr long long kSpIdle   = 1ll << 22; // passes without progress before giving up
+constexpr uint32_t  kNoCell   = 1u << 23; // sort key of positions reduce() excluded
+constexpr int       kSpBs     = 256;
+constexpr long long kSpIdle   = 1ll << 22; // polls of an unwritten queue slot before giving up
+constexpr int       kSpUnroll = 4;         // neighbourhood entries in flight per lane
 
 struct SampleArgs {
     KdView          t;
-    const float    *nodeBox;
-    const int      *leafOf;
     float           org[3], g;
     int             dim[3];
-    const uint32_t *sortPos;  // tree positions grouped by cell, tree order inside a cell
+    const float4   *ent;      // cell runs: {x, y, z, tree position bits}, tree order in a run
+    const float    *ex;       // the entries' excursions from their leaves' build-time boxes
+    const int      *cellOf;   // per entry: its cell's occupied rank (-1 past the active ones)
     const int      *cellRank; // dense cell -> occupied rank (-1: empty)
     const int      *cellList; // occupied rank -> dense cell
-    const int      *cellEnd;  // occupied rank -> end of its run in sortPos
-    int            *cursor;   // occupied rank -> next undecided entry of its run
-    int            *cursorPos;// occupied rank -> tree position of that entry (INT_MAX: done)
-    int            *keptCnt;  // occupied rank -> kept points
-    float4         *kept;     // occupied rank x cap: {x, y, z, tree position bits}
-    int             cap, ncells;
+    const int      *cellBeg;  // occupied rank -> its run [beg, end) of the entries
+    const int      *cellEnd;
+    int            *cnt;      // per entry: earlier points within the step not yet decided
+    int            *dec;      // per entry: 0 open, 1 kept, 2 dropped
+    int            *queue;    // entries in the order they were decided (-1: not written)
+    int            *head, *tail;
+    const int      *nact;     // number of entries of active points (device)
+    int             m;
     float           r2;
     double          safe2;
     int            *keptFlag; // per tree position
-    int            *err;      // [0] kept capacity, [1] wait limit
+    int            *err;      // a bounded wait expired
 };
 
 __device__ __forceinline__ int ld_vol(const int *p) { return *(const volatile int *)p; }
@@ -621,107 +625,215 @@ __global__ void k_sp_heads(const uint32_t *__restrict__ key, int m, int *__restr
     head[k] = (k < m && key[k] != kNoCell && (k == 0 || key[k - 1] != key[k])) ? 1 : 0;
 }
 
-__global__ void k_sp_cells(const uint32_t *__restrict__ key, const uint32_t *__restrict__ val,
-                           int m, const int *__restrict__ head, const int *__restrict__ rank,
-                           int *__restrict__ cellRank, int *__restrict__ cellList,
-                           int *__restrict__ cellEnd, int *__restrict__ cursor,
-                           int *__restrict__ cursorPos, int *__restrict__ keptCnt) {
+__global__ void k_sp_cells(const uint32_t *__restrict__ key, int m, const int *__restrict__ head,
+                           const int *__restrict__ rank, int *__restrict__ cellRank,
+                           int *__restrict__ cellList, int *__restrict__ cellBeg,
+                           int *__restrict__ cellEnd, int *__restrict__ cellOf,
+                           int *__restrict__ nact) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= m || key[k] == kNoCell)
+    if (k >= m)
         return;
+    if (key[k] == kNoCell) {
+        cellOf[k] = -1;
+        return;
+    }
     const int r = rank[k] + head[k] - 1; // the run's occupied rank
+    cellOf[k]   = r;
     if (head[k]) {
         cellRank[key[k]] = r;
         cellList[r]      = (int)key[k];
-        cursor[r]        = k;
-        cursorPos[r]     = (int)val[k];
-        keptCnt[r]       = 0;
+        cellBeg[r]       = k;
     }
     if (k == m - 1 || key[k + 1] != key[k])
         cellEnd[r] = k + 1;
+    if (k == m - 1 || key[k + 1] == kNoCell)
+        *nact = k + 1; // the active entries sort first
 }
 
-// One warp per cell (cells dealt round-robin to the warps of a co-resident grid); a warp
-// sweeps its cells, advancing each cursor as far as its neighbours allow, until all are
-// done.
+// The cell runs' points in run order: {x, y, z, tree position bits} and the point's
+// excursion from its leaf's build-time box.
+__global__ void k_sp_entries(const uint32_t *__restrict__ sortPos, int m, KdView t,
+                             const float *__restrict__ nodeBox, const int *__restrict__ leafOf,
+                             float4 *__restrict__ ent, float *__restrict__ ex) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m)
+        return;
+    const int ip = (int)sortPos[k];
+    const int id = t.vacc[ip];
+    if (id < 0)
+        return;
+    const float4 p = t.pos[id];
+    ent[k]         = make_float4(p.x, p.y, p.z, __int_as_float(ip));
+    ex[k]          = (float)excursion(nodeBox + 6 * (size_t)leafOf[ip], p);
+}
+
+// The 27 cells around a cell: lane l < 27 gets the first entry of neighbour l's run; returns
+// the lane's exclusive prefix of the runs' lengths and writes their total to tot.
+__device__ __forceinline__ int nb_runs(const SampleArgs &a, int cid, int &nb, int &tot) {
+    const int lane = threadIdx.x & 31;
+    const int cx = cid % a.dim[0], cy = (cid / a.dim[0]) % a.dim[1], cz = cid / (a.dim[0] * a.dim[1]);
+    nb      = 0;
+    int len = 0;
+    if (lane < 27) {
+        const int x = cx + lane % 3 - 1, y = cy + (lane / 3) % 3 - 1, z = cz + lane / 9 - 1;
+        if (x >= 0 && y >= 0 && z >= 0 && x < a.dim[0] && y < a.dim[1] && z < a.dim[2]) {
+            const int nr = a.cellRank[(z * a.dim[1] + y) * a.dim[0] + x];
+            if (nr >= 0) {
+                nb  = a.cellBeg[nr];
+                len = a.cellEnd[nr] - nb;
+            }
+        }
+    }
+    const int incl = warp_incl_scan(len);
+    tot            = __shfl_sync(0xffffffffu, incl, 31);
+    return incl - len;
+}
+
+// Entry of flattened neighbourhood index t: binary search over the lanes' prefixes.
+__device__ __forceinline__ int nb_entry(int t, int excl, int nb) {
+    int lo = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+        const int mid = lo + step;
+        const int ev  = __shfl_sync(0xffffffffu, excl, mid & 31);
+        if (mid < 27 && ev <= t)
+            lo = mid;
+    }
+    return __shfl_sync(0xffffffffu, nb, lo) + (t - __shfl_sync(0xffffffffu, excl, lo));
+}
+
+// Step 1, a warp per point p: the earlier points (lower tree position) within the step of
+// p - squared distance from that point to p below step^2, the first test of its radius
+// search. p's decision waits for theirs. Points without any are kept at once and queued.
+__global__ void __launch_bounds__(kSpBs) k_sp_count(SampleArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int nw   = (int)(((long long)gridDim.x * blockDim.x) >> 5);
+    for (int k = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5); k < a.m; k += nw) {
+        if (a.cellOf[k] < 0)
+            break; // past the active entries
+        const float4 p  = a.ent[k];
+        const int    ip = __float_as_int(p.w);
+        int          nb, tot;
+        const int    excl = nb_runs(a, a.cellList[a.cellOf[k]], nb, tot);
+        int          cnt  = 0;
+        for (int base = 0; base < tot; base += 32 * kSpUnroll) {
+            int    kb[kSpUnroll];
+            float4 b[kSpUnroll];
+#pragma unroll
+            for (int u = 0; u < kSpUnroll; u++)
+                kb[u] = nb_entry(min(base + u * 32 + lane, tot - 1), excl, nb);
+#pragma unroll
+            for (int u = 0; u < kSpUnroll; u++)
+                b[u] = a.ent[max(kb[u], 0)];
+#pragma unroll
+            for (int u = 0; u < kSpUnroll; u++)
+                if (base + u * 32 + lane < tot && __float_as_int(b[u].w) < ip) {
+                    const float bq[3] = {b[u].x, b[u].y, b[u].z};
+                    cnt += smk::eval_metric(bq, p) < a.r2 ? 1 : 0;
+                }
+        }
+        cnt = __reduce_add_sync(0xffffffffu, cnt);
+        if (lane == 0) {
+            a.cnt[k] = cnt;
+            if (cnt == 0) {
+                a.dec[k]                      = 1;
+                a.queue[atomicAdd(a.tail, 1)] = k;
+            }
+        }
+    }
+}
+
+// Decide entry p (open -> fate) and queue it, unless it is decided already.
+__device__ __forceinline__ void sp_push(const SampleArgs &a, int p, int fate) {
+    if (atomicCAS(&a.dec[p], 0, fate) == 0) {
+        const int slot = atomicAdd(a.tail, 1);
+        __threadfence();
+        atomicExch(&a.queue[slot], p);
+    }
+}
+
+// Step 2, a warp per queued point b, in queue order (every active point is queued exactly
+// once). A kept b drops every later point its search reaches (and queues it); every other
+// later point within the step that is still open counts b as decided, and the last of its
+// earlier points to be decided queues it as kept. Dropping happens before counting, so a
+// point that a kept point reaches never runs out of count. Each queued point waits only on
+// points queued before it, so the warps that took the earliest slots always progress.
 __global__ void __launch_bounds__(kSpBs) k_sp_run(SampleArgs a) {
-    const int  lane = threadIdx.x & 31;
-    const int  gw   = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
-    const int  nw   = (int)(((long long)gridDim.x * blockDim.x) >> 5);
-    long long  idle = 0;
+    const int lane = threadIdx.x & 31;
     for (;;) {
-        bool open = false, moved = false;
-        for (int r = gw; r < a.ncells; r += nw) {
-            int       k   = ld_vol(&a.cursor[r]);
-            const int end = a.cellEnd[r];
-            if (k >= end)
-                continue;
-            open          = true;
-            const int cid = a.cellList[r];
-            const int cx = cid % a.dim[0], cy = (cid / a.dim[0]) % a.dim[1],
-                      cz = cid / (a.dim[0] * a.dim[1]);
-            int nr = -1;
-            if (lane < 27) {
-                const int x = cx + lane % 3 - 1, y = cy + (lane / 3) % 3 - 1, z = cz + lane / 9 - 1;
-                if (x >= 0 && y >= 0 && z >= 0 && x < a.dim[0] && y < a.dim[1] && z < a.dim[2])
-                    nr = a.cellRank[(z * a.dim[1] + y) * a.dim[0] + x];
-            }
-            while (k < end) {
-                const int ip = (int)a.sortPos[k];
-                bool      ok = true;
-                if (nr >= 0 && nr != r)
-                    ok = ld_vol(&a.cursorPos[nr]) >= ip;
-                if (!__all_sync(0xffffffffu, ok))
+        int slot = 0;
+        if (lane == 0)
+            slot = atomicAdd(a.head, 1);
+        slot = __shfl_sync(0xffffffffu, slot, 0);
+        if (slot >= *a.nact)
+            return;
+        int b = -1;
+        if (lane == 0) {
+            for (long long it = 0;; it++) {
+                b = ld_vol(&a.queue[slot]);
+                if (b >= 0)
                     break;
-                __threadfence(); // the neighbours' kept lists are complete below ip
-                const float4 p = a.t.pos[a.t.vacc[ip]];
-                const double e = excursion(a.nodeBox + 6 * (size_t)a.leafOf[ip], p);
-                bool         cov = false;
-                if (nr >= 0) {
-                    const int kc = ld_vol(&a.keptCnt[nr]);
-                    for (int t = 0; t < kc && !cov; t++) {
-                        const volatile float4 *qp = a.kept + (size_t)nr * a.cap + t;
-                        const float4 q = make_float4(qp->x, qp->y, qp->z, qp->w);
-                        if (__float_as_int(q.w) < ip)
-                            cov = reaches(a, q, p, ip, e);
-                    }
+                if (ld_vol(a.err) || it > kSpIdle) {
+                    atomicExch(a.err, 1);
+                    break;
                 }
-                cov = __any_sync(0xffffffffu, cov);
-                k++;
-                if (lane == 0) {
-                    if (!cov) {
-                        const int kc = a.keptCnt[r];
-                        if (kc < a.cap) {
-                            a.kept[(size_t)r * a.cap + kc] = make_float4(p.x, p.y, p.z, __int_as_float(ip));
-                            __threadfence();
-                            *(volatile int *)&a.keptCnt[r] = kc + 1;
-                        } else {
-                            atomicExch(&a.err[0], 1);
-                        }
-                        a.keptFlag[ip] = 1;
-                    }
+                __nanosleep(32);
+            }
+        }
+        b = __shfl_sync(0xffffffffu, b, 0);
+        if (b < 0)
+            return;
+        __threadfence();
+        const int    fate = ld_vol(&a.dec[b]);
+        const float4 q    = a.ent[b];
+        const int    iq   = __float_as_int(q.w);
+        if (fate == 1 && lane == 0)
+            a.keptFlag[iq] = 1;
+        int         nb, tot;
+        const int   excl  = nb_runs(a, a.cellList[a.cellOf[b]], nb, tot);
+        const float qq[3] = {q.x, q.y, q.z};
+        for (int base = 0; base < tot; base += 32 * kSpUnroll) {
+            int    kp[kSpUnroll];
+            float4 p[kSpUnroll];
+#pragma unroll
+            for (int u = 0; u < kSpUnroll; u++)
+                kp[u] = nb_entry(min(base + u * 32 + lane, tot - 1), excl, nb);
+#pragma unroll
+            for (int u = 0; u < kSpUnroll; u++)
+                p[u] = a.ent[max(kp[u], 0)];
+            // the later points within the step that are still open
+            bool live[kSpUnroll];
+#pragma unroll
+            for (int u = 0; u < kSpUnroll; u++)
+                live[u] = base + u * 32 + lane < tot && __float_as_int(p[u].w) > iq &&
+                          smk::eval_metric(qq, p[u]) < a.r2;
+#pragma unroll
+            for (int u = 0; u < kSpUnroll; u++)
+                live[u] = live[u] && ld_vol(&a.dec[kp[u]]) == 0;
+            bool count[kSpUnroll];
+#pragma unroll
+            for (int u = 0; u < kSpUnroll; u++) {
+                count[u] = false;
+                if (!live[u])
+                    continue;
+                if (fate == 1 && reaches(a, q, p[u], __float_as_int(p[u].w), (double)a.ex[kp[u]])) {
+                    sp_push(a, kp[u], 2);
+                    continue;
+                }
+                count[u] = true;
+            }
+            __threadfence();
+            int old[kSpUnroll];
+#pragma unroll
+            for (int u = 0; u < kSpUnroll; u++)
+                old[u] = count[u] ? atomicSub(&a.cnt[kp[u]], 1) : 0;
+#pragma unroll
+            for (int u = 0; u < kSpUnroll; u++)
+                if (old[u] == 1) {
                     __threadfence();
-                    *(volatile int *)&a.cursor[r]    = k;
-                    *(volatile int *)&a.cursorPos[r] = k < end ? (int)a.sortPos[k] : INT_MAX;
+                    sp_push(a, kp[u], 1);
                 }
-                __syncwarp();
-                moved = true;
-            }
         }
-        if (!open)
-            return;
-        if (moved) {
-            idle = 0;
-        } else {
-            if (++idle > kSpIdle) {
-                if (lane == 0)
-                    atomicExch(&a.err[1], 1);
-                return;
-            }
-            __nanosleep(128);
-        }
-        if (ld_vol(&a.err[1]))
-            return;
     }
 }
 
@@ -906,6 +1018,38 @@ __global__ void __launch_bounds__(kRlBs)
             out[o] = cand[sT[k]];
 }
 
+// Leaves holding an active position flag themselves and their ancestors (a walk stops at
+// an ancestor another walk has flagged).
+__global__ void k_kd_nonempty(const int4 *__restrict__ nd, const int *__restrict__ parent,
+                              int nnodes, const int *__restrict__ vacc, int *__restrict__ flags) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nnodes)
+        return;
+    const int4 n = nd[v];
+    if (!smk::is_leaf(n))
+        return;
+    bool any = false;
+    for (int i = n.x; i < n.y && !any; i++)
+        any = vacc[i] >= 0;
+    for (int u = v; any && u >= 0; u = parent[u])
+        if (atomicExch(&flags[u], 1) == 1)
+            break;
+}
+
+__global__ void k_kd_tpos(const int *__restrict__ vacc, int m, const float4 *__restrict__ pos,
+                          float4 *__restrict__ tpos) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m)
+        return;
+    const int id = vacc[i];
+    if (id < 0) {
+        tpos[i] = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+        return;
+    }
+    const float4 p = pos[id];
+    tpos[i]        = make_float4(p.x, p.y, p.z, __int_as_float(id));
+}
+
 } // namespace
 
 // =======================================================================================
@@ -923,6 +1067,7 @@ void build_kdtree(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
     T.treePos = c.arena.get<int>(tag + ".tpos", std::max(npoints, 1));
     T.rec     = c.arena.get<float4>(tag + ".rec", std::max(m, 1));
     int *parent  = c.arena.get<int>(tag + ".par", cap);
+    T.parent     = parent;
     int *arrive  = c.arena.get<int>(tag + ".arr", cap);
     int *cnt     = c.arena.get<int>(tag + ".cnt", 8); // nodes, nnext, nsmall, err
     int *segOf   = c.arena.get<int>(tag + ".segof", std::max(m, 1));
@@ -1018,58 +1163,61 @@ int kd_sample(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos,
     k_sp_heads<<<nblocks((long long)m + 1, 256), 256, 0, c.stream>>>(key, m, head);
     SM_LAUNCH_CHECK();
     const int ncells = scan_excl(c, head, rank, (long long)m + 1, tag + ".hs", true);
-    // kept capacity per cell: points pairwise at least `step` apart inside a cube of side g
-    // fit disjoint balls of radius step/2 inside the cube grown by step/2; doubled for
-    // points that a pruned search did not reach
-    const double sc  = (double)gp.g / (double)step;
-    const int    cap = 2 * ((int)std::floor((sc + 1.0) * (sc + 1.0) * (sc + 1.0) / (3.14159265358979 / 6.0)) + 1);
-    int    *cellList  = c.arena.get<int>(tag + ".clist", std::max(ncells, 1));
-    int    *cellEnd   = c.arena.get<int>(tag + ".cend", std::max(ncells, 1));
-    int    *cursor    = c.arena.get<int>(tag + ".cur", std::max(ncells, 1));
-    int    *cursorPos = c.arena.get<int>(tag + ".cpos", std::max(ncells, 1));
-    int    *keptCnt   = c.arena.get<int>(tag + ".kc", std::max(ncells, 1));
-    float4 *kept      = c.arena.get<float4>(tag + ".kept", (size_t)std::max(ncells, 1) * cap);
-    int    *flag      = c.arena.get<int>(tag + ".flag", (size_t)m + 1);
-    int    *err       = c.arena.get<int>(tag + ".err", 2);
+    int    *cellList = c.arena.get<int>(tag + ".clist", std::max(ncells, 1));
+    int    *cellBeg  = c.arena.get<int>(tag + ".cbeg", std::max(ncells, 1));
+    int    *cellEnd  = c.arena.get<int>(tag + ".cend", std::max(ncells, 1));
+    int    *cellOf   = c.arena.get<int>(tag + ".cof", m);
+    float4 *ent      = c.arena.get<float4>(tag + ".ent", m);
+    float  *ex       = c.arena.get<float>(tag + ".ex", m);
+    int    *cnt      = c.arena.get<int>(tag + ".cnt", m);
+    int    *dec      = c.arena.get<int>(tag + ".dec", m);
+    int    *queue    = c.arena.get<int>(tag + ".q", m);
+    int    *flag     = c.arena.get<int>(tag + ".flag", (size_t)m + 1);
+    int    *ctl      = c.arena.get<int>(tag + ".ctl", 4); // head, tail, active entries, error
     SM_CUDA(cudaMemsetAsync(cRank, 0xff, (size_t)nc * 4, c.stream));
     SM_CUDA(cudaMemsetAsync(flag, 0, ((size_t)m + 1) * 4, c.stream));
-    SM_CUDA(cudaMemsetAsync(err, 0, 2 * sizeof(int), c.stream));
-    k_sp_cells<<<nblocks(m, 256), 256, 0, c.stream>>>(key, val, m, head, rank, cRank, cellList,
-                                                     cellEnd, cursor, cursorPos, keptCnt);
+    SM_CUDA(cudaMemsetAsync(ctl, 0, 4 * sizeof(int), c.stream));
+    SM_CUDA(cudaMemsetAsync(dec, 0, (size_t)m * 4, c.stream));
+    SM_CUDA(cudaMemsetAsync(queue, 0xff, (size_t)m * 4, c.stream));
+    k_sp_cells<<<nblocks(m, 256), 256, 0, c.stream>>>(key, m, head, rank, cRank, cellList, cellBeg,
+                                                     cellEnd, cellOf, ctl + 2);
+    SM_LAUNCH_CHECK();
+    k_sp_entries<<<nblocks(m, 256), 256, 0, c.stream>>>(val, m, T.view(vaccA, pos), T.box,
+                                                        T.leafOf, ent, ex);
     SM_LAUNCH_CHECK();
     SampleArgs a{};
-    a.t        = T.view(vaccA, pos);
-    a.nodeBox  = T.box;
-    a.leafOf   = T.leafOf;
+    a.t = T.view(vaccA, pos);
     for (int d = 0; d < 3; d++) {
         a.org[d] = gp.org[d];
         a.dim[d] = gp.dim[d];
     }
-    a.g         = gp.g;
-    a.sortPos   = val;
-    a.cellRank  = cRank;
-    a.cellList  = cellList;
-    a.cellEnd   = cellEnd;
-    a.cursor    = cursor;
-    a.cursorPos = cursorPos;
-    a.keptCnt   = keptCnt;
-    a.kept      = kept;
-    a.cap       = cap;
-    a.ncells    = ncells;
-    a.r2        = step * step;
-    a.safe2     = (double)a.r2 * (1.0 - 1e-4);
-    a.keptFlag  = flag;
-    a.err       = err;
+    a.g        = gp.g;
+    a.ent      = ent;
+    a.ex       = ex;
+    a.cellOf   = cellOf;
+    a.cellRank = cRank;
+    a.cellList = cellList;
+    a.cellBeg  = cellBeg;
+    a.cellEnd  = cellEnd;
+    a.cnt      = cnt;
+    a.dec      = dec;
+    a.queue    = queue;
+    a.head     = ctl;
+    a.tail     = ctl + 1;
+    a.nact     = ctl + 2;
+    a.m        = m;
+    a.r2       = step * step;
+    a.safe2    = (double)a.r2 * (1.0 - 1e-4);
+    a.keptFlag = flag;
+    a.err      = ctl + 3;
     if (ncells > 0) {
-        // every block resident at once (a cooperative launch guarantees it): warps wait on
-        // cells that other warps own
-        int dev = c.device, nsm = 0, perSm = 0;
-        SM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-        SM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_sp_run, kSpBs, 0));
-        const int want = (ncells + kSpBs / 32 - 1) / (kSpBs / 32);
-        const int grid = std::max(1, std::min(want, nsm * std::max(perSm, 1)));
-        void     *args[] = {&a};
-        SM_CUDA(cudaLaunchCooperativeKernel((const void *)k_sp_run, grid, kSpBs, args, 0, c.stream));
+        int nsm = 0;
+        SM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device));
+        const int wpb = kSpBs / 32;
+        k_sp_count<<<std::min(nblocks(m, wpb), nsm * 16), kSpBs, 0, c.stream>>>(a);
+        SM_LAUNCH_CHECK();
+        // the queue's consumers: each queued point is taken by one warp, in queue order
+        k_sp_run<<<std::min(nblocks(m, wpb), nsm * 4), kSpBs, 0, c.stream>>>(a);
         SM_LAUNCH_CHECK();
     }
     int *pre = c.arena.get<int>(tag + ".pre", (size_t)m + 1);
@@ -1077,12 +1225,10 @@ int kd_sample(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos,
     k_sp_out<<<nblocks(m, 256), 256, 0, c.stream>>>(flag, pre, m, vaccA, outIds, ioi);
     SM_LAUNCH_CHECK();
     SM_CUDA(cudaMemcpyAsync(c.hostCounts, pre + m, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-    SM_CUDA(cudaMemcpyAsync(c.hostCounts + 1, err, 2 * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    SM_CUDA(cudaMemcpyAsync(c.hostCounts + 1, ctl + 3, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     c.sync_checked();
-    if (c.hostCounts[2])
-        throw Error(SM_ERR_RUNTIME, "tree-order sampler: a bounded wait expired");
     if (c.hostCounts[1])
-        throw Error(SM_ERR_CAPACITY, "tree-order sampler: kept-point capacity per cell exceeded");
+        throw Error(SM_ERR_RUNTIME, "tree-order sampler: a bounded wait expired");
     return c.hostCounts[0];
 }
 
@@ -1093,10 +1239,12 @@ void kd_knn(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos,
         return;
     if (k < 1 || k > kMaxKnn)
         throw Error(SM_ERR_RANGE, "knnNormal larger than " + std::to_string(kMaxKnn) + " is not supported");
-    int *err = c.arena.get<int>("kd.knn.err", 1);
+    int    *err  = c.arena.get<int>("kd.knn.err", 1);
+    float4 *tpos = c.arena.get<float4>("kd.knn.tpos", T.m);
     SM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c.stream));
-    k_kd_knn<<<nblocks(nqMax, 128), 128, 0, c.stream>>>(T.view(vaccActive, pos), qpos, list, nq, k,
-                                                        nbr, dist, cnt, err, nrm, need);
+    kd_tree_positions(c, T, vaccActive, pos, tpos);
+    k_kd_knn<<<nblocks(nqMax, 128), 128, 0, c.stream>>>(T.view(vaccActive, pos, nullptr, tpos), qpos,
+                                                        list, nq, k, nbr, dist, cnt, err, nrm, need);
     SM_LAUNCH_CHECK();
 }
 
@@ -1124,6 +1272,25 @@ int kd_vote_lists(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *
     k_kd_fill<<<K, kRlBs, 0, c.stream>>>(mask, words, cand, ncand, off, tail, ids);
     SM_LAUNCH_CHECK();
     return total;
+}
+
+void kd_mark_nonempty(Ctx &c, const KdTree &T, const int *vaccActive, int *flags) {
+    if (T.nnodes <= 0)
+        return;
+    SM_CUDA(cudaMemsetAsync(flags, 0, (size_t)T.nnodes * 4, c.stream));
+    k_kd_nonempty<<<nblocks(T.nnodes, 256), 256, 0, c.stream>>>(T.nd, T.parent, T.nnodes,
+                                                                vaccActive ? vaccActive : T.vacc,
+                                                                flags);
+    SM_LAUNCH_CHECK();
+}
+
+void kd_tree_positions(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos,
+                       float4 *tpos) {
+    if (T.m <= 0)
+        return;
+    k_kd_tpos<<<nblocks(T.m, 256), 256, 0, c.stream>>>(vaccActive ? vaccActive : T.vacc, T.m, pos,
+                                                        tpos);
+    SM_LAUNCH_CHECK();
 }
 
 } // namespace sm

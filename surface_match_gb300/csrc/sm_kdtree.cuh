@@ -33,6 +33,13 @@ struct KdView {
     const float  *box;  // root's tight box: lo xyz, hi xyz (nanoflann's root_bbox_)
     const int    *vacc; // per tree position: point id, or -1 where reduce() excluded it
     const float4 *pos;  // live point positions by id (normal estimation moves points)
+    // per node: nonzero when its subtree holds a point of vacc (nullptr: all do). A search
+    // that skips a subtree without points finds and changes nothing the reference's would
+    // not: entering it adds no point and its bounds are restored on the way out.
+    const int    *nonEmpty = nullptr;
+    // tree-ordered live positions, w = point id bits (-1: excluded); when set, a leaf scan
+    // reads one record per entry instead of vacc and then pos
+    const float4 *tpos = nullptr;
 };
 
 __device__ __forceinline__ bool is_leaf(const int4 &n) { return n.z == -1; }
@@ -146,10 +153,20 @@ template <class RS> __device__ bool kd_search(const KdView &t, const float q[3],
         if (is_leaf(n)) {
             const float worst = rs.worst();
             for (int i = n.x; i < n.y; i++) {
-                const int id = t.vacc[i];
-                if (id < 0)
-                    continue;
-                const float d = eval_metric(q, t.pos[id]);
+                float4 p;
+                int    id;
+                if (t.tpos) {
+                    p  = t.tpos[i];
+                    id = __float_as_int(p.w);
+                    if (id < 0)
+                        continue;
+                } else {
+                    id = t.vacc[i];
+                    if (id < 0)
+                        continue;
+                    p = t.pos[id];
+                }
+                const float d = eval_metric(q, p);
                 if (d < worst)
                     rs.add(d, id, i);
             }
@@ -189,17 +206,54 @@ template <class RS> __device__ bool kd_search(const KdView &t, const float q[3],
             other = c1;
             cut   = (val - dlow) * (val - dlow);
         }
-        if (sp >= kMaxDepth)
-            return false;
-        Frame &f = st[sp++];
-        f.other  = other;
-        f.idx    = idx;
-        f.cut    = cut;
-        f.mind   = mindist;
-        f.d[0]   = dists[0];
-        f.d[1]   = dists[1];
-        f.d[2]   = dists[2];
-        v        = best;
+        const bool bestIn  = !t.nonEmpty || t.nonEmpty[best];
+        const bool otherIn = !t.nonEmpty || t.nonEmpty[other];
+        if (bestIn) {
+            if (otherIn) {
+                if (sp >= kMaxDepth)
+                    return false;
+                Frame &f = st[sp++];
+                f.other  = other;
+                f.idx    = idx;
+                f.cut    = cut;
+                f.mind   = mindist;
+                f.d[0]   = dists[0];
+                f.d[1]   = dists[1];
+                f.d[2]   = dists[2];
+            }
+            v = best;
+            continue;
+        }
+        // the near child holds no point: its search would return at once, so the far child
+        // is checked now with the bound the search computes after it
+        if (otherIn) {
+            const float dst = dists[idx];
+            const float md  = mindist + cut - dst;
+            if (md * 1.0f <= rs.worst()) {
+                dists[idx] = cut;
+                mindist    = md;
+                v          = other;
+                continue;
+            }
+        }
+        // neither child is entered: resume the deepest pending far child
+        v = -1;
+        while (sp > 0) {
+            const Frame &f   = st[--sp];
+            const float  dst = f.d[f.idx];
+            const float  md  = f.mind + f.cut - dst;
+            if (md * 1.0f <= rs.worst()) {
+                dists[0]     = f.d[0];
+                dists[1]     = f.d[1];
+                dists[2]     = f.d[2];
+                dists[f.idx] = f.cut;
+                mindist      = md;
+                v            = f.other;
+                break;
+            }
+        }
+        if (v < 0)
+            return true;
     }
 }
 

@@ -174,12 +174,16 @@ struct KdTree {
     int    *leafOf  = nullptr; // per tree position: its leaf
     int    *treePos = nullptr; // per point id: tree position (-1: not in the tree)
     float4 *rec     = nullptr; // build-time positions in tree order (w = point id)
-    smk::KdView view(const int *vaccActive, const float4 *pos) const {
+    int    *parent  = nullptr; // per node: its parent (-1 for the root)
+    smk::KdView view(const int *vaccActive, const float4 *pos, const int *nonEmpty = nullptr,
+                     const float4 *tpos = nullptr) const {
         smk::KdView v;
-        v.nd   = nd;
-        v.box  = box;
-        v.vacc = vaccActive ? vaccActive : vacc;
-        v.pos  = pos;
+        v.nd       = nd;
+        v.box      = box;
+        v.vacc     = vaccActive ? vaccActive : vacc;
+        v.pos      = pos;
+        v.nonEmpty = nonEmpty;
+        v.tpos     = tpos;
         return v;
     }
 };
@@ -202,6 +206,14 @@ int kd_sample(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos,
 void kd_knn(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos,
             const float4 *qpos, const int *list, const int *nq, int nqMax, int k, int *nbr,
             float *dist, int *cnt, const float4 *nrm = nullptr, int *need = nullptr);
+// flags[v] = 1 when node v's subtree holds a position whose vaccActive entry is >= 0
+// (the searches of a reduce()d tree skip the others).
+void kd_mark_nonempty(Ctx &c, const KdTree &T, const int *vaccActive, int *flags);
+// tpos[i] = pos[id] with w = id bits for the tree positions i whose vaccActive entry id is
+// >= 0, else w = -1 bits: the leaf records of the searches (taken after the positions last
+// moved).
+void kd_tree_positions(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos,
+                       float4 *tpos);
 // The voting stage's radius searches (ppf.cpp:273-276) in the reduced tree: for each of the
 // K keypoints the candidates (cand[0..ncand), the sampled points) its search of radius^2 r2
 // returns, as CSR lists (*offOut: K + 1 offsets, *idsOut: ids) whose last (rows mod 8) rows
@@ -261,6 +273,8 @@ struct IcpScene {
     // rankR; the grids are then unused (only their point counts m are read)
     const KdTree *tree = nullptr;
     const int    *ioiS = nullptr, *ioiR = nullptr, *rankS = nullptr, *rankR = nullptr;
+    const int    *neS = nullptr, *neR = nullptr;                  // non-empty node flags
+    const float4 *tpS = nullptr, *tpR = nullptr, *tpF = nullptr; // leaf records
 };
 struct IcpParams {
     int   sparse, dense, denseSteps;
