@@ -31,7 +31,7 @@ def build(force: bool = False) -> str:
     if not force and os.path.exists(SO) and os.path.getmtime(SO) >= newest:
         return SO
     tmp = SO + f".tmp{os.getpid()}"
-    cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
+    cmd = ["g++", "-std=c++17", "-O3", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
            "-fPIC", "-shared", "-Wno-array-bounds", "-o", tmp,
            os.path.join(HERE, "sm_oracle.cpp")]
     subprocess.run(cmd, check=True)

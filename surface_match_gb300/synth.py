@@ -506,7 +506,15 @@ def pose_error_sym(A, B, syms):
     B = A * S for the symmetry S closest to A^-1 B."""
     Ra, Rb = A[:3, :3].astype(np.float64), B[:3, :3].astype(np.float64)
     Rs = Ra.T @ Rb
-    ang = min(np.degrees(np.arccos(np.clip((np.trace(S.T @ Rs) - 1) / 2, -1, 1))) for S in syms)
+
+    def angle(R):
+        # atan2(sin, cos) of the rotation angle: the skew part gives the sine, so a float32
+        # rotation compared with itself reads 0 (arccos of the trace alone reads its
+        # non-orthonormality as a few hundredths of a degree)
+        w = np.array([R[2, 1] - R[1, 2], R[0, 2] - R[2, 0], R[1, 0] - R[0, 1]]) / 2.0
+        return np.degrees(np.arctan2(np.linalg.norm(w), (np.trace(R) - 1.0) / 2.0))
+
+    ang = min(angle(S.T @ Rs) for S in syms)
     return ang, float(np.linalg.norm(A[:3, 3].astype(np.float64) - B[:3, 3]))
 
 
