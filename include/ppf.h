@@ -170,9 +170,17 @@ struct MatchResult {
     PointCloud keyPoint;
 };
 
+// Search order of a Detector (extension; the reference has one order, its k-d tree's).
+// Reference: the reference's k-d tree built on the GPU, its sampling order, neighbour order
+// and search pruning - results bit-identical to the reference algorithm run single-threaded.
+// Grid (default): the same rules in uniform-grid order, several times faster; equally valid
+// samples, not the same ones. See sm_model_set_search_order.
+enum class SearchOrder { Grid = SM_ORDER_GRID, Reference = SM_ORDER_REFERENCE };
+
 class Detector {
 public:
     Detector() = default;
+    explicit Detector(SearchOrder order) : order_(order) {}
     ~Detector() {
         if (model_)
             sm_model_destroy(model_);
@@ -230,6 +238,14 @@ public:
             fill_result(scene, *matchResult);
     }
 
+    // Applies to later trainModel and matchScene calls.
+    void setSearchOrder(SearchOrder order) {
+        order_ = order;
+        if (model_)
+            detail::check(sm_model_set_search_order(model_, (int)order_));
+    }
+    SearchOrder searchOrder() const { return order_; }
+
     void save(const std::string &filename) const {
         if (!trained_)
             throw std::runtime_error("No trained model in save");
@@ -246,8 +262,10 @@ private:
     void ensure() {
         if (!ctx_)
             detail::check(sm_context_create(0, nullptr, &ctx_));
-        if (!model_)
+        if (!model_) {
             detail::check(sm_model_create(ctx_, &model_));
+            detail::check(sm_model_set_search_order(model_, (int)order_));
+        }
     }
     void fill_result(const PointCloud &scene, MatchResult &r) {
         auto ids = [&](int field) {
@@ -278,9 +296,10 @@ private:
         extract(ids(1), r.keyPoint);
         extract(ids(0), r.sampledScene);
     }
-    sm_context ctx_     = nullptr;
-    sm_model   model_   = nullptr;
-    bool       trained_ = false;
+    sm_context  ctx_     = nullptr;
+    sm_model    model_   = nullptr;
+    bool        trained_ = false;
+    SearchOrder order_   = SearchOrder::Grid;
 };
 
 // estimateNormalMLS (privateUtil.h:13, util.cpp:336-457) on the device: moving-least-squares
