@@ -36,14 +36,17 @@ static thread_local std::string g_lastError;
 long long                       g_launches = 0;
 
 void Model::free_device() {
-    void *ps[] = {sp, sn, rp, rn, hkeys, boff, entries};
+    void *ps[] = {sp, sn, rp, rn, hkeys, boff, entries, dkeys, doffs};
     for (void *p : ps)
         if (p)
             cudaFree(p);
     sp = sn = rp = rn = nullptr;
     hkeys = boff = nullptr;
     entries      = nullptr;
+    dkeys = doffs = nullptr;
+    hostValid     = false;
 }
+
 
 namespace {
 
@@ -213,6 +216,12 @@ void upload_model(Model &m, const std::vector<float> &sp, const std::vector<floa
     }
     SM_CUDA(cudaMalloc((void **)&m.entries, ent.size() * sizeof(uint2)));
     SM_CUDA(cudaMemcpy(m.entries, ent.data(), ent.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+    SM_CUDA(cudaMalloc((void **)&m.dkeys, std::max<size_t>(keys.size(), 1) * 4));
+    SM_CUDA(cudaMalloc((void **)&m.doffs, offs.size() * 4));
+    if (!keys.empty())
+        SM_CUDA(cudaMemcpy(m.dkeys, keys.data(), keys.size() * 4, cudaMemcpyHostToDevice));
+    SM_CUDA(cudaMemcpy(m.doffs, offs.data(), offs.size() * 4, cudaMemcpyHostToDevice));
+    m.hostValid = true;
     m.h_sp     = sp;
     m.h_sn     = sn;
     m.h_rp     = rp;
@@ -236,6 +245,34 @@ std::vector<float> download4(const float4 *d, int n) {
     }
     return o;
 }
+
+} // namespace
+
+void Model::ensure_host() {
+    if (hostValid)
+        return;
+    h_sp = download4(sp, ns);
+    h_sn = download4(sn, ns);
+    h_rp = download4(rp, nr);
+    h_rn = download4(rn, nr);
+    h_keys.resize(nkeys);
+    h_offs.resize((size_t)nkeys + 1);
+    std::vector<uint2> ent((size_t)nentries);
+    if (nkeys)
+        SM_CUDA(cudaMemcpy(h_keys.data(), dkeys, (size_t)nkeys * 4, cudaMemcpyDeviceToHost));
+    SM_CUDA(cudaMemcpy(h_offs.data(), doffs, ((size_t)nkeys + 1) * 4, cudaMemcpyDeviceToHost));
+    if (nentries)
+        SM_CUDA(cudaMemcpy(ent.data(), entries, (size_t)nentries * 8, cudaMemcpyDeviceToHost));
+    h_refs.resize((size_t)nentries);
+    h_alphas.resize((size_t)nentries);
+    for (size_t e = 0; e < ent.size(); e++) {
+        h_refs[e] = ent[e].x;
+        memcpy(&h_alphas[e], &ent[e].y, 4);
+    }
+    hostValid = true;
+}
+
+namespace {
 
 // Query-grid cell for k-nearest-neighbour searches: about 1.6x the expected k-NN radius,
 // from the point density the greedy sampling reveals (n_sampled points at `step` cover an
@@ -330,40 +367,28 @@ void train(Ctx &c, Model &m, const float *xyzIn, const float *nrmIn, int64_t n64
     float    *alphas = c.arena.get<float>("t.alphas", std::max<long long>(npair, 1));
     int      *pv     = c.arena.get<int>("t.pv", std::max<long long>(npair, 1));
     model_pairs(c, sp, sn, n1, angleStep, distStep, keys, alphas, pv);
-    std::vector<uint32_t> hk(npair);
-    std::vector<float>    ha(npair);
-    std::vector<int>      hv(npair);
-    if (npair) {
-        SM_CUDA(cudaMemcpyAsync(hk.data(), keys, npair * 4, cudaMemcpyDeviceToHost, c.stream));
-        SM_CUDA(cudaMemcpyAsync(ha.data(), alphas, npair * 4, cudaMemcpyDeviceToHost, c.stream));
-        SM_CUDA(cudaMemcpyAsync(hv.data(), pv, npair * 4, cudaMemcpyDeviceToHost, c.stream));
+    // the table grouped on the device by key in pair order - the reference's single-threaded
+    // insertion order (ppf.cpp:125-143) - into model-owned arrays
+    m.free_device();
+    m.ns = n1;
+    m.nr = n2;
+    for (int a = 0; a < 3; a++) {
+        m.box.mn[a] = box.mn[a];
+        m.box.mx[a] = box.mx[a];
     }
-    std::vector<float> hsp = download4(sp, n1), hsn = download4(sn, n1);
-    std::vector<float> hrp = download4(rp, n2), hrn = download4(rn, n2);
-    c.sync_checked();
-    // group by key, stable in pair order
-    std::vector<uint32_t> order;
-    order.reserve(npair);
-    for (long long t = 0; t < npair; t++)
-        if (hv[t])
-            order.push_back((uint32_t)t);
-    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return hk[a] < hk[b]; });
-    std::vector<uint32_t> K, O, R;
-    std::vector<float>    AL;
-    R.reserve(order.size());
-    AL.reserve(order.size());
-    for (size_t e = 0; e < order.size(); e++) {
-        const uint32_t t = order[e];
-        if (e == 0 || hk[t] != hk[order[e - 1]]) {
-            K.push_back(hk[t]);
-            O.push_back((uint32_t)e);
-        }
-        R.push_back(t / (uint32_t)n1);
-        AL.push_back(ha[t]);
-    }
-    O.push_back((uint32_t)order.size());
-    const float b6[6] = {box.mn[0], box.mn[1], box.mn[2], box.mx[0], box.mx[1], box.mx[2]};
-    upload_model(m, hsp, hsn, hrp, hrn, b6, K, O, R, AL);
+    auto own4 = [&](const float4 *src, int cnt, float4 *&dst) {
+        SM_CUDA(cudaMalloc((void **)&dst, (size_t)std::max(cnt, 1) * sizeof(float4)));
+        if (cnt)
+            SM_CUDA(cudaMemcpyAsync(dst, src, (size_t)cnt * sizeof(float4), cudaMemcpyDeviceToDevice,
+                                    c.stream));
+    };
+    own4(sp, n1, m.sp);
+    own4(sn, n1, m.sn);
+    own4(rp, n2, m.rp);
+    own4(rn, n2, m.rn);
+    build_model_table(c, m, keys, alphas, pv, n1);
+    m.trained   = true;
+    m.hostValid = false;
     m.sdRel = sdRel;
     m.tp    = tp;
 }
@@ -1144,6 +1169,8 @@ SM_API int sm_model_download(sm_model m, float *sxyz, float *snrm, float *rxyz, 
             throw Error(SM_ERR_ARG, "NULL model");
         if (!m->m.trained)
             throw Error(SM_ERR_RUNTIME, "No trained model in save");
+        SM_CUDA(cudaSetDevice(m->m.device));
+        m->m.ensure_host();
         const Model &M = m->m;
         auto cp = [](void *dst, const void *src, size_t b) {
             if (dst && b)
@@ -1179,9 +1206,11 @@ SM_API int sm_model_save(sm_model m, const char *path) {
         std::ofstream f(path, std::ios::out | std::ios::binary);
         if (!f.is_open())
             throw Error(SM_ERR_RUNTIME, std::string("failed to open file:") + path);
-        const Model &M = m->m;
-        if (!M.trained)
+        if (!m->m.trained)
             throw Error(SM_ERR_RUNTIME, "No trained model in save");
+        SM_CUDA(cudaSetDevice(m->m.device));
+        m->m.ensure_host();
+        const Model &M = m->m;
         std::string o;
         put<int>(o, kMagic);
         put<int>(o, kVersion);

@@ -188,11 +188,15 @@ struct Model {
     uint32_t  emptyKeySlot = 0xffffffffu; // bucket of key 0xffffffff if present
     uint32_t *boff  = nullptr;  // bucket offsets (nkeys + 1)
     uint2    *entries = nullptr; // (ref, alpha bits) in bucket order
-    // host copies (download / save)
+    uint32_t *dkeys   = nullptr; // bucket keys, ascending (nkeys)
+    uint32_t *doffs   = nullptr; // bucket offsets (nkeys + 1)
+    // host copies for download / save, fetched from the device on first use after a train
+    bool                  hostValid = false;
     std::vector<float>    h_sp, h_sn, h_rp, h_rn;
     std::vector<uint32_t> h_keys, h_offs, h_refs;
     std::vector<float>    h_alphas;
     void free_device();
+    void ensure_host();
 };
 
 } // namespace sm

@@ -255,6 +255,11 @@ void vote_fused(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, co
 // All ordered model pairs (trainModel's table rows): key and alpha per (i, j).
 void model_pairs(Ctx &c, const float4 *sp, const float4 *sn, int ns, float angleStep,
                  float distStep, uint32_t *keys, float *alphas, int *valid);
+// trainModel's hash table (ppf.cpp:125-143) from the n1 x n1 pair rows: the valid pairs
+// grouped by key, stable in pair order (reference point i, then column j), into the
+// model's device arrays (keys, offsets, entries, open-addressed slot table).
+void build_model_table(Ctx &c, Model &m, const uint32_t *keys, const float *alphas,
+                       const int *valid, int n1);
 
 // ---- cluster.cu -----------------------------------------------------------------------
 // Pose clustering (clusterPose, avgClusters, sortPoses, clusterPose2) of np poses

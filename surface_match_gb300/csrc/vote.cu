@@ -207,7 +207,125 @@ __global__ void k_model_pairs(const float4 *__restrict__ sp, const float4 *__res
     valid[t]  = smm::fisnan(al) ? 0 : 1;
 }
 
+// ---- the model table on the device ----------------------------------------------------
+__global__ void k_pair_compact(const uint32_t *__restrict__ keys, const int *__restrict__ valid,
+                               const int *__restrict__ pre, long long n, uint32_t *__restrict__ ck,
+                               uint32_t *__restrict__ cv) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n || !valid[t])
+        return;
+    ck[pre[t]] = keys[t];
+    cv[pre[t]] = (uint32_t)t;
+}
+
+__global__ void k_bucket_heads(const uint32_t *__restrict__ ck, int e, int *__restrict__ head) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > e)
+        return;
+    head[i] = (i < e && (i == 0 || ck[i] != ck[i - 1])) ? 1 : 0;
+}
+
+// Entry e of the sorted pairs: bucket key and offset at a bucket's first entry, and the
+// (reference point, alpha bits) record.
+__global__ void k_bucket_fill(const uint32_t *__restrict__ ck, const uint32_t *__restrict__ cv,
+                              int e, const int *__restrict__ head, const int *__restrict__ bidx,
+                              const float *__restrict__ alphas, int n1, uint32_t *__restrict__ dkeys,
+                              uint32_t *__restrict__ doffs, uint2 *__restrict__ ent, int nkeys) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= e) {
+        if (i == e)
+            doffs[nkeys] = (uint32_t)e;
+        return;
+    }
+    if (head[i]) {
+        dkeys[bidx[i]] = ck[i];
+        doffs[bidx[i]] = (uint32_t)i;
+    }
+    const uint32_t t = cv[i];
+    ent[i]           = make_uint2(t / (uint32_t)n1, __float_as_uint(alphas[t]));
+}
+
+// Bucket b into the open-addressed table (linear probing from key & mask; slots are claimed
+// by compare-and-swap, so placement depends on timing but every key sits after an unbroken
+// run of occupied slots from its home slot, which is all a probe needs). The slot's last
+// word is the bucket's largest number of entries of one reference point: entries are in
+// pair order, so a reference point's entries are consecutive.
+__global__ void k_bucket_insert(const uint32_t *__restrict__ dkeys, const uint32_t *__restrict__ doffs,
+                                const uint2 *__restrict__ ent, int nkeys, uint32_t mask,
+                                int *__restrict__ claim, uint4 *__restrict__ tab) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nkeys)
+        return;
+    const uint32_t k = dkeys[b], o0 = doffs[b], o1 = doffs[b + 1];
+    uint32_t       best = 0, run = 0, prev = 0xffffffffu;
+    for (uint32_t e = o0; e < o1; e++) {
+        const uint32_t r = ent[e].x;
+        run              = r == prev ? run + 1 : 1;
+        prev             = r;
+        best             = run > best ? run : best;
+    }
+    uint32_t i = k & mask;
+    for (uint32_t n = 0; n <= mask; n++) {
+        if (atomicCAS(&claim[i], -1, b) == -1) {
+            tab[i] = make_uint4(k, o0, o1 - o0, best);
+            return;
+        }
+        i = (i + 1) & mask;
+    }
+}
+
 } // namespace
+
+void build_model_table(Ctx &c, Model &m, const uint32_t *keys, const float *alphas,
+                       const int *valid, int n1) {
+    const long long npair = (long long)n1 * n1;
+    int *pre = c.arena.get<int>("t.tab.pre", (size_t)npair + 1);
+    int  E   = 0;
+    if (npair > 0) {
+        // valid flags of npair entries, exclusive scan with the total (pre[npair])
+        scan_excl(c, valid, pre, npair, "t.tab.s1", false);
+        SM_CUDA(cudaMemcpyAsync(c.hostCounts, pre + npair - 1, sizeof(int), cudaMemcpyDeviceToHost,
+                                c.stream));
+        SM_CUDA(cudaMemcpyAsync(c.hostCounts + 1, valid + npair - 1, sizeof(int),
+                                cudaMemcpyDeviceToHost, c.stream));
+        c.sync_checked();
+        E = c.hostCounts[0] + c.hostCounts[1];
+    }
+    uint32_t *ck = c.arena.get<uint32_t>("t.tab.ck", std::max(E, 1));
+    uint32_t *cv = c.arena.get<uint32_t>("t.tab.cv", std::max(E, 1));
+    if (E > 0) {
+        k_pair_compact<<<nblocks(npair, 256), 256, 0, c.stream>>>(keys, valid, pre, npair, ck, cv);
+        SM_LAUNCH_CHECK();
+        radix_sort_pairs(c, ck, cv, E, 32, "t.tab");
+    }
+    int *head = c.arena.get<int>("t.tab.head", (size_t)E + 1);
+    int *bidx = c.arena.get<int>("t.tab.bidx", (size_t)E + 1);
+    k_bucket_heads<<<nblocks((long long)E + 1, 256), 256, 0, c.stream>>>(ck, E, head);
+    SM_LAUNCH_CHECK();
+    const int nkeys = scan_excl(c, head, bidx, (long long)E + 1, "t.tab.s2", true);
+    m.nkeys    = nkeys;
+    m.nentries = E;
+    SM_CUDA(cudaMalloc((void **)&m.dkeys, (size_t)std::max(nkeys, 1) * 4));
+    SM_CUDA(cudaMalloc((void **)&m.doffs, ((size_t)nkeys + 1) * 4));
+    SM_CUDA(cudaMalloc((void **)&m.entries, (size_t)std::max(E, 1) * sizeof(uint2)));
+    k_bucket_fill<<<nblocks((long long)E + 1, 256), 256, 0, c.stream>>>(
+        ck, cv, E, head, bidx, alphas, n1, m.dkeys, m.doffs, m.entries, nkeys);
+    SM_LAUNCH_CHECK();
+    uint32_t size = 16;
+    while (size < 2u * (uint32_t)nkeys)
+        size <<= 1;
+    m.hmask    = size - 1;
+    int *claim = c.arena.get<int>("t.tab.claim", size);
+    SM_CUDA(cudaMalloc((void **)&m.hkeys, (size_t)size * sizeof(uint4)));
+    SM_CUDA(cudaMemsetAsync(claim, 0xff, (size_t)size * 4, c.stream));
+    SM_CUDA(cudaMemsetAsync(m.hkeys, 0, (size_t)size * sizeof(uint4), c.stream));
+    if (nkeys > 0) {
+        k_bucket_insert<<<nblocks(nkeys, 128), 128, 0, c.stream>>>(m.dkeys, m.doffs, m.entries, nkeys,
+                                                                  m.hmask, claim, (uint4 *)m.hkeys);
+        SM_LAUNCH_CHECK();
+    }
+    c.sync_checked();
+}
 
 void fill_vote_model(const Model &m, float minScore, VoteArgs &a) {
     a.sp            = m.sp;
