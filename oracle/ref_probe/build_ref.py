@@ -1,7 +1,7 @@
-"""Build recipe for oracle/_ref/ (test infrastructure only): compiles the probe of the
-reference's own k-d tree against the reference's vendored nanoflann, in place, and the
-reference's scalar MurmurHash3 function (util.cpp:643-688) extracted into a temporary
-file. Needs the reference source tree; outputs only into oracle/_ref/."""
+"""Build recipe for oracle/_ref/ (test infrastructure only): compiles, from the reference's
+source tree in place, a probe of its k-d tree against its vendored nanoflann, its scalar
+MurmurHash3 function (util.cpp:643-688, extracted into a temporary file) and its vendored
+rply PLY reader with a probe. Outputs only into oracle/_ref/."""
 from __future__ import annotations
 
 import os
@@ -28,6 +28,20 @@ def build_kd() -> str:
         return so
     subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
                     "-I", os.path.join(REF, "kdtree"), "-o", so, src], check=True)
+    return so
+
+
+def build_ply() -> str:
+    """Compile the reference's vendored rply (third_party/rply/rply/rply.c) with a probe that
+    reads PLY files through it the way the reference's readPLY does."""
+    os.makedirs(OUT, exist_ok=True)
+    so = os.path.join(OUT, "libply_ref_probe.so")
+    src = os.path.join(HERE, "ply_ref_probe.c")
+    rply = os.path.join(REF, "third_party", "rply", "rply")
+    if os.path.exists(so) and os.path.getmtime(so) >= os.path.getmtime(src):
+        return so
+    subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-I", rply, "-o", so, src,
+                    os.path.join(rply, "rply.c")], check=True)
     return so
 
 

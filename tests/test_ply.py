@@ -115,44 +115,48 @@ def test_round_trips_between_the_writers_and_readers(tool, tmp_path, ascii_, nor
         same(Pc, P), same(Nc, N), same(Fc, F)
 
 
+FOREIGN_P = np.array([[0, 0, 0], [2, 0, 0], [2, 2, 0], [0, 2, 0], [1, 1, 0],
+                      [3, 0, 1], [5, 0, 1], [5, 3, 1], [4, 1, 1], [3, 3, 1]], np.float32)
+FOREIGN_POLYS = [[0, 1, 2, 3], [1, 2, 4], [5, 6, 7, 8, 9]]
+
+
+def write_foreign(tmp_path, fmt):
+    """A hand-made file: extra vertex properties (colours, a double intensity, a list), an
+    extra element before the vertices, quads and a concave pentagon."""
+    P, polys = FOREIGN_P, FOREIGN_POLYS
+    h = ["ply", f"format {fmt} 1.0", "comment made by hand", "element camera 1",
+         "property float fx", "element vertex 10", "property uchar red", "property float x",
+         "property float y", "property double intensity", "property float z",
+         "property list uchar int tags", "property uchar green", "element face 3",
+         "property list uchar uint vertex_indices", "end_header"]
+    path = tmp_path / f"{fmt}.ply"
+    with open(path, "wb") as f:
+        f.write(("\n".join(h) + "\n").encode())
+        if fmt == "ascii":
+            f.write(b"500.5\n")
+            for i, p in enumerate(P):
+                f.write(f"7 {p[0]} {p[1]} 0.25 {p[2]} 2 {i} {i + 1} 9\n".encode())
+            for poly in polys:
+                f.write((f"{len(poly)} " + " ".join(map(str, poly)) + "\n").encode())
+        else:
+            e = "<" if fmt == "binary_little_endian" else ">"
+            f.write(struct.pack(e + "f", 500.5))
+            for i, p in enumerate(P):
+                f.write(struct.pack(e + "Bffdf", 7, p[0], p[1], 0.25, p[2]))
+                f.write(struct.pack(e + "Bii", 2, i, i + 1) + struct.pack(e + "B", 9))
+            for poly in polys:
+                f.write(struct.pack(e + "B" + "I" * len(poly), len(poly), *poly))
+    return path
+
+
 def test_foreign_layouts_polygons_and_byte_orders(tool, tmp_path):
     """Extra vertex properties (colours, a double intensity, a list), an extra element,
     quads and a concave pentagon cut into triangles; big-endian binary reads like ASCII."""
     from surface_match_gb300.ply import read_ply
-    P = np.array([[0, 0, 0], [2, 0, 0], [2, 2, 0], [0, 2, 0], [1, 1, 0],
-                  [3, 0, 1], [5, 0, 1], [5, 3, 1], [4, 1, 1], [3, 3, 1]], np.float32)
-    polys = [[0, 1, 2, 3], [1, 2, 4], [5, 6, 7, 8, 9]]
-    head = ["ply", None, "comment made by hand", "element camera 1", "property float fx",
-            "element vertex 10", "property uchar red", "property float x", "property float y",
-            "property double intensity", "property float z", "property list uchar int tags",
-            "property uchar green", "element face 3", "property list uchar uint vertex_indices",
-            "end_header"]
-
-    def write(fmt):
-        h = list(head)
-        h[1] = f"format {fmt} 1.0"
-        path = tmp_path / f"{fmt}.ply"
-        with open(path, "wb") as f:
-            f.write(("\n".join(h) + "\n").encode())
-            if fmt == "ascii":
-                f.write(b"500.5\n")
-                for i, p in enumerate(P):
-                    f.write(f"7 {p[0]} {p[1]} 0.25 {p[2]} 2 {i} {i + 1} 9\n".encode())
-                for poly in polys:
-                    f.write((f"{len(poly)} " + " ".join(map(str, poly)) + "\n").encode())
-            else:
-                e = "<" if fmt == "binary_little_endian" else ">"
-                f.write(struct.pack(e + "f", 500.5))
-                for i, p in enumerate(P):
-                    f.write(struct.pack(e + "Bffdf", 7, p[0], p[1], 0.25, p[2]))
-                    f.write(struct.pack(e + "Bii", 2, i, i + 1) + struct.pack(e + "B", 9))
-                for poly in polys:
-                    f.write(struct.pack(e + "B" + "I" * len(poly), len(poly), *poly))
-        return path
-
+    P = FOREIGN_P
     ref = None
     for fmt in ("ascii", "binary_little_endian", "binary_big_endian"):
-        path = write(fmt)
+        path = write_foreign(tmp_path, fmt)
         r = read_ply(path)
         same(r.point, P)
         assert r.normal is None
@@ -179,3 +183,73 @@ def test_failures_like_the_reference(tool, tmp_path):
         read_ply(bad)
     r, out = cpp_read(tool, bad, tmp_path)
     assert r is None and "number of vertex <= 0" in out
+
+
+def _ref_ply():
+    """The reference's own PLY reader (its vendored rply, compiled in place by the oracle's
+    recipe) or None where its source is absent."""
+    import ctypes as C
+    import sys
+    from conftest import reference_dir
+    if reference_dir() is None:
+        return None
+    sys.path.insert(0, os.path.join(ROOT, "oracle", "ref_probe"))
+    try:
+        import build_ref
+        L = C.CDLL(build_ref.build_ply())
+    finally:
+        sys.path.pop(0)
+    L.ref_ply_counts.argtypes = [C.c_char_p, C.POINTER(C.c_long)]
+    L.ref_ply_read.argtypes = [C.c_char_p] + [C.c_void_p] * 4
+    return L
+
+
+def ref_read(L, path):
+    import ctypes as C
+    cnt = (C.c_long * 4)()
+    assert L.ref_ply_counts(str(path).encode(), cnt) == 0
+    nv, nn, nf, ni = (int(v) for v in cnt)
+    P = np.zeros((nv, 3), np.float32)
+    N = np.zeros((nn, 3), np.float32)
+    ln = np.zeros(max(nf, 1), np.int32)
+    ix = np.zeros(max(ni, 1), np.int32)
+    assert L.ref_ply_read(str(path).encode(), P.ctypes.data, N.ctypes.data, ln.ctypes.data,
+                          ix.ctypes.data) == 0
+    polys, o = [], 0
+    for k in ln[:nf]:
+        polys.append(ix[o:o + k].tolist())
+        o += k
+    return P, (N if nn else None), polys
+
+
+def test_readers_match_the_reference_rply(tool, tmp_path):
+    """Both readers against the reference's own rply, read the way its readPLY reads
+    (filePLY.cpp:199-257): identical vertices and normals (doubles stored to floats),
+    triangles as written, and polygons cut into n - 2 triangles of their own corners."""
+    L = _ref_ply()
+    if L is None:
+        pytest.skip("the reference's source tree is not present")
+    from surface_match_gb300 import PointCloud
+    from surface_match_gb300.ply import read_ply, write_ply
+    P, N, F = cloud()
+    files = []
+    for ascii_ in (True, False):
+        for normals in (True, False):
+            path = tmp_path / f"w_{int(ascii_)}_{int(normals)}.ply"
+            write_ply(path, PointCloud(P, N if normals else None, None, F), write_ascii=ascii_)
+            files.append((path, None))
+    for fmt in ("ascii", "binary_little_endian", "binary_big_endian"):
+        files.append((write_foreign(tmp_path, fmt), FOREIGN_POLYS))
+    for path, polys in files:
+        rP, rN, rpolys = ref_read(L, path)
+        r = read_ply(path)
+        (Pc, Nc, Fc), _ = cpp_read(tool, path, tmp_path)
+        for got_P, got_N, got_F in ((r.point, r.normal, r.face), (Pc, Nc, Fc)):
+            same(got_P, rP), same(got_N, rN)
+            if polys is None:
+                same(got_F, np.array(rpolys, np.int32))
+            else:
+                assert rpolys == polys
+                assert len(got_F) == sum(len(q) - 2 for q in rpolys)
+                for t in got_F.tolist():
+                    assert any(set(t) <= set(q) for q in rpolys), t
