@@ -365,6 +365,11 @@ void vote_fused(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, co
     // the same test switch as the pipelined stage: 32-bit counters for every keypoint
     const char *fw = std::getenv("SM_VOTE_FORCE_WIDE");
     a.forceWide    = (fw && fw[0] == '1') ? 1 : 0;
+    // SM_VOTE_FINGERPRINT=1 folds every accumulator into stats column 4 (checked by tests
+    // against the oracle); without it the column is 0 and the peak scan skips the work
+    const char *fp = std::getenv("SM_VOTE_FINGERPRINT");
+    a.fingerprint  = (fp && fp[0] == '1') ? 1 : 0;
+
     int optin = 0, perSM = 0;
     SM_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));
     SM_CUDA(cudaDeviceGetAttribute(&perSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c.device));

@@ -387,6 +387,11 @@ void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const in
     // bound otherwise reserves for extreme inputs, so that tests reach it
     const char *fw = std::getenv("SM_VOTE_FORCE_WIDE");
     a.forceWide    = (fw && fw[0] == '1') ? 1 : 0;
+    // SM_VOTE_FINGERPRINT=1 folds every accumulator into stats column 4 (checked by tests
+    // against the oracle); without it the column is 0 and the peak scan skips the work
+    const char *fp = std::getenv("SM_VOTE_FINGERPRINT");
+    a.fingerprint  = (fp && fp[0] == '1') ? 1 : 0;
+
     const bool csr = nbrOff != nullptr;
 
     int optin = 0, perSM = 0;

@@ -7,6 +7,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
+# The voting stage folds every accumulator into a fingerprint (statistics column 4) only when
+# asked; the tests compare it with the oracle's, so the whole session asks.
+os.environ.setdefault("SM_VOTE_FINGERPRINT", "1")
+
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300); run with -m gpu")
