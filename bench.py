@@ -168,20 +168,22 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def run_batch(args):
-    """Batched vs plain GPU matching of the batching workload (wall-clock around the
-    synchronous calls; scenes resident in HBM for `value`, pinned host buffers for e2e)."""
-    import numpy as np
+def measure_batch(n_scenes, steps, warmup, sd=0.04, kp=0.2):
+    """The batching workload (64 seeded scenes of 50k-2M points, 1-12 instances of a gear,
+    an L-bracket or a torus each): matchScene of every scene through sm_match_batch
+    (concurrency picked by measurement among 2/4/8/12/16/24) against the same scenes one by one
+    through sm_match. Wall clock around the synchronous calls; scenes resident in HBM for
+    `value`, pinned host buffers (copies inside the call) for `e2e`."""
     import torch
     from surface_match_gb300 import Detector, MatchParam, PointCloud, match_batch, synth
     models = synth.batch_models()
     dets = {}
     for name, (cloud, _, _) in models.items():
         d = Detector()
-        d.trainModel(PointCloud(cloud.xyz, cloud.normal), SD)
+        d.trainModel(PointCloud(cloud.xyz, cloud.normal), sd)
         dets[name] = d
     t = time.time()
-    scenes = synth.batch_scenes(args.batch_scenes, models=models)
+    scenes = synth.batch_scenes(n_scenes, models=models)
     gen_s = time.time() - t
     param = MatchParam(numMatches=NUM_MATCHES)
     dev = [(dets[nm], PointCloud(torch.from_numpy(sc.cloud.xyz).cuda(), None, sc.viewpoint))
@@ -194,46 +196,56 @@ def run_batch(args):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for d, pc in jobs:
-            d.matchScene(pc, SD, KP, MS, param)
+            d.matchScene(pc, sd, kp, MS, param)
         return time.perf_counter() - t0
 
     def batched(jobs, conc):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        out, st = match_batch(jobs, SD, KP, MS, param, concurrency=conc)
+        out, st = match_batch(jobs, sd, kp, MS, param, concurrency=conc)
         return time.perf_counter() - t0, st
 
-    for _ in range(max(1, args.warmup)):
-        match_batch(dev, SD, KP, MS, param, concurrency=4)
+    for _ in range(max(1, warmup)):
+        match_batch(dev, sd, kp, MS, param, concurrency=4)
     plain(dev[:4])
     tune = {}
-    for conc in (2, 4, 8, 12):  # concurrency picked by measurement
+    for conc in (2, 4, 8, 12, 16, 24):  # concurrency picked by measurement
         tune[conc] = batched(dev, conc)[0]
     best = min(tune, key=tune.get)
     times, votes = [], 0
-    for _ in range(args.steps):
+    for _ in range(steps):
         dt, st = batched(dev, best)
         times.append(dt)
         votes = sum(x["n_votes"] for x in st)
-    e2e_times = [batched(host, best)[0] for _ in range(max(1, args.steps // 2))]
-    t_plain = [plain(dev) for _ in range(max(1, args.steps // 2))]
+    e2e_times = [batched(host, best)[0] for _ in range(max(1, steps // 2))]
+    t_plain = [plain(dev) for _ in range(max(1, steps // 2))]
     n = len(scenes)
-    v = n / statistics.median(times)
-    line = {"metric": METRIC, "value": v, "unit": "scenes/s", "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000 * statistics.median(times),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded procedural gear / L-bracket / torus scenes)",
-            "config": {"workload": WORKLOADS["batch"][3], "scenes": n,
-                       "total_points": int(total_pts), "generation_s": round(gen_s, 1),
-                       "timing": "wall clock around the synchronous batch call",
-                       "concurrency": best,
-                       "concurrency_sweep_ms": {str(k): round(1000 * x, 2) for k, x in tune.items()}},
+    return {"workload": WORKLOADS["batch"][3], "scenes": n, "total_points": int(total_pts),
+            "generation_s": round(gen_s, 1), "steps": steps,
+            "timing": "wall clock around the synchronous batch call (median of steps)",
+            "value": n / statistics.median(times), "unit": "scenes/s",
+            "ms_per_batch": 1000 * statistics.median(times),
             "plain_value": n / statistics.median(t_plain),
             "batched_over_plain": statistics.median(t_plain) / statistics.median(times),
             "votes_per_s": votes / statistics.median(times),
+            "concurrency": best,
+            "concurrency_sweep_ms": {str(k): round(1000 * x, 2) for k, x in tune.items()},
             "e2e": {"value": n / statistics.median(e2e_times), "unit": "scenes/s",
                     "h2d_bytes_per_step": int(total_pts * 12),
                     "d2h_bytes_per_step": int(n * NUM_MATCHES * 68)}}
+
+
+def run_batch(args):
+    """The batching workload as the headline line."""
+    b = measure_batch(args.batch_scenes, args.steps, args.warmup, SD, KP)
+    line = {"metric": METRIC, "value": b["value"], "unit": "scenes/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": b["ms_per_batch"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded procedural gear / L-bracket / torus scenes)",
+            "config": {k: b[k] for k in ("workload", "scenes", "total_points", "generation_s",
+                                         "timing", "concurrency", "concurrency_sweep_ms")},
+            "plain_value": b["plain_value"], "batched_over_plain": b["batched_over_plain"],
+            "votes_per_s": b["votes_per_s"], "e2e": b["e2e"]}
     print(json.dumps(line), flush=True)
 
 
@@ -649,6 +661,8 @@ def main():
                         "results bit-identical to the reference-order restatement (see "
                         "reference_order_parity); grid: the same rules in uniform-grid "
                         "orders (faster, another sample)"}}
+    if rank == 0 and args.batch_scenes > 0:
+        line["batched"] = measure_batch(args.batch_scenes, max(2, min(args.steps, 4)), 1)
     if rank == 0 and not args.no_cpu_baseline:
         dt, r = cpu_match(model.xyz, model.normal, scene, args.cpu_threads, reps=3)
         line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "scenes/s",
