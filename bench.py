@@ -235,6 +235,21 @@ def measure_batch(n_scenes, steps, warmup, sd=0.04, kp=0.2):
                     "d2h_bytes_per_step": int(n * NUM_MATCHES * 68)}}
 
 
+def run_profile(args):
+    """warmup + steps matchScene calls of the workload scene (scene resident in HBM) in the
+    chosen search order, nothing else: the command that profiler captures run."""
+    import torch
+    from surface_match_gb300 import Detector, MatchParam, PointCloud
+    model, scene = workload()
+    det = Detector(search_order=args.search_order)
+    det.trainModel(PointCloud(model.xyz, model.normal), SD)
+    xyz = torch.from_numpy(scene.cloud.xyz).cuda()
+    for _ in range(args.warmup + args.steps):
+        det.matchScene(PointCloud(xyz, None, scene.viewpoint), SD, KP, MS,
+                       MatchParam(numMatches=NUM_MATCHES))
+    torch.cuda.synchronize()
+
+
 def run_batch(args):
     """The batching workload as the headline line."""
     b = measure_batch(args.batch_scenes, args.steps, args.warmup, SD, KP)
@@ -438,6 +453,9 @@ def main():
     ap.add_argument("--cpu-threads", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS))
+    ap.add_argument("--profile", action="store_true",
+                    help="only run warmup + steps matchScene calls of the workload in the given "
+                         "search order (for profiler captures); prints no result line")
     ap.add_argument("--search-order", default="grid", choices=["grid", "reference"],
                     help="search order of the headline measurement; the other order is "
                          "measured beside it")
@@ -468,6 +486,8 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.profile:
+        return run_profile(args)
 
     import numpy as np
     import torch
