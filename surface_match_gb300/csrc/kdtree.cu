@@ -556,6 +556,7 @@ struct SampleArgs {
     const int      *cellList; // occupied rank -> dense cell
     const int      *cellBeg;  // occupied rank -> its run [beg, end) of the entries
     const int      *cellEnd;
+    int            *open;     // occupied rank -> its points not yet decided
     int            *cnt;      // per entry: earlier points within the step not yet decided
     int            *dec;      // per entry: 0 open, 1 kept, 2 dropped
     int            *queue;    // entries in the order they were decided (-1: not written)
@@ -629,7 +630,7 @@ __global__ void k_sp_cells(const uint32_t *__restrict__ key, int m, const int *_
                            const int *__restrict__ rank, int *__restrict__ cellRank,
                            int *__restrict__ cellList, int *__restrict__ cellBeg,
                            int *__restrict__ cellEnd, int *__restrict__ cellOf,
-                           int *__restrict__ nact) {
+                           int *__restrict__ open, int *__restrict__ nact) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= m)
         return;
@@ -639,6 +640,7 @@ __global__ void k_sp_cells(const uint32_t *__restrict__ key, int m, const int *_
     }
     const int r = rank[k] + head[k] - 1; // the run's occupied rank
     cellOf[k]   = r;
+    atomicAdd(&open[r], 1);
     if (head[k]) {
         cellRank[key[k]] = r;
         cellList[r]      = (int)key[k];
@@ -669,7 +671,10 @@ __global__ void k_sp_entries(const uint32_t *__restrict__ sortPos, int m, KdView
 
 // The 27 cells around a cell: lane l < 27 gets the first entry of neighbour l's run; returns
 // the lane's exclusive prefix of the runs' lengths and writes their total to tot.
-__device__ __forceinline__ int nb_runs(const SampleArgs &a, int cid, int &nb, int &tot) {
+// With onlyOpen, cells whose points are all decided count as empty: a decided point needs
+// nothing from its neighbours any more.
+__device__ __forceinline__ int nb_runs(const SampleArgs &a, int cid, int &nb, int &tot,
+                                       bool onlyOpen) {
     const int lane = threadIdx.x & 31;
     const int cx = cid % a.dim[0], cy = (cid / a.dim[0]) % a.dim[1], cz = cid / (a.dim[0] * a.dim[1]);
     nb      = 0;
@@ -678,7 +683,7 @@ __device__ __forceinline__ int nb_runs(const SampleArgs &a, int cid, int &nb, in
         const int x = cx + lane % 3 - 1, y = cy + (lane / 3) % 3 - 1, z = cz + lane / 9 - 1;
         if (x >= 0 && y >= 0 && z >= 0 && x < a.dim[0] && y < a.dim[1] && z < a.dim[2]) {
             const int nr = a.cellRank[(z * a.dim[1] + y) * a.dim[0] + x];
-            if (nr >= 0) {
+            if (nr >= 0 && !(onlyOpen && ld_vol(&a.open[nr]) == 0)) {
                 nb  = a.cellBeg[nr];
                 len = a.cellEnd[nr] - nb;
             }
@@ -714,7 +719,7 @@ __global__ void __launch_bounds__(kSpBs) k_sp_count(SampleArgs a) {
         const float4 p  = a.ent[k];
         const int    ip = __float_as_int(p.w);
         int          nb, tot;
-        const int    excl = nb_runs(a, a.cellList[a.cellOf[k]], nb, tot);
+        const int    excl = nb_runs(a, a.cellList[a.cellOf[k]], nb, tot, false);
         int          cnt  = 0;
         for (int base = 0; base < tot; base += 32 * kSpUnroll) {
             int    kb[kSpUnroll];
@@ -738,6 +743,7 @@ __global__ void __launch_bounds__(kSpBs) k_sp_count(SampleArgs a) {
             if (cnt == 0) {
                 a.dec[k]                      = 1;
                 a.queue[atomicAdd(a.tail, 1)] = k;
+                atomicSub(&a.open[a.cellOf[k]], 1);
             }
         }
     }
@@ -746,6 +752,7 @@ __global__ void __launch_bounds__(kSpBs) k_sp_count(SampleArgs a) {
 // Decide entry p (open -> fate) and queue it, unless it is decided already.
 __device__ __forceinline__ void sp_push(const SampleArgs &a, int p, int fate) {
     if (atomicCAS(&a.dec[p], 0, fate) == 0) {
+        atomicSub(&a.open[a.cellOf[p]], 1);
         const int slot = atomicAdd(a.tail, 1);
         __threadfence();
         atomicExch(&a.queue[slot], p);
@@ -790,7 +797,9 @@ __global__ void __launch_bounds__(kSpBs) k_sp_run(SampleArgs a) {
         if (fate == 1 && lane == 0)
             a.keptFlag[iq] = 1;
         int         nb, tot;
-        const int   excl  = nb_runs(a, a.cellList[a.cellOf[b]], nb, tot);
+        // only neighbour cells that still hold an undecided point: after a kept point's
+        // wave of drops most cells around a dropped point are settled
+        const int   excl  = nb_runs(a, a.cellList[a.cellOf[b]], nb, tot, true);
         const float qq[3] = {q.x, q.y, q.z};
         for (int base = 0; base < tot; base += 32 * kSpUnroll) {
             int    kp[kSpUnroll];
@@ -1170,6 +1179,7 @@ int kd_sample(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos,
     float4 *ent      = c.arena.get<float4>(tag + ".ent", m);
     float  *ex       = c.arena.get<float>(tag + ".ex", m);
     int    *cnt      = c.arena.get<int>(tag + ".cnt", m);
+    int    *open     = c.arena.get<int>(tag + ".open", std::max(ncells, 1));
     int    *dec      = c.arena.get<int>(tag + ".dec", m);
     int    *queue    = c.arena.get<int>(tag + ".q", m);
     int    *flag     = c.arena.get<int>(tag + ".flag", (size_t)m + 1);
@@ -1178,9 +1188,10 @@ int kd_sample(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos,
     SM_CUDA(cudaMemsetAsync(flag, 0, ((size_t)m + 1) * 4, c.stream));
     SM_CUDA(cudaMemsetAsync(ctl, 0, 4 * sizeof(int), c.stream));
     SM_CUDA(cudaMemsetAsync(dec, 0, (size_t)m * 4, c.stream));
+    SM_CUDA(cudaMemsetAsync(open, 0, (size_t)std::max(ncells, 1) * 4, c.stream));
     SM_CUDA(cudaMemsetAsync(queue, 0xff, (size_t)m * 4, c.stream));
     k_sp_cells<<<nblocks(m, 256), 256, 0, c.stream>>>(key, m, head, rank, cRank, cellList, cellBeg,
-                                                     cellEnd, cellOf, ctl + 2);
+                                                     cellEnd, cellOf, open, ctl + 2);
     SM_LAUNCH_CHECK();
     k_sp_entries<<<nblocks(m, 256), 256, 0, c.stream>>>(val, m, T.view(vaccA, pos), T.box,
                                                         T.leafOf, ent, ex);
@@ -1200,6 +1211,7 @@ int kd_sample(Ctx &c, const KdTree &T, const int *vaccActive, const float4 *pos,
     a.cellBeg  = cellBeg;
     a.cellEnd  = cellEnd;
     a.cnt      = cnt;
+    a.open     = open;
     a.dec      = dec;
     a.queue    = queue;
     a.head     = ctl;
