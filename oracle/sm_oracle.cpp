@@ -231,47 +231,83 @@ struct Grid {
     }
 };
 
-// 8-phase grid greedy thinning over `sub` (any order); returns kept ids ascending.
+// 8-phase grid greedy thinning over `sub` (any order); returns kept ids ascending. Cells of
+// side smg::thin_cell are held sparse (only occupied cells), as the GPU's hashed grid: a
+// point is kept unless a kept point of its 3x3x3 cell block lies within the step, visiting
+// phase by phase, cell by cell (cells of one phase do not interact) and by ascending index.
 std::vector<int> grid_sample(const std::vector<V3> &P, const std::vector<int> &sub,
                              const Box &box, float step) {
-    float ext[3] = {box.mx.x - box.mn.x, box.mx.y - box.mn.y, box.mx.z - box.mn.z};
-    Grid  G;
-    G.build(P, sub, box, smg::sample_cell(step, ext));
-    const float        r2 = step * step;
-    std::vector<char>  kept(P.size(), 0);
-    std::vector<std::vector<int>> keptIn(G.start.size() - 1);
+    if (!(step > 0.0f)) { // nothing lies at a squared distance below zero: all kept
+        std::vector<int> out(sub);
+        std::sort(out.begin(), out.end());
+        return out;
+    }
+    float       ext[3] = {box.mx.x - box.mn.x, box.mx.y - box.mn.y, box.mx.z - box.mn.z};
+    const float g      = smg::thin_cell(step, ext);
+    int         dim[3];
+    for (int a = 0; a < 3; a++)
+        dim[a] = smg::dim_of(ext[a], g);
+    auto key_of = [&](int x, int y, int z) {
+        return ((uint64_t)z * (uint64_t)dim[1] + (uint64_t)y) * (uint64_t)dim[0] + (uint64_t)x;
+    };
+    // points by (cell key, id)
+    std::vector<std::pair<uint64_t, int>> pk(sub.size());
+    for (size_t i = 0; i < sub.size(); i++) {
+        const V3 &p = P[sub[i]];
+        pk[i]       = {key_of(smg::coord(p.x, box.mn.x, g, dim[0]), smg::coord(p.y, box.mn.y, g, dim[1]),
+                        smg::coord(p.z, box.mn.z, g, dim[2])),
+                 sub[i]};
+    }
+    std::sort(pk.begin(), pk.end());
+    std::vector<uint64_t>            cellKey;
+    std::vector<std::pair<int, int>> range;
+    std::unordered_map<uint64_t, int> cellOf;
+    for (size_t i = 0; i < pk.size();) {
+        size_t j = i;
+        while (j < pk.size() && pk[j].first == pk[i].first)
+            j++;
+        cellOf[pk[i].first] = (int)range.size();
+        range.push_back({(int)i, (int)j});
+        cellKey.push_back(pk[i].first);
+        i = j;
+    }
+    const float                   r2 = step * step;
+    std::vector<char>             kept(P.size(), 0);
+    std::vector<std::vector<int>> keptIn(range.size());
+    const uint64_t                xy = (uint64_t)dim[0] * (uint64_t)dim[1];
     for (int phase = 0; phase < 8; phase++) {
-        for (int z = 0; z < G.dim[2]; z++)
-            for (int y = 0; y < G.dim[1]; y++)
-                for (int x = 0; x < G.dim[0]; x++) {
-                    if (smg::phase_of(x, y, z) != phase) continue;
-                    int cell = (z * G.dim[1] + y) * G.dim[0] + x;
-                    for (int k = G.start[cell]; k < G.start[cell + 1]; k++) {
-                        int       id = G.ids[k];
-                        const V3 &q  = P[id];
-                        bool      ok = true;
-                        for (int dz = -1; dz <= 1 && ok; dz++)
-                            for (int dy = -1; dy <= 1 && ok; dy++)
-                                for (int dx = -1; dx <= 1 && ok; dx++) {
-                                    int xx = x + dx, yy = y + dy, zz = z + dz;
-                                    if (xx < 0 || yy < 0 || zz < 0 || xx >= G.dim[0] ||
-                                        yy >= G.dim[1] || zz >= G.dim[2])
-                                        continue;
-                                    int nc = (zz * G.dim[1] + yy) * G.dim[0] + xx;
-                                    for (int o : keptIn[nc]) {
-                                        const V3 &p = P[o];
-                                        if (smm::dist2(p.x, p.y, p.z, q.x, q.y, q.z) < r2) {
-                                            ok = false;
-                                            break;
-                                        }
-                                    }
+        for (size_t ci = 0; ci < range.size(); ci++) {
+            const uint64_t key = cellKey[ci];
+            const int      x = (int)(key % (uint64_t)dim[0]), y = (int)((key / (uint64_t)dim[0]) % (uint64_t)dim[1]);
+            const int      z = (int)(key / xy);
+            if (smg::phase_of(x, y, z) != phase) continue;
+            for (int k = range[ci].first; k < range[ci].second; k++) {
+                const int id = pk[k].second;
+                const V3 &q  = P[id];
+                bool      ok = true;
+                for (int dz = -1; dz <= 1 && ok; dz++)
+                    for (int dy = -1; dy <= 1 && ok; dy++)
+                        for (int dx = -1; dx <= 1 && ok; dx++) {
+                            const int xx = x + dx, yy = y + dy, zz = z + dz;
+                            if (xx < 0 || yy < 0 || zz < 0 || xx >= dim[0] || yy >= dim[1] ||
+                                zz >= dim[2])
+                                continue;
+                            const auto it = cellOf.find(key_of(xx, yy, zz));
+                            if (it == cellOf.end()) continue;
+                            for (int o : keptIn[it->second]) {
+                                const V3 &p = P[o];
+                                if (smm::dist2(p.x, p.y, p.z, q.x, q.y, q.z) < r2) {
+                                    ok = false;
+                                    break;
                                 }
-                        if (ok) {
-                            kept[id] = 1;
-                            keptIn[cell].push_back(id);
+                            }
                         }
-                    }
+                if (ok) {
+                    kept[id] = 1;
+                    keptIn[ci].push_back(id);
                 }
+            }
+        }
     }
     std::vector<int> out;
     for (int id : sub)

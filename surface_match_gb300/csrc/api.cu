@@ -695,7 +695,9 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
     if (overlap) {
         waiter.h = nullptr;
         c.helper->wait(); // rethrows the preparation's error
-    } else {
+    } else if (ncand > 0) {
+        // in place: only when a cluster is left to refine (nothing reads the refinement
+        // scene otherwise; the resampled count then reads 0)
         prepare_dense(c);
     }
     record(c, 6);

@@ -4,6 +4,7 @@
 // Reference counterparts: removeNan / computeBoundingBox (util.cpp:86-105, 178-207), the
 // k-d tree (kdtree/kdtree.h) replaced by uniform grids, samplePointCloud (util.cpp:107-139),
 // estimateNormal / computeNormal (util.cpp:234-334), normalizeNormal (util.cpp:163-176).
+#include <atomic>
 #include <climits>
 #include <cmath>
 
@@ -234,27 +235,79 @@ __global__ void k_scatter_flags(const int *__restrict__ flags, const int *__rest
 }
 
 // ---------------------------------------------------------------------------------------
-// Dense sampler grid, counting pass: the point's cell and its slot within the cell; the
-// point that opens a cell also counts the cell in its phase (ph[0..7]).
-__global__ void k_grid_count(const float4 *__restrict__ pos, const int *__restrict__ ids, int m,
-                             GridParams gp, int *__restrict__ cellOf, int *__restrict__ sub,
-                             int *__restrict__ cnt, int *__restrict__ ph) {
+constexpr int kSpHeavy = 128; // sampler cells with more points are taken by a whole CTA
+
+// The sampler's cells keep their side just above the step whatever the scene's extent
+// (the work per point is then bounded by the packing of kept points, not by how coarse a
+// capped grid would have to be). Their table is dense (slot = cell key) when the cell box is
+// small against the points (see sample_points), else hashed: keys[slot] holds the cell key
+// (open addressing, ~0 = empty), so only occupied cells are stored. A cell's points are
+// contiguous in pts from start[slot] (an empty dense slot has start[slot + 1] == start[slot]);
+// rankCnt[slot] = {the cell's kept-point record (its place in the phase lists), kept count},
+// written for occupied cells only.
+struct ThinView {
+    float                     org[3];
+    float                     g;
+    int                       dim[3];
+    const unsigned long long *keys; // nullptr: dense table
+    uint32_t                  mask;
+    const int                *start; // table slots + 1
+    const float4             *pts;
+    // the table slot of the cell with key `key`, -1 when the cell holds no point
+    __device__ __forceinline__ int find(unsigned long long key) const {
+        if (!keys)
+            return start[key + 1] > start[key] ? (int)key : -1;
+        uint32_t h = (uint32_t)smm::mix64(key) & mask;
+        for (uint32_t p = 0; p <= mask; p++) {
+            const unsigned long long k = keys[h];
+            if (k == key)
+                return (int)h;
+            if (k == ~0ull)
+                return -1;
+            h = (h + 1) & mask;
+        }
+        return -1;
+    }
+};
+
+__device__ __forceinline__ unsigned long long cell_key(int x, int y, int z, int dim0, int dim1) {
+    return ((unsigned long long)z * (unsigned)dim1 + (unsigned)y) * (unsigned)dim0 + (unsigned)x;
+}
+
+// Counting pass: the point's cell enters the table (slotOf) and the point takes its place
+// within the cell (sub); the point that opens a cell also counts the cell in its phase
+// (ph[0..7]). A hashed table has at least twice as many slots as points, so every cell
+// finds one; a dense one (keys == nullptr) files the cell under its key.
+__global__ void k_thin_insert(const float4 *__restrict__ pos, const int *__restrict__ ids, int m,
+                              GridParams gp, unsigned long long *__restrict__ keys, uint32_t mask,
+                              int *__restrict__ slotOf, int *__restrict__ sub,
+                              int *__restrict__ cnt, int *__restrict__ ph) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m)
         return;
-    const float4 p  = pos[ids[i]];
-    const int    cx = smg::coord(p.x, gp.org[0], gp.g, gp.dim[0]);
-    const int    cy = smg::coord(p.y, gp.org[1], gp.g, gp.dim[1]);
-    const int    cz = smg::coord(p.z, gp.org[2], gp.g, gp.dim[2]);
-    const int    c  = (cz * gp.dim[1] + cy) * gp.dim[0] + cx;
-    cellOf[i]       = c;
-    const int k     = atomicAdd(&cnt[c], 1);
-    sub[i]          = k;
-    if (k == 0)
-        atomicAdd(&ph[smg::phase_of(cx, cy, cz)], 1);
+    const float4             p   = pos[ids[i]];
+    const int                cx  = smg::coord(p.x, gp.org[0], gp.g, gp.dim[0]);
+    const int                cy  = smg::coord(p.y, gp.org[1], gp.g, gp.dim[1]);
+    const int                cz  = smg::coord(p.z, gp.org[2], gp.g, gp.dim[2]);
+    const unsigned long long key = cell_key(cx, cy, cz, gp.dim[0], gp.dim[1]);
+    uint32_t                 h   = keys ? (uint32_t)smm::mix64(key) & mask : (uint32_t)key;
+    for (uint32_t q = 0; q <= mask; q++) {
+        const unsigned long long prev = keys ? atomicCAS(&keys[h], ~0ull, key) : key;
+        if (prev == ~0ull || prev == key) {
+            slotOf[i]   = (int)h;
+            const int k = atomicAdd(&cnt[h], 1);
+            sub[i]      = k;
+            if (k == 0)
+                atomicAdd(&ph[smg::phase_of(cx, cy, cz)], 1);
+            return;
+        }
+        h = (h + 1) & mask;
+    }
 }
 
-// ph[8..15] = list offsets of the phases, ph[16..23] = their fill pointers.
+// ph[0..7] = occupied cells per phase; this sets ph[8..15] = the phases' list offsets and
+// ph[16..23] = their front fill pointers (ph[24..31] count heavy cells placed from the
+// back, ph[32..39] hand heavy cells to CTAs; both start at 0).
 __global__ void k_phase_offsets(int *__restrict__ ph) {
     if (threadIdx.x != 0)
         return;
@@ -267,94 +320,246 @@ __global__ void k_phase_offsets(int *__restrict__ ph) {
 }
 
 // Placing pass: the point's position (its place i in the ascending id list in w: list order
-// is index order) at its cell slot; the point in slot 0
-// lists the cell in its phase (any order: cells of one phase do not interact) and records
-// rankCnt[cell] = {its list slot (the index of the cell's kept-point record), 0 kept}.
-__global__ void k_grid_scatter(const float4 *__restrict__ pos, const int *__restrict__ ids, int m,
-                               const int *__restrict__ cellOf, const int *__restrict__ sub,
-                               const int *__restrict__ start, int dim0, int dim1,
+// is index order) at its place in the cell; the point with place 0 lists the cell's slot in
+// its phase (any order: cells of one phase do not interact) and records
+// rankCnt[slot] = {its list place (the index of the cell's kept-point record), 0 kept}.
+__global__ void k_thin_scatter(const float4 *__restrict__ pos, const int *__restrict__ ids, int m,
+                               const int *__restrict__ slotOf, const int *__restrict__ sub,
+                               const int *__restrict__ start,
+                               const unsigned long long *__restrict__ keys, int dim0, int dim1,
                                float4 *__restrict__ pts, int *__restrict__ ph,
                                int *__restrict__ lists, int2 *__restrict__ rankCnt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m)
         return;
-    const int    id = ids[i];
-    const int    c  = cellOf[i];
-    const float4 p  = pos[id];
-    const int    k  = sub[i];
-    pts[start[c] + k] = make_float4(p.x, p.y, p.z, __int_as_float(i));
+    const int    h = slotOf[i];
+    const int    k = sub[i];
+    const float4 p = pos[ids[i]];
+    pts[start[h] + k] = make_float4(p.x, p.y, p.z, __int_as_float(i));
     if (k == 0) {
-        const int cx = c % dim0, cy = (c / dim0) % dim1, cz = c / (dim0 * dim1);
-        const int slot = atomicAdd(&ph[16 + smg::phase_of(cx, cy, cz)], 1);
-        lists[slot]    = c;
-        rankCnt[c]     = make_int2(slot, 0);
+        const unsigned long long key = keys ? keys[h] : (unsigned long long)h;
+        const unsigned long long xy  = (unsigned long long)dim0 * (unsigned)dim1;
+        const int cx = (int)(key % (unsigned)dim0), cy = (int)((key / (unsigned)dim0) % (unsigned)dim1);
+        const int cz    = (int)(key / xy);
+        const int phase = smg::phase_of(cx, cy, cz);
+        // light cells fill the phase's list region from the front, heavy ones (more than
+        // kSpHeavy points, taken by whole CTAs) from the back
+        const int slot = start[h + 1] - start[h] > kSpHeavy
+                             ? ph[8 + phase] + ph[phase] - 1 - atomicAdd(&ph[24 + phase], 1)
+                             : atomicAdd(&ph[16 + phase], 1);
+        lists[slot]    = h;
+        rankCnt[h]     = make_int2(slot, 0);
     }
 }
 
 // ---------------------------------------------------------------------------------------
-constexpr int kSpWarps = 4;   // warps (cells) per CTA of the phase kernel
-constexpr int kSpIds   = 192; // cell points held in shared memory
-constexpr int kSpStage = 256; // neighbours' kept points staged in shared memory
+constexpr int kSpWarps  = 8;   // warps per CTA of the phase kernel (a warp per light cell)
+constexpr int kSpReg    = kSpHeavy / 32; // light cell: points per lane, held in registers
+constexpr int kSpHStage = 448; // heavy cell: neighbours' kept points staged (26 x 16 + 32)
+constexpr int kSpStage  = 128; // light cell: neighbours' kept points staged per warp
+constexpr int kSpBuf    = kSpWarps * kSpStage > kSpHStage ? kSpWarps * kSpStage : kSpHStage;
+constexpr int kSpPh     = 40;  // ph[]: counts, offsets, light fill, heavy fill, heavy take
 
-// One warp per occupied cell of the current phase. The sequential greedy visits the cell's
-// points by ascending index and keeps a point unless a kept point lies within the step;
-// the kept points of the 26 neighbour cells (earlier phases) are fixed, so the warp first
-// drops every point within the step of one of them (order-free), then repeats "keep the
-// smallest surviving index, drop the survivors within the step of it" - the same kept set
-// as the sequential visit, at (kept points x cell size / 32) work and without sorting.
-// Kept points are recorded as positions (keptPos, `cap` per cell) and their number in
-// rankCnt[cell].y, next to the cell's record index (one load per neighbour). Points are
-// named by their place in the ascending id list (same order as the index), and keptFlag is
-// over those places. The neighbours' kept points and the cell's points (positions with the
-// place in w, contiguous per cell) are staged in shared memory; cells too large for the
-// staging buffers take the same steps in global memory (`alive` flags in aliveTmp).
+// The 26 neighbours of cell (cx, cy, cz) without its centre, lane l < 26 taking one:
+// the neighbour's kept-point record and kept count (cells of later phases have none yet,
+// empty cells have no record: -1, 0).
+__device__ __forceinline__ void sp_neighbour(const ThinView &G, const int2 *__restrict__ rankCnt,
+                                             int cx, int cy, int cz, int l, int &nr, int &cnt) {
+    nr  = -1;
+    cnt = 0;
+    const int o = l < 13 ? l : l + 1;
+    const int x = cx + o % 3 - 1, y = cy + (o / 3) % 3 - 1, z = cz + o / 9 - 1;
+    if (x >= 0 && y >= 0 && z >= 0 && x < G.dim[0] && y < G.dim[1] && z < G.dim[2]) {
+        const int t = G.find(cell_key(x, y, z, G.dim[0], G.dim[1]));
+        if (t >= 0) {
+            const int2 v = rankCnt[t];
+            nr           = v.x;
+            cnt          = nr >= 0 ? v.y : 0;
+        }
+    }
+}
+
+__device__ __forceinline__ void cell_coords(const ThinView &G, int cell, int &cx, int &cy, int &cz) {
+    const unsigned long long key = G.keys ? G.keys[cell] : (unsigned long long)cell;
+    cx = (int)(key % (unsigned)G.dim[0]);
+    cy = (int)((key / (unsigned)G.dim[0]) % (unsigned)G.dim[1]);
+    cz = (int)(key / ((unsigned long long)G.dim[0] * (unsigned)G.dim[1]));
+}
+
+// One warp per light cell, one CTA per heavy cell of the current phase. The sequential
+// greedy visits the cell's points by ascending index and keeps a point unless a kept point
+// lies within the step; the kept points of the 26 neighbour cells (earlier phases) are
+// fixed, so the cell first drops every point within the step of one of them (order-free),
+// then repeats "keep the smallest surviving index, drop the survivors within the step of
+// it" - the same kept set as the sequential visit, at (kept points x cell size / threads)
+// work and without sorting. Kept points are recorded as positions (keptPos, `cap` per cell)
+// and their number in rankCnt[slot].y, next to the cell's record index (one load per
+// neighbour). Points are named by their place in the ascending id list (same order as the
+// index), and keptFlag is over those places. A light cell's points sit in its warp's
+// registers (kSpReg per lane) and the neighbours' kept points are read once each by the
+// warp; heavy cells (more than kSpHeavy points) spread each step over the CTA, which takes
+// them first, one at a time from a per-phase counter (neighbours' kept points staged in
+// shared memory when they fit, `alive` flags in aliveTmp).
 __global__ void __launch_bounds__(kSpWarps * 32)
-    k_sample_phase(GridView G, const int *__restrict__ lists, const int *__restrict__ ph,
-                   int phase, int2 *__restrict__ rankCnt, float4 *__restrict__ keptPos, int cap,
-                   float r2, int *__restrict__ keptFlag, int *__restrict__ overflow,
+    k_sample_phase(ThinView G, const int *__restrict__ lists, int *__restrict__ ph, int phase,
+                   int2 *__restrict__ rankCnt, float4 *__restrict__ keptPos, int cap, float r2,
+                   int *__restrict__ keptFlag, int *__restrict__ overflow,
                    int *__restrict__ aliveTmp) {
-    __shared__ float4 stage[kSpWarps][kSpStage];
-    __shared__ float4 cpos[kSpWarps][kSpIds];
-    __shared__ int    calive[kSpWarps][kSpIds];
-    __shared__ int    snr[kSpWarps][26], scnt[kSpWarps][26];
-    const int  wl     = threadIdx.x >> 5;
-    const int  lane   = threadIdx.x & 31;
-    const int  ncells = ph[phase];
-    const int *cells  = lists + ph[8 + phase];
-    for (int w = blockIdx.x * kSpWarps + wl; w < ncells; w += gridDim.x * kSpWarps) {
+    __shared__ float4 stageBuf[kSpBuf]; // heavy cell: [0, kSpHStage); light warp w: its slice
+    __shared__ int    snr[26], scnt[26];
+    __shared__ int    sCell, sMin[kSpWarps];
+    __shared__ float4 sKeep;
+    const int  wl    = threadIdx.x >> 5;
+    const int  lane  = threadIdx.x & 31;
+    const int  tid   = threadIdx.x;
+    const int  off   = ph[8 + phase];
+    const int  total = ph[phase];
+    const int  nl    = ph[16 + phase] - off; // light cells: list front
+    const int  nh    = ph[24 + phase];       // heavy cells: list back
+    const int *cells = lists + off;
+
+    // ---- heavy cells: the whole CTA on one cell
+    for (; nh > 0;) {
+        if (tid == 0)
+            sCell = atomicAdd(&ph[32 + phase], 1);
+        __syncthreads();
+        const int hc = sCell;
+        __syncthreads(); // every thread has read sCell before it is taken again
+        if (hc >= nh)
+            break;
+        const int cell = cells[total - 1 - hc];
+        const int rk   = rankCnt[cell].x;
+        int       cx, cy, cz;
+        cell_coords(G, cell, cx, cy, cz);
+        const int s = G.start[cell], n = G.start[cell + 1] - s;
+        if (wl == 0) {
+            int nr = -1, cnt = 0;
+            if (lane < 26)
+                sp_neighbour(G, rankCnt, cx, cy, cz, lane, nr, cnt);
+            const int incl = warp_incl_scan(cnt);
+            if (lane < 26) {
+                snr[lane]  = nr;
+                scnt[lane] = incl - cnt; // exclusive prefix
+            }
+            if (lane == 31)
+                sMin[0] = incl; // NK
+        }
+        __syncthreads();
+        const int  NK      = sMin[0];
+        const bool stageNb = NK <= kSpHStage;
+        if (stageNb) {
+            for (int t = tid; t < NK; t += kSpWarps * 32) {
+                int j = 0;
+                while (j < 25 && scnt[j + 1] <= t)
+                    j++;
+                stageBuf[t] = keptPos[(size_t)snr[j] * cap + (t - scnt[j])];
+            }
+        }
+        __syncthreads();
+        int *alive = aliveTmp + s;
+        for (int i = tid; i < n; i += kSpWarps * 32) {
+            const float4 q  = G.pts[s + i];
+            bool         ok = true;
+            if (stageNb) {
+                for (int k = 0; k < NK && ok; k++) {
+                    const float4 o = stageBuf[k];
+                    if (smm::dist2(o.x, o.y, o.z, q.x, q.y, q.z) < r2)
+                        ok = false;
+                }
+            } else {
+                for (int j = 0; j < 26 && ok; j++) {
+                    const int nj = snr[j];
+                    const int cj = (j < 25 ? scnt[j + 1] : NK) - scnt[j];
+                    for (int k = 0; k < cj && ok; k++) {
+                        const float4 o = keptPos[(size_t)nj * cap + k];
+                        if (smm::dist2(o.x, o.y, o.z, q.x, q.y, q.z) < r2)
+                            ok = false;
+                    }
+                }
+            }
+            alive[i] = ok ? 1 : 0;
+        }
+        __syncthreads();
+        float4 *mine = keptPos + (size_t)rk * cap;
+        int     nk   = 0;
+        for (;;) {
+            int    myMin = INT_MAX;
+            float4 myP   = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int i = tid; i < n; i += kSpWarps * 32)
+                if (alive[i]) {
+                    const float4 q  = G.pts[s + i];
+                    const int    id = __float_as_int(q.w);
+                    if (id < myMin) {
+                        myMin = id;
+                        myP   = q;
+                    }
+                }
+            const int wm = __reduce_min_sync(0xffffffffu, myMin);
+            if (lane == 0)
+                sMin[wl] = wm;
+            __syncthreads();
+            int m = INT_MAX;
+            for (int k = 0; k < kSpWarps; k++)
+                m = min(m, sMin[k]);
+            if (m == INT_MAX)
+                break; // (uniform: every thread read the same minima)
+            if (myMin == m)
+                sKeep = make_float4(myP.x, myP.y, myP.z, 0.0f); // the unique holder
+            __syncthreads();
+            const float4 kp = sKeep;
+            if (tid == 0) {
+                keptFlag[m] = 1;
+                if (nk < cap)
+                    mine[nk] = kp;
+                else
+                    atomicExch(overflow, 1);
+            }
+            nk = min(nk + 1, cap);
+            for (int i = tid; i < n; i += kSpWarps * 32) {
+                if (!alive[i])
+                    continue;
+                const float4 q = G.pts[s + i];
+                if (__float_as_int(q.w) == m || smm::dist2(kp.x, kp.y, kp.z, q.x, q.y, q.z) < r2)
+                    alive[i] = 0;
+            }
+            __syncthreads(); // drops done and sMin / sKeep read before the next round
+        }
+        if (tid == 0)
+            rankCnt[cell].y = nk;
+        __syncthreads(); // the buffers are reused by the next cell
+    }
+
+    // ---- light cells: a warp each, the cell's points in registers (kSpReg per lane)
+    for (int w = blockIdx.x * kSpWarps + wl; w < nl; w += gridDim.x * kSpWarps) {
         const int cell = cells[w];
         const int rk   = rankCnt[cell].x;
-        const int cx = cell % G.dim[0], cy = (cell / G.dim[0]) % G.dim[1],
-                  cz = cell / (G.dim[0] * G.dim[1]);
-        const int s = G.start[cell], e = G.start[cell + 1], n = e - s;
-        // the cell's first 32 points, read while the neighbours are looked up
-        const float4 q0 = lane < n ? G.pts[s + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
-        // neighbour l (lane < 26) of the 3x3x3 block without its centre; cells of later
-        // phases have no kept points yet (count 0), empty cells have no record (-1)
-        int nr = -1, cnt = 0;
-        if (lane < 26) {
-            const int o = lane < 13 ? lane : lane + 1;
-            const int x = cx + o % 3 - 1, y = cy + (o / 3) % 3 - 1, z = cz + o / 9 - 1;
-            if (x >= 0 && y >= 0 && z >= 0 && x < G.dim[0] && y < G.dim[1] && z < G.dim[2]) {
-                const int2 v = rankCnt[grid_cell(G, x, y, z)];
-                nr           = v.x;
-                cnt          = nr >= 0 ? v.y : 0;
-            }
-            snr[wl][lane]  = nr;
-            scnt[wl][lane] = cnt;
+        int       cx, cy, cz;
+        cell_coords(G, cell, cx, cy, cz);
+        const int s = G.start[cell], n = G.start[cell + 1] - s; // n <= kSpHeavy
+        float4    q[kSpReg];
+        unsigned  alive = 0u; // bit j: point lane + 32 j is still a candidate
+#pragma unroll
+        for (int j = 0; j < kSpReg; j++) {
+            const int i = lane + 32 * j;
+            q[j]        = i < n ? G.pts[s + i] : make_float4(0.f, 0.f, 0.f, 0.f);
+            alive |= (i < n ? 1u : 0u) << j;
         }
-        __syncwarp();
-        const int  incl    = warp_incl_scan(cnt);
-        const int  excl    = incl - cnt;
-        const int  NK      = __shfl_sync(0xffffffffu, incl, 31);
-        const bool stageNb = NK <= kSpStage;
-        const bool stageC  = n <= kSpIds;
-        float4    *st      = stage[wl];
-        if (stageNb) {
+        int nr = -1, cnt = 0;
+        if (lane < 26)
+            sp_neighbour(G, rankCnt, cx, cy, cz, lane, nr, cnt);
+        // survivors of the neighbours' kept points, each tested against every point the lane
+        // holds: staged in shared memory by the whole warp at once when they fit, else the
+        // neighbours one by one, each kept point read once by the warp (a broadcast)
+        const int incl = warp_incl_scan(cnt);
+        const int excl = incl - cnt;
+        const int NK   = __shfl_sync(0xffffffffu, incl, 31);
+        unsigned  nz   = __ballot_sync(0xffffffffu, cnt > 0);
+        if (NK <= kSpStage) {
+            float4 *st = stageBuf + wl * kSpStage;
             for (int base = 0; base < NK; base += 32) {
                 const int t  = base + lane;
-                int       lo = 0;
-    #pragma unroll
+                int       lo = 0; // the neighbour holding kept point t: last with excl <= t
+#pragma unroll
                 for (int step = 16; step >= 1; step >>= 1) {
                     const int mid = lo + step;
                     const int ev  = __shfl_sync(0xffffffffu, excl, mid & 31);
@@ -366,34 +571,31 @@ __global__ void __launch_bounds__(kSpWarps * 32)
                 if (t < NK)
                     st[t] = keptPos[(size_t)nj * cap + (t - ej)];
             }
-        }
-        int          *alive = stageC ? calive[wl] : aliveTmp + s;
-        const float4 *cp    = stageC ? cpos[wl] : G.pts + s;
-        // survivors of the neighbours' kept points
-        for (int i = lane; i < n; i += 32) {
-            const float4 q  = i < 32 ? q0 : G.pts[s + i];
-            bool         ok = true;
-            if (stageNb) {
-                for (int k = 0; k < NK && ok; k++) {
-                    const float4 o = st[k];
-                    if (smm::dist2(o.x, o.y, o.z, q.x, q.y, q.z) < r2)
-                        ok = false;
-                }
-            } else {
-                for (int j = 0; j < 26 && ok; j++) {
-                    const int nj = snr[wl][j], cj = scnt[wl][j];
-                    for (int k = 0; k < cj && ok; k++) {
-                        const float4 o = keptPos[(size_t)nj * cap + k];
-                        if (smm::dist2(o.x, o.y, o.z, q.x, q.y, q.z) < r2)
-                            ok = false;
-                    }
-                }
+            __syncwarp();
+            for (int kk = 0; kk < NK; kk++) {
+                const float4 o = st[kk];
+#pragma unroll
+                for (int j = 0; j < kSpReg; j++)
+                    if (smm::dist2(o.x, o.y, o.z, q[j].x, q[j].y, q[j].z) < r2)
+                        alive &= ~(1u << j);
             }
-            alive[i] = ok ? 1 : 0;
-            if (stageC)
-                cpos[wl][i] = q;
+            __syncwarp(); // the slice is refilled by the warp's next cell
+            nz = 0u;
         }
-        __syncwarp();
+        while (nz && __any_sync(0xffffffffu, alive != 0u)) {
+            const int jn = __ffs(nz) - 1;
+            nz &= nz - 1u;
+            const int     nj = __shfl_sync(0xffffffffu, nr, jn);
+            const int     cj = __shfl_sync(0xffffffffu, cnt, jn);
+            const float4 *kn = keptPos + (size_t)nj * cap;
+            for (int k = 0; k < cj; k++) {
+                const float4 o = kn[k];
+#pragma unroll
+                for (int j = 0; j < kSpReg; j++)
+                    if (smm::dist2(o.x, o.y, o.z, q[j].x, q[j].y, q[j].z) < r2)
+                        alive &= ~(1u << j);
+            }
+        }
         // keep the smallest surviving index, drop the survivors within the step, repeat; the
         // lane that holds the kept point hands its position to the warp
         float4 *mine = keptPos + (size_t)rk * cap;
@@ -401,19 +603,15 @@ __global__ void __launch_bounds__(kSpWarps * 32)
         for (;;) {
             int    myMin = INT_MAX;
             float4 myP   = make_float4(0.f, 0.f, 0.f, 0.f);
-            for (int i = lane; i < n; i += 32)
-                if (alive[i]) {
-                    const float4 q  = cp[i];
-                    const int    id = __float_as_int(q.w);
-                    if (id < myMin) {
-                        myMin = id;
-                        myP   = q;
-                    }
+#pragma unroll
+            for (int j = 0; j < kSpReg; j++) {
+                const int id = __float_as_int(q[j].w);
+                if (((alive >> j) & 1u) && id < myMin) {
+                    myMin = id;
+                    myP   = q[j];
                 }
-            int m = myMin;
-    #pragma unroll
-            for (int o = 16; o >= 1; o >>= 1)
-                m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+            }
+            const int m = __reduce_min_sync(0xffffffffu, myMin);
             if (m == INT_MAX)
                 break;
             const int    src = __ffs(__ballot_sync(0xffffffffu, myMin == m)) - 1;
@@ -428,18 +626,14 @@ __global__ void __launch_bounds__(kSpWarps * 32)
                     atomicExch(overflow, 1);
             }
             nk = min(nk + 1, cap);
-            for (int i = lane; i < n; i += 32) {
-                if (!alive[i])
-                    continue;
-                const float4 q = cp[i];
-                if (__float_as_int(q.w) == m || smm::dist2(kp.x, kp.y, kp.z, q.x, q.y, q.z) < r2)
-                    alive[i] = 0;
-            }
-            __syncwarp();
+#pragma unroll
+            for (int j = 0; j < kSpReg; j++)
+                if (__float_as_int(q[j].w) == m ||
+                    smm::dist2(kp.x, kp.y, kp.z, q[j].x, q[j].y, q[j].z) < r2)
+                    alive &= ~(1u << j);
         }
         if (lane == 0)
             rankCnt[cell].y = nk;
-        __syncwarp(); // the next cell reuses the warp's staging buffers
     }
 }
 
@@ -456,7 +650,8 @@ __global__ void k_mark_todo(const int *__restrict__ ids, int m, const float4 *__
 
 // One warp per query (exact k nearest neighbours, sm_device.cuh warp_knn_sorted); lane j
 // writes the j-th neighbour, and with smoothing marks it when it still needs a normal.
-__global__ void k_knn(const int *__restrict__ list, const int *__restrict__ nlp, HGridView G, const float4 *__restrict__ pos,
+__global__ void __launch_bounds__(256, 6)
+    k_knn(const int *__restrict__ list, const int *__restrict__ nlp, HGridView G, const float4 *__restrict__ pos,
                       int k, int *__restrict__ nbr, int *__restrict__ nbrCnt, int markNeighbours,
                       const float4 *__restrict__ nrm, int *__restrict__ need) {
     const int nl = *nlp; // device-side count of the list
@@ -903,40 +1098,65 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
                   float step, int *outIds, const std::string &tag) {
     if (m <= 0)
         return 0;
-    float ext[3] = {box.ext(0), box.ext(1), box.ext(2)};
-    const float g = smg::sample_cell(step, ext);
-    // dense grid over the points, its occupied cells listed per phase on the device (no host
-    // round trip; at most min(cells, points) of them)
-    Grid G;
-    G.g = g;
-    for (int a = 0; a < 3; a++) {
-        G.org[a] = box.mn[a];
-        G.dim[a] = smg::dim_of(ext[a], g);
+    if (!(step > 0.0f)) {
+        // no point lies at a squared distance below zero: every point is kept (the list is
+        // ascending already)
+        SM_CUDA(cudaMemcpyAsync(outIds, ids, (size_t)m * sizeof(int), cudaMemcpyDeviceToDevice,
+                                c.stream));
+        return m;
     }
-    G.nc                   = (long long)G.dim[0] * G.dim[1] * G.dim[2];
-    G.m                    = m;
-    const long long maxOcc = std::max<long long>(1, std::min<long long>(G.nc, m));
-    int *cnt    = c.arena.get<int>(tag + ".g.cnt", G.nc + 1);
-    G.start     = c.arena.get<int>(tag + ".g.start", G.nc + 1);
-    G.pts       = c.arena.get<float4>(tag + ".g.pts", std::max(m, 1));
-    int *cellOf = c.arena.get<int>(tag + ".g.cellOf", std::max(m, 1));
-    int *sub    = c.arena.get<int>(tag + ".g.sub", std::max(m, 1));
-    int  *ph      = c.arena.get<int>(tag + ".ph", 24);
-    int2 *rankCnt = c.arena.get<int2>(tag + ".rank", G.nc);
-    int  *lists   = c.arena.get<int>(tag + ".phl", maxOcc);
-    SM_CUDA(cudaMemsetAsync(cnt, 0, (G.nc + 1) * sizeof(int), c.stream));
-    SM_CUDA(cudaMemsetAsync(ph, 0, 24 * sizeof(int), c.stream));
-    SM_CUDA(cudaMemsetAsync(rankCnt, 0xff, G.nc * sizeof(int2), c.stream));
-    const GridParams gpar = grid_params(box, g, G.dim);
-    k_grid_count<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, m, gpar, cellOf, sub, cnt, ph);
+    float ext[3] = {box.ext(0), box.ext(1), box.ext(2)};
+    const float g = smg::thin_cell(step, ext);
+    // the cell table over the points (dense or hashed, see ThinView), its occupied cells
+    // listed per phase on the device (no host round trip; at most m of them)
+    int dim[3];
+    for (int a = 0; a < 3; a++)
+        dim[a] = smg::dim_of(ext[a], g);
+    uint32_t T = 1024;
+    while (T < 2u * (uint32_t)m)
+        T <<= 1;
+    // dense table (slot = cell key) when the cell box has at most 2^22 cells or 16 per
+    // point (its counts and their scan move 12 bytes a cell, the hashed table's key claims
+    // and scattered placing cost more a point), never above 2^27 cells
+    const unsigned long long ncell = (unsigned long long)dim[0] * dim[1] * dim[2];
+    const unsigned long long dmax  = std::max<unsigned long long>(1ull << 22, 16ull * (unsigned)m);
+    const bool               dense = ncell <= std::min<unsigned long long>(dmax, 1ull << 27);
+    if (dense)
+        T = (uint32_t)ncell;
+    const long long maxOcc = m;
+    auto *keys = dense ? nullptr : c.arena.get<unsigned long long>(tag + ".g.keys", T);
+    int   *cnt     = c.arena.get<int>(tag + ".g.cnt", (size_t)T + 1);
+    int   *start   = c.arena.get<int>(tag + ".g.start", (size_t)T + 1);
+    float4 *pts    = c.arena.get<float4>(tag + ".g.pts", m);
+    int   *slotOf  = c.arena.get<int>(tag + ".g.slotOf", m);
+    int   *sub     = c.arena.get<int>(tag + ".g.sub", m);
+    int   *ph      = c.arena.get<int>(tag + ".ph", kSpPh);
+    int2  *rankCnt = c.arena.get<int2>(tag + ".rank", T);
+    int   *lists   = c.arena.get<int>(tag + ".phl", maxOcc);
+    if (!dense)
+        SM_CUDA(cudaMemsetAsync(keys, 0xff, (size_t)T * 8, c.stream));
+    SM_CUDA(cudaMemsetAsync(cnt, 0, ((size_t)T + 1) * sizeof(int), c.stream));
+    SM_CUDA(cudaMemsetAsync(ph, 0, kSpPh * sizeof(int), c.stream));
+    const GridParams gpar = grid_params(box, g, dim);
+    k_thin_insert<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, m, gpar, keys, dense ? 0u : T - 1,
+                                                         slotOf, sub, cnt, ph);
     SM_LAUNCH_CHECK();
-    scan_excl(c, cnt, G.start, G.nc + 1, tag + ".g", false);
+    scan_excl(c, cnt, start, (long long)T + 1, tag + ".g", false);
     k_phase_offsets<<<1, 32, 0, c.stream>>>(ph);
     SM_LAUNCH_CHECK();
-    k_grid_scatter<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, m, cellOf, sub, G.start,
-                                                          G.dim[0], G.dim[1], G.pts, ph, lists,
-                                                          rankCnt);
+    k_thin_scatter<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, m, slotOf, sub, start, keys,
+                                                          dim[0], dim[1], pts, ph, lists, rankCnt);
     SM_LAUNCH_CHECK();
+    ThinView V;
+    for (int a = 0; a < 3; a++) {
+        V.org[a] = box.mn[a];
+        V.dim[a] = dim[a];
+    }
+    V.g     = g;
+    V.keys  = keys;
+    V.mask  = dense ? 0u : T - 1;
+    V.start = start;
+    V.pts   = pts;
     // kept-list capacity: points at pairwise distance >= step inside a cube of side g fit
     // disjoint balls of radius step/2 inside the cube grown by step/2.
     const double s   = (double)g / (double)step;
@@ -947,9 +1167,20 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
     int    *overflow = keptFlag + m;
     SM_CUDA(cudaMemsetAsync(keptFlag, 0, ((size_t)m + 1) * sizeof(int), c.stream));
     const float r2 = step * step;
-    const int   gp = (int)std::min<long long>((maxOcc + kSpWarps - 1) / kSpWarps, 152LL * 16);
+    // one resident wave: heavy cells are handed out by a counter, light cells by stride
+    static std::atomic<int> resident[64];
+    const int               dev = c.device >= 0 && c.device < 64 ? c.device : 0;
+    int                     per = resident[dev].load();
+    if (per <= 0) {
+        SM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sample_phase, kSpWarps * 32, 0));
+        per = std::max(per, 1);
+        resident[dev].store(per);
+    }
+    int nsm = 0;
+    SM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device));
+    const int gp = (int)std::min<long long>((maxOcc + kSpWarps - 1) / kSpWarps, (long long)nsm * per);
     for (int p = 0; p < 8; p++) {
-        k_sample_phase<<<gp, kSpWarps * 32, 0, c.stream>>>(G.view(), lists, ph, p, rankCnt,
+        k_sample_phase<<<gp, kSpWarps * 32, 0, c.stream>>>(V, lists, ph, p, rankCnt,
                                                            keptPos, cap, r2, keptFlag, overflow,
                                                            aliveTmp);
         SM_LAUNCH_CHECK();

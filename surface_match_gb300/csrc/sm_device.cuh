@@ -2,6 +2,8 @@
 // grid searches, ordered float atomics, warp/block helpers.
 #pragma once
 
+#include <climits>
+
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -10,7 +12,8 @@
 
 namespace smd {
 
-constexpr int kMaxKnn = 32; // largest supported knnNormal
+constexpr int kMaxKnn      = 32; // largest supported knnNormal
+constexpr int kKnnMaxShell = 24; // shells a k-nearest walk visits before it scans every point
 
 // Device view of a dense uniform grid over a subset of points: cells are stored cell-major
 // as a CSR (start[cell] .. start[cell+1] into pts, the positions in cell order with the
@@ -40,6 +43,7 @@ struct HGridView {
     const float4 *pts;
     const uint32_t *occ;   // one bit per cell of the dim box (nullptr: not built)
     const int2     *dense; // {first, count} per cell of the dim box (nullptr: not built)
+    int             m;     // points in pts
     __device__ __forceinline__ unsigned long long key_of(int x, int y, int z) const {
         return ((unsigned long long)z * (unsigned)dim[1] + (unsigned)y) * (unsigned)dim[0] +
                (unsigned)x;
@@ -179,25 +183,45 @@ __device__ __forceinline__ bool warp_visit_cells(const G &g, int b, int e, V &&v
 // 32 cells at a time (occupancy bit, table) and warp_visit_cells visits their points. After
 // each shell, stop(s) - evaluated by all lanes, warp-uniform - ends the walk. Every point of
 // shells s0..s is visited exactly once before stop(s), so a search written on it sees the
-// same points as one that walks the cells one by one.
+// same points as one that walks the cells one by one. Returns false when it stopped at
+// shell smax before stop() or the grid's last shell ended it.
 template <class G, class V, class S>
-__device__ __forceinline__ void warp_walk(const G &g, float qx, float qy, float qz, V &&visit,
-                                          S &&stop, int s0 = 1) {
+__device__ __forceinline__ bool warp_walk(const G &g, float qx, float qy, float qz, V &&visit,
+                                          S &&stop, int s0 = 1, int smax = INT_MAX) {
     const int lane = threadIdx.x & 31;
     int       c[3];
     grid_cc(g, qx, qy, qz, c);
     const int ms = max(grid_max_shell(g, c), 1);
     for (int s = s0; s <= ms; s++) {
-        const int lo = s == 1 ? 0 : s, w = 2 * s + 1, cube = w * w * w;
-        for (int t0 = 0; t0 < cube; t0 += 32) {
+        if (s > smax)
+            return false; // the walk gave up before stop() ended it
+        // shell 1 is the whole 3x3x3 block; a later shell s is its ring of 24 s^2 + 2 cells:
+        // the two z faces, then the square perimeters (8 s cells) of the 2 s - 1 layers between
+        const int w = 2 * s + 1, F = w * w;
+        const int N = s == 1 ? 27 : 24 * s * s + 2;
+        for (int t0 = 0; t0 < N; t0 += 32) {
             const int t = t0 + lane;
             int       b = 0, e = 0;
-            if (t < cube) {
-                const int dx = t % w - s, dy = (t / w) % w - s, dz = t / (w * w) - s;
-                const int r  = max(abs(dx), max(abs(dy), abs(dz)));
+            if (t < N) {
+                int dx, dy, dz;
+                if (s == 1) {
+                    dx = t % 3 - 1;
+                    dy = (t / 3) % 3 - 1;
+                    dz = t / 9 - 1;
+                } else if (t < 2 * F) {
+                    const int u = t < F ? t : t - F;
+                    dz          = t < F ? -s : s;
+                    dx          = u % w - s;
+                    dy          = u / w - s;
+                } else {
+                    const int u = t - 2 * F, per = 8 * s;
+                    dz          = u / per - (s - 1);
+                    const int p = u % per, side = p / (2 * s), q = p % (2 * s);
+                    dx          = side == 0 ? -s + q : side == 1 ? s : side == 2 ? s - q : -s;
+                    dy          = side == 0 ? -s : side == 1 ? -s + q : side == 2 ? s : s - q;
+                }
                 const int x = c[0] + dx, y = c[1] + dy, z = c[2] + dz;
-                if (r >= lo && x >= 0 && y >= 0 && z >= 0 && x < g.dim[0] && y < g.dim[1] &&
-                    z < g.dim[2])
+                if (x >= 0 && y >= 0 && z >= 0 && x < g.dim[0] && y < g.dim[1] && z < g.dim[2])
                     g.range(x, y, z, b, e);
             }
             warp_visit_cells(g, b, e, [&](const float4 &p, bool valid) {
@@ -206,8 +230,9 @@ __device__ __forceinline__ void warp_walk(const G &g, float qx, float qy, float 
             });
         }
         if (stop(s))
-            return;
+            return true;
     }
+    return true; // every shell of the grid visited
 }
 
 // Lower bound of the squared distance from q to any point filed under cell (x, y, z): the
@@ -345,42 +370,54 @@ __device__ __forceinline__ int band_end(int done, int ms, float b2, float g) {
     return hi;
 }
 
-// Exact k nearest neighbours (k <= 32) of q by (squared distance, index), one warp per
-// query, on warp_walk: each round of 32 points is sorted across the lanes and merged into
-// the running 32 best (lane j holds the j-th smallest key: distance bits, index); rounds with
-// no point below the current k-th best are skipped. The search ends after shell s once k
-// points were seen and the k-th distance is below the ring bound of s (every unvisited point
-// is farther), so the result is the exact k nearest. Returns the number found (<= k); lane
-// j < that count gets the j-th neighbour's index in *id and squared distance in *d.
-template <class G>
-__device__ __forceinline__ int warp_knn_sorted(const G &g, float qx, float qy, float qz, int k,
-                                               int *id, float *d) {
-    unsigned long long best = ~0ull; // lane j: j-th smallest so far
-    int                seen = 0;
-    warp_walk(
-        g, qx, qy, qz,
-        [&](const float4 &p, bool valid) {
-            seen += __popc(__ballot_sync(0xffffffffu, valid));
-            unsigned long long key = ~0ull;
-            if (valid) {
-                const float dd = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
-                key = ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)__float_as_int(p.w);
-            }
-            const unsigned long long kth = __shfl_sync(0xffffffffu, best, k - 1);
-            if (__any_sync(0xffffffffu, key < kth))
+// k nearest by a scan of every point of g, for a query whose shell walk gave up (a point
+// far from the others would walk shells up to the grid's extent). The scan starts over
+// (best and seen reset: each point is visited once, so the result is the same exact k
+// nearest) and keeps only points within a bound on the k-th distance: the walk's k-th when
+// it saw k points, else the k-th of a strided sample of the points; a merge runs only for a
+// round with a point below the current k-th. It runs for few queries and is kept lean (two
+// loads in flight per lane) so that the walk's register count stays as it is.
+static __device__ __noinline__ void knn_scan_all(const HGridView &g, float qx, float qy, float qz, int k,
+                                          unsigned long long &best, int &seen) {
+    const int lane  = threadIdx.x & 31;
+    unsigned  bound = 0xffffffffu; // distance bits
+    auto      key_of = [&](const float4 &p) {
+        const float dd = smm::dist2(qx, qy, qz, p.x, p.y, p.z);
+        return ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)__float_as_int(p.w);
+    };
+    if (seen >= k) {
+        bound = (unsigned)(__shfl_sync(0xffffffffu, best, k - 1) >> 32);
+    } else {
+        const int          stride = max(1, g.m / 4096);
+        unsigned long long sb     = ~0ull;
+        int                ss     = 0;
+        for (long long base = 0; base < g.m; base += 32ll * stride) {
+            const long long          r   = base + (long long)lane * stride;
+            const unsigned long long key = r < g.m ? key_of(g.pts[r]) : ~0ull;
+            ss += __popc(__ballot_sync(0xffffffffu, r < g.m));
+            if (__any_sync(0xffffffffu, key < __shfl_sync(0xffffffffu, sb, k - 1)))
+                sb = warp_merge_low(sb, warp_bitonic_sort(key));
+        }
+        if (ss >= k)
+            bound = (unsigned)(__shfl_sync(0xffffffffu, sb, k - 1) >> 32);
+    }
+    best = ~0ull;
+    seen = 0;
+    for (int base = 0; base < g.m; base += 64) {
+        const int    r0 = base + lane, r1 = base + 32 + lane;
+        const float4 p0 = r0 < g.m ? g.pts[r0] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 p1 = r1 < g.m ? g.pts[r1] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            const int          r   = j ? r1 : r0;
+            unsigned long long key = r < g.m ? key_of(j ? p1 : p0) : ~0ull;
+            if ((unsigned)(key >> 32) > bound)
+                key = ~0ull;
+            seen += __popc(__ballot_sync(0xffffffffu, r < g.m));
+            if (__any_sync(0xffffffffu, key < __shfl_sync(0xffffffffu, best, k - 1)))
                 best = warp_merge_low(best, warp_bitonic_sort(key));
-        },
-        [&](int s) {
-            if (seen < k)
-                return false;
-            const unsigned long long kth = __shfl_sync(0xffffffffu, best, k - 1);
-            const float              bnd = smg::ring_bound(s, g.g);
-            return __uint_as_float((unsigned)(kth >> 32)) < bnd * bnd;
-        });
-    const int n = min(seen, k);
-    *id         = (int)(unsigned)(best & 0xffffffffu);
-    *d          = __uint_as_float((unsigned)(best >> 32));
-    return n;
+        }
+    }
 }
 
 // Exact k nearest neighbours (k <= 32) of q by (squared distance, index), one warp per
@@ -459,8 +496,8 @@ __device__ __forceinline__ int warp_knn_sorted(const HGridView &g, float qx, flo
         const float bnd = smg::ring_bound(s, g.g);
         return __uint_as_float((unsigned)(kth() >> 32)) < bnd * bnd;
     };
-    if (!done(1) && ms >= 2)
-        warp_walk(g, qx, qy, qz, visit, done, 2);
+    if (!done(1) && ms >= 2 && !warp_walk(g, qx, qy, qz, visit, done, 2, kKnnMaxShell))
+        knn_scan_all(g, qx, qy, qz, k, best, seen);
     const int n = min(seen, k);
     *id         = (int)(unsigned)(best & 0xffffffffu);
     *d          = __uint_as_float((unsigned)(best >> 32));

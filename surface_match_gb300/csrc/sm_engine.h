@@ -156,6 +156,7 @@ struct HGrid {
         v.pts  = pts;
         v.occ   = occ;
         v.dense = dense;
+        v.m     = m;
         return v;
     }
 };

@@ -24,9 +24,25 @@ SM_HD long long cells_of(const float ext[3], float g) {
            (long long)dim_of(ext[2], g);
 }
 
-// Cell side for greedy sampling at `step`: slightly larger than the step so that two
-// cells of the same phase never hold a conflicting pair, doubled until the dense grid
-// fits the cap.
+// Cell side of the grid-order greedy sampler at `step`: slightly larger than the step so
+// that two cells of the same phase never hold a conflicting pair. The sampler's grid is
+// hashed (occupied cells only), so the side is doubled only while an axis would reach 2^20
+// cells (cell keys stay within 60 bits).
+SM_HD float thin_cell(float step, const float ext[3]) {
+    float g = step * (1.0f + 1.0f / 1024.0f);
+    // dim_of(e, g) >= 2^20  <=>  e / g >= 2^20 - 1 (compared in float: no int overflow)
+    const float lim = (float)((1 << 20) - 1);
+    for (int it = 0; it < 256; it++) {
+        if (smm::fdiv(ext[0], g) < lim && smm::fdiv(ext[1], g) < lim && smm::fdiv(ext[2], g) < lim)
+            break;
+        g = g * 2.0f;
+    }
+    return g;
+}
+
+// Cell side of a dense acceleration grid for searches within `step` (the reference-order
+// sampler's cell lists): slightly larger than the step, doubled until the dense grid fits
+// the cap.
 SM_HD float sample_cell(float step, const float ext[3]) {
     float g = step * (1.0f + 1.0f / 1024.0f);
     while (cells_of(ext, g) > kMaxCells)

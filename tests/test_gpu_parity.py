@@ -249,3 +249,29 @@ def test_workspace_reuse_across_scene_sizes():
         p2, s2 = fresh.matchScene(pc, SD, KP, MS, param)
         np.testing.assert_array_equal(s1, s2)
         np.testing.assert_array_equal(p1, p2)
+
+
+def test_sampler_heavy_cells_and_wide_extent_bit_exact(data):
+    """The grid-order sampler on a scene that stresses its cell table: a clump of 6000
+    points inside one sampling cell (cells above 192 points are thinned by a whole CTA) and
+    two far points that stretch the box to ~10^10 cells at the refinement step (only
+    occupied cells are stored; the cell side stays at the step). Sampled, keypoint and
+    resampled sets equal the oracle's."""
+    from oracle import MODE_GRID, MatchParam as OMP, Oracle
+    from surface_match_gb300 import Detector, MatchParam, PointCloud
+    mc, sc = data
+    rng = np.random.default_rng(17)
+    diam = float(np.linalg.norm(mc.xyz.max(0) - mc.xyz.min(0)))
+    c0 = sc.cloud.xyz[np.isfinite(sc.cloud.xyz).all(1)].mean(0)
+    clump = c0 + rng.normal(0, 0.3 * SD * diam, (6000, 3))
+    far = np.array([c0 - 120 * diam, c0 + 120 * diam])
+    xyz = np.ascontiguousarray(np.vstack([sc.cloud.xyz, clump, far]), np.float32)
+    det = Detector()
+    det.trainModel(PointCloud(mc.xyz, mc.normal), SD)
+    det.matchScene(PointCloud(xyz, None, sc.viewpoint), SD, KP, MS, MatchParam(numMatches=8))
+    o = Oracle(mode=MODE_GRID, threads=8)
+    m = o.train(mc.xyz, mc.normal, SD)
+    r = o.match(m, xyz, None, sc.viewpoint, SD, KP, MS, OMP(numMatches=8))
+    np.testing.assert_array_equal(det.debug(0), r.sampled)
+    np.testing.assert_array_equal(det.debug(1), r.keypoints)
+    np.testing.assert_array_equal(det.debug(2), r.resampled)
