@@ -618,6 +618,31 @@ def main():
         if i:
             iso_ms.append(st[0]["vote_ms"][1])
     vk_iso = statistics.mean(iso_ms)
+    # The latency-bound kernels of the path, timed per launch by the library's opt-in clock
+    # (a CUDA event pair around each launch on its stream) over 3 matchScene calls after the
+    # timed steps, against their algorithmic bytes.
+    det.ctx.kernel_clock(True)
+    for _ in range(3):
+        det.matchScene(PointCloud(xyz_dev, None, vp), SD, KP, MS, param)
+    clock_rep = det.ctx.kernel_report()
+    det.ctx.kernel_clock(False)
+    per_unit = {"k_sample_phase": "20 B per point of a sampling (position read, kept flag "
+                                  "written), spread over its 8 phase launches",
+                "k_scan_lookback": "8 B per scanned value (read, written)",
+                "k_corr": "88 B per searched (candidate, model point): point and normal "
+                          "read, moved point and normal, 3 indices written, winner atomic"}
+    kernel_rooflines = []
+    for name, r in clock_rep.items():
+        if r["launches"] and r["ms"] > 0:
+            ach = r["bytes"] / (r["ms"] / 1000.0) / 1e9
+            kernel_rooflines.append({
+                "kernel": name, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                "frac": ach / hbm, "launch_ms": r["ms"] / r["launches"],
+                "launches_per_call": r["launches"] / 3.0,
+                "alg_bytes_per_launch": r["bytes"] / r["launches"],
+                "alg_bytes": per_unit[name], "traffic": None,
+                "how": "CUDA events around each launch (sm_context_kernel_clock), 3 "
+                       "matchScene calls after the timed steps"})
     line = {"metric": METRIC, "value": value, "unit": "scenes/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -661,6 +686,7 @@ def main():
                                     "steps: the same matchScene without the dense preparation "
                                     "running beside the vote kernel (launch_ms above is "
                                     "measured in the timed, overlapped steps)"}},
+            "kernel_rooflines": kernel_rooflines,
             "vote_stage_ms": {"pairs_probe_k_ppf": statistics.mean(ppf_ms),
                               "accumulate_k_vote_acc": vk,
                               "stage": stats["ms"][3]},

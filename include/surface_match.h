@@ -115,6 +115,19 @@ SM_API void *sm_context_stream(sm_context ctx);
 /* Device bytes the context's workspace holds (both of its streams' workspaces). It grows on
  * demand and is reused across calls; no counterpart in the reference. */
 SM_API int sm_context_workspace_bytes(sm_context ctx, int64_t *bytes);
+/* Opt-in per-launch timing of the matching path's latency-bound kernels, for throughput
+ * reports: on != 0 resets the counters and records a CUDA event pair around each launch of
+ * them on their stream from then on; 0 stops. No counterpart in the reference. */
+SM_API int sm_context_kernel_clock(sm_context ctx, int on);
+/* Totals since the clock was switched on for kernel `kind` (SM_KERNEL_*): summed launch
+ * durations, algorithmic bytes (per kind: SM_KERNEL_SAMPLE_PHASE 20 per sampled point,
+ * SM_KERNEL_SCAN 8 per value, SM_KERNEL_CORR 88 per searched (candidate, source point)) and
+ * launches. */
+#define SM_KERNEL_SAMPLE_PHASE 0
+#define SM_KERNEL_SCAN 1
+#define SM_KERNEL_CORR 2
+SM_API int sm_context_kernel_report(sm_context ctx, int kind, double *ms, double *bytes,
+                                    int64_t *launches);
 
 /* Model handle (ppf::Detector::IMPL, privateType.h:56-66). */
 SM_API int sm_model_create(sm_context ctx, sm_model *out);

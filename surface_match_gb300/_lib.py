@@ -55,6 +55,9 @@ _SIGNATURES = {
     "sm_context_synchronize": (C.c_int, [_vp]),
     "sm_context_stream": (_vp, [_vp]),
     "sm_context_workspace_bytes": (C.c_int, [_vp, _i64p]),
+    "sm_context_kernel_clock": (C.c_int, [_vp, C.c_int]),
+    "sm_context_kernel_report": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_double),
+                                           C.POINTER(C.c_double), _i64p]),
     "sm_model_create": (C.c_int, [_vp, C.POINTER(_vp)]),
     "sm_model_destroy": (C.c_int, [_vp]),
     "sm_model_train": (C.c_int, [_vp, _f32p, _f32p, C.c_int64, C.c_float,

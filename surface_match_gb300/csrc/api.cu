@@ -646,7 +646,8 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
         }
     } waiter;
     if (overlap) {
-        dctx = &aux_ctx(c);
+        dctx            = &aux_ctx(c);
+        dctx->clock.on  = c.clock.on;
         SM_CUDA(cudaEventRecord(c.fork, c.stream));
         Ctx *d = dctx;
         c.helper->post([&, d] {
@@ -725,6 +726,20 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
     }
     record(c, 7);
     c.sync_checked();
+    if (c.clock.on) {
+        // the timed launches of this call (the refinement searches' bytes from their count:
+        // per (candidate, source point) 16 + 16 bytes read, 16 + 16 + 3 x 4 written, 8 of
+        // winner atomic)
+        if (ncand > 0) {
+            unsigned long long live = 0;
+            SM_CUDA(cudaMemcpy(&live, c.arena.get<unsigned long long>("icp.live", 1), sizeof(live),
+                               cudaMemcpyDeviceToHost));
+            c.clock.bytes[KernelClock::kCorr] += 88.0 * (double)live;
+        }
+        c.clock.resolve();
+        if (c.aux)
+            c.aux->clock.resolve();
+    }
     // selection walk (ppf.cpp:439-495) and ordering by score (ppf.cpp:498-507)
     std::vector<int> acc;
     for (int i = 0; i < ncand; i++) {
@@ -936,6 +951,43 @@ SM_API int sm_context_synchronize(sm_context c) {
 }
 
 SM_API void *sm_context_stream(sm_context c) { return c ? (void *)c->ctx.stream : nullptr; }
+
+SM_API int sm_context_kernel_clock(sm_context c, int on) {
+    return guarded([&] {
+        if (!c)
+            throw Error(SM_ERR_ARG, "NULL argument");
+        SM_CUDA(cudaSetDevice(c->ctx.device));
+        c->ctx.sync();
+        for (Ctx *x : {&c->ctx, c->ctx.aux.get()}) {
+            if (!x)
+                continue;
+            x->clock.resolve();
+            if (on)
+                x->clock.reset(); // a new count; switching off keeps the totals for reading
+            x->clock.on = on != 0;
+        }
+    });
+}
+
+SM_API int sm_context_kernel_report(sm_context c, int kind, double *ms, double *bytes,
+                                    int64_t *launches) {
+    return guarded([&] {
+        if (!c || !ms || !bytes || !launches)
+            throw Error(SM_ERR_ARG, "NULL argument");
+        if (kind < 0 || kind >= KernelClock::kKinds)
+            throw Error(SM_ERR_ARG, "unknown kernel kind");
+        *ms       = 0.0;
+        *bytes    = 0.0;
+        *launches = 0;
+        for (Ctx *x : {&c->ctx, c->ctx.aux.get()}) {
+            if (!x)
+                continue;
+            *ms += x->clock.ms[kind];
+            *bytes += x->clock.bytes[kind];
+            *launches += x->clock.launches[kind];
+        }
+    });
+}
 
 SM_API int sm_context_workspace_bytes(sm_context c, int64_t *bytes) {
     return guarded([&] {

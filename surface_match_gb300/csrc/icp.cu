@@ -67,6 +67,7 @@ struct Work {
     unsigned long long *win;    // ncand x maxDst
     int                 maxSrc, maxDst;
     float              *trace;  // ncand x kTraceFloats (nullable)
+    unsigned long long *live;   // (candidate, source point) searches of K1 (nullable: not counted)
 };
 
 __device__ __forceinline__ unsigned long long win_key(float d, int i) {
@@ -88,6 +89,8 @@ __global__ void __launch_bounds__(kT, 4) k_corr(Work w, Stage s, int usePrev) {
     const Cand &C = w.cand[ci];
     if (!cand_live(C, s))
         return; // (a candidate that is not live has no nearest points of this stage)
+    if (w.live && blockIdx.x == 0 && threadIdx.x == 0)
+        atomicAdd(w.live, (unsigned long long)s.n);
     for (; i < s.n; i += gridDim.x * kW) {
         const size_t o = (size_t)ci * w.maxSrc + i;
         float4       x, y;
@@ -132,6 +135,8 @@ __global__ void __launch_bounds__(kT) k_corr_tree(Work w, Stage s) {
     const Cand &C  = w.cand[ci];
     if (!cand_live(C, s))
         return;
+    if (w.live && blockIdx.x == 0 && threadIdx.x == 0)
+        atomicAdd(w.live, (unsigned long long)s.n);
     for (int i = blockIdx.x * kT + threadIdx.x; i < s.n; i += gridDim.x * kT) {
         const size_t o  = (size_t)ci * w.maxSrc + i;
         const float4 sp = s.src[i], sn = s.srcN[i];
@@ -575,11 +580,13 @@ void run_stage(Ctx &c, Work &w, const Stage &s, int ncand) {
     k_stage_begin<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand);
     SM_LAUNCH_CHECK();
     for (int it = 0; it < s.iters; it++) {
+        cudaEvent_t t0 = c.clock.begin(c.stream);
         if (tree)
             k_corr_tree<<<gt, kT, 0, c.stream>>>(w, s);
         else
             k_corr<<<gw, kT, 0, c.stream>>>(w, s, it > 0 ? 1 : 0);
         SM_LAUNCH_CHECK();
+        c.clock.end(c.stream, t0, KernelClock::kCorr, 0.0); // bytes from the live count
         k_centroids<<<gr, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
         k_solve<<<gr, kT, 0, c.stream>>>(w, s);
@@ -617,6 +624,11 @@ void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, con
     SM_CUDA(cudaMemsetAsync(w.ctr, 0, (size_t)ncand * sizeof(int), c.stream));
     w.win    = c.arena.get<unsigned long long>("icp.win", (size_t)ncand * w.maxDst);
     w.trace  = trace;
+    w.live   = nullptr;
+    if (c.clock.on) {
+        w.live = c.arena.get<unsigned long long>("icp.live", 1);
+        SM_CUDA(cudaMemsetAsync(w.live, 0, sizeof(unsigned long long), c.stream));
+    }
     SM_CUDA(cudaMemsetAsync(w.win, 0xff, (size_t)ncand * w.maxDst * 8, c.stream));
     k_init<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, cands, ncand, p.voteThreshold, p.sparse);
     SM_LAUNCH_CHECK();

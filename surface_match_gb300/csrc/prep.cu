@@ -958,9 +958,11 @@ static void scan_into(Ctx &c, const int *in, int *out, long long n, int eq, int 
         return;
     }
     const unsigned epoch = scan_state(c, nparts);
+    cudaEvent_t    t0    = c.clock.begin(c.stream);
     k_scan_lookback<<<nparts, kScanBs, 0, c.stream>>>(in, out, n, eq, c.scan.status, c.scan.ticket,
                                                       nparts, epoch, total);
     SM_LAUNCH_CHECK();
+    c.clock.end(c.stream, t0, KernelClock::kScan, 8.0 * (double)n); // 4-byte value in, 4 out
 }
 
 static int scan_impl(Ctx &c, const int *in, int *out, long long n, int eq, const std::string &tag,
@@ -1180,10 +1182,14 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
     SM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device));
     const int gp = (int)std::min<long long>((maxOcc + kSpWarps - 1) / kSpWarps, (long long)nsm * per);
     for (int p = 0; p < 8; p++) {
+        cudaEvent_t t0 = c.clock.begin(c.stream);
         k_sample_phase<<<gp, kSpWarps * 32, 0, c.stream>>>(V, lists, ph, p, rankCnt,
                                                            keptPos, cap, r2, keptFlag, overflow,
                                                            aliveTmp);
         SM_LAUNCH_CHECK();
+        // algorithmic bytes of a sampling: each point's position read and its flag written
+        // once (16 + 4 bytes), spread over the 8 phases
+        c.clock.end(c.stream, t0, KernelClock::kSamplePhase, 20.0 * (double)m / 8.0);
     }
     // the kept points in index order (list order), and the overflow flag, in one round trip
     int *pre   = c.arena.get<int>(tag + ".out.pre", std::max(m, 1));

@@ -84,6 +84,79 @@ private:
     std::thread             th_;
 };
 
+// Opt-in timing of chosen kernels for throughput reports: an event pair around each launch
+// on the launching stream, resolved after the call's final synchronisation, with the
+// launch's algorithmic bytes (host-known, or added from a device count). Off by default:
+// nothing is recorded.
+struct KernelClock {
+    enum Kind { kSamplePhase = 0, kScan = 1, kCorr = 2, kKinds = 3 };
+    bool      on = false;
+    double    ms[kKinds]       = {};
+    double    bytes[kKinds]    = {};
+    long long launches[kKinds] = {};
+    struct Rec {
+        int         kind;
+        double      bytes;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec>         open;
+    std::vector<cudaEvent_t> pool;
+    cudaEvent_t take() {
+        if (!pool.empty()) {
+            cudaEvent_t e = pool.back();
+            pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e = nullptr;
+        SM_CUDA(cudaEventCreate(&e));
+        return e;
+    }
+    // before the launch; nullptr when off
+    cudaEvent_t begin(cudaStream_t s) {
+        if (!on)
+            return nullptr;
+        cudaEvent_t a = take();
+        SM_CUDA(cudaEventRecord(a, s));
+        return a;
+    }
+    // after the launch
+    void end(cudaStream_t s, cudaEvent_t a, int kind, double algBytes) {
+        if (!a)
+            return;
+        cudaEvent_t b = take();
+        SM_CUDA(cudaEventRecord(b, s));
+        open.push_back({kind, algBytes, a, b});
+    }
+    // once the stream has synchronised
+    void resolve() {
+        for (const Rec &r : open) {
+            float t = 0.0f;
+            SM_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
+            ms[r.kind] += t;
+            bytes[r.kind] += r.bytes;
+            launches[r.kind]++;
+            pool.push_back(r.a);
+            pool.push_back(r.b);
+        }
+        open.clear();
+    }
+    void reset() {
+        for (int k = 0; k < kKinds; k++) {
+            ms[k]       = 0.0;
+            bytes[k]    = 0.0;
+            launches[k] = 0;
+        }
+    }
+    ~KernelClock() {
+        for (const Rec &r : open) {
+            cudaEventDestroy(r.a);
+            cudaEventDestroy(r.b);
+        }
+        for (cudaEvent_t e : pool)
+            cudaEventDestroy(e);
+    }
+};
+
 struct Ctx {
     int          device    = 0;
     cudaStream_t stream    = nullptr;
@@ -112,6 +185,7 @@ struct Ctx {
         int                 cap    = 0;
         unsigned            epoch  = 0;
     } scan;
+    KernelClock clock; // opt-in per-launch timing (sm_context_kernel_clock)
     void sync() { SM_CUDA(cudaStreamSynchronize(stream)); }
     // sync, then fail loudly if a bounded device wait of the scans expired
     void sync_checked() {

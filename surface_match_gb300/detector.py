@@ -169,6 +169,24 @@ class Context:
     def synchronize(self):
         _check(_lib.load().sm_context_synchronize(self.handle))
 
+    KERNELS = ("k_sample_phase", "k_scan_lookback", "k_corr")
+
+    def kernel_clock(self, on: bool = True):
+        """Start (counters reset) or stop per-launch event timing of the latency-bound
+        kernels (sm_context_kernel_clock)."""
+        _check(_lib.load().sm_context_kernel_clock(self.handle, 1 if on else 0))
+
+    def kernel_report(self) -> dict:
+        """{kernel: {"ms", "bytes", "launches"}} since the clock was started."""
+        L = _lib.load()
+        out = {}
+        for kind, name in enumerate(self.KERNELS):
+            ms, b, n = C.c_double(), C.c_double(), C.c_int64()
+            _check(L.sm_context_kernel_report(self.handle, kind, C.byref(ms), C.byref(b),
+                                              C.byref(n)))
+            out[name] = {"ms": ms.value, "bytes": b.value, "launches": n.value}
+        return out
+
     def close(self):
         if self.handle:
             _lib.load().sm_context_destroy(self.handle)
