@@ -27,6 +27,11 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# Hardware work queues of the CUDA context (read when it is created, before torch loads):
+# the batching workload's worker streams (up to 24) would otherwise share 8 queues, and
+# kernels of unrelated scenes queued behind each other (measured: 64-scene batch 50 ->
+# 44 ms). A deployment setting of the process, as sm_match_batch's callers would use it.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 METRIC = ("scenes/sec and votes/sec on 1 GB300, batched vs plain GPU vs host CPU; "
           "p50/p99 ms")
