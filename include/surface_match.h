@@ -126,6 +126,10 @@ SM_API int sm_context_kernel_clock(sm_context ctx, int on);
 #define SM_KERNEL_SAMPLE_PHASE 0
 #define SM_KERNEL_SCAN 1
 #define SM_KERNEL_CORR 2
+/* the refinement's other per-iteration launches (durations and launches only) */
+#define SM_KERNEL_FIT 3
+#define SM_KERNEL_RESID 4
+#define SM_KERNEL_UPDATE 5
 SM_API int sm_context_kernel_report(sm_context ctx, int kind, double *ms, double *bytes,
                                     int64_t *launches);
 

@@ -2,31 +2,38 @@
 // (icp.cpp:214-278) with findCorresponds (icp.cpp:123-167), the symmetric point-to-plane
 // step (icp.cpp:39-121) and inliner (util.cpp:628-641).
 //
-// All candidates are refined at once and each candidate's source points are spread over
-// several CTAs, so the whole GPU works even for a handful of candidates. One ICP iteration
-// is five launches: correspondences (one warp per source point on the grid cell walker; per
+// All candidates are refined at once; the searches spread each candidate's source points
+// over many CTAs, so the whole GPU works even for a handful of candidates. One ICP iteration
+// is four launches: correspondences (one warp per source point on the grid cell walker; per
 // scene point the closest source point wins a 64-bit atomicMin of (distance bits, source
 // index), which is the reference's "first minimum in model order" without its O(n*m)
-// grouping scan), pair selection with the pair count and centroids, normal-equation terms
-// with their reduction and the FP64 solve, residual distances, and their reduction + the
-// convergence logic. Every reduction has the same fixed layout: kIcpSlots slots (slot = source index mod
-// kIcpSlots, kIcpBlocks CTAs of 256 per candidate), each a Kahan sum over its source points
-// in ascending order, merged by a fixed tree (warp, CTA, then the last CTA over the CTA
-// partials) - the layout the CPU oracle emulates, so poses are bit-identical. The selection
-// walk over the candidates (numMatches) runs on the host afterwards and only reads the
-// per-candidate results.
+// grouping scan); pair selection, pair count, centroids, normal-equation terms and the FP64
+// solve in one thread-block cluster per candidate; residual distances; and their reduction +
+// the convergence logic in one cluster per candidate. Every reduction has the same fixed
+// layout: kIcpSlots slots (slot = source index mod kIcpSlots, a thread each), each a Kahan sum
+// over its source points in ascending order, merged by a fixed tree (warp, the CTA's warps,
+// then the cluster's CTAs through distributed shared memory) - the layout the CPU oracle
+// emulates, so poses are bit-identical. The selection walk over the candidates
+// (numMatches) runs on the host afterwards and only reads the per-candidate results.
 #include <cfloat>
+
+#include <cooperative_groups.h>
 
 #include "sm_icp.h"
 #include "sm_stages.h"
 
 namespace sm {
 using namespace smd;
+namespace cg = cooperative_groups;
 
 namespace {
 
-constexpr int kT = smi::kIcpThreads; // slots per reduction = threads per CTA
-constexpr int kW = kT / 32;
+constexpr int kT  = 256;              // search CTAs: a warp (or a thread) per point
+constexpr int kW  = kT / 32;
+constexpr int kR  = smi::kIcpThreads; // reduction CTAs: a slot per thread
+constexpr int kRW = kR / 32;
+constexpr int kRC = smi::kIcpBlocks;  // reduction CTAs per candidate: one thread-block cluster
+constexpr int kFitU = 4;              // pairs whose loads a reduction thread has in flight
 constexpr int kTraceIters  = 32;
 constexpr int kTraceFloats = 2 * kTraceIters * 4 + 2;
 
@@ -62,8 +69,6 @@ struct Work {
     float4             *x4;     // ncand x maxSrc: moved source point, w = squared distance
     float4             *n4;     // ncand x maxSrc: rotated source normal
     float              *resid;  // ncand x maxSrc: residual distance of each pair
-    float2             *part;   // ncand x kIcpBlocks x 27: block partials {sum, compensation}
-    int                *ctr;    // ncand: blocks of the current reduction that are done
     unsigned long long *win;    // ncand x maxDst
     int                 maxSrc, maxDst;
     float              *trace;  // ncand x kTraceFloats (nullable)
@@ -182,28 +187,16 @@ __global__ void __launch_bounds__(kT) k_resid_tree(Work w, Stage s) {
     }
 }
 
-// Fixed-layout reduction of W quantities (sm_icp.h): block b of candidate ci holds slots
-// b * 256 + tid; slot t sums, with Kahan, the terms of the pairs i = t, t + kIcpSlots, ...
-// in ascending order; the block merges its slots by the tree (warp shfl_down, then warp 0
-// over the warp partials) and publishes the result; the last block of the candidate to
-// finish merges the kIcpBlocks partials by the block tree. Returns true on that block, whose
-// thread 0 then holds the total in v.
-template <int W, class F>
-__device__ bool slot_reduce(const Work &w, const Stage &s, int ci, F &&term, smi::KahanF (&v)[W],
-                            float (*red)[W][2], int *flag) {
-    const int tid = threadIdx.x;
-    for (int k = 0; k < W; k++)
-        v[k].init();
-    const int *nnId = w.nnId + (size_t)ci * w.maxSrc;
-    for (int i = blockIdx.x * kT + tid; i < s.n; i += smi::kIcpSlots) {
-        if (nnId[i] < 0)
-            continue;
-        float t[W];
-        term(i, t);
-        for (int k = 0; k < W; k++)
-            v[k].add(t[k]);
-    }
-    const int lane = tid & 31, wp = tid >> 5;
+// The reductions of one refinement iteration run in one thread-block cluster of kRC CTAs
+// (kR threads each) per candidate, with the fixed layout of sm_icp.h: slot t (CTA t / kR,
+// thread t % kR) sums, with Kahan, the terms of the pairs i = t, t + kIcpSlots, ... in
+// ascending order; each CTA merges its slots by the tree (warp shfl_down offsets 16..1, then
+// warp 0 over the warp partials, offsets kRW/2..1) and publishes its totals in its shared
+// memory; rank 0 reads the kRC partials through distributed shared memory and merges them
+// by the block tree (offsets kRC/2..1). No global fence or counter between CTAs, and the
+// centroids, the normal equations and the solve share one launch.
+template <int W> __device__ void block_tree(smi::KahanF (&v)[W], float (*red)[W][2]) {
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1)
         for (int k = 0; k < W; k++) {
@@ -220,11 +213,11 @@ __device__ bool slot_reduce(const Work &w, const Stage &s, int ci, F &&term, smi
     __syncthreads();
     if (wp == 0) {
         for (int k = 0; k < W; k++) {
-            v[k].s = lane < kW ? red[lane][k][0] : 0.f;
-            v[k].c = lane < kW ? red[lane][k][1] : 0.f;
+            v[k].s = lane < kRW ? red[lane][k][0] : 0.f;
+            v[k].c = lane < kRW ? red[lane][k][1] : 0.f;
         }
 #pragma unroll
-        for (int off = kW / 2; off >= 1; off >>= 1)
+        for (int off = kRW / 2; off >= 1; off >>= 1)
             for (int k = 0; k < W; k++) {
                 smi::KahanF o;
                 o.s = __shfl_down_sync(0xffffffffu, v[k].s, off);
@@ -232,132 +225,196 @@ __device__ bool slot_reduce(const Work &w, const Stage &s, int ci, F &&term, smi
                 v[k].merge(o);
             }
     }
-    // publish the block's partial; the last block of the candidate merges them all
-    float2 *P = w.part + ((size_t)ci * smi::kIcpBlocks) * smi::kNumSystem;
-    if (tid == 0) {
-        for (int k = 0; k < W; k++)
-            P[(size_t)blockIdx.x * smi::kNumSystem + k] = make_float2(v[k].s, v[k].c);
-        __threadfence();
-        const int done = atomicAdd(&w.ctr[ci], 1);
-        *flag          = done == smi::kIcpBlocks - 1;
-    }
-    __syncthreads();
-    if (!*flag)
-        return false;
-    __threadfence();
-    if (wp == 0) {
-        for (int k = 0; k < W; k++) {
-            const float2 pb = lane < smi::kIcpBlocks
-                                  ? __ldcg(&P[(size_t)lane * smi::kNumSystem + k])
-                                  : make_float2(0.f, 0.f);
-            v[k].s = pb.x;
-            v[k].c = pb.y;
-        }
-#pragma unroll
-        for (int off = smi::kIcpBlocks / 2; off >= 1; off >>= 1)
-            for (int k = 0; k < W; k++) {
-                smi::KahanF o;
-                o.s = __shfl_down_sync(0xffffffffu, v[k].s, off);
-                o.c = __shfl_down_sync(0xffffffffu, v[k].c, off);
-                v[k].merge(o);
-            }
-        if (lane == 0)
-            w.ctr[ci] = 0; // ready for the next reduction of this candidate
-    }
-    return true;
+    __syncthreads(); // red may be reused
 }
 
-// K2: pair selection, pair count and centroids
-__global__ void __launch_bounds__(kT) k_centroids(Work w, Stage s) {
-    __shared__ float red[kW][6][2];
-    __shared__ int   icnt[kW];
-    __shared__ int   flag;
-    const int        ci = blockIdx.y;
-    Cand            &C  = w.cand[ci];
+__device__ __forceinline__ int block_sum_int(int x, int *red) {
+    x = __reduce_add_sync(0xffffffffu, x);
+    if ((threadIdx.x & 31) == 0)
+        red[threadIdx.x >> 5] = x;
+    __syncthreads();
+    int t = 0;
+    for (int k = 0; k < kRW; k++)
+        t += red[k];
+    __syncthreads();
+    return t;
+}
+
+// Rank 0's warp 0: the cluster's kRC published partials (lane r < kRC reads CTA r's through
+// distributed shared memory), merged by the block tree; lane 0 ends with the totals.
+template <int W>
+__device__ void cluster_merge(cg::cluster_group &cl, float (*part)[2], smi::KahanF (&v)[W]) {
+    const int lane = threadIdx.x & 31;
+    for (int k = 0; k < W; k++) {
+        float ps = 0.f, pc = 0.f;
+        if (lane < kRC) {
+            const float *rp = cl.map_shared_rank(&part[k][0], (unsigned)lane);
+            ps              = rp[0];
+            pc              = rp[1];
+        }
+        v[k].s = ps;
+        v[k].c = pc;
+    }
+#pragma unroll
+    for (int off = kRC / 2; off >= 1; off >>= 1)
+        for (int k = 0; k < W; k++) {
+            smi::KahanF o;
+            o.s = __shfl_down_sync(0xffffffffu, v[k].s, off);
+            o.c = __shfl_down_sync(0xffffffffu, v[k].c, off);
+            v[k].merge(o);
+        }
+}
+
+// K2: pair selection (the closest source point per scene point: the atomicMin winner), pair
+// count and centroids, then the normal-equation terms of the pairs and the FP64 solve.
+__global__ void __cluster_dims__(kRC, 1, 1) __launch_bounds__(kR) k_fit(Work w, Stage s) {
+    __shared__ float red[kRW][smi::kNumSystem][2];
+    __shared__ float part[smi::kNumSystem][2]; // this CTA's totals, read by rank 0
+    __shared__ int   ired[kRW];
+    __shared__ int   pcnt;
+    __shared__ float sPQ[6]; // rank 0: the centroids, read by every CTA
+    __shared__ int   sTotal;
+    cg::cluster_group cl = cg::this_cluster();
+    const int         rk = (int)cl.block_rank();
+    const int         ci = blockIdx.x / kRC;
+    Cand             &C  = w.cand[ci];
     if (!cand_live(C, s))
-        return;
-    // keep only the closest source point per scene point (the atomicMin winner); the thread
-    // that drops a pair is the one that reduces it below
+        return; // (the whole cluster: one candidate)
     int          *nnId = w.nnId + (size_t)ci * w.maxSrc;
     const int    *nnR  = w.nnR + (size_t)ci * w.maxSrc;
     const float4 *x4   = w.x4 + (size_t)ci * w.maxSrc;
-    int           cnt  = 0;
-    for (int i = blockIdx.x * kT + threadIdx.x; i < s.n; i += smi::kIcpSlots) {
-        const int r = nnR[i];
-        if (r < 0)
-            continue;
-        if (w.win[(size_t)ci * w.maxDst + r] == win_key(x4[i].w, i))
-            cnt++;
-        else
-            nnId[i] = -1;
-    }
-    cnt = __reduce_add_sync(0xffffffffu, cnt);
-    if ((threadIdx.x & 31) == 0)
-        icnt[threadIdx.x >> 5] = cnt;
-    smi::KahanF v[6];
-    __syncthreads();
-    if (threadIdx.x == 0) { // the block's pair count rides in the spare partial slot 26
-        int t = 0;
-        for (int k = 0; k < kW; k++)
-            t += icnt[k];
-        w.part[((size_t)ci * smi::kIcpBlocks + blockIdx.x) * smi::kNumSystem + 26] =
-            make_float2(__int_as_float(t), 0.f);
-    }
-    const bool last = slot_reduce<6>(w, s, ci,
-                                     [&](int i, float *t) {
-                                         const float4 q = s.dPos[nnId[i]];
-                                         t[0]           = x4[i].x;
-                                         t[1]           = x4[i].y;
-                                         t[2]           = x4[i].z;
-                                         t[3]           = q.x;
-                                         t[4]           = q.y;
-                                         t[5]           = q.z;
-                                     },
-                                     v, red, &flag);
-    if (last && threadIdx.x == 0) {
-        int total = 0;
-        for (int b = 0; b < smi::kIcpBlocks; b++)
-            total += __float_as_int(
-                __ldcg(&w.part[((size_t)ci * smi::kIcpBlocks + b) * smi::kNumSystem + 26]).x);
-        const float fc = (float)total;
-        for (int k = 0; k < 3; k++) {
-            C.Pm[k] = smm::fdiv(v[k].value(), fc);
-            C.Qm[k] = smm::fdiv(v[3 + k].value(), fc);
+    const float4 *n4   = w.n4 + (size_t)ci * w.maxSrc;
+    const int     slot = rk * kR + threadIdx.x;
+    smi::KahanF   m[6];
+    for (int k = 0; k < 6; k++)
+        m[k].init();
+    // a thread's pairs i = slot, slot + kIcpSlots, ... in ascending order, kFitU of them
+    // loaded at once (their loads are independent; the sums still take them in order)
+    int cnt = 0;
+    for (int base = slot; base < s.n; base += kFitU * smi::kIcpSlots) {
+        int                r[kFitU];
+        float4             x[kFitU], q[kFitU];
+        unsigned long long wk[kFitU];
+#pragma unroll
+        for (int u = 0; u < kFitU; u++) {
+            const int i = base + u * smi::kIcpSlots;
+            r[u]        = i < s.n ? nnR[i] : -1;
         }
-        C.cnt = total;
+#pragma unroll
+        for (int u = 0; u < kFitU; u++) {
+            wk[u] = 0ull;
+            if (r[u] >= 0) {
+                x[u]  = x4[base + u * smi::kIcpSlots];
+                wk[u] = w.win[(size_t)ci * w.maxDst + r[u]];
+                q[u]  = s.dPos[r[u]];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kFitU; u++) {
+            const int i = base + u * smi::kIcpSlots;
+            if (r[u] < 0)
+                continue;
+            if (wk[u] != win_key(x[u].w, i)) {
+                nnId[i] = -1; // this thread reads it again below
+                continue;
+            }
+            cnt++;
+            m[0].add(x[u].x);
+            m[1].add(x[u].y);
+            m[2].add(x[u].z);
+            m[3].add(q[u].x);
+            m[4].add(q[u].y);
+            m[5].add(q[u].z);
+        }
     }
-}
-
-// K3: the normal-equation terms of the pairs (computed in place), reduced; FP64 solve
-__global__ void __launch_bounds__(kT) k_solve(Work w, Stage s) {
-    __shared__ float red[kW][smi::kNumSystem][2];
-    __shared__ int   flag;
-    const int        ci = blockIdx.y;
-    Cand            &C  = w.cand[ci];
-    if (!cand_live(C, s) || C.cnt < 6)
+    const int cntB = block_sum_int(cnt, ired);
+    block_tree<6>(m, reinterpret_cast<float (*)[6][2]>(&red[0][0][0]));
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < 6; k++) {
+            part[k][0] = m[k].s;
+            part[k][1] = m[k].c;
+        }
+        pcnt = cntB;
+    }
+    cl.sync(); // the partials are published
+    if (rk == 0 && threadIdx.x < 32) {
+        smi::KahanF mm[6];
+        cluster_merge<6>(cl, part, mm);
+        if (threadIdx.x == 0) {
+            int total = 0;
+            for (int r = 0; r < kRC; r++)
+                total += *cl.map_shared_rank(&pcnt, (unsigned)r);
+            const float fc = (float)total;
+            for (int k = 0; k < 3; k++) {
+                C.Pm[k]    = smm::fdiv(mm[k].value(), fc);
+                C.Qm[k]    = smm::fdiv(mm[3 + k].value(), fc);
+                sPQ[k]     = C.Pm[k];
+                sPQ[3 + k] = C.Qm[k];
+            }
+            C.cnt  = total;
+            sTotal = total;
+        }
+    }
+    cl.sync(); // rank 0 has read the partials and published the centroids
+    const float *pq    = cl.map_shared_rank(sPQ, 0u);
+    const float  Pm0   = pq[0], Pm1 = pq[1], Pm2 = pq[2];
+    const float  Qm0   = pq[3], Qm1 = pq[4], Qm2 = pq[5];
+    const int    total = *cl.map_shared_rank(&sTotal, 0u);
+    cl.sync(); // every CTA has read rank 0's centroids (rank 0 may leave after this)
+    if (total < 6)
         return;
-    const float Pm0 = C.Pm[0], Pm1 = C.Pm[1], Pm2 = C.Pm[2];
-    const float Qm0 = C.Qm[0], Qm1 = C.Qm[1], Qm2 = C.Qm[2];
-    const size_t o0 = (size_t)ci * w.maxSrc;
-    smi::KahanF  v[smi::kNumSystem];
-    const bool   last = slot_reduce<smi::kNumSystem>(
-        w, s, ci,
-        [&](int i, float *t) {
-            const int    id = w.nnId[o0 + i];
-            const float4 x = w.x4[o0 + i], xn = w.n4[o0 + i], q = s.dPos[id], qn = s.dNrm[id];
-            smi::system_terms(x.x - Pm0, x.y - Pm1, x.z - Pm2, q.x - Qm0, q.y - Qm1, q.z - Qm2,
-                              xn.x + qn.x, xn.y + qn.y, xn.z + qn.z, t);
-        },
-        v, red, &flag);
-    if (last && threadIdx.x < 32) {
-        // the totals are on thread 0; warp 0 solves with one row of the system per lane
+    smi::KahanF v[smi::kNumSystem];
+    for (int k = 0; k < smi::kNumSystem; k++)
+        v[k].init();
+    for (int base = slot; base < s.n; base += 2 * smi::kIcpSlots) {
+        int    id[2];
+        float4 x[2], xn[2], q[2], qn[2];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int i = base + u * smi::kIcpSlots;
+            id[u]       = i < s.n ? nnId[i] : -1;
+        }
+#pragma unroll
+        for (int u = 0; u < 2; u++)
+            if (id[u] >= 0) {
+                const int i = base + u * smi::kIcpSlots;
+                x[u]        = x4[i];
+                xn[u]       = n4[i];
+                q[u]        = s.dPos[id[u]];
+                qn[u]       = s.dNrm[id[u]];
+            }
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            if (id[u] < 0)
+                continue;
+            float t[smi::kNumSystem];
+            smi::system_terms(x[u].x - Pm0, x[u].y - Pm1, x[u].z - Pm2, q[u].x - Qm0,
+                              q[u].y - Qm1, q[u].z - Qm2, xn[u].x + qn[u].x, xn[u].y + qn[u].y,
+                              xn[u].z + qn[u].z, t);
+            for (int k = 0; k < smi::kNumSystem; k++)
+                v[k].add(t[k]);
+        }
+    }
+    block_tree<smi::kNumSystem>(v, red);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < smi::kNumSystem; k++) {
+            part[k][0] = v[k].s;
+            part[k][1] = v[k].c;
+        }
+    cl.sync(); // the partials are published
+    if (rk == 0 && threadIdx.x < 32) {
+        cluster_merge<smi::kNumSystem>(cl, part, v);
+        cl.sync(); // (rank 0 has read every partial: the others may leave)
+        // the totals are on lane 0; warp 0 solves with one row of the system per lane
         float sys[smi::kNumSystem];
         for (int k = 0; k < smi::kNumSystem; k++)
             sys[k] = __shfl_sync(0xffffffffu, v[k].value(), 0);
-        const float       pm[3] = {C.Pm[0], C.Pm[1], C.Pm[2]}, qm[3] = {C.Qm[0], C.Qm[1], C.Qm[2]};
+        const float       pm[3] = {Pm0, Pm1, Pm2}, qm[3] = {Qm0, Qm1, Qm2};
         const smi::Pose34 st    = smi::solve_step_warp(sys, pm, qm);
         if (threadIdx.x == 0)
             C.step = st;
+    } else {
+        cl.sync();
     }
 }
 
@@ -382,31 +439,57 @@ __global__ void __launch_bounds__(kT, 5) k_resid(Work w, Stage s) {
     }
 }
 
-// K5: mean residual, the regist loop logic (icp.cpp:233-272), winner reset
-__global__ void __launch_bounds__(kT) k_update(Work w, Stage s) {
-    __shared__ float red[kW][1][2];
-    __shared__ int   flag;
-    const int        ci = blockIdx.y;
-    Cand            &C  = w.cand[ci];
+// K5: mean residual, the regist loop logic (icp.cpp:233-272), winner reset; one cluster per
+// candidate (the same layout as K2), rank 0's thread 0 runs the logic
+__global__ void __cluster_dims__(kRC, 1, 1) __launch_bounds__(kR) k_update(Work w, Stage s) {
+    __shared__ float red[kRW][1][2];
+    __shared__ float part[1][2];
+    cg::cluster_group cl = cg::this_cluster();
+    const int         rk = (int)cl.block_rank();
+    const int         ci = blockIdx.x / kRC;
+    Cand             &C  = w.cand[ci];
     if (!cand_live(C, s))
         return;
-    const int *nnR = w.nnR + (size_t)ci * w.maxSrc;
-    for (int i = blockIdx.x * kT + threadIdx.x; i < s.n; i += smi::kIcpSlots)
+    const int  slot = rk * kR + threadIdx.x;
+    const int *nnR  = w.nnR + (size_t)ci * w.maxSrc;
+    for (int i = slot; i < s.n; i += smi::kIcpSlots)
         if (nnR[i] >= 0)
             w.win[(size_t)ci * w.maxDst + nnR[i]] = ~0ull;
     const int cnt = C.cnt;
     float     mse = FLT_MAX;
     if (cnt >= 6) {
-        const float *D = w.resid + (size_t)ci * w.maxSrc;
+        const float *D    = w.resid + (size_t)ci * w.maxSrc;
+        const int   *nnId = w.nnId + (size_t)ci * w.maxSrc;
         smi::KahanF  v[1];
-        if (!slot_reduce<1>(w, s, ci, [&](int i, float *t) { t[0] = D[i]; }, v, red, &flag))
-            return;
-        if (threadIdx.x == 0)
-            mse = smm::fdiv(v[0].value(), (float)cnt);
-    } else if (blockIdx.x != 0) {
-        return;
+        v[0].init();
+        for (int base = slot; base < s.n; base += kFitU * smi::kIcpSlots) {
+            int   id[kFitU];
+            float d[kFitU];
+#pragma unroll
+            for (int u = 0; u < kFitU; u++) {
+                const int i = base + u * smi::kIcpSlots;
+                id[u]       = i < s.n ? nnId[i] : -1;
+                d[u]        = i < s.n ? D[i] : 0.0f;
+            }
+#pragma unroll
+            for (int u = 0; u < kFitU; u++)
+                if (id[u] >= 0)
+                    v[0].add(d[u]);
+        }
+        block_tree<1>(v, red);
+        if (threadIdx.x == 0) {
+            part[0][0] = v[0].s;
+            part[0][1] = v[0].c;
+        }
+        cl.sync(); // the partials are published
+        if (rk == 0 && threadIdx.x < 32) {
+            cluster_merge<1>(cl, part, v);
+            if (threadIdx.x == 0)
+                mse = smm::fdiv(v[0].value(), (float)cnt);
+        }
+        cl.sync(); // rank 0 has read every partial: the others may leave
     }
-    if (threadIdx.x != 0)
+    if (rk != 0 || threadIdx.x != 0)
         return;
     if (w.trace && C.iterations < kTraceIters) {
         float *t = w.trace + (size_t)ci * kTraceFloats + (s.traceOff * kTraceIters + C.iterations) * 4;
@@ -573,7 +656,7 @@ __global__ void k_finish(Work w, int ncand, int refine, float minScore, int *sta
 
 
 void run_stage(Ctx &c, Work &w, const Stage &s, int ncand) {
-    const dim3 gr(smi::kIcpBlocks, ncand);                    // reductions
+    const dim3 gc(ncand * kRC);                               // reductions: a cluster per candidate
     const dim3 gw(std::max(1, nblocks(s.n, kW)), ncand); // warp kernels: a warp per point
     const dim3 gt(std::max(1, nblocks(s.n, kT)), ncand); // tree searches: a thread per point
     const bool tree = s.tree.nd != nullptr;
@@ -587,17 +670,21 @@ void run_stage(Ctx &c, Work &w, const Stage &s, int ncand) {
             k_corr<<<gw, kT, 0, c.stream>>>(w, s, it > 0 ? 1 : 0);
         SM_LAUNCH_CHECK();
         c.clock.end(c.stream, t0, KernelClock::kCorr, 0.0); // bytes from the live count
-        k_centroids<<<gr, kT, 0, c.stream>>>(w, s);
+        t0 = c.clock.begin(c.stream);
+        k_fit<<<gc, kR, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
-        k_solve<<<gr, kT, 0, c.stream>>>(w, s);
-        SM_LAUNCH_CHECK();
+        c.clock.end(c.stream, t0, KernelClock::kFit, 0.0);
+        t0 = c.clock.begin(c.stream);
         if (tree)
             k_resid_tree<<<gt, kT, 0, c.stream>>>(w, s);
         else
             k_resid<<<gw, kT, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
-        k_update<<<gr, kT, 0, c.stream>>>(w, s);
+        c.clock.end(c.stream, t0, KernelClock::kResid, 0.0);
+        t0 = c.clock.begin(c.stream);
+        k_update<<<gc, kR, 0, c.stream>>>(w, s);
         SM_LAUNCH_CHECK();
+        c.clock.end(c.stream, t0, KernelClock::kUpdate, 0.0);
     }
 }
 
@@ -619,9 +706,6 @@ void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, con
     w.x4     = c.arena.get<float4>("icp.x4", (size_t)ncand * w.maxSrc);
     w.n4     = c.arena.get<float4>("icp.n4", (size_t)ncand * w.maxSrc);
     w.resid  = c.arena.get<float>("icp.resid", (size_t)ncand * w.maxSrc);
-    w.part   = c.arena.get<float2>("icp.part", (size_t)ncand * smi::kIcpBlocks * smi::kNumSystem);
-    w.ctr    = c.arena.get<int>("icp.ctr", ncand);
-    SM_CUDA(cudaMemsetAsync(w.ctr, 0, (size_t)ncand * sizeof(int), c.stream));
     w.win    = c.arena.get<unsigned long long>("icp.win", (size_t)ncand * w.maxDst);
     w.trace  = trace;
     w.live   = nullptr;

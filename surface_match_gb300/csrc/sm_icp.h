@@ -8,7 +8,8 @@
 // summation layout, so the GPU and the oracle produce bit-identical poses: kIcpSlots
 // strided partial sums (slot = source index mod kIcpSlots, ascending within a slot), merged
 // by fixed binary trees - within each group of 32 slots (offsets 16..1), over the
-// kIcpThreads / 32 groups of a block (offsets 4..1), then over the kIcpBlocks blocks.
+// kIcpThreads / 32 groups of a block (offsets 8..1), then over the kIcpBlocks blocks
+// (offsets 2..1; a candidate's blocks form one thread-block cluster).
 #pragma once
 
 #include "sm_linalg.h"
@@ -16,8 +17,8 @@
 
 namespace smi {
 
-constexpr int kIcpThreads = 256;                       // ICP CTA size
-constexpr int kIcpBlocks  = 8;                         // CTAs per candidate and reduction
+constexpr int kIcpThreads = 512;                       // ICP reduction CTA size
+constexpr int kIcpBlocks  = 4;                         // CTAs per candidate and reduction
 constexpr int kIcpSlots   = kIcpThreads * kIcpBlocks;  // strided partial sums
 
 // Kahan-compensated FP32 accumulator; value() = s - c.

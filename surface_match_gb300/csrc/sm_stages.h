@@ -89,7 +89,15 @@ private:
 // launch's algorithmic bytes (host-known, or added from a device count). Off by default:
 // nothing is recorded.
 struct KernelClock {
-    enum Kind { kSamplePhase = 0, kScan = 1, kCorr = 2, kKinds = 3 };
+    enum Kind {
+        kSamplePhase = 0,
+        kScan        = 1,
+        kCorr        = 2,
+        kFit         = 3, // the refinement's other per-iteration launches: time only
+        kResid       = 4,
+        kUpdate      = 5,
+        kKinds       = 6
+    };
     bool      on = false;
     double    ms[kKinds]       = {};
     double    bytes[kKinds]    = {};

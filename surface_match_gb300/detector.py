@@ -169,7 +169,7 @@ class Context:
     def synchronize(self):
         _check(_lib.load().sm_context_synchronize(self.handle))
 
-    KERNELS = ("k_sample_phase", "k_scan_lookback", "k_corr")
+    KERNELS = ("k_sample_phase", "k_scan_lookback", "k_corr", "k_fit", "k_resid", "k_update")
 
     def kernel_clock(self, on: bool = True):
         """Start (counters reset) or stop per-launch event timing of the latency-bound
