@@ -638,7 +638,7 @@ def main():
                           "read, moved point and normal, 3 indices written, winner atomic"}
     kernel_rooflines = []
     for name, r in clock_rep.items():
-        if r["launches"] and r["ms"] > 0:
+        if name in per_unit and r["launches"] and r["ms"] > 0:
             ach = r["bytes"] / (r["ms"] / 1000.0) / 1e9
             kernel_rooflines.append({
                 "kernel": name, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
