@@ -306,6 +306,13 @@ SM_API const char *sm_version(void);
 /* Number of CUDA kernels the library has launched so far in this process. */
 SM_API int64_t sm_launch_count(void);
 
+/* Page-locked (pinned) host memory for scene input (filePLY.cpp's reader fills pageable
+ * vectors; no counterpart in the reference): a scene read into such a buffer is uploaded by
+ * the matching calls as an asynchronous DMA on the context's stream instead of a staged
+ * copy. *out = NULL for bytes == 0. Free with sm_host_free. */
+SM_API int sm_host_alloc(int64_t bytes, void **out);
+SM_API int sm_host_free(void *p);
+
 /* Measured rate of the vote stage's bounding operation on `device`: shared-memory atomic
  * increments of 16-bit counters at pseudo-random cells of a 48 KB accumulator, 512-thread
  * CTAs, two per SM (the vote kernel's shape). Writes increments per second (whole GPU).

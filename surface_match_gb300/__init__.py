@@ -6,9 +6,10 @@ the C++ Detector over it, and this package is the Python mirror of the same API.
 """
 from .detector import (Context, Detector, MatchParam, MatchResult, PointCloud,  # noqa: F401
                        RangeError, Server, TrainParam, estimateNormalMLS, match_batch,
-                       probe_vote_atomics)
+                       pinned_empty, probe_vote_atomics)
 from .ply import read_ply, write_ply  # noqa: F401
 
 __all__ = ["Context", "Detector", "MatchParam", "MatchResult", "PointCloud", "RangeError",
-           "Server", "TrainParam", "estimateNormalMLS", "match_batch", "probe_vote_atomics",
+           "Server", "TrainParam", "estimateNormalMLS", "match_batch", "pinned_empty",
+           "probe_vote_atomics",
            "read_ply", "write_ply"]

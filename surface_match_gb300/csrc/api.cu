@@ -883,6 +883,31 @@ SM_API const char *sm_last_error(void) { return g_lastError.c_str(); }
 SM_API const char *sm_version(void) { return "surface_match_gb300 0.1 (sm_103a)"; }
 SM_API int64_t     sm_launch_count(void) { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
 
+SM_API int sm_host_alloc(int64_t bytes, void **out) {
+    return guarded([&] {
+        if (!out || bytes < 0)
+            throw Error(SM_ERR_ARG, "invalid host allocation arguments");
+        *out = nullptr;
+        if (bytes == 0)
+            return;
+        void *p = nullptr;
+        const cudaError_t e = cudaHostAlloc(&p, (size_t)bytes, cudaHostAllocPortable);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            throw Error(e == cudaErrorMemoryAllocation ? SM_ERR_NOMEM : SM_ERR_CUDA,
+                        std::string("page-locked host allocation failed: ") + cudaGetErrorString(e));
+        }
+        *out = p;
+    });
+}
+
+SM_API int sm_host_free(void *p) {
+    return guarded([&] {
+        if (p)
+            SM_CUDA(cudaFreeHost(p));
+    });
+}
+
 SM_API void sm_train_param_default(sm_train_param *p) {
     if (p)
         *p = sm_train_param{0.04f, 30, 0.01f, 10, 1};

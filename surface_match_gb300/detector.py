@@ -30,6 +30,36 @@ def _check(status):
     raise RuntimeError(msg)
 
 
+class _PinnedBlock:
+    """Page-locked host memory from sm_host_alloc, freed with the last array that views it."""
+
+    def __init__(self, nbytes: int):
+        p = C.c_void_p()
+        _check(_lib.load().sm_host_alloc(int(nbytes), C.byref(p)))
+        self.ptr = p.value
+        self.nbytes = int(nbytes)
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            try:
+                _lib.load().sm_host_free(C.c_void_p(self.ptr))
+            except Exception:
+                pass
+            self.ptr = None
+
+
+def pinned_empty(shape, dtype=np.float32) -> np.ndarray:
+    """A numpy array in page-locked host memory (sm_host_alloc): scenes read into it are
+    uploaded by matchScene as an asynchronous DMA on the context's stream."""
+    dt = np.dtype(dtype)
+    n = int(np.prod(shape))
+    nbytes = max(n * dt.itemsize, 1)
+    blk = _PinnedBlock(nbytes)
+    buf = (C.c_char * nbytes).from_address(blk.ptr)
+    buf._sm_pinned_block = blk  # the array's buffer keeps the block alive
+    return np.frombuffer(buf, dtype=dt, count=n).reshape(shape)
+
+
 def probe_vote_atomics(device: int = 0) -> float:
     """Measured shared-memory atomic increments per second of the vote kernel's access
     pattern on `device` (include/surface_match.h sm_probe_vote_atomics)."""

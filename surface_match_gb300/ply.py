@@ -87,9 +87,10 @@ def _triangulate(pts, idx, out):
     return True
 
 
-def read_ply(path) -> PointCloud:
+def read_ply(path, pinned: bool = False) -> PointCloud:
     """PointCloud with point (n, 3) float32, normal (n, 3) or None, face (m, 3) int32 or
-    None."""
+    None. With `pinned`, point and normal sit in page-locked host memory (pinned_empty), so
+    matchScene uploads them as an asynchronous DMA."""
     try:
         f = open(path, "rb")
     except OSError:
@@ -160,6 +161,15 @@ def read_ply(path) -> PointCloud:
                 raise ValueError("Read PLY failed: A polygon in the mesh could not be "
                                  "decomposed into triangles.")
     face = np.array(faces, np.int32).reshape(-1, 3) if faces else None
+    if pinned:
+        from .detector import pinned_empty
+        p = pinned_empty(point.shape, np.float32)
+        p[...] = point
+        point = p
+        if normal is not None:
+            q = pinned_empty(normal.shape, np.float32)
+            q[...] = normal
+            normal = q
     return PointCloud(point, normal, None, face)
 
 
