@@ -24,8 +24,8 @@
 //      std::sort (util.cpp:487, ppf.cpp:498); pose list in keypoint order (the reference
 //      appends under omp critical, ppf.cpp:407).
 //   Accumulations: centroid/covariance in FP32 Kahan per point; ICP sums in FP32 Kahan over
-//      256 strided partials merged by a fixed tree (the GPU's layout). ORC_PREC_FP64 runs
-//      the same pipeline with FP64 accumulation (the precision reference).
+//      smi::kIcpSlots strided partials merged by a fixed tree (the GPU's layout, sm_icp.h).
+//      ORC_PREC_FP64 runs the same pipeline with FP64 accumulation (the precision reference).
 #include "../surface_match_gb300/csrc/sm_grid.h"
 #include "../surface_match_gb300/csrc/sm_icp.h"
 #include "../surface_match_gb300/csrc/sm_linalg.h"
