@@ -436,6 +436,11 @@ def run_precision(args):
     print(json.dumps(line), flush=True)
 
 
+def _lib_tuned_block(device):
+    from surface_match_gb300 import _lib
+    return int(_lib.load().sm_vote_tuned_block(int(device)))
+
+
 def vote_traffic():
     """DRAM bytes (read + write) of one k_vote_acc launch of this workload, from the ncu capture
     summarised in profiles/k_vote_acc_<workload>.md (its line "dram_bytes_per_launch = N");
@@ -692,6 +697,12 @@ def main():
                                     "running beside the vote kernel (launch_ms above is "
                                     "measured in the timed, overlapped steps)"}},
             "kernel_rooflines": kernel_rooflines,
+            "vote_launch_tuning": {
+                "threads_per_cta": _lib_tuned_block(local),
+                "candidates": [256, 512, 1024],
+                "how": "the library's launch tuner: the first call on the device with at least "
+                       "512 keypoints times each size twice on its own data (CUDA events) and "
+                       "keeps the fastest for the process"},
             "vote_stage_ms": {"pairs_probe_k_ppf": statistics.mean(ppf_ms),
                               "accumulate_k_vote_acc": vk,
                               "stage": stats["ms"][3]},

@@ -901,6 +901,8 @@ SM_API int sm_host_alloc(int64_t bytes, void **out) {
     });
 }
 
+SM_API int sm_vote_tuned_block(int device) { return vote_tuned_block(device); }
+
 SM_API int sm_host_free(void *p) {
     return guarded([&] {
         if (p)

@@ -16,7 +16,9 @@
 //  6. k_vote_acc: one CTA per keypoint votes its hits into a shared-memory (reference
 //     point x angle bin) accumulator - 16-bit counters when the keypoint's vote count
 //     allows - then extracts peaks, the top three candidates and their poses.
+#include <atomic>
 #include <cstdlib>
+#include <mutex>
 
 #include "sm_stages.h"
 #include "sm_vote.cuh"
@@ -31,7 +33,9 @@ namespace {
 
 constexpr int kKpWarps   = 8;    // keypoints per CTA of the radius kernel
 constexpr int kTile      = 1024; // candidates per shared-memory tile
-constexpr int kAccBs     = 512;
+// vote accumulation CTA sizes the launch tuner chooses between (every one computes the same
+// accumulators, peaks and candidates)
+constexpr int kAccShapes[3] = {256, 512, 1024};
 constexpr int kHitChunk  = 1024; // hits staged in shared memory per round
 constexpr int kLptBins   = 40;
 
@@ -289,12 +293,13 @@ __global__ void k_lpt(const unsigned long long *__restrict__ votes, int K, int *
         order[atomicAdd(&start[lpt_bin(votes[c])], 1)] = c;
 }
 
-__global__ void __launch_bounds__(kAccBs, 2) k_vote_acc(VoteArgs a, PipeBufs b) {
+template <int BS>
+__global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : 2) k_vote_acc(VoteArgs a, PipeBufs b) {
     extern __shared__ uint32_t acc[];
     __shared__ int       hOff[kHitChunk], hCnt[kHitChunk], cPre[kHitChunk + 1];
     __shared__ float     hAs[kHitChunk], hAsT[kHitChunk];
     __shared__ int       sh[33];
-    __shared__ Cand      wc[kAccBs / 32][3];
+    __shared__ Cand      wc[BS / 32][3];
     __shared__ unsigned long long shash;
 
     const int  c    = b.order[blockIdx.x];
@@ -320,13 +325,13 @@ __global__ void __launch_bounds__(kAccBs, 2) k_vote_acc(VoteArgs a, PipeBufs b) 
         const int r1     = min(r0 + chunk, a.ns);
         const int nElem  = (r1 - r0) * a.A;
         const int nWords = narrow ? (nElem + 1) >> 1 : nElem;
-        for (int i = tid; i < nWords; i += kAccBs)
+        for (int i = tid; i < nWords; i += BS)
             acc[i] = 0u;
         for (int h0 = 0; h0 < nH; h0 += kHitChunk) {
             const int n = min(kHitChunk, nH - h0);
             __syncthreads();
             int T = 0;
-            for (int j0 = 0; j0 < n; j0 += kAccBs) {
+            for (int j0 = 0; j0 < n; j0 += BS) {
                 const int j   = j0 + tid;
                 int       nit = 0;
                 if (j < n) {
@@ -356,7 +361,65 @@ __global__ void __launch_bounds__(kAccBs, 2) k_vote_acc(VoteArgs a, PipeBufs b) 
     finish_keypoint(a, c, b.rt[c], top, myHash, info.x, nH, V, bound, wc, &shash);
 }
 
+const void *vote_acc_fn(int shape) {
+    return shape == 0 ? (const void *)k_vote_acc<kAccShapes[0]>
+                      : shape == 1 ? (const void *)k_vote_acc<kAccShapes[1]>
+                                   : (const void *)k_vote_acc<kAccShapes[2]>;
+}
+
+// Dynamic shared memory of the accumulator for launch shape `shape` (its static shared
+// memory differs a little by CTA size); 0 when it does not fit.
+size_t vote_acc_smem(int shape, const Ctx &c, VoteArgs &a) {
+    int optin = 0, perSM = 0;
+    SM_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));
+    SM_CUDA(cudaDeviceGetAttribute(&perSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c.device));
+    cudaFuncAttributes fa;
+    SM_CUDA(cudaFuncGetAttributes(&fa, vote_acc_fn(shape)));
+    const size_t smem = acc_sizing(a.ns, a.A, (long long)fa.sharedSizeBytes, optin, perSM,
+                                   &a.refChunk, &a.refChunkWide);
+    if (smem && smem > allow_dynamic_smem(vote_acc_fn(shape), c.device))
+        return 0;
+    return smem;
+}
+
+void launch_vote_acc(int shape, const Ctx &c, const VoteArgs &a, const PipeBufs &b, int K,
+                     size_t smem) {
+    if (shape == 0)
+        k_vote_acc<kAccShapes[0]><<<K, kAccShapes[0], smem, c.stream>>>(a, b);
+    else if (shape == 1)
+        k_vote_acc<kAccShapes[1]><<<K, kAccShapes[1], smem, c.stream>>>(a, b);
+    else
+        k_vote_acc<kAccShapes[2]><<<K, kAccShapes[2], smem, c.stream>>>(a, b);
+    SM_LAUNCH_CHECK();
+}
+
+// The launch tuner: per device, the vote accumulation CTA size measured fastest on the first
+// call with at least kTuneMinK keypoints (each shape timed twice with CUDA events on the
+// call's own data, the faster of the two runs kept), then used for every later call.
+// SM_VOTE_SHAPE=256|512|1024 in the environment fixes the shape instead (tests).
+constexpr int    kTuneMinK = 512;
+std::atomic<int> g_voteShape[64] = {};     // 0 untuned, else 1 + shape index
+std::mutex       g_tuneMu;
+
+int forced_vote_shape() {
+    const char *e = std::getenv("SM_VOTE_SHAPE");
+    if (!e)
+        return -1;
+    const int v = std::atoi(e);
+    for (int s = 0; s < 3; s++)
+        if (kAccShapes[s] == v)
+            return s;
+    return -1;
+}
+
 } // namespace
+
+int vote_tuned_block(int device) {
+    if (device < 0 || device >= 64)
+        return 0;
+    const int t = g_voteShape[device].load();
+    return t > 0 ? kAccShapes[t - 1] : 0;
+}
 
 void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const int *kp, int K,
           const int *nbrOff, const int *nbrIds, const int *cand, int ncand, float minScore,
@@ -394,13 +457,12 @@ void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const in
 
     const bool csr = nbrOff != nullptr;
 
-    int optin = 0, perSM = 0;
-    SM_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));
-    SM_CUDA(cudaDeviceGetAttribute(&perSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c.device));
-    cudaFuncAttributes fa;
-    SM_CUDA(cudaFuncGetAttributes(&fa, k_vote_acc));
-    const size_t smem = acc_sizing(a.ns, a.A, (long long)fa.sharedSizeBytes, optin, perSM,
-                                   &a.refChunk, &a.refChunkWide);
+    // the accumulation's launch shape: forced, tuned on this device, or the default (512)
+    const int dev    = c.device >= 0 && c.device < 64 ? c.device : 0;
+    const int forced = forced_vote_shape();
+    int       shape  = forced >= 0 ? forced : (g_voteShape[dev].load() > 0 ? g_voteShape[dev].load() - 1 : 1);
+    const bool tune  = forced < 0 && g_voteShape[dev].load() == 0 && K >= kTuneMinK;
+    size_t     smem  = vote_acc_smem(shape, c, a);
     if (!smem)
         throw Error(SM_ERR_CAPACITY, "featAngleResolution too large for the vote accumulator");
 
@@ -441,11 +503,42 @@ void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const in
     SM_CUDA(cudaEventRecord(c.ev[11], c.stream));
     k_lpt<<<1, 1024, 0, c.stream>>>(b.votes, K, b.order);
     SM_LAUNCH_CHECK();
+    if (tune) {
+        // every shape computes the same outputs: time each on this call's keypoints, keep
+        // the fastest for the device (one process-wide decision, taken once)
+        std::lock_guard<std::mutex> lk(g_tuneMu);
+        if (g_voteShape[dev].load() == 0) {
+            cudaEvent_t e0, e1;
+            SM_CUDA(cudaEventCreate(&e0));
+            SM_CUDA(cudaEventCreate(&e1));
+            float best[3] = {1e30f, 1e30f, 1e30f};
+            for (int rep = 0; rep < 2; rep++)
+                for (int sh = 0; sh < 3; sh++) {
+                    VoteArgs     at = a;
+                    const size_t sm = vote_acc_smem(sh, c, at);
+                    if (!sm)
+                        continue;
+                    SM_CUDA(cudaEventRecord(e0, c.stream));
+                    launch_vote_acc(sh, c, at, b, K, sm);
+                    SM_CUDA(cudaEventRecord(e1, c.stream));
+                    SM_CUDA(cudaEventSynchronize(e1));
+                    float ms = 0.0f;
+                    SM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                    best[sh] = std::min(best[sh], ms);
+                }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            int pick = 1;
+            for (int sh = 0; sh < 3; sh++)
+                if (best[sh] < best[pick])
+                    pick = sh;
+            g_voteShape[dev].store(1 + pick);
+        }
+        shape = g_voteShape[dev].load() - 1;
+        smem  = vote_acc_smem(shape, c, a);
+    }
     SM_CUDA(cudaEventRecord(c.ev[12], c.stream));
-    if (smem > allow_dynamic_smem((const void *)k_vote_acc, c.device))
-        throw Error(SM_ERR_CAPACITY, "shared-memory request above the device limit");
-    k_vote_acc<<<K, kAccBs, smem, c.stream>>>(a, b);
-    SM_LAUNCH_CHECK();
+    launch_vote_acc(shape, c, a, b, K, smem);
     SM_CUDA(cudaEventRecord(c.ev[13], c.stream));
 }
 

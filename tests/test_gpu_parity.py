@@ -275,3 +275,44 @@ def test_sampler_heavy_cells_and_wide_extent_bit_exact(data):
     np.testing.assert_array_equal(det.debug(0), r.sampled)
     np.testing.assert_array_equal(det.debug(1), r.keypoints)
     np.testing.assert_array_equal(det.debug(2), r.resampled)
+
+
+@pytest.mark.parametrize("shape", ["256", "512", "1024"])
+def test_vote_launch_shapes_give_identical_results(data, oracle_grid, monkeypatch, shape):
+    """The voting stage's launch tuner picks among CTA sizes that must not change anything:
+    with each size forced, per-keypoint statistics (with the accumulator fingerprints),
+    candidates, the pose list and the final poses equal the oracle's."""
+    from surface_match_gb300 import Detector, MatchParam, PointCloud
+    mc, sc = data
+    _, r = oracle_grid
+    monkeypatch.setenv("SM_VOTE_SHAPE", shape)
+    det = Detector()
+    det.trainModel(PointCloud(mc.xyz, mc.normal), SD)
+    poses, scores = det.matchScene(PointCloud(sc.cloud.xyz, None, sc.viewpoint), SD, KP, MS,
+                                   MatchParam(numMatches=8))
+    np.testing.assert_array_equal(det.debug(7), r.kp_stats)
+    np.testing.assert_array_equal(det.debug(8), r.kp_cands)
+    np.testing.assert_array_equal(det.debug(9).view(np.uint32), r.pose_list.view(np.uint32))
+    np.testing.assert_array_equal(scores, r.scores)
+
+
+def test_vote_launch_tuner_picks_a_shape_once():
+    """On a scene with at least 512 keypoints the tuner times the CTA sizes once per device
+    and reports its choice; later calls keep it."""
+    import os
+    from surface_match_gb300 import Detector, MatchParam, PointCloud, _lib, synth
+    if os.environ.get("SM_VOTE_SHAPE"):
+        pytest.skip("launch size fixed by the environment")
+    model, _, _ = synth.gear_model(20000, seed=7)
+    scene = synth.scene_large(seed=2, model=synth.gear_model(20000, seed=7))
+    det = Detector()
+    det.trainModel(PointCloud(model.xyz, model.normal), 0.03)
+    det.matchScene(PointCloud(scene.cloud.xyz, None, scene.viewpoint), 0.03, 0.2, 0.2,
+                   MatchParam(numMatches=16))
+    assert det.last_stats["n_keypoints"] >= 512
+    L = _lib.load()
+    first = L.sm_vote_tuned_block(0)
+    assert first in (256, 512, 1024)
+    det.matchScene(PointCloud(scene.cloud.xyz, None, scene.viewpoint), 0.03, 0.2, 0.2,
+                   MatchParam(numMatches=16))
+    assert L.sm_vote_tuned_block(0) == first
