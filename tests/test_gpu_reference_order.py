@@ -4,7 +4,8 @@ oracle's reference-order pipeline, which restates the reference single-threaded 
 vendored nanoflann's orders. Bit-exact stage by stage on the tiny scene; at the full sizes
 of the workloads (the small scene of about 108k points and the large scene of about 0.92M
 points) the samples, keypoints, per-keypoint vote statistics, candidates and final poses
-and scores are bit-exact."""
+and scores are bit-exact - in the reference order against the oracle's reference-order mode,
+and in the grid order against its grid-order mode."""
 import numpy as np
 import pytest
 
@@ -63,12 +64,14 @@ def test_reference_order_stages_bit_exact(tiny):
     np.testing.assert_array_equal(poses[:, :3, :].reshape(len(scores), -1), r.results[:, :12])
 
 
+@pytest.mark.parametrize("order", ["reference", "grid"])
 @pytest.mark.parametrize("which", ["small", "large"])
-def test_reference_order_workload_scenes_bit_exact(which):
-    """The two single-scene workloads at full size: the 3-gear scene (about 108k points,
-    trainModel(0.04), matchScene(0.04, 0.1, 0.2)) and the 10-gear scene (about 0.92M points,
-    trainModel(0.03), matchScene(0.03, 0.2, 0.2)), numMatches 16."""
-    from oracle import MODE_REF, MatchParam as OMP, Oracle
+def test_workload_scenes_bit_exact(which, order):
+    """The two single-scene workloads at full size, in both search orders against the
+    oracle's matching mode: the 3-gear scene (about 108k points, trainModel(0.04),
+    matchScene(0.04, 0.1, 0.2)) and the 10-gear scene (about 0.92M points, trainModel(0.03),
+    matchScene(0.03, 0.2, 0.2)), numMatches 16."""
+    from oracle import MODE_GRID, MODE_REF, MatchParam as OMP, Oracle
     from surface_match_gb300 import Detector, MatchParam, PointCloud, synth
     model = synth.gear_model(20000, seed=7)
     if which == "small":
@@ -76,10 +79,10 @@ def test_reference_order_workload_scenes_bit_exact(which):
     else:
         sc, sd, kp = synth.scene_large(seed=2, model=model), 0.03, 0.2
     mc = model[0]
-    o = Oracle(mode=MODE_REF, threads=16)
+    o = Oracle(mode=MODE_REF if order == "reference" else MODE_GRID, threads=16)
     om = o.train(mc.xyz, mc.normal, sd)
     r = o.match(om, sc.cloud.xyz, None, sc.viewpoint, sd, kp, MS, OMP(numMatches=16))
-    det = Detector(search_order="reference")
+    det = Detector(search_order=order)
     det.trainModel(PointCloud(mc.xyz, mc.normal), sd)
     d = det.download()
     np.testing.assert_array_equal(d["keys"], om.keys)
