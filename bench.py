@@ -436,9 +436,12 @@ def run_precision(args):
     print(json.dumps(line), flush=True)
 
 
-def _lib_tuned_block(device):
+def _lib_tuned_shape(device):
+    import ctypes as C
     from surface_match_gb300 import _lib
-    return int(_lib.load().sm_vote_tuned_block(int(device)))
+    t, p = C.c_int(0), C.c_int(0)
+    _lib.load().sm_vote_tuned_shape(int(device), C.byref(t), C.byref(p))
+    return {"threads_per_cta": t.value, "persistent": bool(p.value)}
 
 
 def vote_traffic():
@@ -698,10 +701,11 @@ def main():
                                     "measured in the timed, overlapped steps)"}},
             "kernel_rooflines": kernel_rooflines,
             "vote_launch_tuning": {
-                "threads_per_cta": _lib_tuned_block(local),
-                "candidates": [256, 512, 1024],
+                "chosen": _lib_tuned_shape(local),
+                "candidates": "256/512/1024 threads per CTA x (a CTA per keypoint | a "
+                              "persistent grid taking keypoints from a device work counter)",
                 "how": "the library's launch tuner: the first call on the device with at least "
-                       "512 keypoints times each size twice on its own data (CUDA events) and "
+                       "512 keypoints times each shape twice on its own data (CUDA events) and "
                        "keeps the fastest for the process"},
             "vote_stage_ms": {"pairs_probe_k_ppf": statistics.mean(ppf_ms),
                               "accumulate_k_vote_acc": vk,

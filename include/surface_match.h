@@ -314,11 +314,13 @@ SM_API int sm_host_alloc(int64_t bytes, void **out);
 SM_API int sm_host_free(void *p);
 
 /* The voting stage's launch tuner: on each device the first call with at least 512
- * keypoints times the vote accumulation kernel at 256, 512 and 1024 threads per CTA on its
- * own data (every size computes the same votes, peaks and candidates) and keeps the fastest
- * for the process. Returns that size, 0 while untuned. SM_VOTE_SHAPE=256|512|1024 in the
- * environment fixes the size instead. */
-SM_API int sm_vote_tuned_block(int device);
+ * keypoints times the vote accumulation kernel in six launch shapes on its own data - 256,
+ * 512 or 1024 threads per CTA, one CTA per keypoint or a persistent resident grid taking
+ * keypoints from a device work counter in LPT order (every shape computes the same votes,
+ * peaks and candidates) - and keeps the fastest for the process. Writes the chosen CTA size
+ * (0 while untuned) and whether it is the persistent grid. SM_VOTE_SHAPE=256|512|1024, with a
+ * trailing 'p' for the persistent grid, in the environment fixes the shape instead. */
+SM_API int sm_vote_tuned_shape(int device, int *threads_per_cta, int *persistent);
 
 /* Measured rate of the vote stage's bounding operation on `device`: shared-memory atomic
  * increments of 16-bit counters at pseudo-random cells of a 48 KB accumulator, 512-thread

@@ -98,7 +98,7 @@ _SIGNATURES = {
     "sm_launch_count": (C.c_int64, []),
     "sm_host_alloc": (C.c_int, [C.c_int64, C.POINTER(_vp)]),
     "sm_host_free": (C.c_int, [_vp]),
-    "sm_vote_tuned_block": (C.c_int, [C.c_int]),
+    "sm_vote_tuned_shape": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "sm_probe_vote_atomics": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
     "sm_estimate_normals_mls": (C.c_int, [_vp, _f32p, _f32p, C.c_int64, _i64p, C.c_int64,
                                           C.c_float, C.c_int, C.c_int, _f32p, _f32p, _f32p]),

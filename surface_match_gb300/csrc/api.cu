@@ -901,7 +901,13 @@ SM_API int sm_host_alloc(int64_t bytes, void **out) {
     });
 }
 
-SM_API int sm_vote_tuned_block(int device) { return vote_tuned_block(device); }
+SM_API int sm_vote_tuned_shape(int device, int *threads_per_cta, int *persistent) {
+    return guarded([&] {
+        if (!threads_per_cta || !persistent)
+            throw Error(SM_ERR_ARG, "NULL argument");
+        *threads_per_cta = vote_tuned_shape(device, persistent);
+    });
+}
 
 SM_API int sm_host_free(void *p) {
     return guarded([&] {

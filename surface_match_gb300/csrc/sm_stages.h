@@ -368,8 +368,8 @@ struct IcpParams {
     float rejectDist, sampleStep, reSampleStep, scoreDist, voteThreshold, minScore;
 };
 // Threads per CTA of the vote accumulation chosen by its launch tuner on `device` (0 while
-// untuned; vote_pipe.cu).
-int vote_tuned_block(int device);
+// untuned), and whether it is the persistent grid (vote_pipe.cu).
+int vote_tuned_shape(int device, int *persistent);
 // ICP refinement + scoring of every candidate in parallel. Outputs per candidate: status,
 // score, refined pose (12 floats).
 void icp_all(Ctx &c, const Model &m, const IcpScene &s, const IcpParams &p, const float *cands,

@@ -18,6 +18,7 @@
 //     allows - then extracts peaks, the top three candidates and their poses.
 #include <atomic>
 #include <cstdlib>
+#include <cstring>
 #include <mutex>
 
 #include "sm_stages.h"
@@ -33,9 +34,11 @@ namespace {
 
 constexpr int kKpWarps   = 8;    // keypoints per CTA of the radius kernel
 constexpr int kTile      = 1024; // candidates per shared-memory tile
-// vote accumulation CTA sizes the launch tuner chooses between (every one computes the same
-// accumulators, peaks and candidates)
-constexpr int kAccShapes[3] = {256, 512, 1024};
+// vote accumulation launch shapes the launch tuner chooses between - CTA size, and one CTA per
+// keypoint or a persistent grid that takes keypoints from a device counter in LPT order;
+// every one computes the same accumulators, peaks and candidates
+constexpr int kAccBs[3]  = {256, 512, 1024};
+constexpr int kAccShapes = 6; // shape s: CTA size kAccBs[s % 3], persistent when s >= 3
 constexpr int kHitChunk  = 1024; // hits staged in shared memory per round
 constexpr int kLptBins   = 40;
 
@@ -51,6 +54,7 @@ struct PipeBufs {
     unsigned long long *votes;   // K
     unsigned long long *bound;   // K: sum of the hits' bucket multiplicities (cell bound)
     int                *order;   // K
+    int                *next;    // persistent accumulation: the next place in `order` to take
 };
 
 // flags: bit 0 = keypoint votes, bit 1 = its normal is not finite
@@ -293,7 +297,9 @@ __global__ void k_lpt(const unsigned long long *__restrict__ votes, int K, int *
         order[atomicAdd(&start[lpt_bin(votes[c])], 1)] = c;
 }
 
-template <int BS>
+// One CTA per keypoint (in LPT order by block index), or with PERSIST a resident grid whose
+// CTAs take the next keypoint of the LPT order from a device counter until none is left.
+template <int BS, bool PERSIST>
 __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : 2) k_vote_acc(VoteArgs a, PipeBufs b) {
     extern __shared__ uint32_t acc[];
     __shared__ int       hOff[kHitChunk], hCnt[kHitChunk], cPre[kHitChunk + 1];
@@ -301,70 +307,91 @@ __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : 2) k_vote_acc(VoteArgs a,
     __shared__ int       sh[33];
     __shared__ Cand      wc[BS / 32][3];
     __shared__ unsigned long long shash;
+    __shared__ int       sNext;
 
-    const int  c    = b.order[blockIdx.x];
-    const int  tid  = threadIdx.x;
-    const int4 info = b.info[c];
-    if (!(info.w & 1)) {
-        skip_keypoint(a, c, info.x, (info.w & 2) != 0);
-        return;
-    }
-    if (tid == 0)
-        shash = 0;
-    const long long V      = (long long)b.votes[c];
-    const long long bound  = (long long)b.bound[c];
-    const int       nH     = b.hitCnt[c];
-    const int4     *H      = b.hits + b.rowOff[c];
-    const bool      narrow = bound <= kNarrowMax && !a.forceWide; // no cell can pass 65535
-    const int       chunk  = narrow ? a.refChunk : a.refChunkWide;
-    Cand            top[3];
-    for (int t = 0; t < 3; t++)
-        top[t] = Cand{-1.0f, INT_MAX, 0};
-    unsigned long long myHash = 0;
-    for (int r0 = 0; r0 < a.ns; r0 += chunk) {
-        const int r1     = min(r0 + chunk, a.ns);
-        const int nElem  = (r1 - r0) * a.A;
-        const int nWords = narrow ? (nElem + 1) >> 1 : nElem;
-        for (int i = tid; i < nWords; i += BS)
-            acc[i] = 0u;
-        for (int h0 = 0; h0 < nH; h0 += kHitChunk) {
-            const int n = min(kHitChunk, nH - h0);
-            __syncthreads();
-            int T = 0;
-            for (int j0 = 0; j0 < n; j0 += BS) {
-                const int j   = j0 + tid;
-                int       nit = 0;
-                if (j < n) {
-                    const int4 hv = H[h0 + j];
-                    hOff[j]       = hv.x;
-                    hCnt[j]       = hv.y;
-                    hAs[j]        = __int_as_float(hv.z);
-                    hAsT[j]       = smm::alpha_tail_shift(__int_as_float(hv.z));
-                    nit           = (hv.y + kItem - 1) / kItem;
-                }
-                int       tot;
-                const int pre = block_excl_scan(nit, sh, &tot);
-                if (j < n)
-                    cPre[j] = T + pre;
-                T += tot;
-            }
+    const int tid = threadIdx.x;
+    for (int it = 0;; it++) {
+        int idx = blockIdx.x;
+        if (PERSIST) {
             if (tid == 0)
-                cPre[n] = T;
+                sNext = atomicAdd(b.next, 1);
             __syncthreads();
-            cast_votes(a, acc, hOff, hCnt, hAs, hAsT, cPre, n, T, r0, r1, narrow);
+            idx = sNext;
+            __syncthreads();
+            if (idx >= a.K)
+                return;
+        } else if (it > 0) {
+            return;
         }
-        __syncthreads();
-        peaks_chunk(a, acc, narrow, r0, r1, top, myHash);
-        dump_chunk(a, c, acc, narrow, r0, r1);
-        __syncthreads();
+        const int  c    = b.order[idx];
+        const int4 info = b.info[c];
+        if (!(info.w & 1)) {
+            skip_keypoint(a, c, info.x, (info.w & 2) != 0);
+            continue;
+        }
+        if (tid == 0)
+            shash = 0;
+        const long long V      = (long long)b.votes[c];
+        const long long bound  = (long long)b.bound[c];
+        const int       nH     = b.hitCnt[c];
+        const int4     *H      = b.hits + b.rowOff[c];
+        const bool      narrow = bound <= kNarrowMax && !a.forceWide; // no cell can pass 65535
+        const int       chunk  = narrow ? a.refChunk : a.refChunkWide;
+        Cand            top[3];
+        for (int t = 0; t < 3; t++)
+            top[t] = Cand{-1.0f, INT_MAX, 0};
+        unsigned long long myHash = 0;
+        for (int r0 = 0; r0 < a.ns; r0 += chunk) {
+            const int r1     = min(r0 + chunk, a.ns);
+            const int nElem  = (r1 - r0) * a.A;
+            const int nWords = narrow ? (nElem + 1) >> 1 : nElem;
+            for (int i = tid; i < nWords; i += BS)
+                acc[i] = 0u;
+            for (int h0 = 0; h0 < nH; h0 += kHitChunk) {
+                const int n = min(kHitChunk, nH - h0);
+                __syncthreads();
+                int T = 0;
+                for (int j0 = 0; j0 < n; j0 += BS) {
+                    const int j   = j0 + tid;
+                    int       nit = 0;
+                    if (j < n) {
+                        const int4 hv = H[h0 + j];
+                        hOff[j]       = hv.x;
+                        hCnt[j]       = hv.y;
+                        hAs[j]        = __int_as_float(hv.z);
+                        hAsT[j]       = smm::alpha_tail_shift(__int_as_float(hv.z));
+                        nit           = (hv.y + kItem - 1) / kItem;
+                    }
+                    int       tot;
+                    const int pre = block_excl_scan(nit, sh, &tot);
+                    if (j < n)
+                        cPre[j] = T + pre;
+                    T += tot;
+                }
+                if (tid == 0)
+                    cPre[n] = T;
+                __syncthreads();
+                cast_votes(a, acc, hOff, hCnt, hAs, hAsT, cPre, n, T, r0, r1, narrow);
+            }
+            __syncthreads();
+            peaks_chunk(a, acc, narrow, r0, r1, top, myHash);
+            dump_chunk(a, c, acc, narrow, r0, r1);
+            __syncthreads();
+        }
+        finish_keypoint(a, c, b.rt[c], top, myHash, info.x, nH, V, bound, wc, &shash);
+        __syncthreads(); // the shared buffers serve the CTA's next keypoint
     }
-    finish_keypoint(a, c, b.rt[c], top, myHash, info.x, nH, V, bound, wc, &shash);
 }
 
 const void *vote_acc_fn(int shape) {
-    return shape == 0 ? (const void *)k_vote_acc<kAccShapes[0]>
-                      : shape == 1 ? (const void *)k_vote_acc<kAccShapes[1]>
-                                   : (const void *)k_vote_acc<kAccShapes[2]>;
+    switch (shape) {
+    case 0: return (const void *)k_vote_acc<kAccBs[0], false>;
+    case 1: return (const void *)k_vote_acc<kAccBs[1], false>;
+    case 2: return (const void *)k_vote_acc<kAccBs[2], false>;
+    case 3: return (const void *)k_vote_acc<kAccBs[0], true>;
+    case 4: return (const void *)k_vote_acc<kAccBs[1], true>;
+    default: return (const void *)k_vote_acc<kAccBs[2], true>;
+    }
 }
 
 // Dynamic shared memory of the accumulator for launch shape `shape` (its static shared
@@ -384,19 +411,32 @@ size_t vote_acc_smem(int shape, const Ctx &c, VoteArgs &a) {
 
 void launch_vote_acc(int shape, const Ctx &c, const VoteArgs &a, const PipeBufs &b, int K,
                      size_t smem) {
-    if (shape == 0)
-        k_vote_acc<kAccShapes[0]><<<K, kAccShapes[0], smem, c.stream>>>(a, b);
-    else if (shape == 1)
-        k_vote_acc<kAccShapes[1]><<<K, kAccShapes[1], smem, c.stream>>>(a, b);
-    else
-        k_vote_acc<kAccShapes[2]><<<K, kAccShapes[2], smem, c.stream>>>(a, b);
+    const int bs = kAccBs[shape % 3];
+    int       g  = K;
+    if (shape >= 3) {
+        // one resident wave, keypoints from the counter
+        int per = 0, nsm = 0;
+        SM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, vote_acc_fn(shape), bs, smem));
+        SM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device));
+        g = std::max(1, std::min(K, std::max(per, 1) * nsm));
+        SM_CUDA(cudaMemsetAsync(b.next, 0, sizeof(int), c.stream));
+    }
+    switch (shape) {
+    case 0: k_vote_acc<kAccBs[0], false><<<g, bs, smem, c.stream>>>(a, b); break;
+    case 1: k_vote_acc<kAccBs[1], false><<<g, bs, smem, c.stream>>>(a, b); break;
+    case 2: k_vote_acc<kAccBs[2], false><<<g, bs, smem, c.stream>>>(a, b); break;
+    case 3: k_vote_acc<kAccBs[0], true><<<g, bs, smem, c.stream>>>(a, b); break;
+    case 4: k_vote_acc<kAccBs[1], true><<<g, bs, smem, c.stream>>>(a, b); break;
+    default: k_vote_acc<kAccBs[2], true><<<g, bs, smem, c.stream>>>(a, b); break;
+    }
     SM_LAUNCH_CHECK();
 }
 
-// The launch tuner: per device, the vote accumulation CTA size measured fastest on the first
+// The launch tuner: per device, the vote accumulation shape measured fastest on the first
 // call with at least kTuneMinK keypoints (each shape timed twice with CUDA events on the
 // call's own data, the faster of the two runs kept), then used for every later call.
-// SM_VOTE_SHAPE=256|512|1024 in the environment fixes the shape instead (tests).
+// SM_VOTE_SHAPE=256|512|1024, with a trailing 'p' for the persistent grid, in the
+// environment fixes the shape instead (tests).
 constexpr int    kTuneMinK = 512;
 std::atomic<int> g_voteShape[64] = {};     // 0 untuned, else 1 + shape index
 std::mutex       g_tuneMu;
@@ -405,20 +445,25 @@ int forced_vote_shape() {
     const char *e = std::getenv("SM_VOTE_SHAPE");
     if (!e)
         return -1;
-    const int v = std::atoi(e);
+    const int  v       = std::atoi(e);
+    const bool persist = std::strchr(e, 'p') != nullptr;
     for (int s = 0; s < 3; s++)
-        if (kAccShapes[s] == v)
-            return s;
+        if (kAccBs[s] == v)
+            return s + (persist ? 3 : 0);
     return -1;
 }
 
 } // namespace
 
-int vote_tuned_block(int device) {
+int vote_tuned_shape(int device, int *persistent) {
+    *persistent = 0;
     if (device < 0 || device >= 64)
         return 0;
     const int t = g_voteShape[device].load();
-    return t > 0 ? kAccShapes[t - 1] : 0;
+    if (t <= 0)
+        return 0;
+    *persistent = t - 1 >= 3 ? 1 : 0;
+    return kAccBs[(t - 1) % 3];
 }
 
 void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const int *kp, int K,
@@ -476,6 +521,7 @@ void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const in
     b.votes  = c.arena.get<unsigned long long>("v.votes", K);
     b.bound  = c.arena.get<unsigned long long>("v.bound", K);
     b.order  = c.arena.get<int>("v.order", K);
+    b.next   = c.arena.get<int>("v.next", 1);
     int *cnt = c.arena.get<int>("v.rowcnt", (size_t)K + 1);
     if (csr) {
         k_kp_csr<<<nblocks((long long)K * 32, 256), 256, 0, c.stream>>>(a, b);
@@ -511,9 +557,11 @@ void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const in
             cudaEvent_t e0, e1;
             SM_CUDA(cudaEventCreate(&e0));
             SM_CUDA(cudaEventCreate(&e1));
-            float best[3] = {1e30f, 1e30f, 1e30f};
+            float best[kAccShapes];
+            for (int sh = 0; sh < kAccShapes; sh++)
+                best[sh] = 1e30f;
             for (int rep = 0; rep < 2; rep++)
-                for (int sh = 0; sh < 3; sh++) {
+                for (int sh = 0; sh < kAccShapes; sh++) {
                     VoteArgs     at = a;
                     const size_t sm = vote_acc_smem(sh, c, at);
                     if (!sm)
@@ -529,7 +577,7 @@ void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const in
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
             int pick = 1;
-            for (int sh = 0; sh < 3; sh++)
+            for (int sh = 0; sh < kAccShapes; sh++)
                 if (best[sh] < best[pick])
                     pick = sh;
             g_voteShape[dev].store(1 + pick);

@@ -277,7 +277,7 @@ def test_sampler_heavy_cells_and_wide_extent_bit_exact(data):
     np.testing.assert_array_equal(det.debug(2), r.resampled)
 
 
-@pytest.mark.parametrize("shape", ["256", "512", "1024"])
+@pytest.mark.parametrize("shape", ["256", "512", "1024", "256p", "512p", "1024p"])
 def test_vote_launch_shapes_give_identical_results(data, oracle_grid, monkeypatch, shape):
     """The voting stage's launch tuner picks among CTA sizes that must not change anything:
     with each size forced, per-keypoint statistics (with the accumulator fingerprints),
@@ -310,9 +310,13 @@ def test_vote_launch_tuner_picks_a_shape_once():
     det.matchScene(PointCloud(scene.cloud.xyz, None, scene.viewpoint), 0.03, 0.2, 0.2,
                    MatchParam(numMatches=16))
     assert det.last_stats["n_keypoints"] >= 512
+    import ctypes as C
     L = _lib.load()
-    first = L.sm_vote_tuned_block(0)
-    assert first in (256, 512, 1024)
+    t, p = C.c_int(0), C.c_int(0)
+    assert L.sm_vote_tuned_shape(0, C.byref(t), C.byref(p)) == 0
+    first = (t.value, p.value)
+    assert first[0] in (256, 512, 1024) and first[1] in (0, 1)
     det.matchScene(PointCloud(scene.cloud.xyz, None, scene.viewpoint), 0.03, 0.2, 0.2,
                    MatchParam(numMatches=16))
-    assert L.sm_vote_tuned_block(0) == first
+    assert L.sm_vote_tuned_shape(0, C.byref(t), C.byref(p)) == 0
+    assert (t.value, p.value) == first
