@@ -176,7 +176,7 @@ def run_reference(args, rank, world):
 def measure_batch(n_scenes, steps, warmup, sd=0.04, kp=0.2):
     """The batching workload (64 seeded scenes of 50k-2M points, 1-12 instances of a gear,
     an L-bracket or a torus each): matchScene of every scene through sm_match_batch
-    (concurrency picked by measurement among 2/4/8/12/16/24) against the same scenes one by one
+    (concurrency picked by measurement among 4/8/12/16/24/32) against the same scenes one by one
     through sm_match. Wall clock around the synchronous calls; scenes resident in HBM for
     `value`, pinned host buffers (copies inside the call) for `e2e`."""
     import torch
@@ -214,7 +214,7 @@ def measure_batch(n_scenes, steps, warmup, sd=0.04, kp=0.2):
         match_batch(dev, sd, kp, MS, param, concurrency=4)
     plain(dev[:4])
     tune = {}
-    for conc in (2, 4, 8, 12, 16, 24):  # concurrency picked by measurement
+    for conc in (4, 8, 12, 16, 24, 32):  # concurrency picked by measurement
         tune[conc] = batched(dev, conc)[0]
     best = min(tune, key=tune.get)
     times, votes = [], 0
