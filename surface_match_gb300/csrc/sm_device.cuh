@@ -15,17 +15,6 @@ namespace smd {
 constexpr int kMaxKnn      = 32; // largest supported knnNormal
 constexpr int kKnnMaxShell = 24; // shells a k-nearest walk visits before it scans every point
 
-// Device view of a dense uniform grid over a subset of points: cells are stored cell-major
-// as a CSR (start[cell] .. start[cell+1] into pts, the positions in cell order with the
-// point index in w). Used where per-cell state is needed (the sampler).
-struct GridView {
-    float         org[3];
-    float         g;
-    int           dim[3];
-    const int    *start;
-    const float4 *pts;
-};
-
 // Device view of a hashed uniform grid: only occupied cells are stored, in an
 // open-addressed table of uint4 {key low, key high, first point, point count} (count 0 =
 // empty slot), so cells can be as fine as the queries want whatever the scene's extent,
@@ -84,10 +73,6 @@ template <class G> __device__ __forceinline__ void grid_cc(const G &g, float x, 
     c[0] = smg::coord(x, g.org[0], g.g, g.dim[0]);
     c[1] = smg::coord(y, g.org[1], g.g, g.dim[1]);
     c[2] = smg::coord(z, g.org[2], g.g, g.dim[2]);
-}
-
-__device__ __forceinline__ int grid_cell(const GridView &G, int x, int y, int z) {
-    return (z * G.dim[1] + y) * G.dim[0] + x;
 }
 
 template <class G> __device__ __forceinline__ int grid_max_shell(const G &g, const int c[3]) {

@@ -109,28 +109,6 @@ private:
     std::map<std::string, std::pair<void *, size_t>> slots_;
 };
 
-// A grid built on the device over a subset of points.
-struct Grid {
-    float     org[3] = {0, 0, 0};
-    float     g      = 1;
-    int       dim[3] = {1, 1, 1};
-    long long nc     = 1;
-    int      *start  = nullptr; // nc + 1
-    float4   *pts    = nullptr; // m: positions in cell order, point index in w
-    int       m      = 0;
-    smd::GridView view() const {
-        smd::GridView v;
-        for (int a = 0; a < 3; a++) {
-            v.org[a] = org[a];
-            v.dim[a] = dim[a];
-        }
-        v.g     = g;
-        v.start = start;
-        v.pts   = pts;
-        return v;
-    }
-};
-
 // A hashed grid built on the device over a subset of points (see smd::HGridView).
 struct HGrid {
     float     org[3] = {0, 0, 0};
