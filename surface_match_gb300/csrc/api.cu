@@ -107,6 +107,7 @@ __global__ void k_gather4(const float4 *__restrict__ src, const int *__restrict_
 
 __global__ void k_gather_poses(const float *__restrict__ poses, const int *__restrict__ slots,
                                int m, float *__restrict__ out) {
+    smd::chain_enter(); // launched chained
     const int i = blockIdx.x;
     if (i >= m)
         return;
@@ -415,6 +416,7 @@ Ctx &aux_ctx(Ctx &c) {
         for (auto &e : a->ev)
             SM_CUDA(cudaEventCreate(&e));
         a->arena.set_stream(a->stream, c.device);
+        a->chain = c.chain;
         SM_CUDA(cudaEventCreateWithFlags(&c.fork, cudaEventDisableTiming));
         c.aux    = std::move(a);
         c.helper.reset(new Helper());
@@ -684,8 +686,7 @@ void match(Ctx &c, const Model &m, const float *xyzIn, const float *nrmIn, int64
     const int np    = compact(c, vo.poseOk, K * 3, slots, "m.cp");
     float    *plist = c.arena.get<float>("m.plist", (size_t)std::max(np, 1) * smi::kPoseFloats);
     if (np) {
-        k_gather_poses<<<np, 32, 0, c.stream>>>(vo.poses, slots, np, plist);
-        SM_LAUNCH_CHECK();
+        launch_chained(c, k_gather_poses, np, 32, 0, vo.poses, slots, np, plist);
     }
     record(c, 4);
     const float center[3] = {(m.box.mn[0] + m.box.mx[0]) / 2.f, (m.box.mn[1] + m.box.mx[1]) / 2.f,

@@ -47,6 +47,7 @@ std::unique_ptr<Ctx> acquire_worker(int device) {
     for (auto &e : c->ev)
         SM_CUDA(cudaEventCreate(&e));
     c->arena.set_stream(c->stream, device);
+    c->chain = false; // many workers share the device (see launch_chained)
     return c;
 }
 

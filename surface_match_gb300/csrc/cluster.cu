@@ -86,6 +86,7 @@ __device__ __forceinline__ bool compat(const float4 &a, const float4 &b, float s
 // (gbuf4), {tx, ty, tz, votes} and quaternions. The votes are staged per CTA in shared
 // memory (all lanes read the same one at a time: a broadcast).
 __global__ void k_cluster_rank(ClArgs a) {
+    smd::chain_enter(); // launched chained
     constexpr int kStage = 8192; // votes staged in shared memory (the rest read from L1/L2)
     __shared__ float sv[kStage];
     const int        np = a.np, ns = min(np, kStage);
@@ -112,6 +113,7 @@ __global__ void k_cluster_rank(ClArgs a) {
 // Compatibility bits over all CTAs: word w of row i (bitsG[w * np + i]), bit b set when
 // sorted pose i is compatible with the earlier sorted pose 32 w + b.
 __global__ void k_cluster_bits(ClArgs a) {
+    smd::chain_enter(); // launched chained
     const int  np = a.np, W = (np + 31) >> 5;
     const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long)np * W)
@@ -130,6 +132,7 @@ __global__ void k_cluster_bits(ClArgs a) {
 }
 
 __global__ void __launch_bounds__(kClBs) k_cluster_a(ClArgs a) {
+    smd::chain_enter(); // launched chained
     extern __shared__ float4 dsm4[];
     __shared__ int sNh;
     const int      tid = threadIdx.x, lane = tid & 31;
@@ -259,6 +262,7 @@ __global__ void __launch_bounds__(kClBs) k_cluster_a(ClArgs a) {
 // same additions in the same order as one thread summing all of them); then the Markley
 // quaternion average in FP64.
 __global__ void k_cluster_avg(ClArgs a) {
+    smd::chain_enter(); // launched chained
     const int lane = threadIdx.x & 31;
     const int nh   = *a.nhOut;
     // moment e of lane e: q[r] * q[s] over the upper triangle in row order
@@ -343,6 +347,7 @@ __global__ void k_cluster_avg(ClArgs a) {
 // kClMaxC clusters); the vote sums keep the sequential order of the walk, and the output
 // records are written by all threads afterwards.
 __global__ void __launch_bounds__(kClBs) k_cluster_b(ClArgs a) {
+    smd::chain_enter(); // launched chained
     __shared__ int    sNout;
     __shared__ float4 sTr[kClMaxC];
     __shared__ float  sVote[kClMaxC], sSum[kClMaxC];
@@ -471,20 +476,15 @@ int cluster(Ctx &c, const float *poses, int np, float distThr, float angThr, con
     const size_t smem  = a.smemState ? state + (a.useBits ? bitsB : 0) : 0;
     if (smem > allow_dynamic_smem((const void *)k_cluster_a, c.device))
         throw Error(SM_ERR_CAPACITY, "shared-memory request above the device limit");
-    k_cluster_rank<<<nblocks(np, 128), 128, 0, c.stream>>>(a);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_cluster_rank, nblocks(np, 128), 128, 0, a);
     a.bitsG = nullptr;
     if (a.useBits) {
         a.bitsG = c.arena.get<uint32_t>(tag + ".bits", (size_t)np * W);
-        k_cluster_bits<<<nblocks((long long)np * W, 256), 256, 0, c.stream>>>(a);
-        SM_LAUNCH_CHECK();
+        launch_chained(c, k_cluster_bits, nblocks((long long)np * W, 256), 256, 0, a);
     }
-    k_cluster_a<<<1, kClBs, smem, c.stream>>>(a);
-    SM_LAUNCH_CHECK();
-    k_cluster_avg<<<std::min(np, 152 * 8), 32, 0, c.stream>>>(a);
-    SM_LAUNCH_CHECK();
-    k_cluster_b<<<1, kClBs, 0, c.stream>>>(a);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_cluster_a, 1, kClBs, smem, a);
+    launch_chained(c, k_cluster_avg, std::min(np, 152 * 8), 32, 0, a);
+    launch_chained(c, k_cluster_b, 1, kClBs, 0, a);
     SM_CUDA(cudaMemcpyAsync(c.hostCounts, a.outCount, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     c.sync();
     return c.hostCounts[0];

@@ -85,6 +85,7 @@ __device__ __forceinline__ bool cand_live(const Cand &c, const Stage &s) {
 
 // K1: correspondences, one warp per source point (warp-cooperative grid search)
 __global__ void __launch_bounds__(kT, 4) k_corr(Work w, Stage s, int usePrev) {
+    chain_enter(); // launched chained
     const int ci   = blockIdx.y;
     const int lane = threadIdx.x & 31;
     int       i    = blockIdx.x * kW + (threadIdx.x >> 5);
@@ -136,6 +137,7 @@ __global__ void __launch_bounds__(kT, 4) k_corr(Work w, Stage s, int usePrev) {
 // reduced k-d tree (findClosestPoint, util.cpp:603-626: a 1-nearest search from the root,
 // with the tree's pruning) - the same pair rules as k_corr.
 __global__ void __launch_bounds__(kT) k_corr_tree(Work w, Stage s) {
+    chain_enter(); // launched chained
     const int   ci = blockIdx.y;
     const Cand &C  = w.cand[ci];
     if (!cand_live(C, s))
@@ -169,6 +171,7 @@ __global__ void __launch_bounds__(kT) k_corr_tree(Work w, Stage s) {
 
 // K4 with the reference's search: residual of each pair, one thread per pair.
 __global__ void __launch_bounds__(kT) k_resid_tree(Work w, Stage s) {
+    chain_enter(); // launched chained
     const int   ci = blockIdx.y;
     const Cand &C  = w.cand[ci];
     if (!cand_live(C, s) || C.cnt < 6)
@@ -268,6 +271,7 @@ __device__ void cluster_merge(cg::cluster_group &cl, float (*part)[2], smi::Kaha
 // K2: pair selection (the closest source point per scene point: the atomicMin winner), pair
 // count and centroids, then the normal-equation terms of the pairs and the FP64 solve.
 __global__ void __cluster_dims__(kRC, 1, 1) __launch_bounds__(kR) k_fit(Work w, Stage s) {
+    chain_enter(); // launched chained
     __shared__ float red[kRW][smi::kNumSystem][2];
     __shared__ float part[smi::kNumSystem][2]; // this CTA's totals, read by rank 0
     __shared__ int   ired[kRW];
@@ -420,6 +424,7 @@ __global__ void __cluster_dims__(kRC, 1, 1) __launch_bounds__(kR) k_fit(Work w, 
 
 // K4: residual distance of each pair after the step, one warp per pair
 __global__ void __launch_bounds__(kT, 5) k_resid(Work w, Stage s) {
+    chain_enter(); // launched chained
     const int   ci = blockIdx.y;
     const Cand &C  = w.cand[ci];
     if (!cand_live(C, s) || C.cnt < 6)
@@ -442,6 +447,7 @@ __global__ void __launch_bounds__(kT, 5) k_resid(Work w, Stage s) {
 // K5: mean residual, the regist loop logic (icp.cpp:233-272), winner reset; one cluster per
 // candidate (the same layout as K2), rank 0's thread 0 runs the logic
 __global__ void __cluster_dims__(kRC, 1, 1) __launch_bounds__(kR) k_update(Work w, Stage s) {
+    chain_enter(); // launched chained
     __shared__ float red[kRW][1][2];
     __shared__ float part[1][2];
     cg::cluster_group cl = cg::this_cluster();
@@ -538,6 +544,7 @@ __global__ void k_init(Work w, const float *__restrict__ cands, int ncand, float
 }
 
 __global__ void k_stage_begin(Work w, int ncand) {
+    chain_enter(); // launched chained
     const int ci = blockIdx.x * blockDim.x + threadIdx.x;
     if (ci >= ncand)
         return;
@@ -551,6 +558,7 @@ __global__ void k_stage_begin(Work w, int ncand) {
 
 // After a refinement: failed candidates get their status; converged ones keep the pose.
 __global__ void k_stage_end(Work w, int ncand, int failStatus) {
+    chain_enter(); // launched chained
     const int ci = blockIdx.x * blockDim.x + threadIdx.x;
     if (ci >= ncand)
         return;
@@ -569,6 +577,7 @@ __global__ void k_stage_end(Work w, int ncand, int failStatus) {
 // distance, one warp per point (warp_any_within).
 __global__ void __launch_bounds__(kT, 6) k_inliers(Work w, const float4 *__restrict__ src, int n,
                                                 HGridView F, float r2) {
+    chain_enter(); // launched chained
     __shared__ int sc[kW];
     const int      ci = blockIdx.y;
     const Cand    &C  = w.cand[ci];
@@ -597,6 +606,7 @@ __global__ void __launch_bounds__(kT, 6) k_inliers(Work w, const float4 *__restr
 // scoring distance (inliner, util.cpp:628-641), one thread per source point.
 __global__ void __launch_bounds__(kT) k_inliers_tree(Work w, const float4 *__restrict__ src, int n,
                                                      smk::KdView F, float r2) {
+    chain_enter(); // launched chained
     __shared__ int sc[kW];
     const int      ci = blockIdx.y;
     const Cand    &C  = w.cand[ci];
@@ -625,6 +635,7 @@ __global__ void __launch_bounds__(kT) k_inliers_tree(Work w, const float4 *__res
 }
 
 __global__ void k_score(Work w, int ncand, int n, float minScore, int failStatus, int slot) {
+    chain_enter(); // launched chained
     const int ci = blockIdx.x * blockDim.x + threadIdx.x;
     if (ci >= ncand)
         return;
@@ -642,6 +653,7 @@ __global__ void k_score(Work w, int ncand, int n, float minScore, int failStatus
 
 __global__ void k_finish(Work w, int ncand, int refine, float minScore, int *status, float *score,
                          float *pose) {
+    chain_enter(); // launched chained
     const int ci = blockIdx.x * blockDim.x + threadIdx.x;
     if (ci >= ncand)
         return;
@@ -660,30 +672,25 @@ void run_stage(Ctx &c, Work &w, const Stage &s, int ncand) {
     const dim3 gw(std::max(1, nblocks(s.n, kW)), ncand); // warp kernels: a warp per point
     const dim3 gt(std::max(1, nblocks(s.n, kT)), ncand); // tree searches: a thread per point
     const bool tree = s.tree.nd != nullptr;
-    k_stage_begin<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_stage_begin, nblocks(ncand, 128), 128, 0, w, ncand);
     for (int it = 0; it < s.iters; it++) {
         cudaEvent_t t0 = c.clock.begin(c.stream);
         if (tree)
-            k_corr_tree<<<gt, kT, 0, c.stream>>>(w, s);
+            launch_chained(c, k_corr_tree, gt, kT, 0, w, s);
         else
-            k_corr<<<gw, kT, 0, c.stream>>>(w, s, it > 0 ? 1 : 0);
-        SM_LAUNCH_CHECK();
+            launch_chained(c, k_corr, gw, kT, 0, w, s, it > 0 ? 1 : 0);
         c.clock.end(c.stream, t0, KernelClock::kCorr, 0.0); // bytes from the live count
         t0 = c.clock.begin(c.stream);
-        k_fit<<<gc, kR, 0, c.stream>>>(w, s);
-        SM_LAUNCH_CHECK();
+        launch_chained(c, k_fit, gc, kR, 0, w, s);
         c.clock.end(c.stream, t0, KernelClock::kFit, 0.0);
         t0 = c.clock.begin(c.stream);
         if (tree)
-            k_resid_tree<<<gt, kT, 0, c.stream>>>(w, s);
+            launch_chained(c, k_resid_tree, gt, kT, 0, w, s);
         else
-            k_resid<<<gw, kT, 0, c.stream>>>(w, s);
-        SM_LAUNCH_CHECK();
+            launch_chained(c, k_resid, gw, kT, 0, w, s);
         c.clock.end(c.stream, t0, KernelClock::kResid, 0.0);
         t0 = c.clock.begin(c.stream);
-        k_update<<<gc, kR, 0, c.stream>>>(w, s);
-        SM_LAUNCH_CHECK();
+        launch_chained(c, k_update, gc, kR, 0, w, s);
         c.clock.end(c.stream, t0, KernelClock::kUpdate, 0.0);
     }
 }
@@ -721,12 +728,11 @@ void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, con
     const bool tree = sc.tree != nullptr;
     auto inliers = [&](const float4 *src, int n) {
         if (tree)
-            k_inliers_tree<<<dim3(std::max(1, nblocks(n, kT)), ncand), kT, 0, c.stream>>>(
-                w, src, n, sc.tree->view(nullptr, sc.pos, nullptr, sc.tpF), sc2);
+            launch_chained(c, k_inliers_tree, dim3(std::max(1, nblocks(n, kT)), ncand), kT, 0,
+                           w, src, n, sc.tree->view(nullptr, sc.pos, nullptr, sc.tpF), sc2);
         else
-            k_inliers<<<dim3(std::max(1, nblocks(n, kW)), ncand), kT, 0, c.stream>>>(
-                w, src, n, sc.full.view(), sc2);
-        SM_LAUNCH_CHECK();
+            launch_chained(c, k_inliers, dim3(std::max(1, nblocks(n, kW)), ncand), kT, 0, w,
+                           src, n, sc.full.view(), sc2);
     };
     if (p.sparse) {
         Stage s{m.sp, m.sn, m.ns, nblocks(m.ns, kT), sc.sampled.view(), sc.posS, sc.nrmS, sc.sampled.m, 5,
@@ -736,11 +742,10 @@ void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, con
             s.rankOf = sc.rankS;
         }
         run_stage(c, w, s, ncand);
-        k_stage_end<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, 2);
-        SM_LAUNCH_CHECK();
+        launch_chained(c, k_stage_end, nblocks(ncand, 128), 128, 0, w, ncand, 2);
         inliers(m.sp, m.ns);
-        k_score<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, m.ns, p.minScore, 3, 0);
-        SM_LAUNCH_CHECK();
+        launch_chained(c, k_score, nblocks(ncand, 128), 128, 0, w, ncand, m.ns, p.minScore, 3,
+                       0);
         if (p.dense) {
             Stage d{m.rp, m.rn, m.nr, nblocks(m.nr, kT), sc.resampled.view(), sc.posR, sc.nrmR,
                     sc.resampled.m, p.denseSteps, p.reSampleStep * 0.5f, p.sampleStep, rej2, 1};
@@ -749,16 +754,14 @@ void icp_all(Ctx &c, const Model &m, const IcpScene &sc, const IcpParams &p, con
                 d.rankOf = sc.rankR;
             }
             run_stage(c, w, d, ncand);
-            k_stage_end<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, 4);
-            SM_LAUNCH_CHECK();
+            launch_chained(c, k_stage_end, nblocks(ncand, 128), 128, 0, w, ncand, 4);
             inliers(m.rp, m.nr);
-            k_score<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, m.nr, p.minScore, 5, 1);
-            SM_LAUNCH_CHECK();
+            launch_chained(c, k_score, nblocks(ncand, 128), 128, 0, w, ncand, m.nr, p.minScore,
+                           5, 1);
         }
     }
-    k_finish<<<nblocks(ncand, 128), 128, 0, c.stream>>>(w, ncand, (p.sparse || p.dense) ? 1 : 0,
-                                                         p.minScore, status, score, pose);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_finish, nblocks(ncand, 128), 128, 0, w, ncand,
+                   (p.sparse || p.dense) ? 1 : 0, p.minScore, status, score, pose);
 }
 
 } // namespace sm

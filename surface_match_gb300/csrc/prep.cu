@@ -149,6 +149,7 @@ __global__ void __launch_bounds__(kScanBs)
     k_scan_lookback(const int *__restrict__ in, int *__restrict__ out, long long n, int eq,
                     unsigned long long *__restrict__ status, int *__restrict__ ticket,
                     int nparts, unsigned epoch, int *__restrict__ total) {
+    chain_enter(); // launched chained
     __shared__ int sh[33];
     __shared__ int sTile, sExcl;
     if (threadIdx.x == 0) {
@@ -226,6 +227,7 @@ __global__ void __launch_bounds__(kScanBs)
 
 __global__ void k_scatter_flags(const int *__restrict__ flags, const int *__restrict__ pre, int n,
                                 int eq, int *__restrict__ out) {
+    chain_enter(); // launched chained
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
@@ -282,6 +284,7 @@ __global__ void k_thin_insert(const float4 *__restrict__ pos, const int *__restr
                               GridParams gp, unsigned long long *__restrict__ keys, uint32_t mask,
                               int *__restrict__ slotOf, int *__restrict__ sub,
                               int *__restrict__ cnt, int *__restrict__ ph) {
+    chain_enter(); // launched chained
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m)
         return;
@@ -309,6 +312,7 @@ __global__ void k_thin_insert(const float4 *__restrict__ pos, const int *__restr
 // ph[16..23] = their front fill pointers (ph[24..31] count heavy cells placed from the
 // back, ph[32..39] hand heavy cells to CTAs; both start at 0).
 __global__ void k_phase_offsets(int *__restrict__ ph) {
+    chain_enter(); // launched chained
     if (threadIdx.x != 0)
         return;
     int o = 0;
@@ -329,6 +333,7 @@ __global__ void k_thin_scatter(const float4 *__restrict__ pos, const int *__rest
                                const unsigned long long *__restrict__ keys, int dim0, int dim1,
                                float4 *__restrict__ pts, int *__restrict__ ph,
                                int *__restrict__ lists, int2 *__restrict__ rankCnt) {
+    chain_enter(); // launched chained
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m)
         return;
@@ -405,6 +410,7 @@ __global__ void __launch_bounds__(kSpWarps * 32)
                    int2 *__restrict__ rankCnt, float4 *__restrict__ keptPos, int cap, float r2,
                    int *__restrict__ keptFlag, int *__restrict__ overflow,
                    int *__restrict__ aliveTmp) {
+    smd::chain_enter(); // phases are chained launches: the previous phase's flags are final
     __shared__ float4 stageBuf[kSpBuf]; // heavy cell: [0, kSpHStage); light warp w: its slice
     __shared__ int    snr[26], scnt[26];
     __shared__ int    sCell, sMin[kSpWarps];
@@ -640,6 +646,7 @@ __global__ void __launch_bounds__(kSpWarps * 32)
 // ---------------------------------------------------------------------------------------
 __global__ void k_mark_todo(const int *__restrict__ ids, int m, const float4 *__restrict__ nrm,
                             int *__restrict__ need) {
+    chain_enter(); // launched chained
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m)
         return;
@@ -654,6 +661,7 @@ __global__ void __launch_bounds__(256, 6)
     k_knn(const int *__restrict__ list, const int *__restrict__ nlp, HGridView G, const float4 *__restrict__ pos,
                       int k, int *__restrict__ nbr, int *__restrict__ nbrCnt, int markNeighbours,
                       const float4 *__restrict__ nrm, int *__restrict__ need) {
+    chain_enter(); // launched chained
     const int nl = *nlp; // device-side count of the list
     const int lane = threadIdx.x & 31;
     const int t    = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
@@ -672,14 +680,13 @@ __global__ void __launch_bounds__(256, 6)
 }
 
 // list[0 .. *nlp) on the device; nlMax bounds it for the launch.
-void launch_knn(cudaStream_t st, const int *list, const int *nlp, int nlMax, const HGridView &G,
+void launch_knn(const Ctx &c, const int *list, const int *nlp, int nlMax, const HGridView &G,
                 const float4 *pos, int k, int *nbr, int *cnt, int mark, const float4 *nrm,
                 int *need) {
     if (nlMax <= 0)
         return;
-    k_knn<<<nblocks((long long)nlMax * 32, 256), 256, 0, st>>>(list, nlp, G, pos, k, nbr, cnt,
-                                                               mark, nrm, need);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_knn, nblocks((long long)nlMax * 32, 256), 256, 0, list, nlp, G, pos, k, nbr,
+                   cnt, mark, nrm, need);
 }
 
 // ---- hashed grid build -----------------------------------------------------------------
@@ -694,6 +701,7 @@ __device__ __forceinline__ unsigned long long hkey(const float4 &p, const GridPa
 __global__ void k_hg_insert(const float4 *__restrict__ pos, const int *__restrict__ ids, int m,
                             GridParams gp, unsigned long long *__restrict__ keys, uint32_t mask,
                             int *__restrict__ slotOf, int *__restrict__ cnt) {
+    chain_enter(); // launched chained
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m)
         return;
@@ -713,6 +721,7 @@ __global__ void k_hg_insert(const float4 *__restrict__ pos, const int *__restric
 __global__ void k_hg_scatter(const float4 *__restrict__ pos, const int *__restrict__ ids,
                              const int *__restrict__ slotOf, int m, int *__restrict__ fill,
                              int *__restrict__ gids, float4 *__restrict__ pts, int wIsRank) {
+    chain_enter(); // launched chained
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m)
         return;
@@ -727,6 +736,7 @@ __global__ void k_hg_scatter(const float4 *__restrict__ pos, const int *__restri
 __global__ void k_gather_subset(const float4 *__restrict__ pos, const float4 *__restrict__ nrm,
                                 const int *__restrict__ ids, int m, float4 *__restrict__ subPos,
                                 float4 *__restrict__ subNrm) {
+    chain_enter(); // launched chained
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= m)
         return;
@@ -739,6 +749,7 @@ __global__ void k_hg_pack_from_start(const unsigned long long *__restrict__ keys
                                      const int *__restrict__ start, uint32_t T,
                                      uint4 *__restrict__ slot, uint32_t *__restrict__ occ,
                                      int2 *__restrict__ dense) {
+    chain_enter(); // launched chained
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= T)
         return;
@@ -755,6 +766,7 @@ __global__ void k_hg_pack_from_start(const unsigned long long *__restrict__ keys
 // (similar cells, shared cache lines, little divergence). flags[k] = need[gids[k]] == eq.
 __global__ void k_flags_grid_order(const int *__restrict__ gids, int m, const int *__restrict__ need,
                                    int eq, int *__restrict__ flags) {
+    chain_enter(); // launched chained
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < m)
         flags[i] = need[gids[i]] == eq ? 1 : 0;
@@ -762,6 +774,7 @@ __global__ void k_flags_grid_order(const int *__restrict__ gids, int m, const in
 
 __global__ void k_scatter_ids(const int *__restrict__ flags, const int *__restrict__ pre, int n,
                               const int *__restrict__ gids, int *__restrict__ out) {
+    chain_enter(); // launched chained
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n && flags[i])
         out[pre[i]] = gids[i];
@@ -771,6 +784,7 @@ __global__ void k_scatter_ids(const int *__restrict__ flags, const int *__restri
 __global__ void k_pca(const int *__restrict__ list, const int *__restrict__ nlp, const int *__restrict__ nbr,
                       const int *__restrict__ nbrCnt, int k, const float4 *__restrict__ pos,
                       float4 *__restrict__ cen, float4 *__restrict__ nout) {
+    chain_enter(); // launched chained
     const int nl = *nlp; // device-side count of the list
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nl)
@@ -819,6 +833,7 @@ __global__ void k_pca(const int *__restrict__ list, const int *__restrict__ nlp,
 __global__ void k_pca_write(const int *__restrict__ list, const int *__restrict__ nlp, const float4 *__restrict__ cen,
                             const float4 *__restrict__ nin, float4 *__restrict__ pos,
                             float4 *__restrict__ nrm) {
+    chain_enter(); // launched chained
     const int nl = *nlp; // device-side count of the list
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nl || cen[t].w < 0.0f)
@@ -832,6 +847,7 @@ __global__ void k_pca_write(const int *__restrict__ list, const int *__restrict_
 __global__ void k_smooth(const int *__restrict__ list, const int *__restrict__ nlp, const int *__restrict__ nbr,
                          const int *__restrict__ nbrCnt, int k, const float4 *__restrict__ nrm,
                          float4 *__restrict__ out) {
+    chain_enter(); // launched chained
     const int nl = *nlp; // device-side count of the list
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nl)
@@ -868,6 +884,7 @@ __global__ void k_smooth(const int *__restrict__ list, const int *__restrict__ n
 
 __global__ void k_smooth_write(const int *__restrict__ list, const int *__restrict__ nlp, const float4 *__restrict__ sm,
                                float4 *__restrict__ nrm) {
+    chain_enter(); // launched chained
     const int nl = *nlp; // device-side count of the list
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nl || sm[t].w < 0.0f)
@@ -879,6 +896,7 @@ __global__ void k_smooth_write(const int *__restrict__ list, const int *__restri
 __global__ void k_orient(const int *__restrict__ ids, int m, const float4 *__restrict__ pos,
                          float4 *__restrict__ nrm, int hasVp, float vx, float vy, float vz,
                          int invert) {
+    chain_enter(); // launched chained
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m)
         return;
@@ -898,6 +916,7 @@ __global__ void k_orient(const int *__restrict__ ids, int m, const float4 *__res
 }
 
 __global__ void k_normalize(float4 *__restrict__ nrm, int n) {
+    chain_enter(); // launched chained
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
@@ -959,9 +978,8 @@ static void scan_into(Ctx &c, const int *in, int *out, long long n, int eq, int 
     }
     const unsigned epoch = scan_state(c, nparts);
     cudaEvent_t    t0    = c.clock.begin(c.stream);
-    k_scan_lookback<<<nparts, kScanBs, 0, c.stream>>>(in, out, n, eq, c.scan.status, c.scan.ticket,
-                                                      nparts, epoch, total);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_scan_lookback, nparts, kScanBs, 0, in, out, n, eq, c.scan.status,
+                   c.scan.ticket, nparts, epoch, total);
     c.clock.end(c.stream, t0, KernelClock::kScan, 8.0 * (double)n); // 4-byte value in, 4 out
 }
 
@@ -993,8 +1011,7 @@ static int compact_eq(Ctx &c, const int *flags, int n, int eq, int *outIds, cons
         return 0;
     int      *pre   = c.arena.get<int>(tag + ".pre", n);
     const int total = scan_impl(c, flags, pre, n, eq, tag, true);
-    k_scatter_flags<<<nblocks(n, 256), 256, 0, c.stream>>>(flags, pre, n, eq, outIds);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_scatter_flags, nblocks(n, 256), 256, 0, flags, pre, n, eq, outIds);
     return total;
 }
 
@@ -1007,8 +1024,7 @@ void compact_known(Ctx &c, const int *flags, int n, int *outIds, const std::stri
         return;
     int *pre = c.arena.get<int>(tag + ".pre", n);
     scan_impl(c, flags, pre, n, kNoEq, tag, false);
-    k_scatter_flags<<<nblocks(n, 256), 256, 0, c.stream>>>(flags, pre, n, kNoEq, outIds);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_scatter_flags, nblocks(n, 256), 256, 0, flags, pre, n, kNoEq, outIds);
 }
 
 // The points p of grid H with need[p] == eq, in H's cell order, into out; returns the device
@@ -1022,11 +1038,10 @@ static int *compact_grid_order(Ctx &c, const HGrid &H, const int *need, int eq, 
         SM_CUDA(cudaMemsetAsync(z, 0, sizeof(int), c.stream));
         return z;
     }
-    k_flags_grid_order<<<nblocks(H.m, 256), 256, 0, c.stream>>>(H.ids, H.m, need, eq, flags);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_flags_grid_order, nblocks(H.m, 256), 256, 0, H.ids, H.m, need, eq,
+                   flags);
     int *total = scan_flags_total(c, flags, pre, H.m, tag + ".gc");
-    k_scatter_ids<<<nblocks(H.m, 256), 256, 0, c.stream>>>(flags, pre, H.m, H.ids, out);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_scatter_ids, nblocks(H.m, 256), 256, 0, flags, pre, H.m, H.ids, out);
     return total;
 }
 
@@ -1057,16 +1072,15 @@ void build_hgrid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &bo
     SM_CUDA(cudaMemsetAsync(cnt, 0, (size_t)(T + 1) * 4, c.stream));
     GridParams gp = grid_params(box, g, H.dim);
     if (m > 0) {
-        k_hg_insert<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, m, gp, keys, H.mask, slotOf, cnt);
-        SM_LAUNCH_CHECK();
+        launch_chained(c, k_hg_insert, nblocks(m, 256), 256, 0, pos, ids, m, gp, keys, H.mask,
+                       slotOf, cnt);
     }
     scan_excl(c, cnt, start, (long long)T + 1, tag, false);
     int *fill = cnt;
     SM_CUDA(cudaMemcpyAsync(fill, start, (size_t)T * 4, cudaMemcpyDeviceToDevice, c.stream));
     if (m > 0) {
-        k_hg_scatter<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, slotOf, m, fill, H.ids, H.pts,
-                                                             wIsRank ? 1 : 0);
-        SM_LAUNCH_CHECK();
+        launch_chained(c, k_hg_scatter, nblocks(m, 256), 256, 0, pos, ids, slotOf, m, fill,
+                       H.ids, H.pts, wIsRank ? 1 : 0);
     }
     // occupancy bits over the cell box, when it has at most 2^28 cells (32 MB)
     const unsigned long long ncell = (unsigned long long)H.dim[0] * H.dim[1] * H.dim[2];
@@ -1083,17 +1097,16 @@ void build_hgrid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &bo
         SM_CUDA(cudaMemsetAsync(H.dense, 0, (size_t)ncell * sizeof(int2), c.stream));
     }
     // counts again for the packed table: start[t+1] - start[t]
-    k_hg_pack_from_start<<<nblocks(T, 256), 256, 0, c.stream>>>(keys, start, T, H.slot, H.occ,
-                                                                H.dense);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_hg_pack_from_start, nblocks(T, 256), 256, 0, keys, start, T, H.slot,
+                   H.occ, H.dense);
 }
 
 void gather_subset(Ctx &c, const float4 *pos, const float4 *nrm, const int *ids, int m,
                    float4 *subPos, float4 *subNrm) {
     if (m <= 0)
         return;
-    k_gather_subset<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, nrm, ids, m, subPos, subNrm);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_gather_subset, nblocks(m, 256), 256, 0, pos, nrm, ids, m, subPos,
+                   subNrm);
 }
 
 int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m, const Box &box,
@@ -1140,15 +1153,12 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
     SM_CUDA(cudaMemsetAsync(cnt, 0, ((size_t)T + 1) * sizeof(int), c.stream));
     SM_CUDA(cudaMemsetAsync(ph, 0, kSpPh * sizeof(int), c.stream));
     const GridParams gpar = grid_params(box, g, dim);
-    k_thin_insert<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, m, gpar, keys, dense ? 0u : T - 1,
-                                                         slotOf, sub, cnt, ph);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_thin_insert, nblocks(m, 256), 256, 0, pos, ids, m, gpar, keys,
+                   dense ? 0u : T - 1, slotOf, sub, cnt, ph);
     scan_excl(c, cnt, start, (long long)T + 1, tag + ".g", false);
-    k_phase_offsets<<<1, 32, 0, c.stream>>>(ph);
-    SM_LAUNCH_CHECK();
-    k_thin_scatter<<<nblocks(m, 256), 256, 0, c.stream>>>(pos, ids, m, slotOf, sub, start, keys,
-                                                          dim[0], dim[1], pts, ph, lists, rankCnt);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_phase_offsets, 1, 32, 0, ph);
+    launch_chained(c, k_thin_scatter, nblocks(m, 256), 256, 0, pos, ids, m, slotOf, sub,
+                   start, keys, dim[0], dim[1], pts, ph, lists, rankCnt);
     ThinView V;
     for (int a = 0; a < 3; a++) {
         V.org[a] = box.mn[a];
@@ -1183,10 +1193,8 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
     const int gp = (int)std::min<long long>((maxOcc + kSpWarps - 1) / kSpWarps, (long long)nsm * per);
     for (int p = 0; p < 8; p++) {
         cudaEvent_t t0 = c.clock.begin(c.stream);
-        k_sample_phase<<<gp, kSpWarps * 32, 0, c.stream>>>(V, lists, ph, p, rankCnt,
-                                                           keptPos, cap, r2, keptFlag, overflow,
-                                                           aliveTmp);
-        SM_LAUNCH_CHECK();
+        launch_chained(c, k_sample_phase, gp, kSpWarps * 32, 0, V, lists, ph, p, rankCnt,
+                       keptPos, cap, r2, keptFlag, overflow, aliveTmp);
         // algorithmic bytes of a sampling: each point's position read and its flag written
         // once (16 + 4 bytes), spread over the 8 phases
         c.clock.end(c.stream, t0, KernelClock::kSamplePhase, 20.0 * (double)m / 8.0);
@@ -1194,8 +1202,7 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
     // the kept points in index order (list order), and the overflow flag, in one round trip
     int *pre   = c.arena.get<int>(tag + ".out.pre", std::max(m, 1));
     int *total = scan_flags_total(c, keptFlag, pre, m, tag + ".out");
-    k_scatter_ids<<<nblocks(m, 256), 256, 0, c.stream>>>(keptFlag, pre, m, ids, outIds);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_scatter_ids, nblocks(m, 256), 256, 0, keptFlag, pre, m, ids, outIds);
     SM_CUDA(cudaMemcpyAsync(c.hostCounts, total, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     SM_CUDA(cudaMemcpyAsync(c.hostCounts + 1, overflow, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     c.sync();
@@ -1211,8 +1218,7 @@ static int *compact_need(Ctx &c, const int *need, int n, int eq, int *out, const
     int *pre   = c.arena.get<int>(tag + ".pre", std::max(n, 1));
     scan_into(c, need, pre, n, eq, total);
     if (n > 0) {
-        k_scatter_flags<<<nblocks(n, 256), 256, 0, c.stream>>>(need, pre, n, eq, out);
-        SM_LAUNCH_CHECK();
+        launch_chained(c, k_scatter_flags, nblocks(n, 256), 256, 0, need, pre, n, eq, out);
     }
     return total;
 }
@@ -1228,8 +1234,7 @@ void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *
         throw Error(SM_ERR_RANGE, "knnNormal larger than " + std::to_string(kMaxKnn) + " is not supported");
     int *need = c.arena.get<int>(tag + ".need", npoints);
     SM_CUDA(cudaMemsetAsync(need, 0, npoints * sizeof(int), c.stream));
-    k_mark_todo<<<nblocks(m, 256), 256, 0, c.stream>>>(ids, m, nrm, need);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_mark_todo, nblocks(m, 256), 256, 0, ids, m, nrm, need);
     // the query lists and their counts stay on the device; launches are sized by bounds
     // with the reference's k-d tree the k nearest come from its depth-first search (ties:
     // first found); the lists are then in index order (the results do not depend on it)
@@ -1242,7 +1247,7 @@ void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *
         kd_knn(c, *tree, nullptr, pos, nullptr, todo, ntodo, m, k, nbrT, nullptr, cntT, nrm,
                smooth ? need : nullptr);
     else
-        launch_knn(c.stream, todo, ntodo, m, query.view(), pos, k, nbrT, cntT, smooth ? 1 : 0, nrm, need);
+        launch_knn(c, todo, ntodo, m, query.view(), pos, k, nbrT, cntT, smooth ? 1 : 0, nrm, need);
     const int  extraMax = smooth ? (int)std::min<long long>(npoints, (long long)m * k) : 0;
     int       *extra = nullptr, *nbrE = nullptr, *cntE = nullptr;
     const int *nextra = nullptr;
@@ -1255,43 +1260,36 @@ void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *
         if (tree)
             kd_knn(c, *tree, nullptr, pos, nullptr, extra, nextra, extraMax, k, nbrE, nullptr, cntE);
         else
-            launch_knn(c.stream, extra, nextra, extraMax, query.view(), pos, k, nbrE, cntE, 0, nrm, need);
+            launch_knn(c, extra, nextra, extraMax, query.view(), pos, k, nbrE, cntE, 0, nrm, need);
     }
     const int nmax = std::max(m, extraMax);
     float4   *cen  = c.arena.get<float4>(tag + ".cen", 2 * (size_t)nmax);
     float4   *nn   = c.arena.get<float4>(tag + ".nn", 2 * (size_t)nmax);
-    k_pca<<<nblocks(m, 128), 128, 0, c.stream>>>(todo, ntodo, nbrT, cntT, k, pos, cen, nn);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_pca, nblocks(m, 128), 128, 0, todo, ntodo, nbrT, cntT, k, pos, cen,
+                   nn);
     if (extraMax > 0) {
-        k_pca<<<nblocks(extraMax, 128), 128, 0, c.stream>>>(extra, nextra, nbrE, cntE, k, pos,
-                                                             cen + nmax, nn + nmax);
-        SM_LAUNCH_CHECK();
+        launch_chained(c, k_pca, nblocks(extraMax, 128), 128, 0, extra, nextra, nbrE, cntE, k,
+                       pos, cen + nmax, nn + nmax);
     }
-    k_pca_write<<<nblocks(m, 256), 256, 0, c.stream>>>(todo, ntodo, cen, nn, pos, nrm);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_pca_write, nblocks(m, 256), 256, 0, todo, ntodo, cen, nn, pos, nrm);
     if (extraMax > 0) {
-        k_pca_write<<<nblocks(extraMax, 256), 256, 0, c.stream>>>(extra, nextra, cen + nmax,
-                                                                   nn + nmax, pos, nrm);
-        SM_LAUNCH_CHECK();
+        launch_chained(c, k_pca_write, nblocks(extraMax, 256), 256, 0, extra, nextra,
+                       cen + nmax, nn + nmax, pos, nrm);
     }
     if (smooth) {
-        k_smooth<<<nblocks(m, 256), 256, 0, c.stream>>>(todo, ntodo, nbrT, cntT, k, nrm, cen);
-        SM_LAUNCH_CHECK();
-        k_smooth_write<<<nblocks(m, 256), 256, 0, c.stream>>>(todo, ntodo, cen, nrm);
-        SM_LAUNCH_CHECK();
+        launch_chained(c, k_smooth, nblocks(m, 256), 256, 0, todo, ntodo, nbrT, cntT, k, nrm,
+                       cen);
+        launch_chained(c, k_smooth_write, nblocks(m, 256), 256, 0, todo, ntodo, cen, nrm);
     }
     const bool hasVp = vp && std::isfinite(vp[0]) && std::isfinite(vp[1]) && std::isfinite(vp[2]);
-    k_orient<<<nblocks(m, 256), 256, 0, c.stream>>>(ids, m, pos, nrm, hasVp ? 1 : 0,
-                                                    hasVp ? vp[0] : 0.f, hasVp ? vp[1] : 0.f,
-                                                    hasVp ? vp[2] : 0.f, invert ? 1 : 0);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_orient, nblocks(m, 256), 256, 0, ids, m, pos, nrm, hasVp ? 1 : 0,
+                   hasVp ? vp[0] : 0.f, hasVp ? vp[1] : 0.f, hasVp ? vp[2] : 0.f, invert ? 1 : 0);
 }
 
 void normalize_normals(Ctx &c, float4 *nrm, int n) {
     if (n <= 0)
         return;
-    k_normalize<<<nblocks(n, 256), 256, 0, c.stream>>>(nrm, n);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_normalize, nblocks(n, 256), 256, 0, nrm, n);
 }
 
 } // namespace sm

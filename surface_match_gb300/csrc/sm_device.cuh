@@ -601,4 +601,16 @@ __device__ __forceinline__ int block_excl_scan(int v, int *sh, int *total) {
     return r;
 }
 
+// Programmatic dependent launch. A kernel launched chained to the previous kernel of its
+// stream (sm::launch_chained) may be scheduled while that kernel is still running; it calls
+// chain_enter() before it touches memory: griddepcontrol.wait returns once the previous
+// kernel has completed and its writes are visible (for an ordinary launch it returns at
+// once), then launch_dependents lets the next chained kernel be scheduled. Since every
+// chained kernel waits before it releases its successor, a kernel that has entered sees the
+// writes of every kernel before it on the stream.
+__device__ __forceinline__ void chain_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 } // namespace smd

@@ -11,6 +11,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "sm_engine.h"
@@ -194,6 +195,9 @@ struct Ctx {
         unsigned            epoch  = 0;
     } scan;
     KernelClock clock; // opt-in per-launch timing (sm_context_kernel_clock)
+    // launches of this context are chained to the previous kernel of its stream (see
+    // launch_chained); off for the batch and serving workers, many of which run at once
+    bool chain = true;
     void sync() { SM_CUDA(cudaStreamSynchronize(stream)); }
     // sync, then fail loudly if a bounded device wait of the scans expired
     void sync_checked() {
@@ -205,6 +209,30 @@ struct Ctx {
             throw Error(SM_ERR_RUNTIME, "device scan: a bounded look-back wait expired");
     }
 };
+
+// Launches kernel k (smem bytes of dynamic shared memory) on the context's stream. With
+// c.chain the launch is chained to the previous kernel of the stream (programmatic dependent
+// launch): it is processed, and the kernel's blocks may be scheduled, while that kernel
+// finishes, which hides the launch latency of a dependent chain on an otherwise idle device.
+// When many streams share the device, blocks parked in their wait would hold slots that
+// other streams' kernels could use, so worker contexts launch ordinarily. Either way the
+// kernel calls smd::chain_enter() before it touches memory.
+template <typename... P, typename... A>
+void launch_chained(const Ctx &c, void (*k)(P...), dim3 grid, dim3 block, size_t smem,
+                    A &&...args) {
+    cudaLaunchAttribute at[1];
+    at[0].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg                           = {};
+    cfg.gridDim                                      = grid;
+    cfg.blockDim                                     = block;
+    cfg.dynamicSmemBytes                             = smem;
+    cfg.stream                                       = c.stream;
+    cfg.attrs                                        = at;
+    cfg.numAttrs                                     = c.chain ? 1 : 0;
+    SM_CUDA(cudaLaunchKernelEx(&cfg, k, std::forward<A>(args)...));
+    SM_LAUNCH_CHECK();
+}
 
 // ---- prep.cu ------------------------------------------------------------------------
 // Convert input xyz (+normals) to float4, mark finite points, reduce the bounding box of

@@ -106,6 +106,7 @@ __device__ __forceinline__ int tail_from_mask(const uint32_t *m, int nw, int nee
 // Radius mode: eight keypoints per CTA, one per warp, over shared-memory tiles of the
 // candidates' positions.
 __global__ void __launch_bounds__(kKpWarps * 32) k_kp_radius(VoteArgs a, PipeBufs b) {
+    smd::chain_enter(); // launched chained
     __shared__ float4 tp[kTile];
     __shared__ int    tid_[kTile];
     const int   lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -158,6 +159,7 @@ __global__ void __launch_bounds__(kKpWarps * 32) k_kp_radius(VoteArgs a, PipeBuf
 
 // CSR mode: one warp per keypoint over its list.
 __global__ void k_kp_csr(VoteArgs a, PipeBufs b) {
+    smd::chain_enter(); // launched chained
     const int lane = threadIdx.x & 31;
     const int c    = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (c >= a.K)
@@ -193,6 +195,7 @@ __global__ void k_kp_csr(VoteArgs a, PipeBufs b) {
 }
 
 __global__ void k_rows_count(const int4 *__restrict__ info, int K, int *__restrict__ cnt) {
+    smd::chain_enter(); // launched chained
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c < K)
         cnt[c] = info[c].y;
@@ -200,6 +203,7 @@ __global__ void k_rows_count(const int4 *__restrict__ info, int K, int *__restri
 
 // The rows of keypoint blockIdx.x into its segment (any order within it).
 __global__ void k_rows_fill(VoteArgs a, PipeBufs b, int csr) {
+    smd::chain_enter(); // launched chained
     __shared__ int sN;
     const int  c    = blockIdx.x;
     const int4 info = b.info[c];
@@ -246,6 +250,7 @@ __global__ void k_rows_fill(VoteArgs a, PipeBufs b, int csr) {
 // One thread per row: PPF key and scene alpha with the row's lane rule, then the model
 // table probe; hits go to the keypoint's segment.
 __global__ void k_ppf(VoteArgs a, PipeBufs b, const int *__restrict__ total) {
+    smd::chain_enter(); // launched chained
     const int n = *total;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         const int2     row = b.rows[r];
@@ -278,6 +283,7 @@ __device__ __forceinline__ int lpt_bin(unsigned long long v) {
 
 // Keypoints by vote count, largest first (binned by powers of two).
 __global__ void k_lpt(const unsigned long long *__restrict__ votes, int K, int *__restrict__ order) {
+    smd::chain_enter(); // launched chained
     __shared__ int hist[kLptBins], start[kLptBins];
     if (threadIdx.x < kLptBins)
         hist[threadIdx.x] = 0;
@@ -301,6 +307,7 @@ __global__ void k_lpt(const unsigned long long *__restrict__ votes, int K, int *
 // CTAs take the next keypoint of the LPT order from a device counter until none is left.
 template <int BS, bool PERSIST>
 __global__ void __launch_bounds__(BS, BS >= 1024 ? 1 : 2) k_vote_acc(VoteArgs a, PipeBufs b) {
+    smd::chain_enter(); // launched chained
     extern __shared__ uint32_t acc[];
     __shared__ int       hOff[kHitChunk], hCnt[kHitChunk], cPre[kHitChunk + 1];
     __shared__ float     hAs[kHitChunk], hAsT[kHitChunk];
@@ -422,14 +429,13 @@ void launch_vote_acc(int shape, const Ctx &c, const VoteArgs &a, const PipeBufs 
         SM_CUDA(cudaMemsetAsync(b.next, 0, sizeof(int), c.stream));
     }
     switch (shape) {
-    case 0: k_vote_acc<kAccBs[0], false><<<g, bs, smem, c.stream>>>(a, b); break;
-    case 1: k_vote_acc<kAccBs[1], false><<<g, bs, smem, c.stream>>>(a, b); break;
-    case 2: k_vote_acc<kAccBs[2], false><<<g, bs, smem, c.stream>>>(a, b); break;
-    case 3: k_vote_acc<kAccBs[0], true><<<g, bs, smem, c.stream>>>(a, b); break;
-    case 4: k_vote_acc<kAccBs[1], true><<<g, bs, smem, c.stream>>>(a, b); break;
-    default: k_vote_acc<kAccBs[2], true><<<g, bs, smem, c.stream>>>(a, b); break;
+    case 0: launch_chained(c, k_vote_acc<kAccBs[0], false>, g, bs, smem, a, b); break;
+    case 1: launch_chained(c, k_vote_acc<kAccBs[1], false>, g, bs, smem, a, b); break;
+    case 2: launch_chained(c, k_vote_acc<kAccBs[2], false>, g, bs, smem, a, b); break;
+    case 3: launch_chained(c, k_vote_acc<kAccBs[0], true>, g, bs, smem, a, b); break;
+    case 4: launch_chained(c, k_vote_acc<kAccBs[1], true>, g, bs, smem, a, b); break;
+    default: launch_chained(c, k_vote_acc<kAccBs[2], true>, g, bs, smem, a, b); break;
     }
-    SM_LAUNCH_CHECK();
 }
 
 // The launch tuner: per device, the vote accumulation shape measured fastest on the first
@@ -523,14 +529,11 @@ void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const in
     b.order  = c.arena.get<int>("v.order", K);
     b.next   = c.arena.get<int>("v.next", 1);
     int *cnt = c.arena.get<int>("v.rowcnt", (size_t)K + 1);
-    if (csr) {
-        k_kp_csr<<<nblocks((long long)K * 32, 256), 256, 0, c.stream>>>(a, b);
-    } else {
-        k_kp_radius<<<nblocks(K, kKpWarps), kKpWarps * 32, 0, c.stream>>>(a, b);
-    }
-    SM_LAUNCH_CHECK();
-    k_rows_count<<<nblocks(K, 256), 256, 0, c.stream>>>(b.info, K, cnt);
-    SM_LAUNCH_CHECK();
+    if (csr)
+        launch_chained(c, k_kp_csr, nblocks((long long)K * 32, 256), 256, 0, a, b);
+    else
+        launch_chained(c, k_kp_radius, nblocks(K, kKpWarps), kKpWarps * 32, 0, a, b);
+    launch_chained(c, k_rows_count, nblocks(K, 256), 256, 0, b.info, K, cnt);
     SM_CUDA(cudaMemsetAsync(cnt + K, 0, sizeof(int), c.stream));
     const int rtot = scan_excl(c, cnt, b.rowOff, (long long)K + 1, "v.scan", true);
     b.rows = c.arena.get<int2>("v.rows", std::max(rtot, 1));
@@ -538,17 +541,14 @@ void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const in
     SM_CUDA(cudaMemsetAsync(b.hitCnt, 0, (size_t)K * sizeof(int), c.stream));
     SM_CUDA(cudaMemsetAsync(b.votes, 0, (size_t)K * sizeof(unsigned long long), c.stream));
     SM_CUDA(cudaMemsetAsync(b.bound, 0, (size_t)K * sizeof(unsigned long long), c.stream));
-    k_rows_fill<<<K, 256, 0, c.stream>>>(a, b, csr ? 1 : 0);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_rows_fill, K, 256, 0, a, b, csr ? 1 : 0);
     SM_CUDA(cudaEventRecord(c.ev[10], c.stream));
     if (rtot > 0) {
         const int g = (int)std::min<long long>(nblocks(rtot, 256), 152LL * 8);
-        k_ppf<<<g, 256, 0, c.stream>>>(a, b, b.rowOff + K);
-        SM_LAUNCH_CHECK();
+        launch_chained(c, k_ppf, g, 256, 0, a, b, b.rowOff + K);
     }
     SM_CUDA(cudaEventRecord(c.ev[11], c.stream));
-    k_lpt<<<1, 1024, 0, c.stream>>>(b.votes, K, b.order);
-    SM_LAUNCH_CHECK();
+    launch_chained(c, k_lpt, 1, 1024, 0, b.votes, K, b.order);
     if (tune) {
         // every shape computes the same outputs: time each on this call's keypoints, keep
         // the fastest for the device (one process-wide decision, taken once)
