@@ -118,6 +118,50 @@ __global__ void k_init_bbox(int *bbox, int *nvalid) {
         *nvalid = 0;
 }
 
+// Up to four buffers of 32-bit words, each set to its value, in one chained launch (a
+// cudaMemsetAsync per buffer would be one stream operation each and break the launch chain).
+struct FillSet {
+    uint32_t *p[4];
+    long long n[4]; // words
+    uint32_t  v[4];
+    int       k = 0;
+    void add(void *ptr, size_t bytes, uint32_t value) {
+        p[k]   = (uint32_t *)ptr;
+        n[k]   = (long long)(bytes / 4);
+        v[k++] = value;
+    }
+};
+
+__global__ void k_fill(FillSet f) {
+    chain_enter(); // launched chained
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long st = (long long)gridDim.x * blockDim.x;
+    for (int s = 0; s < f.k; s++) {
+        uint32_t *p  = f.p[s];
+        const long long n  = f.n[s];
+        const uint32_t  v  = f.v[s];
+        // 16-byte stores over an aligned buffer's body, 4-byte stores for the rest
+        const long long n4 = ((uintptr_t)p & 15) == 0 ? n / 4 : 0;
+        uint4          *q  = reinterpret_cast<uint4 *>(p);
+        for (long long i = t0; i < n4; i += st)
+            q[i] = make_uint4(v, v, v, v);
+        for (long long i = n4 * 4 + t0; i < n; i += st)
+            p[i] = v;
+    }
+}
+
+static void fill(Ctx &c, const FillSet &f) {
+    long long words = 0;
+    for (int s = 0; s < f.k; s++)
+        words += f.n[s];
+    if (words == 0)
+        return;
+    int nsm = 0;
+    SM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device));
+    const int g = (int)std::min<long long>(nblocks((words + 3) / 4, 256), 8LL * std::max(nsm, 1));
+    launch_chained(c, k_fill, g, 256, 0, f);
+}
+
 // ---------------------------------------------------------------------------------------
 __device__ __forceinline__ int scan_val(const int *in, long long i, long long n, int eq) {
     if (i >= n)
@@ -332,11 +376,15 @@ __global__ void k_thin_scatter(const float4 *__restrict__ pos, const int *__rest
                                const int *__restrict__ start,
                                const unsigned long long *__restrict__ keys, int dim0, int dim1,
                                float4 *__restrict__ pts, int *__restrict__ ph,
-                               int *__restrict__ lists, int2 *__restrict__ rankCnt) {
+                               int *__restrict__ lists, int2 *__restrict__ rankCnt,
+                               int *__restrict__ keptFlag) {
     chain_enter(); // launched chained
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m)
         return;
+    keptFlag[i] = 0; // the phases' kept flags (and, at m, the overflow word) start clear
+    if (i == 0)
+        keptFlag[m] = 0;
     const int    h = slotOf[i];
     const int    k = sub[i];
     const float4 p = pos[ids[i]];
@@ -1068,8 +1116,21 @@ void build_hgrid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &bo
     H.ids        = c.arena.get<int>(tag + ".ids", std::max(m, 1));
     H.pts        = c.arena.get<float4>(tag + ".pts", std::max(m, 1));
     H.slot       = c.arena.get<uint4>(tag + ".slot", T);
-    SM_CUDA(cudaMemsetAsync(keys, 0xff, (size_t)T * 8, c.stream));
-    SM_CUDA(cudaMemsetAsync(cnt, 0, (size_t)(T + 1) * 4, c.stream));
+    // occupancy bits over the cell box, when it has at most 2^28 cells (32 MB), and a direct
+    // {first, count} table too when it has at most 2^22 cells (32 MB); all cleared with the
+    // key and count tables in one launch
+    const unsigned long long ncell = (unsigned long long)H.dim[0] * H.dim[1] * H.dim[2];
+    const size_t             words = (size_t)((ncell + 31) / 32);
+    H.occ   = ncell <= (1ull << 28) ? c.arena.get<uint32_t>(tag + ".occ", words) : nullptr;
+    H.dense = ncell <= (1ull << 22) ? c.arena.get<int2>(tag + ".dense", (size_t)ncell) : nullptr;
+    FillSet clear;
+    clear.add(keys, (size_t)T * 8, 0xffffffffu);
+    clear.add(cnt, (size_t)(T + 1) * 4, 0u);
+    if (H.occ)
+        clear.add(H.occ, words * 4, 0u);
+    if (H.dense)
+        clear.add(H.dense, (size_t)ncell * sizeof(int2), 0u);
+    fill(c, clear);
     GridParams gp = grid_params(box, g, H.dim);
     if (m > 0) {
         launch_chained(c, k_hg_insert, nblocks(m, 256), 256, 0, pos, ids, m, gp, keys, H.mask,
@@ -1081,20 +1142,6 @@ void build_hgrid(Ctx &c, const float4 *pos, const int *ids, int m, const Box &bo
     if (m > 0) {
         launch_chained(c, k_hg_scatter, nblocks(m, 256), 256, 0, pos, ids, slotOf, m, fill,
                        H.ids, H.pts, wIsRank ? 1 : 0);
-    }
-    // occupancy bits over the cell box, when it has at most 2^28 cells (32 MB)
-    const unsigned long long ncell = (unsigned long long)H.dim[0] * H.dim[1] * H.dim[2];
-    H.occ = nullptr;
-    if (ncell <= (1ull << 28)) {
-        const size_t words = (size_t)((ncell + 31) / 32);
-        H.occ              = c.arena.get<uint32_t>(tag + ".occ", words);
-        SM_CUDA(cudaMemsetAsync(H.occ, 0, words * 4, c.stream));
-    }
-    // a direct {first, count} table too when the cell box has at most 2^22 cells (32 MB)
-    H.dense = nullptr;
-    if (ncell <= (1ull << 22)) {
-        H.dense = c.arena.get<int2>(tag + ".dense", (size_t)ncell);
-        SM_CUDA(cudaMemsetAsync(H.dense, 0, (size_t)ncell * sizeof(int2), c.stream));
     }
     // counts again for the packed table: start[t+1] - start[t]
     launch_chained(c, k_hg_pack_from_start, nblocks(T, 256), 256, 0, keys, start, T, H.slot,
@@ -1148,17 +1195,21 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
     int   *ph      = c.arena.get<int>(tag + ".ph", kSpPh);
     int2  *rankCnt = c.arena.get<int2>(tag + ".rank", T);
     int   *lists   = c.arena.get<int>(tag + ".phl", maxOcc);
+    int   *keptFlag = c.arena.get<int>(tag + ".kf", (size_t)m + 1); // over the list places
+    int   *overflow = keptFlag + m;
+    FillSet clear;
     if (!dense)
-        SM_CUDA(cudaMemsetAsync(keys, 0xff, (size_t)T * 8, c.stream));
-    SM_CUDA(cudaMemsetAsync(cnt, 0, ((size_t)T + 1) * sizeof(int), c.stream));
-    SM_CUDA(cudaMemsetAsync(ph, 0, kSpPh * sizeof(int), c.stream));
+        clear.add(keys, (size_t)T * 8, 0xffffffffu);
+    clear.add(cnt, ((size_t)T + 1) * sizeof(int), 0u);
+    clear.add(ph, kSpPh * sizeof(int), 0u);
+    fill(c, clear);
     const GridParams gpar = grid_params(box, g, dim);
     launch_chained(c, k_thin_insert, nblocks(m, 256), 256, 0, pos, ids, m, gpar, keys,
                    dense ? 0u : T - 1, slotOf, sub, cnt, ph);
     scan_excl(c, cnt, start, (long long)T + 1, tag + ".g", false);
     launch_chained(c, k_phase_offsets, 1, 32, 0, ph);
     launch_chained(c, k_thin_scatter, nblocks(m, 256), 256, 0, pos, ids, m, slotOf, sub,
-                   start, keys, dim[0], dim[1], pts, ph, lists, rankCnt);
+                   start, keys, dim[0], dim[1], pts, ph, lists, rankCnt, keptFlag);
     ThinView V;
     for (int a = 0; a < 3; a++) {
         V.org[a] = box.mn[a];
@@ -1175,9 +1226,6 @@ int sample_points(Ctx &c, const float4 *pos, int npoints, const int *ids, int m,
     const int    cap = (int)std::floor((s + 1.0) * (s + 1.0) * (s + 1.0) / (3.14159265358979 / 6.0)) + 1;
     float4 *keptPos  = c.arena.get<float4>(tag + ".kp", (size_t)maxOcc * cap);
     int    *aliveTmp = c.arena.get<int>(tag + ".al", std::max(m, 1));
-    int    *keptFlag = c.arena.get<int>(tag + ".kf", (size_t)m + 1); // over the list places
-    int    *overflow = keptFlag + m;
-    SM_CUDA(cudaMemsetAsync(keptFlag, 0, ((size_t)m + 1) * sizeof(int), c.stream));
     const float r2 = step * step;
     // one resident wave: heavy cells are handed out by a counter, light cells by stride
     static std::atomic<int> resident[64];
@@ -1233,7 +1281,9 @@ void estimate_normals(Ctx &c, float4 *pos, float4 *nrm, int npoints, const int *
     if (k > kMaxKnn)
         throw Error(SM_ERR_RANGE, "knnNormal larger than " + std::to_string(kMaxKnn) + " is not supported");
     int *need = c.arena.get<int>(tag + ".need", npoints);
-    SM_CUDA(cudaMemsetAsync(need, 0, npoints * sizeof(int), c.stream));
+    FillSet clear;
+    clear.add(need, (size_t)npoints * sizeof(int), 0u);
+    fill(c, clear);
     launch_chained(c, k_mark_todo, nblocks(m, 256), 256, 0, ids, m, nrm, need);
     // the query lists and their counts stay on the device; launches are sized by bounds
     // with the reference's k-d tree the k nearest come from its depth-first search (ties:

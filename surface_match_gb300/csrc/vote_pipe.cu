@@ -194,11 +194,20 @@ __global__ void k_kp_csr(VoteArgs a, PipeBufs b) {
     }
 }
 
-__global__ void k_rows_count(const int4 *__restrict__ info, int K, int *__restrict__ cnt) {
+// Row counts per keypoint (cnt[K] = 0 closes the scan's input), and the per-keypoint hit
+// counters and vote totals cleared for k_ppf.
+__global__ void k_rows_count(const int4 *__restrict__ info, int K, int *__restrict__ cnt,
+                             PipeBufs b) {
     smd::chain_enter(); // launched chained
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < K)
-        cnt[c] = info[c].y;
+    if (c == 0)
+        cnt[K] = 0;
+    if (c < K) {
+        cnt[c]      = info[c].y;
+        b.hitCnt[c] = 0;
+        b.votes[c]  = 0ull;
+        b.bound[c]  = 0ull;
+    }
 }
 
 // The rows of keypoint blockIdx.x into its segment (any order within it).
@@ -282,9 +291,12 @@ __device__ __forceinline__ int lpt_bin(unsigned long long v) {
 }
 
 // Keypoints by vote count, largest first (binned by powers of two).
-__global__ void k_lpt(const unsigned long long *__restrict__ votes, int K, int *__restrict__ order) {
+__global__ void k_lpt(const unsigned long long *__restrict__ votes, int K, int *__restrict__ order,
+                      int *__restrict__ next) {
     smd::chain_enter(); // launched chained
     __shared__ int hist[kLptBins], start[kLptBins];
+    if (threadIdx.x == 0)
+        *next = 0; // the persistent vote grid's work counter
     if (threadIdx.x < kLptBins)
         hist[threadIdx.x] = 0;
     __syncthreads();
@@ -416,8 +428,10 @@ size_t vote_acc_smem(int shape, const Ctx &c, VoteArgs &a) {
     return smem;
 }
 
+// counterClear: the persistent grid's work counter is zero already (k_lpt clears it; each
+// of the tuner's timed launches uses it up).
 void launch_vote_acc(int shape, const Ctx &c, const VoteArgs &a, const PipeBufs &b, int K,
-                     size_t smem) {
+                     size_t smem, bool counterClear) {
     const int bs = kAccBs[shape % 3];
     int       g  = K;
     if (shape >= 3) {
@@ -426,7 +440,8 @@ void launch_vote_acc(int shape, const Ctx &c, const VoteArgs &a, const PipeBufs 
         SM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, vote_acc_fn(shape), bs, smem));
         SM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device));
         g = std::max(1, std::min(K, std::max(per, 1) * nsm));
-        SM_CUDA(cudaMemsetAsync(b.next, 0, sizeof(int), c.stream));
+        if (!counterClear)
+            SM_CUDA(cudaMemsetAsync(b.next, 0, sizeof(int), c.stream));
     }
     switch (shape) {
     case 0: launch_chained(c, k_vote_acc<kAccBs[0], false>, g, bs, smem, a, b); break;
@@ -533,14 +548,10 @@ void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const in
         launch_chained(c, k_kp_csr, nblocks((long long)K * 32, 256), 256, 0, a, b);
     else
         launch_chained(c, k_kp_radius, nblocks(K, kKpWarps), kKpWarps * 32, 0, a, b);
-    launch_chained(c, k_rows_count, nblocks(K, 256), 256, 0, b.info, K, cnt);
-    SM_CUDA(cudaMemsetAsync(cnt + K, 0, sizeof(int), c.stream));
+    launch_chained(c, k_rows_count, nblocks(K, 256), 256, 0, b.info, K, cnt, b);
     const int rtot = scan_excl(c, cnt, b.rowOff, (long long)K + 1, "v.scan", true);
     b.rows = c.arena.get<int2>("v.rows", std::max(rtot, 1));
     b.hits = c.arena.get<int4>("v.hits", std::max(rtot, 1));
-    SM_CUDA(cudaMemsetAsync(b.hitCnt, 0, (size_t)K * sizeof(int), c.stream));
-    SM_CUDA(cudaMemsetAsync(b.votes, 0, (size_t)K * sizeof(unsigned long long), c.stream));
-    SM_CUDA(cudaMemsetAsync(b.bound, 0, (size_t)K * sizeof(unsigned long long), c.stream));
     launch_chained(c, k_rows_fill, K, 256, 0, a, b, csr ? 1 : 0);
     SM_CUDA(cudaEventRecord(c.ev[10], c.stream));
     if (rtot > 0) {
@@ -548,7 +559,7 @@ void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const in
         launch_chained(c, k_ppf, g, 256, 0, a, b, b.rowOff + K);
     }
     SM_CUDA(cudaEventRecord(c.ev[11], c.stream));
-    launch_chained(c, k_lpt, 1, 1024, 0, b.votes, K, b.order);
+    launch_chained(c, k_lpt, 1, 1024, 0, b.votes, K, b.order, b.next);
     if (tune) {
         // every shape computes the same outputs: time each on this call's keypoints, keep
         // the fastest for the device (one process-wide decision, taken once)
@@ -567,7 +578,7 @@ void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const in
                     if (!sm)
                         continue;
                     SM_CUDA(cudaEventRecord(e0, c.stream));
-                    launch_vote_acc(sh, c, at, b, K, sm);
+                    launch_vote_acc(sh, c, at, b, K, sm, false);
                     SM_CUDA(cudaEventRecord(e1, c.stream));
                     SM_CUDA(cudaEventSynchronize(e1));
                     float ms = 0.0f;
@@ -586,7 +597,7 @@ void vote(Ctx &c, const Model &m, const float4 *pos, const float4 *nrm, const in
         smem  = vote_acc_smem(shape, c, a);
     }
     SM_CUDA(cudaEventRecord(c.ev[12], c.stream));
-    launch_vote_acc(shape, c, a, b, K, smem);
+    launch_vote_acc(shape, c, a, b, K, smem, !tune);
     SM_CUDA(cudaEventRecord(c.ev[13], c.stream));
 }
 
