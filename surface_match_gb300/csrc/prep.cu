@@ -126,6 +126,8 @@ struct FillSet {
     uint32_t  v[4];
     int       k = 0;
     void add(void *ptr, size_t bytes, uint32_t value) {
+        if (k == 4)
+            throw Error(SM_ERR_RUNTIME, "buffer clear: more than four buffers in one launch");
         p[k]   = (uint32_t *)ptr;
         n[k]   = (long long)(bytes / 4);
         v[k++] = value;
@@ -137,9 +139,9 @@ __global__ void k_fill(FillSet f) {
     const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long st = (long long)gridDim.x * blockDim.x;
     for (int s = 0; s < f.k; s++) {
-        uint32_t *p  = f.p[s];
-        const long long n  = f.n[s];
-        const uint32_t  v  = f.v[s];
+        uint32_t       *p = f.p[s];
+        const long long n = f.n[s];
+        const uint32_t  v = f.v[s];
         // 16-byte stores over an aligned buffer's body, 4-byte stores for the rest
         const long long n4 = ((uintptr_t)p & 15) == 0 ? n / 4 : 0;
         uint4          *q  = reinterpret_cast<uint4 *>(p);
